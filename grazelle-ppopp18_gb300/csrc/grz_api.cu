@@ -1,0 +1,367 @@
+// grz_api.cu -- graph context, ingest, queries and the exported C ABI (include/grazelle_gb300.h).
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "grz_internal.cuh"
+#include "../../include/grazelle_gb300.h"
+
+// grz_pr.cu
+int grz_pr_init_state(grz_graph* g, double damping);
+int grz_pr_fused_iteration(grz_graph* g, int write_double_props);
+int grz_pr_props_to_double(grz_graph* g);
+
+int grz_set_error(grz_graph* g, int code, const char* fmt, ...)
+{
+    if (g) {
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(g->err, sizeof(g->err), fmt, ap);
+        va_end(ap);
+    }
+    return code;
+}
+
+int grz_cuda_check(grz_graph* g, cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess) return GRZ_OK;
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return grz_set_error(g, GRZ_ERR_NOMEM, "%s: %s", what, cudaGetErrorString(e));
+    }
+    return grz_set_error(g, GRZ_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+extern "C" const char* grz_error_string(int code)
+{
+    switch (code) {
+        case GRZ_OK: return "ok";
+        case GRZ_ERR_ARG: return "bad argument";
+        case GRZ_ERR_CUDA: return "CUDA error";
+        case GRZ_ERR_NOMEM: return "out of device memory";
+        case GRZ_ERR_UNSORTED: return "edge list not grouped by its shared vertex in ascending order";
+        case GRZ_ERR_RANGE: return "vertex ID or size out of range";
+        case GRZ_ERR_STATE: return "call out of order";
+        case GRZ_ERR_IO: return "file missing, truncated or inconsistent";
+        case GRZ_ERR_TIMEOUT: return "bounded device wait timed out";
+        default: return "unknown error";
+    }
+}
+
+extern "C" const char* grz_graph_last_error(const grz_graph* g) { return g ? g->err : "no graph"; }
+
+static void free_list(grz_list* L)
+{
+    cudaFree(L->vs);
+    cudaFree(L->vindex);
+    cudaFree(L->nbr);
+    cudaFree(L->shared);
+    cudaFree(L->rowptr);
+    cudaFree(L->tile_coord);
+    memset(L, 0, sizeof(*L));
+}
+
+static void free_graph_data(grz_graph* g)
+{
+    free_list(&g->pull);
+    free_list(&g->push);
+    void* ptrs[] = { g->outdeg, g->degree, g->inv_deg, g->pr_fx[0], g->pr_fx[1], g->pr_sum, g->pr_split_acc,
+                     g->pr_split_cnt, g->prop, g->accum, g->glob, g->vote, g->scratch };
+    for (void* p : ptrs) cudaFree(p);
+    g->outdeg = nullptr; g->degree = nullptr; g->inv_deg = nullptr;
+    g->pr_fx[0] = g->pr_fx[1] = nullptr; g->pr_sum = nullptr; g->pr_split_acc = nullptr; g->pr_split_cnt = nullptr;
+    g->prop = nullptr; g->accum = nullptr; g->glob = nullptr; g->vote = nullptr; g->scratch = nullptr;
+    g->scratch_bytes = 0;
+    g->V = g->E = 0;
+}
+
+int grz_scratch(grz_graph* g, size_t bytes, void** out)
+{
+    if (bytes > g->scratch_bytes) {
+        cudaFree(g->scratch);
+        g->scratch = nullptr;
+        g->scratch_bytes = 0;
+        GRZ_CK(g, cudaMalloc(&g->scratch, bytes));
+        g->scratch_bytes = bytes;
+    }
+    *out = g->scratch;
+    return GRZ_OK;
+}
+
+extern "C" int grz_graph_create(grz_graph** out, int device, void* stream)
+{
+    if (!out) return GRZ_ERR_ARG;
+    *out = nullptr;
+    grz_graph* g = (grz_graph*)calloc(1, sizeof(grz_graph));
+    if (!g) return GRZ_ERR_NOMEM;
+    g->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+        free(g);
+        cudaGetLastError();
+        return GRZ_ERR_CUDA;
+    }
+    if (stream) {
+        g->stream = (cudaStream_t)stream;
+        g->own_stream = 0;
+    } else {
+        e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            free(g);
+            cudaGetLastError();
+            return GRZ_ERR_CUDA;
+        }
+        g->own_stream = 1;
+    }
+    *out = g;
+    return GRZ_OK;
+}
+
+extern "C" int grz_graph_set_stream(grz_graph* g, void* stream)
+{
+    if (!g) return GRZ_ERR_ARG;
+    cudaSetDevice(g->device);
+    if (g->own_stream) {
+        cudaStreamSynchronize(g->stream);
+        cudaStreamDestroy(g->stream);
+        g->own_stream = 0;
+    }
+    if (stream) {
+        g->stream = (cudaStream_t)stream;
+    } else {
+        GRZ_CK(g, cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+        g->own_stream = 1;
+    }
+    return GRZ_OK;
+}
+
+extern "C" void grz_graph_destroy(grz_graph* g)
+{
+    if (!g) return;
+    cudaSetDevice(g->device);
+    cudaStreamSynchronize(g->stream);
+    free_graph_data(g);
+    if (g->own_stream) cudaStreamDestroy(g->stream);
+    free(g);
+}
+
+extern "C" int grz_sync(grz_graph* g)
+{
+    if (!g) return GRZ_ERR_ARG;
+    GRZ_CK(g, cudaStreamSynchronize(g->stream));
+    return GRZ_OK;
+}
+
+static bool is_device_ptr(const void* p)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+extern "C" int grz_graph_load_pairs(grz_graph* g, uint64_t V, uint64_t E, const uint64_t* pull_pairs,
+                                    const uint64_t* push_pairs)
+{
+    if (!g || (E > 0 && !pull_pairs)) return GRZ_ERR_ARG;
+    if (V >= 0xffffffffull) return grz_set_error(g, GRZ_ERR_RANGE, "V = %llu exceeds the 32-bit device ID limit", (unsigned long long)V);
+    GRZ_CK(g, cudaSetDevice(g->device));
+    free_graph_data(g);
+    g->V = V;
+    g->E = E;
+    cudaStream_t st = g->stream;
+    const size_t pbytes = sizeof(uint64_t) * 2 * E;
+    int rc = GRZ_OK;
+    uint64_t* dpairs = nullptr;
+    // pull list
+    for (int which = 0; which < 2 && rc == GRZ_OK; ++which) {
+        const uint64_t* src = which == 0 ? pull_pairs : push_pairs;
+        if (which == 1 && !src) break;
+        const uint64_t* dp = src;
+        if (E > 0 && !is_device_ptr(src)) {
+            if (!dpairs) {
+                cudaError_t e = cudaMalloc((void**)&dpairs, pbytes);
+                if (e != cudaSuccess) { rc = grz_cuda_check(g, e, "cudaMalloc pairs"); break; }
+            }
+            cudaError_t e = cudaMemcpyAsync(dpairs, src, pbytes, cudaMemcpyHostToDevice, st);
+            if (e != cudaSuccess) { rc = grz_cuda_check(g, e, "H2D pairs"); break; }
+            dp = dpairs;
+        }
+        rc = grz_build_list(g, which == 0 ? &g->pull : &g->push, dp, E, which == 0 ? 1 : 0);
+        if (rc == GRZ_OK && which == 0) rc = grz_build_outdegrees(g, dp, E);
+        if (rc == GRZ_OK) rc = grz_cuda_check(g, cudaStreamSynchronize(st), "layout build");
+    }
+    if (dpairs) cudaFree(dpairs);
+    if (rc == GRZ_OK) {
+        cudaError_t e;
+        if ((e = cudaMalloc((void**)&g->prop, sizeof(double) * (V + 8))) != cudaSuccess) rc = grz_cuda_check(g, e, "props");
+        else if ((e = cudaMalloc((void**)&g->accum, sizeof(double) * (V + 8))) != cudaSuccess) rc = grz_cuda_check(g, e, "accum");
+        else if ((e = cudaMalloc((void**)&g->glob, sizeof(u128))) != cudaSuccess) rc = grz_cuda_check(g, e, "glob");
+        else if ((e = cudaMalloc((void**)&g->vote, sizeof(unsigned long long))) != cudaSuccess) rc = grz_cuda_check(g, e, "vote");
+        else {
+            cudaMemsetAsync(g->prop, 0, sizeof(double) * (V + 8), st);
+            cudaMemsetAsync(g->accum, 0, sizeof(double) * (V + 8), st);
+            cudaMemsetAsync(g->glob, 0, sizeof(u128), st);
+            cudaMemsetAsync(g->vote, 0, sizeof(unsigned long long), st);
+            rc = grz_cuda_check(g, cudaStreamSynchronize(st), "state init");
+        }
+    }
+    if (rc != GRZ_OK) free_graph_data(g);
+    return rc;
+}
+
+extern "C" int grz_graph_load_files(grz_graph* g, const char* base)
+{
+    if (!g || !base) return GRZ_ERR_ARG;
+    char path[2][4096];
+    snprintf(path[0], sizeof(path[0]), "%s-pull", base);
+    snprintf(path[1], sizeof(path[1]), "%s-push", base);
+    uint64_t hdr[2][2] = { { 0, 0 }, { 0, 0 } };
+    uint64_t* pairs[2] = { nullptr, nullptr };
+    int rc = GRZ_OK;
+    for (int i = 0; i < 2 && rc == GRZ_OK; ++i) {
+        FILE* f = fopen(path[i], "rb");
+        if (!f) {
+            if (i == 1) break;  // the push list is optional
+            return grz_set_error(g, GRZ_ERR_IO, "unable to read file \"%s\"", path[i]);
+        }
+        if (fread(hdr[i], sizeof(uint64_t), 2, f) != 2) {
+            rc = grz_set_error(g, GRZ_ERR_IO, "\"%s\": missing {V, E} header", path[i]);
+        } else if (i == 1 && (hdr[1][0] != hdr[0][0] || hdr[1][1] != hdr[0][1])) {
+            rc = grz_set_error(g, GRZ_ERR_IO, "\"%s\": header {V, E} differs from the -pull file", path[i]);
+        } else {
+            const uint64_t E = hdr[i][1];
+            if (E > (1ull << 40)) {
+                rc = grz_set_error(g, GRZ_ERR_IO, "\"%s\": implausible edge count %llu", path[i], (unsigned long long)E);
+            } else {
+                cudaError_t e = cudaMallocHost((void**)&pairs[i], sizeof(uint64_t) * 2 * (E ? E : 1));
+                if (e != cudaSuccess) {
+                    rc = grz_cuda_check(g, e, "pinned host buffer");
+                } else if (fread(pairs[i], sizeof(uint64_t), 2 * E, f) != 2 * E) {
+                    rc = grz_set_error(g, GRZ_ERR_IO, "\"%s\": truncated (header says %llu edges)", path[i], (unsigned long long)E);
+                }
+            }
+        }
+        fclose(f);
+    }
+    if (rc == GRZ_OK) rc = grz_graph_load_pairs(g, hdr[0][0], hdr[0][1], pairs[0], pairs[1]);
+    for (int i = 0; i < 2; ++i) if (pairs[i]) cudaFreeHost(pairs[i]);
+    return rc;
+}
+
+extern "C" int grz_graph_get_info(const grz_graph* g, grz_graph_info_t* out)
+{
+    if (!g || !out) return GRZ_ERR_ARG;
+    memset(out, 0, sizeof(*out));
+    out->num_vertices = g->V;
+    out->num_edges = g->E;
+    out->pull_vectors = g->pull.nvec;
+    out->push_vectors = g->push.nvec;
+    out->pull_index_start = g->pull.vindex_start;
+    out->pull_index_end = g->pull.vindex_end;
+    out->push_index_start = g->push.vindex_start;
+    out->push_index_end = g->push.vindex_end;
+    out->pull_list_device = g->pull.vs;
+    out->push_list_device = g->push.vs;
+    uint64_t b = 0;
+    const grz_list* Ls[2] = { &g->pull, &g->push };
+    for (const grz_list* L : Ls)
+        if (L->vs) b += L->nvec * (32 + 16 + 4) + (g->V + 64) * 8 + (g->V + 1) * 4;
+    b += (g->V + 8) * 8 * 3 + g->V * 12;
+    if (g->pr_fx[0]) b += g->V * (16 * 3 + 4);
+    out->device_bytes = b;
+    return GRZ_OK;
+}
+
+static const grz_list* list_of(const grz_graph* g, int list) { return list == GRZ_LIST_PUSH ? &g->push : &g->pull; }
+
+extern "C" int grz_graph_copy_list(grz_graph* g, int list, uint64_t* host, uint64_t cap)
+{
+    if (!g || !host) return GRZ_ERR_ARG;
+    const grz_list* L = list_of(g, list);
+    if (!L->vs) return grz_set_error(g, GRZ_ERR_STATE, "list not built");
+    if (cap < L->nvec) return grz_set_error(g, GRZ_ERR_ARG, "capacity %llu < %llu vectors", (unsigned long long)cap, (unsigned long long)L->nvec);
+    GRZ_CK(g, cudaMemcpyAsync(host, L->vs, sizeof(uint64_t) * 4 * L->nvec, cudaMemcpyDeviceToHost, g->stream));
+    GRZ_CK(g, cudaStreamSynchronize(g->stream));
+    return GRZ_OK;
+}
+
+extern "C" int grz_graph_copy_vertex_index(grz_graph* g, int list, uint64_t* host, uint64_t cap)
+{
+    if (!g || !host) return GRZ_ERR_ARG;
+    const grz_list* L = list_of(g, list);
+    if (!L->vindex) return grz_set_error(g, GRZ_ERR_STATE, "list not built");
+    if (cap < g->V + 64) return grz_set_error(g, GRZ_ERR_ARG, "capacity below V + 64");
+    GRZ_CK(g, cudaMemcpyAsync(host, L->vindex, sizeof(uint64_t) * (g->V + 64), cudaMemcpyDeviceToHost, g->stream));
+    GRZ_CK(g, cudaStreamSynchronize(g->stream));
+    return GRZ_OK;
+}
+
+extern "C" int grz_graph_copy_outdegrees(grz_graph* g, double* host, uint64_t cap)
+{
+    if (!g || !host) return GRZ_ERR_ARG;
+    if (!g->outdeg) return grz_set_error(g, GRZ_ERR_STATE, "no graph loaded");
+    if (cap < g->V) return grz_set_error(g, GRZ_ERR_ARG, "capacity below V");
+    GRZ_CK(g, cudaMemcpyAsync(host, g->outdeg, sizeof(double) * g->V, cudaMemcpyDeviceToHost, g->stream));
+    GRZ_CK(g, cudaStreamSynchronize(g->stream));
+    return GRZ_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// PageRank
+
+extern "C" int grz_pr_init(grz_graph* g, double damping)
+{
+    if (!g) return GRZ_ERR_ARG;
+    if (!g->outdeg) return grz_set_error(g, GRZ_ERR_STATE, "no graph loaded");
+    if (!(damping >= 0.0 && damping <= 1.0)) return grz_set_error(g, GRZ_ERR_ARG, "damping must be in [0, 1]");
+    GRZ_CK(g, cudaSetDevice(g->device));
+    g->app = GRZ_APP_PAGERANK;
+    return grz_pr_init_state(g, damping);
+}
+
+extern "C" int grz_pr_iterate(grz_graph* g, uint32_t iterations)
+{
+    if (!g) return GRZ_ERR_ARG;
+    if (!g->pr_fx[0]) return grz_set_error(g, GRZ_ERR_STATE, "grz_pr_init not called");
+    for (uint32_t i = 0; i < iterations; ++i) {
+        int rc = grz_pr_fused_iteration(g, 0);
+        if (rc) return rc;
+    }
+    return GRZ_OK;
+}
+
+extern "C" int grz_pr_time_iterations(grz_graph* g, uint32_t iterations, float* ms_out)
+{
+    if (!g || !ms_out) return GRZ_ERR_ARG;
+    if (!g->pr_fx[0]) return grz_set_error(g, GRZ_ERR_STATE, "grz_pr_init not called");
+    cudaEvent_t e0, e1;
+    GRZ_CK(g, cudaEventCreate(&e0));
+    GRZ_CK(g, cudaEventCreate(&e1));
+    int rc = GRZ_OK;
+    cudaEventRecord(e0, g->stream);
+    for (uint32_t i = 0; i < iterations && rc == GRZ_OK; ++i) rc = grz_pr_fused_iteration(g, 0);
+    cudaEventRecord(e1, g->stream);
+    if (rc == GRZ_OK) rc = grz_cuda_check(g, cudaEventSynchronize(e1), "event sync");
+    if (rc == GRZ_OK) cudaEventElapsedTime(ms_out, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+extern "C" int grz_read_props(grz_graph* g, double* host, uint64_t cap)
+{
+    if (!g || !host) return GRZ_ERR_ARG;
+    if (cap < g->V) return grz_set_error(g, GRZ_ERR_ARG, "capacity below V");
+    GRZ_CK(g, cudaSetDevice(g->device));
+    if (g->app == GRZ_APP_PAGERANK && g->pr_fx[0]) {
+        int rc = grz_pr_props_to_double(g);
+        if (rc) return rc;
+    }
+    GRZ_CK(g, cudaMemcpyAsync(host, g->prop, sizeof(double) * g->V, cudaMemcpyDeviceToHost, g->stream));
+    GRZ_CK(g, cudaStreamSynchronize(g->stream));
+    return GRZ_OK;
+}

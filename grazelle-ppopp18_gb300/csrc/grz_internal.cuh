@@ -1,0 +1,221 @@
+// grz_internal.cuh -- shared device/host definitions of the GB300 Grazelle engine.
+//
+// Data layout in HBM for one graph (V vertices, E edges, N vector-sparse vectors per list):
+//
+//   Reference layout (bit-identical to Grazelle's host packer, source/graphdata.c:143-173):
+//     list[l].vs        uint64[4N]   4-lane 256-bit vectors: valid bit 63, spread shared ID in
+//                                    bits 62:48, 48-bit neighbour ID in bits 47:0
+//     list[l].vindex    uint64[V+64] first vector of each shared vertex (graphdata.c:219-267)
+//   Execution layout (what the kernels stream):
+//     list[l].nbr       uint4[N]     the four neighbour IDs as uint32, invalid lane = 0xffffffff
+//     list[l].shared    uint32[N]    shared vertex of each vector (dst for pull, src for push)
+//     list[l].rowptr    uint32[V+1]  CSR over vectors: vectors of vertex v are [rowptr[v], rowptr[v+1])
+//   Per-vertex state:
+//     outdeg            double[V+8]  outdegree from the -pull list (graphdata.c:792-821)
+//     degree            uint32[V]    same, integer
+//     inv_deg           double[V]    1 / (outdeg == 0 ? V : outdeg)
+//     pr_fx[2]          u128[V]      PageRank props as unsigned 4.124 fixed point (ping-pong)
+//
+// All IDs on the device are 32-bit, so V and N must stay below 2^32 - 1.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define GRZ_INVALID_ID 0xffffffffu
+#define GRZ_FX_FRAC 124  // fractional bits of the u128 fixed-point PageRank values
+
+// ----------------------------------------------------------------------------------------------
+// error codes (also in include/grazelle_gb300.h)
+#define GRZ_OK 0
+#define GRZ_ERR_ARG -1
+#define GRZ_ERR_CUDA -2
+#define GRZ_ERR_NOMEM -3
+#define GRZ_ERR_UNSORTED -4
+#define GRZ_ERR_RANGE -5
+#define GRZ_ERR_STATE -6
+#define GRZ_ERR_IO -7
+#define GRZ_ERR_TIMEOUT -8
+
+// ----------------------------------------------------------------------------------------------
+// 128-bit unsigned fixed point
+
+struct __align__(16) u128 {
+    unsigned long long lo, hi;
+};
+
+__host__ __device__ __forceinline__ u128 u128_zero() { u128 r; r.lo = 0; r.hi = 0; return r; }
+
+__host__ __device__ __forceinline__ u128 u128_add(u128 a, u128 b)
+{
+    u128 r;
+    r.lo = a.lo + b.lo;
+    r.hi = a.hi + b.hi + (r.lo < a.lo ? 1ull : 0ull);
+    return r;
+}
+
+// a * d (mod 2^128); exact when the true product is below 2^128
+__device__ __forceinline__ u128 u128_mul32(u128 a, uint32_t d)
+{
+    u128 r;
+    r.lo = a.lo * (unsigned long long)d;
+    r.hi = a.hi * (unsigned long long)d + __umul64hi(a.lo, (unsigned long long)d);
+    return r;
+}
+
+// Exact conversion of a non-negative double below 16 to 4.124 fixed point.  Values below
+// 2^-72 lose their bits beneath 2^-124 (truncation); zero and subnormals map to 0.
+__host__ __device__ __forceinline__ u128 fx_from_double(double x)
+{
+    unsigned long long b;
+#ifdef __CUDA_ARCH__
+    b = (unsigned long long)__double_as_longlong(x);
+#else
+    __builtin_memcpy(&b, &x, 8);
+#endif
+    const int e = (int)((b >> 52) & 0x7ff);
+    u128 r = u128_zero();
+    if (e == 0) return r;
+    const unsigned long long m = (b & 0x000fffffffffffffull) | 0x0010000000000000ull;
+    const int sh = e - 1075 + GRZ_FX_FRAC;  // x = m * 2^(e-1075)
+    if (sh >= 0) {
+        if (sh == 0) { r.lo = m; }
+        else if (sh < 64) { r.lo = m << sh; r.hi = m >> (64 - sh); }
+        else if (sh < 128) { r.hi = m << (sh - 64); }
+    } else if (sh > -64) {
+        r.lo = m >> (-sh);
+    }
+    return r;
+}
+
+// Round-to-nearest-even conversion of 4.124 fixed point to double, integer arithmetic only.
+__host__ __device__ __forceinline__ double fx_to_double(u128 a)
+{
+    if ((a.hi | a.lo) == 0) return 0.0;
+#ifdef __CUDA_ARCH__
+    const int lz = a.hi ? __clzll((long long)a.hi) : 64 + __clzll((long long)a.lo);
+#else
+    const int lz = a.hi ? __builtin_clzll(a.hi) : 64 + __builtin_clzll(a.lo);
+#endif
+    const int msb = 127 - lz;
+    unsigned long long m;
+    int exp2 = msb - GRZ_FX_FRAC;  // value in [2^exp2, 2^(exp2+1))
+    if (msb <= 52) {
+        // fits: shift left so the leading bit lands on bit 52 (msb <= 52 implies a.hi == 0)
+        m = a.lo << (52 - msb);
+    } else {
+        const int sh = msb - 52;  // 1..75
+        unsigned long long rem_hi_bit, rem_rest;
+        // m = a >> sh (53 bits); round bit = bit (sh-1); sticky = bits below
+        if (sh < 64) {
+            m = (a.lo >> sh) | (sh ? (a.hi << (64 - sh)) : 0ull);
+            rem_hi_bit = (a.lo >> (sh - 1)) & 1ull;
+            rem_rest = (sh >= 2) ? (a.lo & ((1ull << (sh - 1)) - 1ull)) : 0ull;
+        } else if (sh == 64) {
+            m = a.hi;
+            rem_hi_bit = a.lo >> 63;
+            rem_rest = a.lo & 0x7fffffffffffffffull;
+        } else {
+            m = a.hi >> (sh - 64);
+            const int rb = sh - 1;  // round bit position (>= 64)
+            rem_hi_bit = (a.hi >> (rb - 64)) & 1ull;
+            rem_rest = ((rb - 64) ? (a.hi & ((1ull << (rb - 64)) - 1ull)) : 0ull) | a.lo;
+        }
+        if (rem_hi_bit && (rem_rest || (m & 1ull))) {
+            ++m;
+            if (m == (1ull << 53)) { m >>= 1; ++exp2; }
+        }
+    }
+    const unsigned long long bits = ((unsigned long long)(exp2 + 1023) << 52) | (m & 0x000fffffffffffffull);
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)bits);
+#else
+    double d;
+    __builtin_memcpy(&d, &bits, 8);
+    return d;
+#endif
+}
+
+// Exact global u128 accumulation: two 64-bit atomics; the low-word wrap-around is carried.
+__device__ __forceinline__ void u128_atomic_add(u128* dst, u128 v)
+{
+    const unsigned long long old = atomicAdd(&dst->lo, v.lo);
+    const unsigned long long carry = (old + v.lo < old) ? 1ull : 0ull;
+    if (v.hi | carry) atomicAdd(&dst->hi, v.hi + carry);
+}
+
+__device__ __forceinline__ u128 u128_shfl_down(u128 v, int off)
+{
+    u128 r;
+    r.lo = __shfl_down_sync(0xffffffffu, v.lo, off);
+    r.hi = __shfl_down_sync(0xffffffffu, v.hi, off);
+    return r;
+}
+
+// ----------------------------------------------------------------------------------------------
+// graph context
+
+struct grz_list {
+    uint64_t nvec;          // number of 4-lane vectors
+    uint64_t* vs;           // reference-format vectors, 4 words each
+    uint64_t* vindex;       // uint64[V+64]
+    uint64_t vindex_start;  // first shared vertex with vectors
+    uint64_t vindex_end;    // last shared vertex with vectors
+    uint4* nbr;             // uint4[nvec]
+    uint32_t* shared;       // uint32[nvec]
+    uint32_t* rowptr;       // uint32[V+1]
+    // merge-path tiles of the PageRank pull kernel: tile t starts at merge item t*items
+    uint32_t ntiles;
+    uint32_t tile_items;
+    uint2* tile_coord;      // (row, vector) at each tile start, ntiles+1 entries
+};
+
+struct grz_graph {
+    int device;
+    cudaStream_t stream;
+    int own_stream;
+    uint64_t V, E;
+    grz_list pull, push;
+    double* outdeg;       // double[V+8]
+    uint32_t* degree;     // uint32[V]
+    double* inv_deg;      // double[V]
+    // PageRank state
+    u128* pr_fx[2];
+    int pr_cur;           // which pr_fx holds the current props
+    u128* pr_sum;         // u128[3] rotating exact sums S_k
+    int pr_sum_cur;
+    u128* pr_split_acc;   // u128[V], partial sums of rows that cross tiles (kept zero between uses)
+    uint32_t* pr_split_cnt;
+    double pr_damping;
+    uint32_t pr_iters_done;
+    double* prop;         // double[V+8]: reference-format vertex props (PR props, CC labels, BFS parents)
+    double* accum;        // double[V+8]: reference accumulators (PR) / HasInfo* bitmap (CC, BFS)
+    // scratch
+    void* scratch;
+    size_t scratch_bytes;
+    // global accumulator of the phase API (exact)
+    u128* glob;           // u128[1] device
+    unsigned long long* vote;  // uint64[1] device
+    int app;              // 0 PR, 1 CC, 2 BFS
+    char err[256];
+};
+
+// host helpers (grz_api.cu)
+int grz_set_error(grz_graph* g, int code, const char* fmt, ...);
+int grz_cuda_check(grz_graph* g, cudaError_t e, const char* what);
+int grz_scratch(grz_graph* g, size_t bytes, void** out);
+
+#define GRZ_CK(g, call)                                         \
+    do {                                                        \
+        cudaError_t e__ = (call);                               \
+        if (e__ != cudaSuccess) return grz_cuda_check((g), e__, #call); \
+    } while (0)
+
+// layout (grz_layout.cu)
+int grz_build_list(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t E, int shared_is_dst);
+int grz_build_outdegrees(grz_graph* g, const uint64_t* d_pull_pairs, uint64_t E);
+int grz_build_pr_tiles(grz_graph* g, grz_list* L, uint32_t tile_items);
+
+// scans (grz_scan.cu): exclusive sum of uint32 into uint32 (n < 2^32), inclusive max of uint32
+int grz_exclusive_sum_u32(grz_graph* g, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total_out_dev);
+int grz_inclusive_max_u32(grz_graph* g, const uint32_t* in, uint32_t* out, uint64_t n);

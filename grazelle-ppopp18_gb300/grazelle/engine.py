@@ -1,0 +1,132 @@
+"""Python front end of the GB300 engine: one ``Graph`` wraps one ``grz_graph``.
+
+Mirrors the reference's driver flow (source/main.c:62-117): load a graph from
+its -pull/-push edge lists, run one application, then read the vertex props
+back in the reference's format (PR: rank/outdegree', CC: labels, BFS: parents,
+all float64).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import native
+
+
+def _ptr(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)
+
+
+class Graph:
+    def __init__(self, device: int = 0, stream: int | None = None):
+        self.lib = native.load()
+        h = C.c_void_p()
+        native.check(self.lib.grz_graph_create(C.byref(h), device, C.c_void_p(stream) if stream else None))
+        self.h = h
+        self.V = 0
+        self.E = 0
+
+    # ------------------------------------------------------------------ lifecycle
+    def close(self):
+        if self.h:
+            self.lib.grz_graph_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc):
+        native.check(rc, self.h)
+
+    def set_stream(self, stream: int | None):
+        self._ck(self.lib.grz_graph_set_stream(self.h, C.c_void_p(stream) if stream else None))
+
+    def sync(self):
+        self._ck(self.lib.grz_sync(self.h))
+
+    # ------------------------------------------------------------------ ingest
+    def load_pairs(self, num_vertices: int, pull_pairs, push_pairs=None):
+        """Interleaved (src, dst) uint64 pairs in file order.  numpy arrays (host) or raw device pointers (int)."""
+        def arg(x):
+            if x is None:
+                return None, 0
+            if isinstance(x, int):
+                return C.c_void_p(x), None
+            x = np.ascontiguousarray(x, dtype=np.uint64)
+            return _ptr(x), x
+        pp, keep1 = arg(pull_pairs)
+        sp, keep2 = arg(push_pairs)
+        if isinstance(pull_pairs, int):
+            raise ValueError("pass the edge count with load_device_pairs for device pointers")
+        E = keep1.shape[0] // 2
+        self._ck(self.lib.grz_graph_load_pairs(self.h, num_vertices, E, pp, sp))
+        self.V, self.E = num_vertices, E
+        return self
+
+    def load_device_pairs(self, num_vertices: int, num_edges: int, pull_ptr: int, push_ptr: int | None = None):
+        self._ck(self.lib.grz_graph_load_pairs(self.h, num_vertices, num_edges, C.c_void_p(pull_ptr),
+                                               C.c_void_p(push_ptr) if push_ptr else None))
+        self.V, self.E = num_vertices, num_edges
+        return self
+
+    def load_files(self, base: str):
+        self._ck(self.lib.grz_graph_load_files(self.h, base.encode()))
+        info = self.info()
+        self.V, self.E = info.num_vertices, info.num_edges
+        return self
+
+    def info(self) -> native.GraphInfo:
+        out = native.GraphInfo()
+        self._ck(self.lib.grz_graph_get_info(self.h, C.byref(out)))
+        return out
+
+    def list_vectors(self, which: int = native.LIST_PULL) -> np.ndarray:
+        info = self.info()
+        n = info.pull_vectors if which == native.LIST_PULL else info.push_vectors
+        out = np.zeros((n, 4), dtype=np.uint64)
+        self._ck(self.lib.grz_graph_copy_list(self.h, which, _ptr(out), n))
+        return out
+
+    def vertex_index(self, which: int = native.LIST_PULL) -> np.ndarray:
+        out = np.zeros(self.V + 64, dtype=np.uint64)
+        self._ck(self.lib.grz_graph_copy_vertex_index(self.h, which, _ptr(out), out.shape[0]))
+        return out
+
+    def outdegrees(self) -> np.ndarray:
+        out = np.zeros(self.V, dtype=np.float64)
+        self._ck(self.lib.grz_graph_copy_outdegrees(self.h, _ptr(out), out.shape[0]))
+        return out
+
+    # ------------------------------------------------------------------ PageRank
+    def pr_init(self, damping: float = 0.875):
+        self._ck(self.lib.grz_pr_init(self.h, damping))
+        return self
+
+    def pr_iterate(self, iterations: int):
+        self._ck(self.lib.grz_pr_iterate(self.h, iterations))
+        return self
+
+    def pr_time(self, iterations: int) -> float:
+        ms = C.c_float()
+        self._ck(self.lib.grz_pr_time_iterations(self.h, iterations, C.byref(ms)))
+        return ms.value
+
+    def pagerank(self, iterations: int, damping: float = 0.875) -> np.ndarray:
+        """Props (rank / outdegree') after `iterations` pull iterations, as the reference stores them."""
+        self.pr_init(damping).pr_iterate(iterations)
+        return self.props()
+
+    def props(self) -> np.ndarray:
+        out = np.zeros(self.V, dtype=np.float64)
+        self._ck(self.lib.grz_read_props(self.h, _ptr(out), out.shape[0]))
+        return out

@@ -1,0 +1,109 @@
+"""ctypes binding of ``libgrazelle_gb300.so`` (the C ABI of ``include/grazelle_gb300.h`` and
+``include/grazelle_phases.h``).
+
+There is no fallback: if the library is missing, or a call reports a CUDA error,
+an exception is raised.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+from . import build as _build
+
+GRZ_OK = 0
+ERRORS = {
+    -1: "GRZ_ERR_ARG", -2: "GRZ_ERR_CUDA", -3: "GRZ_ERR_NOMEM", -4: "GRZ_ERR_UNSORTED",
+    -5: "GRZ_ERR_RANGE", -6: "GRZ_ERR_STATE", -7: "GRZ_ERR_IO", -8: "GRZ_ERR_TIMEOUT",
+}
+APP_PAGERANK, APP_CONNECTED_COMPONENTS, APP_BREADTH_FIRST_SEARCH = 0, 1, 2
+LIST_PULL, LIST_PUSH = 0, 1
+
+
+class GrzError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "GRZ_ERR"), code, msg))
+        self.code = code
+
+
+class GraphInfo(C.Structure):
+    _fields_ = [
+        ("num_vertices", C.c_uint64), ("num_edges", C.c_uint64),
+        ("pull_vectors", C.c_uint64), ("push_vectors", C.c_uint64),
+        ("pull_index_start", C.c_uint64), ("pull_index_end", C.c_uint64),
+        ("push_index_start", C.c_uint64), ("push_index_end", C.c_uint64),
+        ("pull_list_device", C.c_void_p), ("push_list_device", C.c_void_p),
+        ("device_bytes", C.c_uint64),
+    ]
+
+
+# every exported symbol with (restype, argtypes); the headers in include/ declare the same set
+_VP, _U64, _U32, _I, _D = C.c_void_p, C.c_uint64, C.c_uint32, C.c_int, C.c_double
+_PU64, _PD = C.POINTER(C.c_uint64), C.POINTER(C.c_double)
+SIGNATURES = {
+    # grazelle_gb300.h
+    "grz_error_string": (C.c_char_p, [_I]),
+    "grz_graph_last_error": (C.c_char_p, [_VP]),
+    "grz_graph_create": (_I, [C.POINTER(_VP), _I, _VP]),
+    "grz_graph_set_stream": (_I, [_VP, _VP]),
+    "grz_graph_destroy": (None, [_VP]),
+    "grz_sync": (_I, [_VP]),
+    "grz_graph_load_pairs": (_I, [_VP, _U64, _U64, _VP, _VP]),
+    "grz_graph_load_files": (_I, [_VP, C.c_char_p]),
+    "grz_graph_get_info": (_I, [_VP, C.POINTER(GraphInfo)]),
+    "grz_graph_copy_list": (_I, [_VP, _I, _VP, _U64]),
+    "grz_graph_copy_vertex_index": (_I, [_VP, _I, _VP, _U64]),
+    "grz_graph_copy_outdegrees": (_I, [_VP, _VP, _U64]),
+    "grz_pr_init": (_I, [_VP, _D]),
+    "grz_pr_iterate": (_I, [_VP, _U32]),
+    "grz_read_props": (_I, [_VP, _VP, _U64]),
+    "grz_pr_time_iterations": (_I, [_VP, _U32, C.POINTER(C.c_float)]),
+    # grazelle_phases.h
+    "grz_phases_bind": (_I, [_VP, _I]),
+    "grz_phases_last_status": (_I, []),
+    "phase_op_reset_global_accum": (None, []),
+    "phase_op_write_global_accum_to_buf": (None, [_VP]),
+    "phase_op_combine_global_var_from_buf": (_U64, [_VP]),
+    "edge_pull_op_merge_with_merge_buffer": (None, [_VP, _U64, _VP]),
+    "perform_edge_pull_phase_pr": (None, [_VP, _U64]),
+    "perform_edge_pull_phase_cc": (None, [_VP, _U64]),
+    "perform_edge_pull_phase_bfs": (None, [_VP, _U64]),
+    "perform_edge_push_phase_pr": (None, [_VP, _U64]),
+    "perform_edge_push_phase_cc": (None, [_VP, _U64]),
+    "perform_edge_push_phase_bfs": (None, [_VP, _U64]),
+    "perform_vertex_phase_pr": (None, [_U64, _U64, _VP]),
+    "perform_vertex_phase_cc": (None, [_U64, _U64, _VP]),
+    "perform_vertex_phase_bfs": (None, [_U64, _U64, _VP]),
+}
+
+_lib = None
+
+
+def library_path() -> Path:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Loads libgrazelle_gb300.so (building it first if asked); raises if it cannot."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not path.exists():
+        if not build_if_missing:
+            raise RuntimeError("libgrazelle_gb300.so is not built (%s); run __graft_entry__.build()" % path)
+        _build.build()
+    lib = C.CDLL(str(path))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc: int, graph_handle=None):
+    if rc != GRZ_OK:
+        lib = load()
+        msg = lib.grz_graph_last_error(graph_handle).decode() if graph_handle else lib.grz_error_string(rc).decode()
+        raise GrzError(rc, msg)

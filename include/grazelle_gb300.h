@@ -1,0 +1,109 @@
+/*
+ * grazelle_gb300.h -- native C ABI of the GB300 Grazelle engine (libgrazelle_gb300.so).
+ *
+ * One grz_graph holds one graph resident in the HBM of one GPU.  It holds the
+ * vector-sparse edge lists, vertex indices, outdegrees and per-application
+ * vertex state.  Every call that launches work enqueues it on the graph's CUDA
+ * stream.  Calls that return data to host memory synchronise that stream.
+ * Plain C types only; pointers may be host or device memory where noted.
+ *
+ * This is the context-handle form of the interface.  The reference's own entry
+ * points (include/phases.h) are declared in grazelle_phases.h and act on the
+ * graph bound with grz_phases_bind().
+ *
+ * Reference counterparts (paths in the Grazelle tree):
+ *   grz_graph_load_pairs / _files   graph_data_read_from_file   source/graphdata.c:957-1049
+ *   grz_graph_copy_list             graph_edges_{gather,scatter}_list_block_bufs_numa  include/graphdata.h:59-65
+ *   grz_graph_copy_vertex_index     graph_vertex_{gather,scatter}_index_numa           include/graphdata.h:80-95
+ *   grz_graph_copy_outdegrees       graph_vertex_outdegrees                            include/graphdata.h:38
+ *   grz_pr_init                     execution_initialize_vertex_prop_pr                source/execution_pr.c:85-88
+ *   grz_pr_iterate                  execution_impl_pr's loop                           source/execution_pr.c:92-168
+ *   grz_cc_run                      execution_impl_cc                                  source/execution_cc.c:94-268
+ *   grz_bfs_run                     execution_impl_bfs                                 source/execution_bfs.c:120-276
+ *   grz_read_props                  graph_vertex_props                                 include/graphdata.h:32
+ */
+#ifndef GRAZELLE_GB300_H
+#define GRAZELLE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define GRZ_OK 0
+#define GRZ_ERR_ARG -1        /* bad argument */
+#define GRZ_ERR_CUDA -2       /* CUDA runtime error (no GPU, launch failure, ...) */
+#define GRZ_ERR_NOMEM -3      /* device allocation failed */
+#define GRZ_ERR_UNSORTED -4   /* an edge list is not grouped by its shared vertex in ascending order */
+#define GRZ_ERR_RANGE -5      /* vertex ID >= V, or a size beyond the 32-bit device ID limit */
+#define GRZ_ERR_STATE -6      /* call out of order (e.g. iterate before init) */
+#define GRZ_ERR_IO -7         /* file missing, truncated or inconsistent with its header */
+#define GRZ_ERR_TIMEOUT -8    /* a bounded device-side wait gave up */
+
+/* application selectors (compile-time ALGORITHM in the reference, Makefile:179-223) */
+#define GRZ_APP_PAGERANK 0
+#define GRZ_APP_CONNECTED_COMPONENTS 1
+#define GRZ_APP_BREADTH_FIRST_SEARCH 2
+
+/* list selectors */
+#define GRZ_LIST_PULL 0   /* in-edge (gather) list: shared vertex = destination */
+#define GRZ_LIST_PUSH 1   /* out-edge (scatter) list: shared vertex = source */
+
+typedef struct grz_graph grz_graph;
+
+typedef struct grz_graph_info_t {
+    uint64_t num_vertices;
+    uint64_t num_edges;
+    uint64_t pull_vectors;          /* graph_edges_gather_list_vector_count */
+    uint64_t push_vectors;          /* graph_edges_scatter_list_vector_count */
+    uint64_t pull_index_start, pull_index_end;   /* graph_vertex_gather_index_{start,end}_numa[0] */
+    uint64_t push_index_start, push_index_end;
+    const void* pull_list_device;   /* device address of the 256-bit pull vectors */
+    const void* push_list_device;
+    uint64_t device_bytes;          /* HBM held by this graph */
+} grz_graph_info_t;
+
+const char* grz_error_string(int code);
+const char* grz_graph_last_error(const grz_graph* g);
+
+/* stream: a cudaStream_t to run on, or NULL to create a private non-blocking stream */
+int grz_graph_create(grz_graph** out, int device, void* stream);
+int grz_graph_set_stream(grz_graph* g, void* stream);
+void grz_graph_destroy(grz_graph* g);
+int grz_sync(grz_graph* g);
+
+/* Loads a graph from its two edge lists in Grazelle's file order: `pull_pairs` grouped by
+ * destination, `push_pairs` grouped by source, each E interleaved (src, dst) uint64 pairs.
+ * Host or device pointers.  push_pairs may be NULL (pull engine only).  Builds the
+ * vector-sparse lists, vertex indices and outdegrees on the device. */
+int grz_graph_load_pairs(grz_graph* g, uint64_t num_vertices, uint64_t num_edges,
+                         const uint64_t* pull_pairs, const uint64_t* push_pairs);
+/* Reads `<base>-pull` and `<base>-push` (README.md "Datasets"); push is optional. */
+int grz_graph_load_files(grz_graph* g, const char* base);
+
+int grz_graph_get_info(const grz_graph* g, grz_graph_info_t* out);
+/* copies the reference-format 256-bit vectors (4 uint64 each) to host memory */
+int grz_graph_copy_list(grz_graph* g, int list, uint64_t* host_vectors, uint64_t capacity_vectors);
+/* copies the vertex index (V + 64 uint64) */
+int grz_graph_copy_vertex_index(grz_graph* g, int list, uint64_t* host_index, uint64_t capacity);
+int grz_graph_copy_outdegrees(grz_graph* g, double* host_outdeg, uint64_t capacity);
+
+/* PageRank (FP64 props; exact fixed-point accumulation).  damping 0.875 reproduces the
+ * reference's hard-coded constant (source/constants.asm:75-79). */
+int grz_pr_init(grz_graph* g, double damping);
+/* enqueues `iterations` fused edge-pull + vertex iterations (one kernel each) */
+int grz_pr_iterate(grz_graph* g, uint32_t iterations);
+/* PageRank props as the reference stores them (rank / outdegree'), V doubles to host */
+int grz_read_props(grz_graph* g, double* host_props, uint64_t capacity);
+
+/* timing helper: milliseconds of `iterations` fused PageRank iterations measured with CUDA
+ * events on the graph's stream (state advances) */
+int grz_pr_time_iterations(grz_graph* g, uint32_t iterations, float* ms_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

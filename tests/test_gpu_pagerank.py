@@ -1,0 +1,167 @@
+"""GPU layout builder and PageRank against the reference's golden outputs and the CPU oracle.
+
+Tolerance: PageRank props must be within 1e-12 relative L1 of the reference
+(FP64; the reference itself differs by up to ~1e-14 between thread counts).
+Layout arrays must be bit-identical.
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+PR_TOL = 1e-12
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def gpu_graph(g):
+    from grazelle.engine import Graph
+    G = Graph(0)
+    G.load_pairs(g.num_vertices, g.pull_order().pairs(), g.push_order().pairs())
+    return G
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_device_layout_bit_identical(name):
+    rec, g = load_golden(name)
+    with gpu_graph(g) as G:
+        from grazelle import native
+        pl = G.list_vectors(native.LIST_PULL)
+        sl = G.list_vectors(native.LIST_PUSH)
+        assert sha(pl) == str(rec["pull_list_sha"])
+        assert sha(sl) == str(rec["push_list_sha"])
+        assert sha(G.vertex_index(native.LIST_PULL)) == str(rec["pull_index_sha"])
+        assert sha(G.vertex_index(native.LIST_PUSH)) == str(rec["push_index_sha"])
+        np.testing.assert_array_equal(G.outdegrees(), rec["outdeg"])
+        info = G.info()
+        assert info.pull_vectors == int(rec["pull_nvec"])
+        assert info.push_vectors == int(rec["push_nvec"])
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_pagerank_matches_reference(name):
+    rec, g = load_golden(name)
+    with gpu_graph(g) as G:
+        p = G.pagerank(16, damping=0.875)
+    assert O.relative_l1(p, rec["pr_n1"]) < PR_TOL
+    assert O.relative_l1(p, rec["pr_n4"]) < PR_TOL
+
+
+def test_pagerank_damping_085_against_oracle():
+    from grazelle import graphgen as gg
+    g = gg.rmat(14, seed=3)
+    L = O.layout(g.num_vertices, g.pull_order().pairs(), g.push_order().pairs())
+    ref = O.pr_pull(L, 16, damping=0.85)
+    with gpu_graph(g) as G:
+        p = G.pagerank(16, damping=0.85)
+    assert O.relative_l1(p, ref) < PR_TOL
+
+
+@pytest.mark.parametrize("scale", [16, 18])
+def test_pagerank_rmat_against_oracle(scale):
+    from grazelle import graphgen as gg
+    g = gg.rmat(scale, seed=scale)
+    L = O.layout(g.num_vertices, g.pull_order().pairs(), g.push_order().pairs())
+    ref = O.pr_pull(L, 16, damping=0.875, units=256)
+    with gpu_graph(g) as G:
+        np.testing.assert_array_equal(G.outdegrees(), L.outdeg)
+        p = G.pagerank(16)
+        p2 = G.pagerank(16)
+    assert O.relative_l1(p, ref) < PR_TOL
+    # exact fixed-point accumulation: repeated runs are bit-identical
+    np.testing.assert_array_equal(p.view(np.uint64), p2.view(np.uint64))
+
+
+def test_pagerank_phase_api_equals_fused():
+    """The reference-named phase entry points compose to exactly the fused iteration."""
+    import ctypes as C
+    from grazelle import graphgen as gg, native
+    g = gg.rmat(15, seed=9)
+    with gpu_graph(g) as G:
+        fused = G.pagerank(8)
+        lib = G.lib
+        G.pr_init(0.875)
+        native.check(lib.grz_phases_bind(G.h, native.APP_PAGERANK))
+        info = G.info()
+        rb = np.zeros(8, dtype=np.uint64)
+        mb = np.zeros(32 * 4, dtype=np.uint64)
+        mb[0::4] = np.uint64(0xFFFFFFFFFFFFFFFF)  # unused merge-buffer entries (graphdata.c:1060-1065)
+        acc_host = np.zeros(g.num_vertices + 8)
+        for _ in range(8):
+            lib.phase_op_reset_global_accum()
+            lib.perform_edge_pull_phase_pr(C.c_void_p(info.pull_list_device), info.pull_vectors)
+            lib.edge_pull_op_merge_with_merge_buffer(C.c_void_p(mb.ctypes.data), 32, C.c_void_p(acc_host.ctypes.data))
+            lib.phase_op_write_global_accum_to_buf(C.c_void_p(rb.ctypes.data))
+            lib.perform_vertex_phase_pr(0, g.num_vertices, C.c_void_p(rb.ctypes.data))
+        assert lib.grz_phases_last_status() == 0
+        phased = G.props()
+    np.testing.assert_array_equal(phased.view(np.uint64), fused.view(np.uint64))
+
+
+def test_pagerank_push_equals_pull():
+    import ctypes as C
+    from grazelle import graphgen as gg, native
+    g = gg.rmat(14, seed=4)
+    with gpu_graph(g) as G:
+        pull = G.pagerank(6)
+        lib = G.lib
+        G.pr_init(0.875)
+        native.check(lib.grz_phases_bind(G.h, native.APP_PAGERANK))
+        info = G.info()
+        rb = np.zeros(8, dtype=np.uint64)
+        for _ in range(6):
+            lib.phase_op_reset_global_accum()
+            lib.perform_edge_push_phase_pr(C.c_void_p(info.push_list_device), info.push_vectors)
+            lib.phase_op_write_global_accum_to_buf(C.c_void_p(rb.ctypes.data))
+            lib.perform_vertex_phase_pr(0, g.num_vertices, C.c_void_p(rb.ctypes.data))
+        assert lib.grz_phases_last_status() == 0
+        push = G.props()
+    np.testing.assert_array_equal(push.view(np.uint64), pull.view(np.uint64))
+
+
+def test_pagerank_scale20_properties():
+    """Full benchmark size (R-MAT scale 20): rank mass and agreement with the oracle."""
+    from grazelle import graphgen as gg
+    g = gg.rmat(20, seed=1)
+    L = O.layout(g.num_vertices, g.pull_order().pairs(), g.push_order().pairs())
+    ref = O.pr_pull(L, 16, damping=0.875, units=256, threads=0, multithreaded=True)
+    with gpu_graph(g) as G:
+        p = G.pagerank(16)
+    assert O.relative_l1(p, ref) < PR_TOL
+    od = np.where(L.outdeg == 0, float(g.num_vertices), L.outdeg)
+    assert abs((p * od).sum() - 1.0) < 1e-9
+
+
+def test_bad_inputs_rejected():
+    from grazelle import graphgen as gg, native
+    from grazelle.engine import Graph
+    g = gg.rmat(10, seed=1)
+    pull = g.pull_order().pairs()
+    with Graph(0) as G:
+        with pytest.raises(native.GrzError) as ei:
+            G.load_pairs(g.num_vertices, g.push_order().pairs())  # src-sorted passed as pull
+        assert ei.value.code == -4
+        bad = pull.copy()
+        bad[1] = np.uint64(g.num_vertices + 5)
+        with pytest.raises(native.GrzError) as ei:
+            G.load_pairs(g.num_vertices, bad)
+        assert ei.value.code in (-4, -5)
+        with pytest.raises(native.GrzError) as ei:
+            G.pr_iterate(1)
+        assert ei.value.code == -6
+
+
+def test_empty_graph():
+    from grazelle.engine import Graph
+    with Graph(0) as G:
+        G.load_pairs(100, np.zeros(0, dtype=np.uint64), np.zeros(0, dtype=np.uint64))
+        assert G.info().pull_vectors == 1
+        p = G.pagerank(4)
+    # every vertex is dangling: prop = rank / V with rank = 1/V in every iteration
+    np.testing.assert_allclose(p, np.full(100, 1.0 / 100 / 100), rtol=1e-12)

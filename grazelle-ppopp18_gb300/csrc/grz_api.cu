@@ -58,7 +58,6 @@ static void free_list(grz_list* L)
     cudaFree(L->nbr);
     cudaFree(L->shared);
     cudaFree(L->rowptr);
-    cudaFree(L->tile_coord);
     memset(L, 0, sizeof(*L));
 }
 
@@ -66,11 +65,10 @@ static void free_graph_data(grz_graph* g)
 {
     free_list(&g->pull);
     free_list(&g->push);
-    void* ptrs[] = { g->outdeg, g->degree, g->inv_deg, g->pr_fx[0], g->pr_fx[1], g->pr_sum, g->pr_split_acc,
-                     g->pr_split_cnt, g->prop, g->accum, g->glob, g->vote, g->scratch };
+    void* ptrs[] = { g->outdeg, g->degree, g->inv_deg, g->pr_fx[0], g->pr_fx[1], g->pr_sum, g->pr_K, g->pr_rowacc, g->prop, g->accum, g->glob, g->vote, g->scratch };
     for (void* p : ptrs) cudaFree(p);
     g->outdeg = nullptr; g->degree = nullptr; g->inv_deg = nullptr;
-    g->pr_fx[0] = g->pr_fx[1] = nullptr; g->pr_sum = nullptr; g->pr_split_acc = nullptr; g->pr_split_cnt = nullptr;
+    g->pr_fx[0] = g->pr_fx[1] = nullptr; g->pr_sum = nullptr; g->pr_K = nullptr; g->pr_rowacc = nullptr;
     g->prop = nullptr; g->accum = nullptr; g->glob = nullptr; g->vote = nullptr; g->scratch = nullptr;
     g->scratch_bytes = 0;
     g->V = g->E = 0;
@@ -136,11 +134,74 @@ extern "C" int grz_graph_set_stream(grz_graph* g, void* stream)
     return GRZ_OK;
 }
 
+// ---------------------------------------------------------------------------------------------
+// kernel profiling
+
+void grz_prof_begin(grz_graph* g, int kind)
+{
+    grz_prof* p = g->prof;
+    if (!p || !p->on || p->n >= GRZ_PROF_MAX) return;
+    if (p->n >= p->created) {
+        cudaEventCreate(&p->ev[p->n][0]);
+        cudaEventCreate(&p->ev[p->n][1]);
+        p->created = p->n + 1;
+    }
+    p->kind[p->n] = kind;
+    cudaEventRecord(p->ev[p->n][0], g->stream);
+}
+
+void grz_prof_end(grz_graph* g)
+{
+    grz_prof* p = g->prof;
+    if (!p || !p->on || p->n >= GRZ_PROF_MAX) return;
+    cudaEventRecord(p->ev[p->n][1], g->stream);
+    p->n++;
+}
+
+extern "C" int grz_profile_enable(grz_graph* g, int on)
+{
+    if (!g) return GRZ_ERR_ARG;
+    if (!g->prof) {
+        g->prof = (grz_prof*)calloc(1, sizeof(grz_prof));
+        if (!g->prof) return GRZ_ERR_NOMEM;
+    }
+    g->prof->on = on;
+    g->prof->n = 0;
+    return GRZ_OK;
+}
+
+extern "C" int grz_profile_read(grz_graph* g, int* kinds, float* ms, int capacity)
+{
+    if (!g || (capacity > 0 && (!kinds || !ms))) return GRZ_ERR_ARG;
+    grz_prof* p = g->prof;
+    if (!p) return 0;
+    GRZ_CK(g, cudaStreamSynchronize(g->stream));
+    const int n = p->n < capacity ? p->n : capacity;
+    for (int i = 0; i < n; ++i) {
+        kinds[i] = p->kind[i];
+        ms[i] = 0.0f;
+        cudaEventElapsedTime(&ms[i], p->ev[i][0], p->ev[i][1]);
+    }
+    p->n = 0;
+    return n;
+}
+
+extern "C" const char* grz_profile_kind_name(int kind)
+{
+    static const char* names[] = { "none", "pr_gather", "pr_apply", "pr_push", "pr_vertex", "cc_pull", "cc_push",
+                                   "bfs_pull", "bfs_push", "frontier", "vertex", "iteration", "mlp", "batch" };
+    return (kind > 0 && kind < GRZ_PROF_KINDS) ? names[kind] : "none";
+}
+
 extern "C" void grz_graph_destroy(grz_graph* g)
 {
     if (!g) return;
     cudaSetDevice(g->device);
     cudaStreamSynchronize(g->stream);
+    if (g->prof) {
+        for (int i = 0; i < g->prof->created; ++i) { cudaEventDestroy(g->prof->ev[i][0]); cudaEventDestroy(g->prof->ev[i][1]); }
+        free(g->prof);
+    }
     free_graph_data(g);
     if (g->own_stream) cudaStreamDestroy(g->stream);
     free(g);
@@ -199,12 +260,12 @@ extern "C" int grz_graph_load_pairs(grz_graph* g, uint64_t V, uint64_t E, const 
         cudaError_t e;
         if ((e = cudaMalloc((void**)&g->prop, sizeof(double) * (V + 8))) != cudaSuccess) rc = grz_cuda_check(g, e, "props");
         else if ((e = cudaMalloc((void**)&g->accum, sizeof(double) * (V + 8))) != cudaSuccess) rc = grz_cuda_check(g, e, "accum");
-        else if ((e = cudaMalloc((void**)&g->glob, sizeof(u128))) != cudaSuccess) rc = grz_cuda_check(g, e, "glob");
+        else if ((e = cudaMalloc((void**)&g->glob, sizeof(u128) * GRZ_SUM_SLOTS)) != cudaSuccess) rc = grz_cuda_check(g, e, "glob");
         else if ((e = cudaMalloc((void**)&g->vote, sizeof(unsigned long long))) != cudaSuccess) rc = grz_cuda_check(g, e, "vote");
         else {
             cudaMemsetAsync(g->prop, 0, sizeof(double) * (V + 8), st);
             cudaMemsetAsync(g->accum, 0, sizeof(double) * (V + 8), st);
-            cudaMemsetAsync(g->glob, 0, sizeof(u128), st);
+            cudaMemsetAsync(g->glob, 0, sizeof(u128) * GRZ_SUM_SLOTS, st);
             cudaMemsetAsync(g->vote, 0, sizeof(unsigned long long), st);
             rc = grz_cuda_check(g, cudaStreamSynchronize(st), "state init");
         }

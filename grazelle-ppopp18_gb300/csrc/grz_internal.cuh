@@ -49,8 +49,12 @@ __host__ __device__ __forceinline__ u128 u128_zero() { u128 r; r.lo = 0; r.hi = 
 __host__ __device__ __forceinline__ u128 u128_add(u128 a, u128 b)
 {
     u128 r;
+#ifdef __CUDA_ARCH__
+    asm("add.cc.u64 %0, %2, %4;\n\taddc.u64 %1, %3, %5;" : "=l"(r.lo), "=l"(r.hi) : "l"(a.lo), "l"(a.hi), "l"(b.lo), "l"(b.hi));
+#else
     r.lo = a.lo + b.lo;
     r.hi = a.hi + b.hi + (r.lo < a.lo ? 1ull : 0ull);
+#endif
     return r;
 }
 
@@ -144,6 +148,15 @@ __device__ __forceinline__ void u128_atomic_add(u128* dst, u128 v)
     if (v.hi | carry) atomicAdd(&dst->hi, v.hi + carry);
 }
 
+// Exact sums that every block adds into are spread over GRZ_SUM_SLOTS slots (block mod slots):
+// thousands of atomics to one address would serialise on one L2 slice.
+#define GRZ_SUM_SLOTS 64
+
+__device__ __forceinline__ void u128_slot_add(u128* slots, u128 v)
+{
+    if (v.lo | v.hi) u128_atomic_add(slots + (blockIdx.x & (GRZ_SUM_SLOTS - 1)), v);
+}
+
 __device__ __forceinline__ u128 u128_shfl_down(u128 v, int off)
 {
     u128 r;
@@ -164,11 +177,9 @@ struct grz_list {
     uint4* nbr;             // uint4[nvec]
     uint32_t* shared;       // uint32[nvec]
     uint32_t* rowptr;       // uint32[V+1]
-    // merge-path tiles of the PageRank pull kernel: tile t starts at merge item t*items
-    uint32_t ntiles;
-    uint32_t tile_items;
-    uint2* tile_coord;      // (row, vector) at each tile start, ntiles+1 entries
 };
+
+struct grz_prof;
 
 struct grz_graph {
     int device;
@@ -182,10 +193,10 @@ struct grz_graph {
     // PageRank state
     u128* pr_fx[2];
     int pr_cur;           // which pr_fx holds the current props
-    u128* pr_sum;         // u128[3] rotating exact sums S_k
+    u128* pr_sum;         // u128[2][V/256]: per-block partials of S_k (ping-pong)
+    double* pr_K;         // per-iteration constant G*d + (1-d)/V, written by the gather kernel
     int pr_sum_cur;
-    u128* pr_split_acc;   // u128[V], partial sums of rows that cross tiles (kept zero between uses)
-    uint32_t* pr_split_cnt;
+    u128* pr_rowacc;      // u128[V+1] exact per-destination accumulators (all zero between iterations)
     double pr_damping;
     uint32_t pr_iters_done;
     double* prop;         // double[V+8]: reference-format vertex props (PR props, CC labels, BFS parents)
@@ -194,10 +205,51 @@ struct grz_graph {
     void* scratch;
     size_t scratch_bytes;
     // global accumulator of the phase API (exact)
-    u128* glob;           // u128[1] device
+    u128* glob;           // u128[GRZ_SUM_SLOTS] device
     unsigned long long* vote;  // uint64[1] device
     int app;              // 0 PR, 1 CC, 2 BFS
+    grz_prof* prof;       // kernel timing (null unless enabled)
     char err[256];
+};
+
+// record an event pair around a launch when profiling is on
+void grz_prof_begin(grz_graph* g, int kind);
+void grz_prof_end(grz_graph* g);
+
+// warp 0 of the calling block: exact sum of GRZ_SUM_SLOTS slots (result valid in lane 0)
+__device__ __forceinline__ u128 u128_warp_sum_slots(const u128* slots)
+{
+    const int lane = threadIdx.x & 31;
+    u128 s = u128_add(slots[lane], slots[lane + 32]);
+    for (int o = 16; o > 0; o >>= 1) s = u128_add(s, u128_shfl_down(s, o));
+    return s;
+}
+
+static inline u128 u128_host_sum(const u128* slots, int n)
+{
+    u128 s = u128_zero();
+    for (int i = 0; i < n; ++i) s = u128_add(s, slots[i]);
+    return s;
+}
+
+// ----------------------------------------------------------------------------------------------
+// kernel-level profiling (CUDA event pairs around launches), the GPU analogue of the reference's
+// EXPERIMENT_ITERATION_PROFILE cycle counts (source/execution_bfs.c:172-215)
+
+#define GRZ_PROF_MAX 8192
+enum grz_prof_kind {
+    GRZ_PROF_PR_GATHER = 1, GRZ_PROF_PR_APPLY, GRZ_PROF_PR_PUSH, GRZ_PROF_PR_VERTEX,
+    GRZ_PROF_CC_PULL, GRZ_PROF_CC_PUSH, GRZ_PROF_BFS_PULL, GRZ_PROF_BFS_PUSH,
+    GRZ_PROF_FRONTIER, GRZ_PROF_VERTEX, GRZ_PROF_ITERATION, GRZ_PROF_MLP, GRZ_PROF_BATCH,
+    GRZ_PROF_KINDS
+};
+
+struct grz_prof {
+    int on;
+    int n;
+    int kind[GRZ_PROF_MAX];
+    cudaEvent_t ev[GRZ_PROF_MAX][2];
+    int created;
 };
 
 // host helpers (grz_api.cu)
@@ -214,7 +266,6 @@ int grz_scratch(grz_graph* g, size_t bytes, void** out);
 // layout (grz_layout.cu)
 int grz_build_list(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t E, int shared_is_dst);
 int grz_build_outdegrees(grz_graph* g, const uint64_t* d_pull_pairs, uint64_t E);
-int grz_build_pr_tiles(grz_graph* g, grz_list* L, uint32_t tile_items);
 
 // scans (grz_scan.cu): exclusive sum of uint32 into uint32 (n < 2^32), inclusive max of uint32
 int grz_exclusive_sum_u32(grz_graph* g, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total_out_dev);

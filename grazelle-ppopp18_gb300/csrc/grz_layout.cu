@@ -162,24 +162,6 @@ __global__ void k_degree_to_double(const uint32_t* __restrict__ degree, uint64_t
     inv_deg[v] = 1.0 / (d == 0.0 ? (double)V : d);
 }
 
-// merge-path tile starts: coordinate (row, vector) of merge item t*items
-__global__ void k_tile_coords(const uint32_t* __restrict__ rowptr, uint64_t V, uint64_t nvec, uint64_t items,
-                              uint32_t ntiles, uint2* __restrict__ coord)
-{
-    const uint64_t t = (uint64_t)blockIdx.x * BT + threadIdx.x;
-    if (t > ntiles) return;
-    const uint64_t total = V + nvec;
-    uint64_t d = t * items;
-    if (d > total) d = total;
-    // rows consumed = number of i with row-end item (rowptr[i+1] + i) < d
-    uint64_t lo = 0, hi = V;
-    while (lo < hi) {
-        const uint64_t mid = (lo + hi) >> 1;
-        if ((uint64_t)rowptr[mid + 1] + mid < d) lo = mid + 1; else hi = mid;
-    }
-    coord[t] = make_uint2((uint32_t)lo, (uint32_t)(d - lo));
-}
-
 }  // namespace
 
 int grz_build_list(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t E, int shared_is_dst)
@@ -291,19 +273,5 @@ int grz_build_outdegrees(grz_graph* g, const uint64_t* d_pull_pairs, uint64_t E)
         k_degree_to_double<<<grid_blocks_for(V), BT, 0, st>>>(g->degree, V, g->outdeg, g->inv_deg);
         GRZ_CK(g, cudaGetLastError());
     }
-    return GRZ_OK;
-}
-
-int grz_build_pr_tiles(grz_graph* g, grz_list* L, uint32_t tile_items)
-{
-    const uint64_t total = g->V + L->nvec;
-    const uint64_t nt = (total + tile_items - 1) / tile_items;
-    if (nt >= 0x7fffffffull) return grz_set_error(g, GRZ_ERR_RANGE, "too many tiles");
-    if (L->tile_coord) { cudaFree(L->tile_coord); L->tile_coord = nullptr; }
-    L->ntiles = (uint32_t)nt;
-    L->tile_items = tile_items;
-    GRZ_CK(g, cudaMalloc((void**)&L->tile_coord, sizeof(uint2) * (nt + 1)));
-    k_tile_coords<<<grid_blocks_for(nt + 1), BT, 0, g->stream>>>(L->rowptr, g->V, L->nvec, tile_items, (uint32_t)nt, L->tile_coord);
-    GRZ_CK(g, cudaGetLastError());
     return GRZ_OK;
 }

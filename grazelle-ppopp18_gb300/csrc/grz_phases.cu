@@ -10,7 +10,7 @@
 #include "grz_internal.cuh"
 #include "../../include/grazelle_phases.h"
 
-int grz_pr_edge_pull(grz_graph* g);
+int grz_pr_edge_pull(grz_graph* g, uint64_t first, uint64_t count);
 int grz_pr_vertex(grz_graph* g, uint64_t first, uint64_t count, double S);
 int grz_pr_push_phase(grz_graph* g, uint64_t first_vec, uint64_t count);
 int grz_pr_vertex_after_push(grz_graph* g, uint64_t first, uint64_t count, double S);
@@ -64,7 +64,7 @@ extern "C" void phase_op_reset_global_accum(void)
 {
     grz_graph* g = g_bound;
     if (!g) { note(GRZ_ERR_STATE); return; }
-    cudaError_t e = cudaMemsetAsync(g->glob, 0, sizeof(u128), g->stream);
+    cudaError_t e = cudaMemsetAsync(g->glob, 0, sizeof(u128) * GRZ_SUM_SLOTS, g->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(g->vote, 0, sizeof(unsigned long long), g->stream);
     note(grz_cuda_check(g, e, "reset global accum"));
 }
@@ -77,11 +77,11 @@ extern "C" void phase_op_write_global_accum_to_buf(uint64_t* reduce_buffer)
     grz_graph* g = g_bound;
     if (!g || !reduce_buffer) { note(GRZ_ERR_STATE); return; }
     if (g_app == GRZ_APP_PAGERANK) {
-        u128 s;
-        cudaError_t e = cudaMemcpyAsync(&s, g->glob, sizeof(u128), cudaMemcpyDeviceToHost, g->stream);
+        u128 slots[GRZ_SUM_SLOTS];
+        cudaError_t e = cudaMemcpyAsync(slots, g->glob, sizeof(slots), cudaMemcpyDeviceToHost, g->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
         if (e != cudaSuccess) { note(grz_cuda_check(g, e, "read global accum")); return; }
-        const double d = fx_to_double(s);
+        const double d = fx_to_double(u128_host_sum(slots, GRZ_SUM_SLOTS));
         memcpy(&reduce_buffer[0], &d, sizeof(double));
     } else {
         unsigned long long v = 0;
@@ -126,9 +126,7 @@ extern "C" void perform_edge_pull_phase_pr(const void* edge_list, const uint64_t
 {
     uint64_t first = 0;
     int rc = resolve(edge_list, count, 0, &first);
-    if (rc == GRZ_OK && (first != 0 || count != g_bound->pull.nvec))
-        rc = grz_set_error(g_bound, GRZ_ERR_ARG, "the PageRank pull phase runs on the whole in-edge list");
-    if (rc == GRZ_OK) rc = grz_pr_edge_pull(g_bound);
+    if (rc == GRZ_OK) rc = grz_pr_edge_pull(g_bound, first, count);
     note(rc);
 }
 

@@ -54,6 +54,20 @@ class Graph:
     def sync(self):
         self._ck(self.lib.grz_sync(self.h))
 
+    # ------------------------------------------------------------------ profiling
+    def profile(self, on: bool = True):
+        self._ck(self.lib.grz_profile_enable(self.h, 1 if on else 0))
+        return self
+
+    def profile_read(self, capacity: int = 8192):
+        """[(kernel kind name, milliseconds)] in launch order since the last read."""
+        kinds = (C.c_int * capacity)()
+        ms = (C.c_float * capacity)()
+        n = self.lib.grz_profile_read(self.h, kinds, ms, capacity)
+        if n < 0:
+            native.check(n, self.h)
+        return [(self.lib.grz_profile_kind_name(kinds[i]).decode(), ms[i]) for i in range(n)]
+
     # ------------------------------------------------------------------ ingest
     def load_pairs(self, num_vertices: int, pull_pairs, push_pairs=None):
         """Interleaved (src, dst) uint64 pairs in file order.  numpy arrays (host) or raw device pointers (int)."""

@@ -58,6 +58,9 @@ SIGNATURES = {
     "grz_pr_iterate": (_I, [_VP, _U32]),
     "grz_read_props": (_I, [_VP, _VP, _U64]),
     "grz_pr_time_iterations": (_I, [_VP, _U32, C.POINTER(C.c_float)]),
+    "grz_profile_enable": (_I, [_VP, _I]),
+    "grz_profile_read": (_I, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_float), _I]),
+    "grz_profile_kind_name": (C.c_char_p, [_I]),
     # grazelle_phases.h
     "grz_phases_bind": (_I, [_VP, _I]),
     "grz_phases_last_status": (_I, []),

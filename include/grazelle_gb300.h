@@ -102,6 +102,14 @@ int grz_read_props(grz_graph* g, double* host_props, uint64_t capacity);
  * events on the graph's stream (state advances) */
 int grz_pr_time_iterations(grz_graph* g, uint32_t iterations, float* ms_out);
 
+/* Kernel profiling: when enabled, every launch is bracketed by a CUDA event pair on the graph's
+ * stream (the GPU form of the reference's EXPERIMENT_ITERATION_PROFILE, source/main.c:43-55).
+ * grz_profile_read synchronises, returns up to `capacity` (kind, milliseconds) records in launch
+ * order, and clears the log. */
+int grz_profile_enable(grz_graph* g, int on);
+int grz_profile_read(grz_graph* g, int* kinds, float* ms, int capacity);
+const char* grz_profile_kind_name(int kind);
+
 #ifdef __cplusplus
 }
 #endif

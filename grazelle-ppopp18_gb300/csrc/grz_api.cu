@@ -63,13 +63,14 @@ static void free_list(grz_list* L)
 
 static void free_graph_data(grz_graph* g)
 {
+    grz_frontier_free(g);
     free_list(&g->pull);
     free_list(&g->push);
-    void* ptrs[] = { g->outdeg, g->degree, g->inv_deg, g->pr_fx[0], g->pr_fx[1], g->pr_sum, g->pr_K, g->pr_rowacc, g->prop, g->accum, g->glob, g->vote, g->scratch };
+    void* ptrs[] = { g->outdeg, g->degree, g->inv_deg, g->pr_fx[0], g->pr_fx[1], g->pr_sum, g->pr_K, g->pr_rowacc, g->prop, g->accum, g->glob, g->scratch };
     for (void* p : ptrs) cudaFree(p);
     g->outdeg = nullptr; g->degree = nullptr; g->inv_deg = nullptr;
     g->pr_fx[0] = g->pr_fx[1] = nullptr; g->pr_sum = nullptr; g->pr_K = nullptr; g->pr_rowacc = nullptr;
-    g->prop = nullptr; g->accum = nullptr; g->glob = nullptr; g->vote = nullptr; g->scratch = nullptr;
+    g->prop = nullptr; g->accum = nullptr; g->glob = nullptr; g->scratch = nullptr;
     g->scratch_bytes = 0;
     g->V = g->E = 0;
 }
@@ -95,6 +96,7 @@ extern "C" int grz_graph_create(grz_graph** out, int device, void* stream)
     if (!g) return GRZ_ERR_NOMEM;
     g->device = device;
     cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e != cudaSuccess) {
         free(g);
         cudaGetLastError();
@@ -261,12 +263,10 @@ extern "C" int grz_graph_load_pairs(grz_graph* g, uint64_t V, uint64_t E, const 
         if ((e = cudaMalloc((void**)&g->prop, sizeof(double) * (V + 8))) != cudaSuccess) rc = grz_cuda_check(g, e, "props");
         else if ((e = cudaMalloc((void**)&g->accum, sizeof(double) * (V + 8))) != cudaSuccess) rc = grz_cuda_check(g, e, "accum");
         else if ((e = cudaMalloc((void**)&g->glob, sizeof(u128) * GRZ_SUM_SLOTS)) != cudaSuccess) rc = grz_cuda_check(g, e, "glob");
-        else if ((e = cudaMalloc((void**)&g->vote, sizeof(unsigned long long))) != cudaSuccess) rc = grz_cuda_check(g, e, "vote");
         else {
             cudaMemsetAsync(g->prop, 0, sizeof(double) * (V + 8), st);
             cudaMemsetAsync(g->accum, 0, sizeof(double) * (V + 8), st);
             cudaMemsetAsync(g->glob, 0, sizeof(u128) * GRZ_SUM_SLOTS, st);
-            cudaMemsetAsync(g->vote, 0, sizeof(unsigned long long), st);
             rc = grz_cuda_check(g, cudaStreamSynchronize(st), "state init");
         }
     }
@@ -421,8 +421,93 @@ extern "C" int grz_read_props(grz_graph* g, double* host, uint64_t cap)
     if (g->app == GRZ_APP_PAGERANK && g->pr_fx[0]) {
         int rc = grz_pr_props_to_double(g);
         if (rc) return rc;
+    } else if (g->app != GRZ_APP_PAGERANK) {
+        int rc = grz_frontier_props(g);
+        if (rc) return rc;
     }
     GRZ_CK(g, cudaMemcpyAsync(host, g->prop, sizeof(double) * g->V, cudaMemcpyDeviceToHost, g->stream));
     GRZ_CK(g, cudaStreamSynchronize(g->stream));
     return GRZ_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Connected Components and BFS
+
+static int frontier_run(grz_graph* g, int app, uint32_t root, int flags, grz_run_stats_t* stats)
+{
+    if (!g) return GRZ_ERR_ARG;
+    GRZ_CK(g, cudaSetDevice(g->device));
+    g->app = app;
+    int rc = grz_frontier_init(g, app, flags, root);
+    if (rc) return rc;
+    cudaEvent_t e0, e1;
+    GRZ_CK(g, cudaEventCreate(&e0));
+    GRZ_CK(g, cudaEventCreate(&e1));
+    cudaEventRecord(e0, g->stream);
+    for (;;) {
+        int engine = -1;
+        uint64_t vote = 0;
+        rc = grz_frontier_step(g, -1, &engine, &vote);
+        if (rc <= 0) break;
+    }
+    cudaEventRecord(e1, g->stream);
+    if (rc == 0) rc = grz_cuda_check(g, cudaEventSynchronize(e1), "run");
+    if (rc == 0 && stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->iterations = g->fr.iter;
+        stats->pull_iterations = g->fr.npull;
+        stats->push_iterations = g->fr.npush;
+        cudaEventElapsedTime(&stats->ms, e0, e1);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+extern "C" int grz_cc_run(grz_graph* g, int flags, grz_run_stats_t* stats)
+{
+    return frontier_run(g, GRZ_APP_CONNECTED_COMPONENTS, 0, flags, stats);
+}
+
+extern "C" int grz_bfs_run(grz_graph* g, uint32_t root, int flags, grz_run_stats_t* stats)
+{
+    return frontier_run(g, GRZ_APP_BREADTH_FIRST_SEARCH, root, flags, stats);
+}
+
+extern "C" int grz_frontier_begin(grz_graph* g, int app, uint32_t root, int flags)
+{
+    if (!g || (app != GRZ_APP_CONNECTED_COMPONENTS && app != GRZ_APP_BREADTH_FIRST_SEARCH)) return GRZ_ERR_ARG;
+    GRZ_CK(g, cudaSetDevice(g->device));
+    g->app = app;
+    return grz_frontier_init(g, app, flags, root);
+}
+
+extern "C" int grz_frontier_next(grz_graph* g, int engine, int* engine_used, uint64_t* vote)
+{
+    if (!g) return GRZ_ERR_ARG;
+    if (!g->fr.label) return grz_set_error(g, GRZ_ERR_STATE, "grz_frontier_begin not called");
+    return grz_frontier_step(g, engine, engine_used, vote);
+}
+
+extern "C" int grz_frontier_current_vote(grz_graph* g, uint64_t* vote, int* threshold_engine)
+{
+    if (!g || !vote) return GRZ_ERR_ARG;
+    *vote = g->fr.vote_host;
+    if (threshold_engine) *threshold_engine = grz_engine_threshold(g, g->fr.vote_host);
+    return GRZ_OK;
+}
+
+extern "C" int grz_read_levels(grz_graph* g, int64_t* host, uint64_t cap)
+{
+    if (!g || !host) return GRZ_ERR_ARG;
+    if (cap < g->V) return grz_set_error(g, GRZ_ERR_ARG, "capacity below V");
+    if (!g->fr.level || g->fr.app != GRZ_APP_BREADTH_FIRST_SEARCH) return grz_set_error(g, GRZ_ERR_STATE, "no BFS result");
+    uint32_t* tmp = (uint32_t*)malloc(sizeof(uint32_t) * (g->V ? g->V : 1));
+    if (!tmp) return GRZ_ERR_NOMEM;
+    cudaError_t e = cudaMemcpyAsync(tmp, g->fr.level, sizeof(uint32_t) * g->V, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e == cudaSuccess)
+        for (uint64_t v = 0; v < g->V; ++v) host[v] = tmp[v] == 0xffffffffu ? -1 : (int64_t)tmp[v];
+    free(tmp);
+    return grz_cuda_check(g, e, "read levels");
 }

@@ -1,20 +1,589 @@
-// grz_ccbfs.cu -- Connected Components and BFS phases (placeholder until the kernels land).
+// grz_ccbfs.cu -- Connected Components and Breadth-First Search: edge-pull, edge-push on a
+// compacted frontier, vertex (frontier) phase, and the engine-switching driver loops.
+//
+// Reference semantics (paths in the Grazelle tree):
+//   CC pull   source/phase_edge_pull_cc.asm:50-392   label[d] = min(label[d], min over valid sources)
+//   CC push   source/phase_edge_push_cc.asm:51-573   for sources in HasInfo: CAS-min into label[dst]
+//   BFS pull  source/phase_edge_pull_bfs.asm:53-211  for dst in WantsInfo: parent = max HasInfo source
+//                                                    of the first vector that holds one
+//   BFS push  source/phase_edge_push_bfs.asm:53-202  for sources in HasInfo: visit dst in WantsInfo
+//   vertex    source/phase_vertex_{cc,bfs}.asm:37-46 zero HasInfo* after the pointer swap
+//   driver    source/execution_cc.c:94-268, source/execution_bfs.c:120-276
+//   vote      include/phasehelpers.inc:388-399       1 + outdeg per changed vertex
+//
+// GPU form:
+//   * Labels and parents live on the device as uint32 (IDs are below 2^32).  The reference's
+//     double props are produced only when the result is read back.  Entry V of the label
+//     array is a permanent +infinity that invalid lanes gather.
+//   * Pull: one thread per vector, a warp-segmented reduction per destination, one atomic per
+//     (warp, destination).  Labels are updated in place, as the reference's CAS loop does, so
+//     a later vector may already see a lowered label.
+//   * Push: HasInfo is compacted into a list of active sources that have out-edges.  Each block
+//     then expands 256 of them, with a block-wide scan over their vector counts, so work per
+//     thread does not depend on source degree.
+//   * Each changed vertex is counted once per iteration: the first setter of its HasInfo* bit
+//     adds 1 + outdeg to the vote.  The reference can count a destination that straddles two
+//     work units twice.  The vote only steers the engine choice.
+//   * BFS parent rules are deterministic, so parents equal the single-thread reference: pull
+//     keeps the largest HasInfo source of the lowest-indexed vector that holds one (a 64-bit
+//     atomicMin on (vector index, ~source)); push keeps the smallest HasInfo source (atomicMin).
+//     A vertex's BFS level is the iteration that visits it, so levels are exact by construction.
+#include <string.h>
+
 #include "grz_internal.cuh"
 
+namespace {
+
+constexpr int T = 256;
+constexpr uint32_t INF = 0xffffffffu;
+
+unsigned blocks_for(uint64_t n) { return (unsigned)((n + T - 1) / T); }
+
+__device__ __forceinline__ bool bit_of(const unsigned long long* bm, uint32_t v) { return (bm[v >> 6] >> (v & 63)) & 1ull; }
+
+// sets bit v; true if this call set it (it was clear)
+__device__ __forceinline__ bool bit_set_first(unsigned long long* bm, uint32_t v)
+{
+    const unsigned long long m = 1ull << (v & 63);
+    return !(atomicOr(bm + (v >> 6), m) & m);
+}
+
+__device__ __forceinline__ void vote_add(unsigned long long* vote, unsigned long long x)
+{
+    // one add per block (the callers aggregate the block first), spread over the vote slots
+    if (x) atomicAdd(vote + (blockIdx.x & (GRZ_VOTE_SLOTS - 1)) * GRZ_VOTE_STRIDE, x);
+}
+
+__device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long x, unsigned long long* red)
+{
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+    __syncthreads();
+    x = 0;
+    if (threadIdx.x < 32) {
+        x = (threadIdx.x < T / 32) ? red[threadIdx.x] : 0ull;
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    }
+    return x;
+}
+
+struct VoteCfg {
+    const uint32_t* degree;
+    int without_count, without_outdeg;
+    __device__ __forceinline__ unsigned long long of(uint32_t v) const
+    {
+        return (without_count ? 0ull : 1ull) + (without_outdeg ? 0ull : (unsigned long long)degree[v]);
+    }
+};
+
+// ---------------------------------------------------------------------------------------------
+// CC pull
+
+__global__ void __launch_bounds__(T) k_cc_pull(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv, uint64_t first,
+                                               uint64_t nvec, uint32_t V, uint32_t* __restrict__ label,
+                                               unsigned long long* __restrict__ has_next, VoteCfg vc,
+                                               unsigned long long* __restrict__ vote)
+{
+    __shared__ unsigned long long red[T / 32];
+    const uint64_t i = (uint64_t)blockIdx.x * T + threadIdx.x;
+    const uint64_t v = first + i;
+    const int lane = threadIdx.x & 31;
+    const bool live = i < nvec;
+    uint32_t key = INF, m = INF;
+    if (live) {
+        const uint4 s = __ldcs(nbr + v);
+        key = __ldcs(dstv + v);
+        // labels change in place during the phase: plain (coherent) loads, not the read-only path
+        const uint32_t a = label[min(s.x, V)], b = label[min(s.y, V)], c = label[min(s.z, V)], d = label[min(s.w, V)];
+        m = min(min(a, b), min(c, d));
+    }
+    const uint32_t prevkey = __shfl_up_sync(0xffffffffu, key, 1);
+    const uint32_t nextkey = __shfl_down_sync(0xffffffffu, key, 1);
+    const bool head = lane == 0 || key != prevkey;
+    const bool tail = lane == 31 || key != nextkey;
+    const unsigned heads = __ballot_sync(0xffffffffu, head);
+    const int segstart = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+    const int maxlen = __reduce_max_sync(0xffffffffu, (unsigned)(lane - segstart + 1));
+    for (int off = 1; off < maxlen; off <<= 1) {
+        const uint32_t o = __shfl_up_sync(0xffffffffu, m, off);
+        if (lane - off >= segstart) m = min(m, o);
+    }
+    unsigned long long my_vote = 0;
+    if (live && tail && m != INF && m < label[key]) {
+        const uint32_t old = atomicMin(label + key, m);
+        if (m < old && bit_set_first(has_next, key)) my_vote = vc.of(key);
+    }
+    my_vote = block_sum_u64(my_vote, red);
+    if (threadIdx.x == 0) vote_add(vote, my_vote);
+}
+
+// ---------------------------------------------------------------------------------------------
+// BFS pull
+
+__global__ void __launch_bounds__(T) k_bfs_pull(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv, uint64_t first,
+                                                uint64_t nvec, uint32_t V, const unsigned long long* __restrict__ has,
+                                                const unsigned long long* __restrict__ wants,
+                                                unsigned long long* __restrict__ cand, uint32_t* __restrict__ touched,
+                                                uint32_t* __restrict__ ntouched)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * T + threadIdx.x;
+    const uint64_t v = first + i;
+    if (i >= nvec) return;
+    const uint32_t key = __ldcs(dstv + v);
+    if (!bit_of(wants, key)) return;  // strong check: destination already visited
+    const uint4 s = __ldcs(nbr + v);
+    const uint32_t ids[4] = { s.x, s.y, s.z, s.w };
+    uint32_t best = 0;
+    bool any = false;
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+        const uint32_t id = ids[l];
+        if (id < V && bit_of(has, id)) {  // weak check on the source
+            best = any ? max(best, id) : id;
+            any = true;
+        }
+    }
+    if (!any) return;
+    const unsigned long long k = ((unsigned long long)v << 32) | (unsigned long long)(~best);
+    if (k < cand[key]) {
+        const unsigned long long old = atomicMin(cand + key, k);
+        if (old == ~0ull) touched[atomicAdd(ntouched, 1u)] = key;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// frontier compaction: active sources (bit set in `has`) that have out-vectors
+
+__global__ void __launch_bounds__(T) k_compact(const unsigned long long* __restrict__ has,
+                                               const unsigned long long* __restrict__ nonempty, uint64_t words,
+                                               uint32_t* __restrict__ frontier, uint32_t* __restrict__ nfrontier)
+{
+    __shared__ uint32_t warp_tot[T / 32];
+    __shared__ uint32_t base;
+    const uint64_t w = (uint64_t)blockIdx.x * T + threadIdx.x;
+    const unsigned long long bits = (w < words) ? (has[w] & nonempty[w]) : 0ull;
+    const uint32_t cnt = __popcll(bits);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (int k = 0; k < T / 32; ++k) { const uint32_t t = warp_tot[k]; warp_tot[k] = run; run += t; }
+        base = run ? atomicAdd(nfrontier, run) : 0u;
+    }
+    __syncthreads();
+    uint32_t pos = base + warp_tot[warp] + x - cnt;
+    unsigned long long b = bits;
+    while (b) {
+        const int k = __ffsll((long long)b) - 1;
+        b &= b - 1;
+        frontier[pos++] = (uint32_t)(w * 64 + (uint64_t)k);
+    }
+}
+
+// Expand the compacted frontier: block c handles frontier entries [256c, 256c+256).  A block
+// scan of their vector counts maps each of the block's vectors to its source by a binary search
+// in shared memory.  Grid-stride over chunks, so the frontier size stays on the device.
+template <bool IsBfs>
+__global__ void __launch_bounds__(T) k_push_expand(const uint32_t* __restrict__ frontier, const uint32_t* __restrict__ nfrontier,
+                                                   const uint32_t* __restrict__ rowptr, const uint4* __restrict__ nbr,
+                                                   uint32_t V, uint32_t* __restrict__ label,
+                                                   unsigned long long* __restrict__ has_next, const unsigned long long* __restrict__ wants,
+                                                   uint32_t* __restrict__ cand32, uint32_t* __restrict__ touched,
+                                                   uint32_t* __restrict__ ntouched, VoteCfg vc, unsigned long long* __restrict__ vote)
+{
+    __shared__ uint32_t src[T];
+    __shared__ uint32_t vbase[T];
+    __shared__ uint32_t off[T + 1];
+    __shared__ uint32_t warp_tot[T / 32];
+    __shared__ unsigned long long red[T / 32];
+    const uint32_t nf = *nfrontier;
+    const uint32_t nchunks = (nf + T - 1) / T;
+    unsigned long long my_vote = 0;
+    for (uint32_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const uint32_t idx = c * T + threadIdx.x;
+        uint32_t cnt = 0;
+        if (idx < nf) {
+            const uint32_t u = frontier[idx];
+            src[threadIdx.x] = u;
+            vbase[threadIdx.x] = rowptr[u];
+            cnt = rowptr[u + 1] - rowptr[u];
+        }
+        // block exclusive scan of cnt
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        uint32_t x = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_tot[warp] = x;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t run = 0;
+            for (int k = 0; k < T / 32; ++k) { const uint32_t t = warp_tot[k]; warp_tot[k] = run; run += t; }
+            off[T] = run;
+        }
+        __syncthreads();
+        off[threadIdx.x] = warp_tot[warp] + x - cnt;
+        __syncthreads();
+        const uint32_t total = off[T];
+        const int nent = (int)min((uint32_t)T, nf - c * T);
+        for (uint32_t t = threadIdx.x; t < total; t += T) {
+            int lo = 0, hi = nent - 1;  // last entry with off <= t
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (off[mid] <= t) lo = mid; else hi = mid - 1;
+            }
+            const uint32_t u = src[lo];
+            const uint4 s = __ldcs(nbr + vbase[lo] + (t - off[lo]));
+            const uint32_t ids[4] = { s.x, s.y, s.z, s.w };
+            if (IsBfs) {
+#pragma unroll
+                for (int l = 0; l < 4; ++l) {
+                    const uint32_t d = ids[l];
+                    if (d < V && bit_of(wants, d) && u < cand32[d]) {
+                        const uint32_t old = atomicMin(cand32 + d, u);
+                        if (old == INF) touched[atomicAdd(ntouched, 1u)] = d;
+                    }
+                }
+            } else {
+                const uint32_t msg = label[u];
+#pragma unroll
+                for (int l = 0; l < 4; ++l) {
+                    const uint32_t d = ids[l];
+                    if (d < V && msg < label[d]) {
+                        const uint32_t old = atomicMin(label + d, msg);
+                        if (msg < old && bit_set_first(has_next, d)) my_vote += vc.of(d);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (!IsBfs) {
+        my_vote = block_sum_u64(my_vote, red);
+        if (threadIdx.x == 0) vote_add(vote, my_vote);
+    }
+}
+
+// BFS: visit the touched destinations (pull: decode the winning (vector, source) key; push: the
+// smallest source), in one pass over the touched list
+template <bool FromPull>
+__global__ void __launch_bounds__(T) k_bfs_visit(const uint32_t* __restrict__ touched, const uint32_t* __restrict__ ntouched,
+                                                 unsigned long long* __restrict__ cand64, uint32_t* __restrict__ cand32,
+                                                 uint32_t* __restrict__ parent, uint32_t* __restrict__ level, uint32_t iter,
+                                                 unsigned long long* __restrict__ wants, unsigned long long* __restrict__ has_next,
+                                                 VoteCfg vc, unsigned long long* __restrict__ vote)
+{
+    __shared__ unsigned long long red[T / 32];
+    const uint32_t n = *ntouched;
+    unsigned long long my_vote = 0;
+    for (uint32_t i = blockIdx.x * T + threadIdx.x; i < n; i += gridDim.x * T) {
+        const uint32_t d = touched[i];
+        uint32_t p;
+        if (FromPull) {
+            p = ~(uint32_t)(cand64[d] & 0xffffffffull);
+            cand64[d] = ~0ull;
+        } else {
+            p = cand32[d];
+            cand32[d] = INF;
+        }
+        parent[d] = p;
+        level[d] = iter;
+        atomicAnd(wants + (d >> 6), ~(1ull << (d & 63)));
+        atomicOr(has_next + (d >> 6), 1ull << (d & 63));
+        my_vote += vc.of(d);
+    }
+    my_vote = block_sum_u64(my_vote, red);
+    if (threadIdx.x == 0) vote_add(vote, my_vote);
+}
+
+// ---------------------------------------------------------------------------------------------
+// init / output
+
+__global__ void k_cc_init(uint32_t* __restrict__ label, uint64_t V)
+{
+    const uint64_t v = (uint64_t)blockIdx.x * T + threadIdx.x;
+    if (v < V) label[v] = (uint32_t)v;  // execution_initialize_vertex_prop_cc: (double)id
+    if (v == V) label[v] = INF;
+}
+
+__global__ void k_bfs_init(uint32_t* __restrict__ parent, uint32_t* __restrict__ level, uint64_t V)
+{
+    const uint64_t v = (uint64_t)blockIdx.x * T + threadIdx.x;
+    if (v <= V) { parent[v] = INF; level[v] = INF; }
+}
+
+// bitmaps: `all_ones` sets bits [0, V); bits at and beyond V stay clear
+__global__ void k_bitmap_init(unsigned long long* __restrict__ bm, uint64_t words, uint64_t V, int all_ones)
+{
+    const uint64_t w = (uint64_t)blockIdx.x * T + threadIdx.x;
+    if (w >= words) return;
+    unsigned long long x = 0;
+    if (all_ones) {
+        const uint64_t lo = w * 64;
+        if (lo + 64 <= V) x = ~0ull;
+        else if (lo < V) x = (1ull << (V - lo)) - 1ull;
+    }
+    bm[w] = x;
+}
+
+// bitmap of vertices that own at least one vector in a list
+__global__ void k_nonempty(const uint32_t* __restrict__ rowptr, uint64_t V, unsigned long long* __restrict__ bm, uint64_t words)
+{
+    const uint64_t w = (uint64_t)blockIdx.x * T + threadIdx.x;
+    if (w >= words) return;
+    unsigned long long x = 0;
+    for (int k = 0; k < 64; ++k) {
+        const uint64_t v = w * 64 + (uint64_t)k;
+        if (v < V && rowptr[v + 1] > rowptr[v]) x |= 1ull << k;
+    }
+    bm[w] = x;
+}
+
+// reference-format output: CC labels as double; BFS parents as double with -1 for unvisited
+// vertices and the root (source/execution_bfs.c:113-116)
+__global__ void k_u32_to_double(const uint32_t* __restrict__ x, uint64_t V, double* __restrict__ out, int bfs)
+{
+    const uint64_t v = (uint64_t)blockIdx.x * T + threadIdx.x;
+    if (v >= V) return;
+    const uint32_t a = x[v];
+    out[v] = (bfs && a == INF) ? -1.0 : (double)a;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+// host side
+
+static uint64_t words_of(uint64_t V) { return (V >> 6) + 2; }
+
+static int ensure_frontier_state(grz_graph* g)
+{
+    if (g->fr.label) return GRZ_OK;
+    const uint64_t V = g->V, W = words_of(V);
+    grz_frontier_state& f = g->fr;
+    GRZ_CK(g, cudaMalloc((void**)&f.label, sizeof(uint32_t) * (V + 1)));
+    GRZ_CK(g, cudaMalloc((void**)&f.level, sizeof(uint32_t) * (V + 1)));
+    GRZ_CK(g, cudaMalloc((void**)&f.has, sizeof(unsigned long long) * W));
+    GRZ_CK(g, cudaMalloc((void**)&f.has_next, sizeof(unsigned long long) * W));
+    GRZ_CK(g, cudaMalloc((void**)&f.wants, sizeof(unsigned long long) * W));
+    GRZ_CK(g, cudaMalloc((void**)&f.nonempty_push, sizeof(unsigned long long) * W));
+    GRZ_CK(g, cudaMalloc((void**)&f.frontier, sizeof(uint32_t) * (V + 1)));
+    GRZ_CK(g, cudaMalloc((void**)&f.touched, sizeof(uint32_t) * (V + 1)));
+    GRZ_CK(g, cudaMalloc((void**)&f.cand64, sizeof(unsigned long long) * (V + 1)));
+    GRZ_CK(g, cudaMalloc((void**)&f.cand32, sizeof(uint32_t) * (V + 1)));
+    GRZ_CK(g, cudaMalloc((void**)&f.counters, sizeof(uint32_t) * 8));
+    GRZ_CK(g, cudaMalloc((void**)&f.vote, sizeof(unsigned long long) * GRZ_VOTE_SLOTS * GRZ_VOTE_STRIDE));
+    GRZ_CK(g, cudaMemsetAsync(f.vote, 0, sizeof(unsigned long long) * GRZ_VOTE_SLOTS * GRZ_VOTE_STRIDE, g->stream));
+    GRZ_CK(g, cudaMemsetAsync(f.cand64, 0xff, sizeof(unsigned long long) * (V + 1), g->stream));
+    GRZ_CK(g, cudaMemsetAsync(f.cand32, 0xff, sizeof(uint32_t) * (V + 1), g->stream));
+    GRZ_CK(g, cudaMemsetAsync(f.nonempty_push, 0, sizeof(unsigned long long) * W, g->stream));
+    if (g->push.rowptr && V) {
+        k_nonempty<<<blocks_for(W), T, 0, g->stream>>>(g->push.rowptr, V, f.nonempty_push, W);
+        GRZ_CK(g, cudaGetLastError());
+    }
+    return GRZ_OK;
+}
+
+static VoteCfg vote_cfg(const grz_graph* g)
+{
+    VoteCfg vc;
+    vc.degree = g->degree;
+    vc.without_count = (g->fr.flags & GRZ_FLAG_WITHOUT_COUNT) ? 1 : 0;
+    vc.without_outdeg = (g->fr.flags & GRZ_FLAG_WITHOUT_OUTDEG) ? 1 : 0;
+    return vc;
+}
+
+int grz_frontier_init(grz_graph* g, int app, int flags, uint32_t root)
+{
+    if (!g->outdeg) return grz_set_error(g, GRZ_ERR_STATE, "no graph loaded");
+    int rc = ensure_frontier_state(g);
+    if (rc) return rc;
+    const uint64_t V = g->V, W = words_of(V);
+    grz_frontier_state& f = g->fr;
+    f.app = app;
+    f.flags = flags;
+    f.root = root;
+    f.iter = 0;
+    f.npull = f.npush = 0;
+    cudaStream_t st = g->stream;
+    if (app == GRZ_APP_CONNECTED_COMPONENTS) {
+        k_cc_init<<<blocks_for(V + 1), T, 0, st>>>(f.label, V);
+        k_bitmap_init<<<blocks_for(W), T, 0, st>>>(f.has, W, V, 1);      // HasInfo = all (execution_cc.c:66-73)
+        k_bitmap_init<<<blocks_for(W), T, 0, st>>>(f.wants, W, V, 1);
+        f.vote_host = 0;
+        if (!(flags & GRZ_FLAG_WITHOUT_OUTDEG)) f.vote_host += g->E;     // execution_cc.c:106-112
+        if (!(flags & GRZ_FLAG_WITHOUT_COUNT)) f.vote_host += V;
+    } else {
+        if (root >= V) return grz_set_error(g, GRZ_ERR_ARG, "root %u >= V", root);
+        k_bfs_init<<<blocks_for(V + 1), T, 0, st>>>(f.label, f.level, V);
+        k_bitmap_init<<<blocks_for(W), T, 0, st>>>(f.has, W, V, 0);
+        k_bitmap_init<<<blocks_for(W), T, 0, st>>>(f.wants, W, V, 1);
+        const unsigned long long rbit = 1ull << (root & 63);
+        unsigned long long w0 = 0, w1 = 0;
+        GRZ_CK(g, cudaMemcpyAsync(&w1, f.wants + (root >> 6), 8, cudaMemcpyDeviceToHost, st));
+        GRZ_CK(g, cudaStreamSynchronize(st));
+        w0 = rbit;
+        w1 &= ~rbit;
+        GRZ_CK(g, cudaMemcpyAsync(f.has + (root >> 6), &w0, 8, cudaMemcpyHostToDevice, st));
+        GRZ_CK(g, cudaMemcpyAsync(f.wants + (root >> 6), &w1, 8, cudaMemcpyHostToDevice, st));
+        const uint32_t zero = 0;
+        GRZ_CK(g, cudaMemcpyAsync(f.level + root, &zero, 4, cudaMemcpyHostToDevice, st));
+        double od = 0;
+        GRZ_CK(g, cudaMemcpyAsync(&od, g->outdeg + root, 8, cudaMemcpyDeviceToHost, st));
+        GRZ_CK(g, cudaStreamSynchronize(st));
+        f.vote_host = 0;
+        if (!(flags & GRZ_FLAG_WITHOUT_OUTDEG)) f.vote_host += (uint64_t)od;  // execution_bfs.c:132-137
+        if (!(flags & GRZ_FLAG_WITHOUT_COUNT)) f.vote_host += 1;
+    }
+    GRZ_CK(g, cudaMemsetAsync(f.has_next, 0, sizeof(unsigned long long) * W, st));
+    GRZ_CK(g, cudaGetLastError());
+    return GRZ_OK;
+}
+
+// the reference's threshold engine choice (execution_bfs.c:146-168, execution_cc.c:120-142)
+int grz_engine_threshold(const grz_graph* g, uint64_t vote)
+{
+    const int flags = g->fr.flags;
+    if (flags & GRZ_FLAG_FORCE_PULL) return 1;
+    if (flags & GRZ_FLAG_FORCE_PUSH) return 0;
+    const uint64_t thr = (flags & GRZ_FLAG_WITHOUT_OUTDEG) ? g->V / 2 : g->E / 5;
+    return vote > thr ? 1 : 0;
+}
+
+// One edge phase on a vector range of the pull (pull=1) or push list.  Leaves the vote of the
+// phase in fr.vote[0] on the device.  The push engine always expands the whole compacted frontier.
+static int edge_phase(grz_graph* g, int pull, uint64_t first, uint64_t count)
+{
+    grz_frontier_state& f = g->fr;
+    const uint32_t V = (uint32_t)g->V;
+    const uint64_t W = words_of(g->V);
+    cudaStream_t st = g->stream;
+    const VoteCfg vc = vote_cfg(g);
+    const bool bfs = f.app == GRZ_APP_BREADTH_FIRST_SEARCH;
+    GRZ_CK(g, cudaMemsetAsync(f.counters, 0, sizeof(uint32_t) * 8, st));
+    if (pull) {
+        if (!g->pull.nbr) return grz_set_error(g, GRZ_ERR_STATE, "pull list not loaded");
+        if (count == 0) return GRZ_OK;
+        grz_prof_begin(g, bfs ? GRZ_PROF_BFS_PULL : GRZ_PROF_CC_PULL);
+        if (bfs) {
+            k_bfs_pull<<<blocks_for(count), T, 0, st>>>(g->pull.nbr, g->pull.shared, first, count, V, f.has, f.wants, f.cand64,
+                                                       f.touched, f.counters + 1);
+            k_bfs_visit<true><<<g->num_sms * 4, T, 0, st>>>(f.touched, f.counters + 1, f.cand64, f.cand32, f.label, f.level,
+                                                            f.iter, f.wants, f.has_next, vc, f.vote);
+        } else {
+            k_cc_pull<<<blocks_for(count), T, 0, st>>>(g->pull.nbr, g->pull.shared, first, count, V, f.label, f.has_next, vc, f.vote);
+        }
+        grz_prof_end(g);
+    } else {
+        if (!g->push.nbr) return grz_set_error(g, GRZ_ERR_STATE, "push list not loaded");
+        grz_prof_begin(g, bfs ? GRZ_PROF_BFS_PUSH : GRZ_PROF_CC_PUSH);
+        k_compact<<<blocks_for(W), T, 0, st>>>(f.has, f.nonempty_push, W, f.frontier, f.counters + 0);
+        const unsigned grid = (unsigned)g->num_sms * 8;
+        if (bfs) {
+            k_push_expand<true><<<grid, T, 0, st>>>(f.frontier, f.counters + 0, g->push.rowptr, g->push.nbr, V, f.label, f.has_next,
+                                                    f.wants, f.cand32, f.touched, f.counters + 1, vc, f.vote);
+            k_bfs_visit<false><<<g->num_sms * 4, T, 0, st>>>(f.touched, f.counters + 1, f.cand64, f.cand32, f.label, f.level,
+                                                             f.iter, f.wants, f.has_next, vc, f.vote);
+        } else {
+            k_push_expand<false><<<grid, T, 0, st>>>(f.frontier, f.counters + 0, g->push.rowptr, g->push.nbr, V, f.label, f.has_next,
+                                                     f.wants, f.cand32, f.touched, f.counters + 1, vc, f.vote);
+        }
+        grz_prof_end(g);
+    }
+    return grz_cuda_check(g, cudaGetLastError(), "edge phase");
+}
+
+// perform_vertex_phase_{cc,bfs}: HasInfo <- HasInfo*, HasInfo* <- 0 (pointer swap + clear)
+int grz_frontier_vertex_phase(grz_graph* g, uint64_t first, uint64_t count)
+{
+    (void)first;
+    (void)count;
+    grz_frontier_state& f = g->fr;
+    if (!f.label) return grz_set_error(g, GRZ_ERR_STATE, "frontier state not initialised");
+    unsigned long long* t = f.has;
+    f.has = f.has_next;
+    f.has_next = t;
+    GRZ_CK(g, cudaMemsetAsync(f.has_next, 0, sizeof(unsigned long long) * words_of(g->V), g->stream));
+    return GRZ_OK;
+}
+
+// the phases.h entry points: one edge phase with a fresh vote, counted into the iteration total
 int grz_cc_phase(grz_graph* g, int pull, uint64_t first_vec, uint64_t count)
 {
-    (void)pull; (void)first_vec; (void)count;
-    return grz_set_error(g, GRZ_ERR_STATE, "connected components not available");
+    if (!g->fr.label || g->fr.app != GRZ_APP_CONNECTED_COMPONENTS) {
+        int rc = grz_frontier_init(g, GRZ_APP_CONNECTED_COMPONENTS, 0, 0);
+        if (rc) return rc;
+    }
+    return edge_phase(g, pull, first_vec, count);
 }
 
 int grz_bfs_phase(grz_graph* g, int pull, uint64_t first_vec, uint64_t count)
 {
-    (void)pull; (void)first_vec; (void)count;
-    return grz_set_error(g, GRZ_ERR_STATE, "bfs not available");
+    if (!g->fr.label || g->fr.app != GRZ_APP_BREADTH_FIRST_SEARCH) {
+        int rc = grz_frontier_init(g, GRZ_APP_BREADTH_FIRST_SEARCH, 0, 0);
+        if (rc) return rc;
+    }
+    grz_frontier_state& f = g->fr;
+    f.iter++;  // a BFS level per edge phase; the root is level 0
+    return edge_phase(g, pull, first_vec, count);
 }
 
-int grz_frontier_vertex_phase(grz_graph* g, uint64_t first, uint64_t count)
+// Runs one iteration: engine choice from the current vote (or the caller's choice), the edge
+// phase, the vote read-back and, unless converged, the vertex phase.  Returns 1 while not
+// converged, 0 when the vote is 0, negative on error.  *engine_out = 1 pull / 0 push.
+int grz_frontier_step(grz_graph* g, int engine, int* engine_out, uint64_t* vote_out)
 {
-    (void)first; (void)count;
-    return grz_set_error(g, GRZ_ERR_STATE, "frontier vertex phase not available");
+    grz_frontier_state& f = g->fr;
+    const int pull = engine >= 0 ? engine : grz_engine_threshold(g, f.vote_host);
+    if (engine_out) *engine_out = pull;
+    GRZ_CK(g, cudaMemsetAsync(f.vote, 0, sizeof(unsigned long long) * GRZ_VOTE_SLOTS * GRZ_VOTE_STRIDE, g->stream));
+    f.iter++;
+    int rc = edge_phase(g, pull, 0, pull ? g->pull.nvec : g->push.nvec);
+    if (rc) return rc;
+    if (pull) f.npull++; else f.npush++;
+    uint64_t v = 0;
+    rc = grz_read_vote(g, &v);
+    if (rc) return rc;
+    f.vote_host = v;
+    if (vote_out) *vote_out = v;
+    if (v == 0) return 0;
+    rc = grz_frontier_vertex_phase(g, 0, g->V);
+    return rc ? rc : 1;
+}
+
+// sum of the vote slots (synchronises the stream)
+int grz_read_vote(grz_graph* g, uint64_t* out)
+{
+    unsigned long long slots[GRZ_VOTE_SLOTS * GRZ_VOTE_STRIDE];
+    GRZ_CK(g, cudaMemcpyAsync(slots, g->fr.vote, sizeof(slots), cudaMemcpyDeviceToHost, g->stream));
+    GRZ_CK(g, cudaStreamSynchronize(g->stream));
+    uint64_t v = 0;
+    for (int i = 0; i < GRZ_VOTE_SLOTS; ++i) v += slots[i * GRZ_VOTE_STRIDE];
+    *out = v;
+    return GRZ_OK;
+}
+
+int grz_frontier_props(grz_graph* g)
+{
+    grz_frontier_state& f = g->fr;
+    if (!f.label) return grz_set_error(g, GRZ_ERR_STATE, "no CC/BFS result");
+    k_u32_to_double<<<blocks_for(g->V), T, 0, g->stream>>>(f.label, g->V, g->prop, f.app == GRZ_APP_BREADTH_FIRST_SEARCH);
+    GRZ_CK(g, cudaGetLastError());
+    return GRZ_OK;
+}
+
+void grz_frontier_free(grz_graph* g)
+{
+    grz_frontier_state& f = g->fr;
+    void* ptrs[] = { f.label, f.level, f.has, f.has_next, f.wants, f.nonempty_push, f.frontier, f.touched, f.cand64, f.cand32,
+                     f.counters, f.vote };
+    for (void* p : ptrs) cudaFree(p);
+    memset(&f, 0, sizeof(f));
 }

@@ -37,6 +37,10 @@
 #define GRZ_ERR_IO -7
 #define GRZ_ERR_TIMEOUT -8
 
+#define GRZ_APP_PAGERANK 0
+#define GRZ_APP_CONNECTED_COMPONENTS 1
+#define GRZ_APP_BREADTH_FIRST_SEARCH 2
+
 // ----------------------------------------------------------------------------------------------
 // 128-bit unsigned fixed point
 
@@ -181,6 +185,35 @@ struct grz_list {
 
 struct grz_prof;
 
+// engine flags (the reference's EXPERIMENTS that change the CC/BFS driver, Makefile:59-176)
+#define GRZ_FLAG_FORCE_PULL 1       // EXPERIMENT_EDGE_FORCE_PULL
+#define GRZ_FLAG_FORCE_PUSH 2       // EXPERIMENT_EDGE_FORCE_PUSH
+#define GRZ_FLAG_WITHOUT_COUNT 4    // EXPERIMENT_THRESHOLD_WITHOUT_COUNT
+#define GRZ_FLAG_WITHOUT_OUTDEG 8   // EXPERIMENT_THRESHOLD_WITHOUT_OUTDEGREES
+
+// the vote is added into GRZ_VOTE_SLOTS counters, 128 bytes apart (block mod slots)
+#define GRZ_VOTE_SLOTS 64
+#define GRZ_VOTE_STRIDE 16
+
+// CC / BFS state (grz_ccbfs.cu)
+struct grz_frontier_state {
+    int app, flags;
+    uint32_t root, iter, npull, npush;
+    uint64_t vote_host;              // the last phase's vote (converge_vote in the reference)
+    uint32_t* label;                 // CC labels / BFS parents, uint32[V+1] (entry V = +inf)
+    uint32_t* level;                 // BFS level of each vertex
+    unsigned long long* has;         // HasInfo bitmap
+    unsigned long long* has_next;    // HasInfo*
+    unsigned long long* wants;       // WantsInfo
+    unsigned long long* nonempty_push;  // vertices with out-vectors
+    uint32_t* frontier;              // compacted active sources
+    uint32_t* touched;               // BFS destinations reached in this phase
+    unsigned long long* cand64;      // BFS pull: (vector index, ~source) per destination
+    uint32_t* cand32;                // BFS push: smallest source per destination
+    uint32_t* counters;              // [0] frontier size, [1] touched count
+    unsigned long long* vote;        // GRZ_VOTE_SLOTS * GRZ_VOTE_STRIDE
+};
+
 struct grz_graph {
     int device;
     cudaStream_t stream;
@@ -206,8 +239,9 @@ struct grz_graph {
     size_t scratch_bytes;
     // global accumulator of the phase API (exact)
     u128* glob;           // u128[GRZ_SUM_SLOTS] device
-    unsigned long long* vote;  // uint64[1] device
     int app;              // 0 PR, 1 CC, 2 BFS
+    int num_sms;
+    grz_frontier_state fr;
     grz_prof* prof;       // kernel timing (null unless enabled)
     char err[256];
 };
@@ -262,6 +296,15 @@ int grz_scratch(grz_graph* g, size_t bytes, void** out);
         cudaError_t e__ = (call);                               \
         if (e__ != cudaSuccess) return grz_cuda_check((g), e__, #call); \
     } while (0)
+
+// CC / BFS (grz_ccbfs.cu)
+int grz_frontier_init(grz_graph* g, int app, int flags, uint32_t root);
+int grz_frontier_step(grz_graph* g, int engine, int* engine_out, uint64_t* vote_out);
+int grz_frontier_vertex_phase(grz_graph* g, uint64_t first, uint64_t count);
+int grz_frontier_props(grz_graph* g);
+int grz_engine_threshold(const grz_graph* g, uint64_t vote);
+int grz_read_vote(grz_graph* g, uint64_t* out);
+void grz_frontier_free(grz_graph* g);
 
 // layout (grz_layout.cu)
 int grz_build_list(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t E, int shared_is_dst);

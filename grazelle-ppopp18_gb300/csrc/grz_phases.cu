@@ -65,7 +65,8 @@ extern "C" void phase_op_reset_global_accum(void)
     grz_graph* g = g_bound;
     if (!g) { note(GRZ_ERR_STATE); return; }
     cudaError_t e = cudaMemsetAsync(g->glob, 0, sizeof(u128) * GRZ_SUM_SLOTS, g->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(g->vote, 0, sizeof(unsigned long long), g->stream);
+    if (e == cudaSuccess && g->fr.vote)
+        e = cudaMemsetAsync(g->fr.vote, 0, sizeof(unsigned long long) * GRZ_VOTE_SLOTS * GRZ_VOTE_STRIDE, g->stream);
     note(grz_cuda_check(g, e, "reset global accum"));
 }
 
@@ -84,10 +85,12 @@ extern "C" void phase_op_write_global_accum_to_buf(uint64_t* reduce_buffer)
         const double d = fx_to_double(u128_host_sum(slots, GRZ_SUM_SLOTS));
         memcpy(&reduce_buffer[0], &d, sizeof(double));
     } else {
-        unsigned long long v = 0;
-        cudaError_t e = cudaMemcpyAsync(&v, g->vote, sizeof(v), cudaMemcpyDeviceToHost, g->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
-        if (e != cudaSuccess) { note(grz_cuda_check(g, e, "read vote")); return; }
+        uint64_t v = 0;
+        if (g->fr.vote) {
+            const int rc = grz_read_vote(g, &v);
+            if (rc) { note(rc); return; }
+        }
+        g->fr.vote_host = v;
         reduce_buffer[0] = v;
     }
 }

@@ -144,3 +144,44 @@ class Graph:
         out = np.zeros(self.V, dtype=np.float64)
         self._ck(self.lib.grz_read_props(self.h, _ptr(out), out.shape[0]))
         return out
+
+    # ------------------------------------------------------------------ CC / BFS
+    def connected_components(self, flags: int = 0, stats: bool = False):
+        """CC labels (float64, as the reference stores them) after running to convergence."""
+        st = native.RunStats()
+        self._ck(self.lib.grz_cc_run(self.h, flags, C.byref(st)))
+        lab = self.props()
+        return (lab, st) if stats else lab
+
+    def bfs(self, root: int = 0, flags: int = 0, stats: bool = False):
+        """(parents float64 with -1 for unvisited/root, levels int64 with -1 for unreached)."""
+        st = native.RunStats()
+        self._ck(self.lib.grz_bfs_run(self.h, root, flags, C.byref(st)))
+        par = self.props()
+        lv = np.zeros(self.V, dtype=np.int64)
+        self._ck(self.lib.grz_read_levels(self.h, _ptr(lv), lv.shape[0]))
+        return (par, lv, st) if stats else (par, lv)
+
+    def frontier_begin(self, app: int, root: int = 0, flags: int = 0):
+        self._ck(self.lib.grz_frontier_begin(self.h, app, root, flags))
+        return self
+
+    def frontier_next(self, engine: int = -1):
+        """One iteration; returns (running, engine used, vote)."""
+        e = C.c_int()
+        v = C.c_uint64()
+        rc = self.lib.grz_frontier_next(self.h, engine, C.byref(e), C.byref(v))
+        if rc < 0:
+            native.check(rc, self.h)
+        return rc == 1, e.value, v.value
+
+    def frontier_vote(self):
+        v = C.c_uint64()
+        e = C.c_int()
+        self._ck(self.lib.grz_frontier_current_vote(self.h, C.byref(v), C.byref(e)))
+        return v.value, e.value
+
+    def levels(self) -> np.ndarray:
+        lv = np.zeros(self.V, dtype=np.int64)
+        self._ck(self.lib.grz_read_levels(self.h, _ptr(lv), lv.shape[0]))
+        return lv

@@ -26,6 +26,14 @@ class GrzError(RuntimeError):
         self.code = code
 
 
+FORCE_PULL, FORCE_PUSH, WITHOUT_COUNT, WITHOUT_OUTDEG = 1, 2, 4, 8
+
+
+class RunStats(C.Structure):
+    _fields_ = [("iterations", C.c_uint32), ("pull_iterations", C.c_uint32), ("push_iterations", C.c_uint32),
+                ("ms", C.c_float)]
+
+
 class GraphInfo(C.Structure):
     _fields_ = [
         ("num_vertices", C.c_uint64), ("num_edges", C.c_uint64),
@@ -58,6 +66,12 @@ SIGNATURES = {
     "grz_pr_iterate": (_I, [_VP, _U32]),
     "grz_read_props": (_I, [_VP, _VP, _U64]),
     "grz_pr_time_iterations": (_I, [_VP, _U32, C.POINTER(C.c_float)]),
+    "grz_cc_run": (_I, [_VP, _I, _VP]),
+    "grz_bfs_run": (_I, [_VP, _U32, _I, _VP]),
+    "grz_read_levels": (_I, [_VP, _VP, _U64]),
+    "grz_frontier_begin": (_I, [_VP, _I, _U32, _I]),
+    "grz_frontier_next": (_I, [_VP, _I, C.POINTER(C.c_int), C.POINTER(C.c_uint64)]),
+    "grz_frontier_current_vote": (_I, [_VP, C.POINTER(C.c_uint64), C.POINTER(C.c_int)]),
     "grz_profile_enable": (_I, [_VP, _I]),
     "grz_profile_read": (_I, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_float), _I]),
     "grz_profile_kind_name": (C.c_char_p, [_I]),

@@ -102,6 +102,37 @@ int grz_read_props(grz_graph* g, double* host_props, uint64_t capacity);
  * events on the graph's stream (state advances) */
 int grz_pr_time_iterations(grz_graph* g, uint32_t iterations, float* ms_out);
 
+/* -------- Connected Components and BFS -------- */
+
+/* engine flags: the reference's compile-time EXPERIMENTS that change the CC/BFS driver
+ * (Makefile:59-176); 0 = the default threshold heuristic (execution_bfs.c:146-168) */
+#define GRZ_FLAG_FORCE_PULL 1       /* EXPERIMENT_EDGE_FORCE_PULL */
+#define GRZ_FLAG_FORCE_PUSH 2       /* EXPERIMENT_EDGE_FORCE_PUSH */
+#define GRZ_FLAG_WITHOUT_COUNT 4    /* EXPERIMENT_THRESHOLD_WITHOUT_COUNT */
+#define GRZ_FLAG_WITHOUT_OUTDEG 8   /* EXPERIMENT_THRESHOLD_WITHOUT_OUTDEGREES */
+
+typedef struct grz_run_stats_t {
+    uint32_t iterations;        /* total_iterations_executed */
+    uint32_t pull_iterations;   /* total_iterations_used_gather */
+    uint32_t push_iterations;   /* total_iterations_used_scatter */
+    float ms;                   /* device time of the run (CUDA events) */
+} grz_run_stats_t;
+
+/* Connected Components to convergence (execution_impl_cc); labels via grz_read_props */
+int grz_cc_run(grz_graph* g, int flags, grz_run_stats_t* stats);
+/* BFS from `root` (the reference fixes root 0, source/execution_bfs.c:28); parents via
+ * grz_read_props (-1 = unvisited or root), levels via grz_read_levels */
+int grz_bfs_run(grz_graph* g, uint32_t root, int flags, grz_run_stats_t* stats);
+int grz_read_levels(grz_graph* g, int64_t* host_levels, uint64_t capacity);
+
+/* Step-wise driver for callers that choose the engine themselves (the learned switch):
+ * begin, then call next until it returns 0 (converged); engine 1 = pull, 0 = push, -1 = the
+ * threshold heuristic.  Returns 1 while running, 0 when the vote reached 0, < 0 on error. */
+int grz_frontier_begin(grz_graph* g, int app, uint32_t root, int flags);
+int grz_frontier_next(grz_graph* g, int engine, int* engine_used, uint64_t* vote);
+/* the vote that decides the next iteration and the heuristic's engine for it */
+int grz_frontier_current_vote(grz_graph* g, uint64_t* vote, int* threshold_engine);
+
 /* Kernel profiling: when enabled, every launch is bracketed by a CUDA event pair on the graph's
  * stream (the GPU form of the reference's EXPERIMENT_ITERATION_PROFILE, source/main.c:43-55).
  * grz_profile_read synchronises, returns up to `capacity` (kind, milliseconds) records in launch

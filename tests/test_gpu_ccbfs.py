@@ -1,0 +1,146 @@
+"""GPU Connected Components and BFS against the reference's golden outputs and the CPU oracle.
+
+CC labels must be bit-exact whichever engine runs.  BFS levels must be
+bit-exact, and the parents must form a legal BFS tree.  The GPU's BFS parent
+rules are deterministic and its vote counts each visited vertex once.  So it
+also reproduces the single-thread reference's parents, engine sequence and
+iteration counts exactly.  The tests check that too.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+CC_VARIANTS = [("cc", 0), ("cc_twc", O.WITHOUT_COUNT), ("cc_pull", O.FORCE_PULL), ("cc_push", O.FORCE_PUSH)]
+BFS_VARIANTS = [("bfs", 0), ("bfs_twc", O.WITHOUT_COUNT), ("bfs_pull", O.FORCE_PULL), ("bfs_push", O.FORCE_PUSH)]
+
+
+def gpu_graph(g):
+    from grazelle.engine import Graph
+    G = Graph(0)
+    G.load_pairs(g.num_vertices, g.pull_order().pairs(), g.push_order().pairs())
+    return G
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_cc_labels_match_reference(name):
+    rec, g = load_golden(name)
+    with gpu_graph(g) as G:
+        for variant, flags in CC_VARIANTS:
+            lab, st = G.connected_components(flags, stats=True)
+            np.testing.assert_array_equal(lab, rec[variant + "_labels"], err_msg=variant)
+            assert st.iterations == st.pull_iterations + st.push_iterations
+            if flags == O.FORCE_PULL:
+                assert st.push_iterations == 0
+            if flags == O.FORCE_PUSH:
+                assert st.pull_iterations == 0
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_bfs_matches_single_thread_reference(name):
+    rec, g = load_golden(name)
+    push = g.push_order().pairs()
+    ref_lv = O.bfs_levels(push, g.num_vertices, 0)
+    with gpu_graph(g) as G:
+        for variant, flags in BFS_VARIANTS:
+            par, lv, st = G.bfs(0, flags, stats=True)
+            np.testing.assert_array_equal(lv, ref_lv, err_msg=variant)
+            assert O.bfs_check_tree(push, g.num_vertices, 0, lv, par.astype(np.int64)) == 0, variant
+            np.testing.assert_array_equal(par, rec[variant + "_parents"], err_msg=variant)
+            np.testing.assert_array_equal([st.iterations, st.pull_iterations, st.push_iterations],
+                                          rec[variant + "_iters"], err_msg=variant)
+
+
+@pytest.mark.parametrize("scale", [16, 18])
+def test_cc_bfs_rmat_against_oracle(scale):
+    from grazelle import graphgen as gg
+    g = gg.rmat(scale, seed=100 + scale)
+    pull, push = g.pull_order().pairs(), g.push_order().pairs()
+    L = O.layout(g.num_vertices, pull, push)
+    with gpu_graph(g) as G:
+        lab = G.connected_components()
+        np.testing.assert_array_equal(lab, O.cc(L)[0])
+        ref_par, ref_it, _ = O.bfs(L)
+        par, lv, st = G.bfs(0, stats=True)
+        np.testing.assert_array_equal(lv, O.bfs_levels(push, g.num_vertices, 0))
+        np.testing.assert_array_equal(par, ref_par)
+        assert st.iterations == ref_it[0]
+
+
+def test_cc_symmetric_graph_components():
+    """On a symmetrised graph the labels are the minimum vertex ID of each weak component."""
+    from grazelle import graphgen as gg
+    g = gg.symmetrize(gg.rmat(15, seed=42))
+    with gpu_graph(g) as G:
+        lab = G.connected_components()
+    # union-find reference
+    parent = np.arange(g.num_vertices)
+
+    def find(x):
+        while parent[x] != x:
+            parent[x] = parent[parent[x]]
+            x = parent[x]
+        return x
+    for s, d in zip(g.src.tolist(), g.dst.tolist()):
+        a, b = find(s), find(d)
+        if a != b:
+            parent[max(a, b)] = min(a, b)
+    comp_min = np.array([find(v) for v in range(g.num_vertices)], dtype=np.float64)
+    np.testing.assert_array_equal(lab, comp_min)
+
+
+def test_bfs_other_roots_equal_relabelled_reference():
+    """A root other than 0 gives the same levels as the reference run on the root<->0 relabelled graph."""
+    from grazelle import graphgen as gg
+    g = gg.rmat(14, seed=5)
+    deg = g.out_degrees()
+    roots = [int(r) for r in np.nonzero(deg)[0][:4]]
+    with gpu_graph(g) as G:
+        for r in roots:
+            par, lv = G.bfs(r)
+            np.testing.assert_array_equal(lv, O.bfs_levels(g.push_order().pairs(), g.num_vertices, r))
+            assert O.bfs_check_tree(g.push_order().pairs(), g.num_vertices, r, lv, par.astype(np.int64)) == 0
+            # same levels as the relabelled graph seen from vertex 0, mapped back
+            h = gg.relabel_swap(g, r)
+            lv0 = O.bfs_levels(h.push_order().pairs(), h.num_vertices, 0)
+            perm = np.arange(g.num_vertices)
+            perm[[0, r]] = perm[[r, 0]]
+            np.testing.assert_array_equal(lv, lv0[perm])
+
+
+def test_phase_api_cc_and_bfs_drivers():
+    """The reference's CC/BFS driver loops (execution_cc.c:94-268, execution_bfs.c:120-276) over the phases.h calls."""
+    from grazelle import graphgen as gg, native
+    g = gg.rmat(13, seed=8)
+    L = O.layout(g.num_vertices, g.pull_order().pairs(), g.push_order().pairs())
+    with gpu_graph(g) as G:
+        lib = G.lib
+        info = G.info()
+        rb = np.zeros(8, dtype=np.uint64)
+        rbp = C.c_void_p(rb.ctypes.data)
+        for app, ref in ((native.APP_CONNECTED_COMPONENTS, O.cc(L)[0]), (native.APP_BREADTH_FIRST_SEARCH, O.bfs(L)[0])):
+            native.check(lib.grz_phases_bind(G.h, app))
+            native.check(lib.grz_frontier_begin(G.h, app, 0, 0))
+            vote, _ = G.frontier_vote()
+            E = info.num_edges
+            pull_phase = lib.perform_edge_pull_phase_cc if app == 1 else lib.perform_edge_pull_phase_bfs
+            push_phase = lib.perform_edge_push_phase_cc if app == 1 else lib.perform_edge_push_phase_bfs
+            vertex_phase = lib.perform_vertex_phase_cc if app == 1 else lib.perform_vertex_phase_bfs
+            for _ in range(10000):
+                lib.phase_op_reset_global_accum()
+                if vote > E // 5:
+                    pull_phase(C.c_void_p(info.pull_list_device), info.pull_vectors)
+                else:
+                    push_phase(C.c_void_p(info.push_list_device), info.push_vectors)
+                lib.phase_op_write_global_accum_to_buf(rbp)
+                vote = lib.phase_op_combine_global_var_from_buf(rbp)
+                if vote == 0:
+                    break
+                vertex_phase(0, info.num_vertices, None)
+            assert lib.grz_phases_last_status() == 0
+            np.testing.assert_array_equal(G.props(), ref)

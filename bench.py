@@ -1,0 +1,446 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 Grazelle engine: one JSON line per run.
+
+Default workload: Connected Components, the configuration the metric is
+quoted on.  The graph is a symmetrised R-MAT of scale 24 (edge factor 16,
+a/b/c/d = .57/.19/.19/.05, seeded), run to convergence with the reference's
+threshold engine switch.  One step is one full CC run.
+
+  value     GTEPS = E x iterations / device time, graph resident in HBM (the reference's
+            "Effective Processing Rate", source/main.c:129)
+  e2e       the same metric through the C ABI from pinned HOST edge lists.  Each step does
+            the H2D copy of both lists, builds the vector-sparse layout on the device, runs CC
+            and reads the labels back (D2H).
+  roofline  the dominant kernel's algorithmic bytes per launch over its mean CUDA-event
+            duration, against the measured HBM copy peak
+  apps      PageRank (R-MAT scale 20, 16 pull iterations) and BFS on the same graph
+  cpu_baseline  the reference's algorithm on the host cores: the reference binary where it
+            runs (x86-64 AVX2), else the OpenMP restatement in oracle/
+
+`--impl reference` times only the CPU implementation, on all host threads.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference]
+                       [--workload cc|pr|bfs] [--scale S]
+Multi-GPU (torchrun): independent replicas, one graph per GPU ("replicas only"): nothing in
+the path exchanges data between GPUs.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+sys.path.insert(0, str(REPO / "grazelle-ppopp18_gb300"))
+
+import numpy as np  # noqa: E402
+
+FALLBACK_HBM_GBS = 6800.0
+DEFAULT_SCALE = {"cc": 24, "pr": 20, "bfs": 24}
+
+
+# ---------------------------------------------------------------------------------------------- helpers
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_hbm():
+    p = REPO / "MEASURED_PEAKS.json"
+    try:
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def profile_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if one exists."""
+    p = REPO / "profiles" / "traffic.json"
+    try:
+        d = json.loads(p.read_text())
+        return d.get(workload, {}).get(kernel)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples every 200 ms while the timed region runs."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if parts[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_graph(workload: str, scale: int, seed: int = 1):
+    from grazelle import graphgen as gg
+    g = gg.rmat(scale, 16, seed=seed, symmetric=workload in ("cc", "bfs"))
+    push = g.push_order().pairs()
+    pull = g.pull_order().pairs()
+    return g, pull, push
+
+
+def pick_roots(g, n: int, seed: int = 7):
+    deg = g.out_degrees()
+    cand = np.nonzero(deg)[0]
+    rng = np.random.default_rng(seed)
+    return [int(x) for x in rng.choice(cand, size=min(n, cand.shape[0]), replace=False)]
+
+
+# ---------------------------------------------------------------------------------------------- native arm
+
+class Timer:
+    """CUDA events on the graph's (torch) stream."""
+
+    def __init__(self, torch, stream):
+        self.torch = torch
+        self.stream = stream
+
+    def __enter__(self):
+        self.e0 = self.torch.cuda.Event(enable_timing=True)
+        self.e1 = self.torch.cuda.Event(enable_timing=True)
+        self.torch.cuda.synchronize()
+        self.e0.record(self.stream)
+        return self
+
+    def __exit__(self, *exc):
+        self.e1.record(self.stream)
+        self.torch.cuda.synchronize()
+        self.ms = self.e0.elapsed_time(self.e1)
+
+
+def kernel_stats(records):
+    agg = {}
+    for k, ms in records:
+        agg.setdefault(k, []).append(ms)
+    return {k: {"n": len(v), "mean_ms": sum(v) / len(v), "total_ms": sum(v)} for k, v in agg.items()}
+
+
+def run_native(a):
+    import torch
+
+    from grazelle.engine import Graph
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    stream = torch.cuda.Stream()
+    wl = a.workload
+    scale = a.scale or DEFAULT_SCALE[wl]
+    t0 = time.time()
+    g, pull, push = make_graph(wl, scale, a.seed)
+    V, E = g.num_vertices, g.num_edges
+    log("graph: %s scale %d V=%d E=%d (%.1fs)" % (wl, scale, V, E, time.time() - t0))
+    pin_pull = torch.from_numpy(pull.view(np.int64)).pin_memory()
+    pin_push = torch.from_numpy(push.view(np.int64)).pin_memory()
+    G = Graph(local, stream=stream.cuda_stream)
+    G.load_pointers(V, E, pin_pull.data_ptr(), pin_push.data_ptr())
+    hbm, hbm_kind = measured_hbm()
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # one step of the workload, graph resident; returns (teps units, iterations)
+    roots = pick_roots(g, 8) if wl == "bfs" else []
+
+    def step(i):
+        if wl == "cc":
+            _, st = G.connected_components(stats=True)
+            return E * st.iterations, st.iterations
+        if wl == "pr":
+            G.pr_init(0.875).pr_iterate(16)
+            G.sync()
+            return E * 16, 16
+        root = roots[i % len(roots)]
+        par, lv, st = G.bfs(root, stats=True)
+        reached = lv >= 0
+        return int(g.out_degrees()[reached].sum()), st.iterations
+
+    for i in range(a.warmup):
+        step(i)
+    barrier()
+    G.profile(True)
+    l0 = G.launch_count()
+    units = 0
+    iters = 0
+    with ClockSampler(local) as clk:
+        with Timer(torch, stream) as tm:
+            for i in range(a.steps):
+                u, it = step(i)
+                units += u
+                iters += it
+    launches = G.launch_count() - l0
+    recs = G.profile_read()
+    G.profile(False)
+    ms = max_over_ranks(tm.ms)
+    value = world * units / (ms * 1e-3) / 1e9
+    ks = kernel_stats(recs)
+    dominant = max(ks.items(), key=lambda kv: kv[1]["total_ms"])[0] if ks else None
+
+    # algorithmic bytes per launch of the dominant kernel (8E + 16V for a pull pass; V/4 more for
+    # the two CC bitmaps)
+    alg = {"pr_gather": 8 * E + 16 * V, "cc_pull": 8 * E + 16 * V + V // 4, "bfs_pull": 8 * E + 16 * V + V // 4}
+    roof = None
+    if dominant:
+        mean_s = ks[dominant]["mean_ms"] * 1e-3
+        if dominant in alg:
+            achieved = alg[dominant] / mean_s / 1e9
+            roof = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": hbm, "peak_kind": hbm_kind,
+                    "unit": "GB/s", "frac": round(achieved / hbm, 4), "algorithmic_bytes": alg[dominant],
+                    "mean_launch_ms": round(ks[dominant]["mean_ms"], 4),
+                    "traffic": profile_traffic(dominant, "%s%d" % (wl, scale))}
+
+    # end to end through the C ABI from pinned host buffers
+    e2e_units = 0
+    d2h = np.zeros(V, dtype=np.float64)
+    for i in range(max(1, min(2, a.warmup))):
+        G.load_pointers(V, E, pin_pull.data_ptr(), pin_push.data_ptr())
+        step(i)
+    barrier()
+    with Timer(torch, stream) as te:
+        for i in range(a.steps):
+            G.load_pointers(V, E, pin_pull.data_ptr(), pin_push.data_ptr())
+            u, _ = step(i)
+            e2e_units += u
+            G.lib.grz_read_props(G.h, d2h.ctypes.data, V)
+    e2e_ms = max_over_ranks(te.ms)
+    e2e = {"value": round(world * e2e_units / (e2e_ms * 1e-3) / 1e9, 3), "unit": "GTEPS",
+           "h2d_bytes_per_step": int(pull.nbytes + push.nbytes), "d2h_bytes_per_step": int(d2h.nbytes),
+           "ms_per_step": round(e2e_ms / a.steps, 3)}
+
+    apps = {}
+    if rank == 0 and not a.no_apps and wl == "cc":
+        apps = extra_apps(a, G, g, torch, stream, hbm, hbm_kind)
+    cpu = None
+    if rank == 0 and not a.no_cpu:
+        cpu = cpu_baseline(wl, g, pull, push, scale, sample=True)
+    if dist:
+        dist.barrier()
+    if rank != 0:
+        return
+    line = {
+        "metric": "GTEPS (%s, E x iterations / time)" % {"cc": "connected components", "pr": "pagerank pull", "bfs": "bfs"}[wl],
+        "value": round(value, 3), "unit": "GTEPS", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": round(ms / a.steps, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": {"cc": "u32", "pr": "u128 fixed point + f64", "bfs": "u32"}[wl], "data": "synthetic (seeded R-MAT)",
+        "config": {"workload": "%s-rmat%d%s" % (wl, scale, "-sym" if wl != "pr" else ""), "scale": scale, "edge_factor": 16,
+                   "rmat_abcd": [0.57, 0.19, 0.19, 0.05], "seed": a.seed, "V": V, "E": E,
+                   "engine": "threshold heuristic (E/5)" if wl != "pr" else "pull", "iterations_per_step": iters / a.steps,
+                   "l2": "inputs larger than L2 (%.1f GB of edge vectors)" % (G.info().pull_vectors * 20 / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": roof, "kernels": {k: {"n": v["n"], "mean_us": round(v["mean_ms"] * 1e3, 2)} for k, v in ks.items()},
+        "e2e": e2e, "gpu_launches": int(launches), "clocks": clk.summary(), "cpu_baseline": cpu, "apps": apps,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def extra_apps(a, G_cc, g_cc, torch, stream, hbm, hbm_kind):
+    """PageRank on R-MAT 20 (16 pull iterations) and BFS from 8 roots on the CC graph."""
+    from grazelle.engine import Graph
+    out = {}
+    # BFS on the CC graph
+    roots = pick_roots(g_cc, 8)
+    deg = g_cc.out_degrees()
+    for r in roots[:2]:
+        G_cc.bfs(r)
+    G_cc.profile(True)
+    teps = 0
+    dev_ms = 0.0
+    iters = []
+    for r in roots:
+        _, lv, st = G_cc.bfs(r, stats=True)  # st.ms: device time of the run (CUDA events); readback excluded
+        teps += int(deg[lv >= 0].sum())
+        dev_ms += st.ms
+        iters.append((st.iterations, st.pull_iterations, st.push_iterations))
+    recs = kernel_stats(G_cc.profile_read())
+    G_cc.profile(False)
+    out["bfs"] = {"workload": "bfs-rmat%d-sym, %d roots" % (int(np.log2(g_cc.num_vertices)), len(roots)),
+                  "gteps": round(teps / (dev_ms * 1e-3) / 1e9, 3), "ms_per_root": round(dev_ms / len(roots), 3),
+                  "iterations_pull_push": iters,
+                  "kernels_us": {k: round(v["mean_ms"] * 1e3, 2) for k, v in recs.items()}}
+    # PageRank
+    g, pull, push = make_graph("pr", 20, a.seed)
+    V, E = g.num_vertices, g.num_edges
+    with Graph(torch.cuda.current_device(), stream=stream.cuda_stream) as G:
+        G.load_pairs(V, pull, push)
+        G.pr_init(0.875).pr_iterate(16)
+        G.profile(True)
+        with Timer(torch, stream) as tp:
+            for _ in range(max(1, a.steps // 2)):
+                G.pr_init(0.875).pr_iterate(16)
+        ks = kernel_stats(G.profile_read())
+        G.profile(False)
+        n = max(1, a.steps // 2)
+        alg = 8 * E + 16 * V
+        gm = ks.get("pr_gather", {}).get("mean_ms", 0)
+        it_ms = tp.ms / (16 * n)
+        out["pagerank"] = {"workload": "pr-rmat20, 16 iterations, d=0.875", "gteps": round(E * 16 * n / (tp.ms * 1e-3) / 1e9, 3),
+                           "us_per_iteration": round(it_ms * 1e3, 2),
+                           "roofline_iteration": {"achieved": round(alg / (it_ms * 1e-3) / 1e9, 1), "peak": hbm,
+                                                  "peak_kind": hbm_kind, "frac": round(alg / (it_ms * 1e-3) / 1e9 / hbm, 4),
+                                                  "algorithmic_bytes": alg},
+                           "kernels_us": {k: round(v["mean_ms"] * 1e3, 2) for k, v in ks.items()},
+                           "gather_roofline_frac": round(alg / (gm * 1e-3) / 1e9 / hbm, 4) if gm else None}
+    return out
+
+
+# ---------------------------------------------------------------------------------------------- CPU
+
+def cpu_baseline(wl, g, pull, push, scale, sample=True, threads=0, steps=1):
+    """The reference's algorithm on the host cores.  The reference binary runs only on x86-64
+    with AVX2, so this uses oracle/'s OpenMP restatement with the same work-unit scheme;
+    `kind` says which."""
+    from oracle import oracle as O
+    t0 = time.time()
+    L = O.layout(g.num_vertices, pull, push)
+    build_s = time.time() - t0
+    cores = os.cpu_count() or 1
+    vals = []
+    n_used = 0
+    it_total = 0
+    for _ in range(steps):
+        t = time.time()
+        if wl == "pr":
+            iters = 4 if sample else 16
+            O.pr_pull(L, iters, 0.875, units=32 * cores, threads=threads, multithreaded=True)
+            units = L.E * iters
+            it_total = iters
+        elif wl == "cc":
+            lab, it, n_used = O.frontier_mt(L, 1, 0, threads=threads)
+            units = L.E * int(it[0])
+            it_total = int(it[0])
+        else:
+            par, it, n_used = O.frontier_mt(L, 2, 0, threads=threads)
+            reached = par >= 0
+            reached[0] = True
+            units = int(L.outdeg[reached].sum())
+            it_total = int(it[0])
+        dt = time.time() - t
+        vals.append(units / dt / 1e9)
+    return {"value": round(max(vals), 4), "unit": "GTEPS", "cores": threads or cores, "kind": "port",
+            "sample": "%s on the same graph, %d iteration(s) per run, best of %d, OpenMP restatement with the "
+                      "reference's work units (oracle/grz_oracle.c); layout build %.1fs not timed" % (
+                          {"pr": "PageRank pull", "cc": "CC to convergence", "bfs": "BFS from root 0"}[wl], it_total,
+                          steps, build_s)}
+
+
+def run_reference(a):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    wl = a.workload
+    scale = a.scale or DEFAULT_SCALE[wl]
+    g, pull, push = make_graph(wl, scale, a.seed)
+    for _ in range(a.warmup):
+        pass  # the CPU run has no warm-up state beyond the layout, which is built once
+    res = cpu_baseline(wl, g, pull, push, scale, sample=False, steps=max(1, a.steps))
+    line = {
+        "impl": "reference", "metric": "GTEPS (%s, E x iterations / time)" % {"cc": "connected components", "pr": "pagerank pull",
+                                                                               "bfs": "bfs"}[wl],
+        "value": res["value"], "unit": "GTEPS", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded R-MAT)",
+        "config": {"workload": "%s-rmat%d%s" % (wl, scale, "-sym" if wl != "pr" else ""), "scale": scale, "edge_factor": 16,
+                   "seed": a.seed, "V": g.num_vertices, "E": g.num_edges},
+        "cpu_baseline": res, "e2e": {"value": res["value"], "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["native", "reference"], default="native")
+    ap.add_argument("--workload", choices=["cc", "pr", "bfs"], default="cc")
+    ap.add_argument("--scale", type=int, default=0)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--no-apps", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    a = ap.parse_args()
+    if a.warmup < 3:
+        log("warm-up raised to 3 steps (timing rule)")
+        a.warmup = 3
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_native(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -511,3 +511,29 @@ extern "C" int grz_read_levels(grz_graph* g, int64_t* host, uint64_t cap)
     free(tmp);
     return grz_cuda_check(g, e, "read levels");
 }
+
+extern "C" unsigned long long grz_launch_count(const grz_graph* g) { return g ? g->nlaunch : 0ull; }
+
+// ---------------------------------------------------------------------------------------------
+// host-side diagnostics of the 4.124 fixed-point arithmetic the PageRank kernels use
+
+extern "C" int grz_fixed_point_roundtrip(double x, double* out)
+{
+    if (!out || !(x >= 0.0) || !(x < 16.0)) return GRZ_ERR_ARG;
+    *out = fx_to_double(fx_from_double(x));
+    return GRZ_OK;
+}
+
+extern "C" int grz_fixed_point_sum(const double* xs, uint64_t n, double* out)
+{
+    if (!out || (n && !xs)) return GRZ_ERR_ARG;
+    u128 s = u128_zero();
+    for (uint64_t i = 0; i < n; ++i) {
+        if (!(xs[i] >= 0.0) || !(xs[i] < 16.0)) return GRZ_ERR_RANGE;
+        const u128 t = u128_add(s, fx_from_double(xs[i]));
+        if (t.hi < s.hi) return GRZ_ERR_RANGE;  // carry out of bit 127: the sum reached 16
+        s = t;
+    }
+    *out = fx_to_double(s);
+    return GRZ_OK;
+}

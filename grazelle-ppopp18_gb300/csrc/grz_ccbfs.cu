@@ -385,7 +385,7 @@ static int ensure_frontier_state(grz_graph* g)
     GRZ_CK(g, cudaMemsetAsync(f.cand32, 0xff, sizeof(uint32_t) * (V + 1), g->stream));
     GRZ_CK(g, cudaMemsetAsync(f.nonempty_push, 0, sizeof(unsigned long long) * W, g->stream));
     if (g->push.rowptr && V) {
-        k_nonempty<<<blocks_for(W), T, 0, g->stream>>>(g->push.rowptr, V, f.nonempty_push, W);
+        k_nonempty<<<blocks_for(W), T, 0, g->stream>>>(g->push.rowptr, V, f.nonempty_push, W); GRZ_COUNT_LAUNCH(g);
         GRZ_CK(g, cudaGetLastError());
     }
     return GRZ_OK;
@@ -414,17 +414,17 @@ int grz_frontier_init(grz_graph* g, int app, int flags, uint32_t root)
     f.npull = f.npush = 0;
     cudaStream_t st = g->stream;
     if (app == GRZ_APP_CONNECTED_COMPONENTS) {
-        k_cc_init<<<blocks_for(V + 1), T, 0, st>>>(f.label, V);
-        k_bitmap_init<<<blocks_for(W), T, 0, st>>>(f.has, W, V, 1);      // HasInfo = all (execution_cc.c:66-73)
-        k_bitmap_init<<<blocks_for(W), T, 0, st>>>(f.wants, W, V, 1);
+        k_cc_init<<<blocks_for(V + 1), T, 0, st>>>(f.label, V); GRZ_COUNT_LAUNCH(g);
+        k_bitmap_init<<<blocks_for(W), T, 0, st>>>(f.has, W, V, 1); GRZ_COUNT_LAUNCH(g);      // HasInfo = all (execution_cc.c:66-73)
+        k_bitmap_init<<<blocks_for(W), T, 0, st>>>(f.wants, W, V, 1); GRZ_COUNT_LAUNCH(g);
         f.vote_host = 0;
         if (!(flags & GRZ_FLAG_WITHOUT_OUTDEG)) f.vote_host += g->E;     // execution_cc.c:106-112
         if (!(flags & GRZ_FLAG_WITHOUT_COUNT)) f.vote_host += V;
     } else {
         if (root >= V) return grz_set_error(g, GRZ_ERR_ARG, "root %u >= V", root);
-        k_bfs_init<<<blocks_for(V + 1), T, 0, st>>>(f.label, f.level, V);
-        k_bitmap_init<<<blocks_for(W), T, 0, st>>>(f.has, W, V, 0);
-        k_bitmap_init<<<blocks_for(W), T, 0, st>>>(f.wants, W, V, 1);
+        k_bfs_init<<<blocks_for(V + 1), T, 0, st>>>(f.label, f.level, V); GRZ_COUNT_LAUNCH(g);
+        k_bitmap_init<<<blocks_for(W), T, 0, st>>>(f.has, W, V, 0); GRZ_COUNT_LAUNCH(g);
+        k_bitmap_init<<<blocks_for(W), T, 0, st>>>(f.wants, W, V, 1); GRZ_COUNT_LAUNCH(g);
         const unsigned long long rbit = 1ull << (root & 63);
         unsigned long long w0 = 0, w1 = 0;
         GRZ_CK(g, cudaMemcpyAsync(&w1, f.wants + (root >> 6), 8, cudaMemcpyDeviceToHost, st));
@@ -474,26 +474,26 @@ static int edge_phase(grz_graph* g, int pull, uint64_t first, uint64_t count)
         grz_prof_begin(g, bfs ? GRZ_PROF_BFS_PULL : GRZ_PROF_CC_PULL);
         if (bfs) {
             k_bfs_pull<<<blocks_for(count), T, 0, st>>>(g->pull.nbr, g->pull.shared, first, count, V, f.has, f.wants, f.cand64,
-                                                       f.touched, f.counters + 1);
+                                                       f.touched, f.counters + 1); GRZ_COUNT_LAUNCH(g);
             k_bfs_visit<true><<<g->num_sms * 4, T, 0, st>>>(f.touched, f.counters + 1, f.cand64, f.cand32, f.label, f.level,
-                                                            f.iter, f.wants, f.has_next, vc, f.vote);
+                                                            f.iter, f.wants, f.has_next, vc, f.vote); GRZ_COUNT_LAUNCH(g);
         } else {
-            k_cc_pull<<<blocks_for(count), T, 0, st>>>(g->pull.nbr, g->pull.shared, first, count, V, f.label, f.has_next, vc, f.vote);
+            k_cc_pull<<<blocks_for(count), T, 0, st>>>(g->pull.nbr, g->pull.shared, first, count, V, f.label, f.has_next, vc, f.vote); GRZ_COUNT_LAUNCH(g);
         }
         grz_prof_end(g);
     } else {
         if (!g->push.nbr) return grz_set_error(g, GRZ_ERR_STATE, "push list not loaded");
         grz_prof_begin(g, bfs ? GRZ_PROF_BFS_PUSH : GRZ_PROF_CC_PUSH);
-        k_compact<<<blocks_for(W), T, 0, st>>>(f.has, f.nonempty_push, W, f.frontier, f.counters + 0);
+        k_compact<<<blocks_for(W), T, 0, st>>>(f.has, f.nonempty_push, W, f.frontier, f.counters + 0); GRZ_COUNT_LAUNCH(g);
         const unsigned grid = (unsigned)g->num_sms * 8;
         if (bfs) {
             k_push_expand<true><<<grid, T, 0, st>>>(f.frontier, f.counters + 0, g->push.rowptr, g->push.nbr, V, f.label, f.has_next,
-                                                    f.wants, f.cand32, f.touched, f.counters + 1, vc, f.vote);
+                                                    f.wants, f.cand32, f.touched, f.counters + 1, vc, f.vote); GRZ_COUNT_LAUNCH(g);
             k_bfs_visit<false><<<g->num_sms * 4, T, 0, st>>>(f.touched, f.counters + 1, f.cand64, f.cand32, f.label, f.level,
-                                                             f.iter, f.wants, f.has_next, vc, f.vote);
+                                                             f.iter, f.wants, f.has_next, vc, f.vote); GRZ_COUNT_LAUNCH(g);
         } else {
             k_push_expand<false><<<grid, T, 0, st>>>(f.frontier, f.counters + 0, g->push.rowptr, g->push.nbr, V, f.label, f.has_next,
-                                                     f.wants, f.cand32, f.touched, f.counters + 1, vc, f.vote);
+                                                     f.wants, f.cand32, f.touched, f.counters + 1, vc, f.vote); GRZ_COUNT_LAUNCH(g);
         }
         grz_prof_end(g);
     }
@@ -574,7 +574,7 @@ int grz_frontier_props(grz_graph* g)
 {
     grz_frontier_state& f = g->fr;
     if (!f.label) return grz_set_error(g, GRZ_ERR_STATE, "no CC/BFS result");
-    k_u32_to_double<<<blocks_for(g->V), T, 0, g->stream>>>(f.label, g->V, g->prop, f.app == GRZ_APP_BREADTH_FIRST_SEARCH);
+    k_u32_to_double<<<blocks_for(g->V), T, 0, g->stream>>>(f.label, g->V, g->prop, f.app == GRZ_APP_BREADTH_FIRST_SEARCH); GRZ_COUNT_LAUNCH(g);
     GRZ_CK(g, cudaGetLastError());
     return GRZ_OK;
 }

@@ -81,3 +81,76 @@ uint64_t grz_unique_no_loops(uint64_t* keys, uint64_t n)
     }
     return w;
 }
+
+/* Parallel LSD radix sort of 64-bit keys (16-bit digits, OpenMP): per-thread histograms of a
+ * contiguous chunk, a column-major prefix over (digit, thread), then a stable scatter. */
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+#include <stdlib.h>
+
+void grz_radix_sort_u64_mt(uint64_t* keys, uint64_t* tmp, uint64_t n, int bits)
+{
+#ifdef _OPENMP
+    const int nt = omp_get_max_threads();
+#else
+    const int nt = 1;
+#endif
+    const int B = 65536;
+    uint64_t* hist = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)B * (size_t)nt);
+    uint64_t* a = keys;
+    uint64_t* b = tmp;
+    for (int shift = 0; shift < bits; shift += 16) {
+#pragma omp parallel num_threads(nt)
+        {
+#ifdef _OPENMP
+            const int t = omp_get_thread_num();
+#else
+            const int t = 0;
+#endif
+            uint64_t* h = hist + (size_t)t * B;
+            for (int i = 0; i < B; ++i) h[i] = 0;
+            const uint64_t lo = n * (uint64_t)t / (uint64_t)nt, hi = n * (uint64_t)(t + 1) / (uint64_t)nt;
+            for (uint64_t i = lo; i < hi; ++i) h[(a[i] >> shift) & 0xffff]++;
+#pragma omp barrier
+#pragma omp single
+            {
+                uint64_t run = 0;
+                for (int d = 0; d < B; ++d)
+                    for (int k = 0; k < nt; ++k) {
+                        const uint64_t c = hist[(size_t)k * B + d];
+                        hist[(size_t)k * B + d] = run;
+                        run += c;
+                    }
+            }
+            for (uint64_t i = lo; i < hi; ++i) b[h[(a[i] >> shift) & 0xffff]++] = a[i];
+        }
+        uint64_t* t2 = a; a = b; b = t2;
+    }
+    if (a != keys) {
+#pragma omp parallel for
+        for (int64_t i = 0; i < (int64_t)n; ++i) keys[i] = a[i];
+    }
+    free(hist);
+}
+
+/* key = (src << 32) | dst for both directions of each draw (symmetrised raw edge keys) */
+void grz_sym_keys(const uint64_t* src, const uint64_t* dst, uint64_t m, uint64_t* keys)
+{
+#pragma omp parallel for
+    for (int64_t i = 0; i < (int64_t)m; ++i) {
+        keys[2 * i] = (src[i] << 32) | dst[i];
+        keys[2 * i + 1] = (dst[i] << 32) | src[i];
+    }
+}
+
+/* interleaved (src, dst) pairs from sorted keys; swap = 1 if the key is (dst << 32) | src */
+void grz_keys_to_pairs(const uint64_t* keys, uint64_t n, int swap, uint64_t* pairs)
+{
+#pragma omp parallel for
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        const uint64_t hi = keys[i] >> 32, lo = keys[i] & 0xffffffffull;
+        pairs[2 * i] = swap ? lo : hi;
+        pairs[2 * i + 1] = swap ? hi : lo;
+    }
+}

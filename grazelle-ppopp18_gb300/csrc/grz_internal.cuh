@@ -243,8 +243,11 @@ struct grz_graph {
     int num_sms;
     grz_frontier_state fr;
     grz_prof* prof;       // kernel timing (null unless enabled)
+    unsigned long long nlaunch;  // kernels launched by this graph (grz_launch_count)
     char err[256];
 };
+
+#define GRZ_COUNT_LAUNCH(g) ((g)->nlaunch++)
 
 // record an event pair around a launch when profiling is on
 void grz_prof_begin(grz_graph* g, int kind);

@@ -183,7 +183,7 @@ int grz_build_list(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t 
         LCK(cudaMallocAsync((void**)&head, sizeof(uint32_t) * E, st));
         LCK(cudaMallocAsync((void**)&vstart, sizeof(uint32_t) * E, st));
         LCK(cudaMallocAsync((void**)&vexcl, sizeof(uint32_t) * (E + 1), st));
-        k_edge_heads<<<grid_blocks_for(E), BT, 0, st>>>(d_pairs, E, V, shared_is_dst, head, flags);
+        k_edge_heads<<<grid_blocks_for(E), BT, 0, st>>>(d_pairs, E, V, shared_is_dst, head, flags); GRZ_COUNT_LAUNCH(g);
         LCK(cudaGetLastError());
         LCK(cudaMemcpyAsync(flags_h, flags, sizeof(flags_h), cudaMemcpyDeviceToHost, st));
         LCK(cudaStreamSynchronize(st));
@@ -191,7 +191,7 @@ int grz_build_list(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t 
         if (flags_h[1]) { rc = grz_set_error(g, GRZ_ERR_RANGE, "%s list holds a vertex ID >= V (%llu)", shared_is_dst ? "pull" : "push", (unsigned long long)V); goto done; }
         rc = grz_inclusive_max_u32(g, head, head, E);  // head[] now holds each edge's run start
         if (rc) goto done;
-        k_vector_starts<<<grid_blocks_for(E), BT, 0, st>>>(head, E, vstart);
+        k_vector_starts<<<grid_blocks_for(E), BT, 0, st>>>(head, E, vstart); GRZ_COUNT_LAUNCH(g);
         LCK(cudaGetLastError());
         rc = grz_exclusive_sum_u32(g, vstart, vexcl, E, vexcl + E);
         if (rc) goto done;
@@ -211,17 +211,17 @@ int grz_build_list(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t 
         LCK(cudaMallocAsync((void**)&l1, sizeof(uint32_t) * nvec * 3, st));
         l2 = l1 + nvec;
         l3 = l2 + nvec;
-        k_vector_first<<<grid_blocks_for(E), BT, 0, st>>>(vstart, vexcl, E, vfirst);
+        k_vector_first<<<grid_blocks_for(E), BT, 0, st>>>(vstart, vexcl, E, vfirst); GRZ_COUNT_LAUNCH(g);
         LCK(cudaGetLastError());
-        k_vector_fill<<<grid_blocks_for(nvec), BT, 0, st>>>(d_pairs, shared_is_dst, vfirst, nvec, E, L->shared, L->nbr, l1, l2, l3);
+        k_vector_fill<<<grid_blocks_for(nvec), BT, 0, st>>>(d_pairs, shared_is_dst, vfirst, nvec, E, L->shared, L->nbr, l1, l2, l3); GRZ_COUNT_LAUNCH(g);
         LCK(cudaGetLastError());
         if ((rc = grz_inclusive_max_u32(g, l1, l1, nvec))) goto done;
         if ((rc = grz_inclusive_max_u32(g, l2, l2, nvec))) goto done;
         if ((rc = grz_inclusive_max_u32(g, l3, l3, nvec))) goto done;
-        k_vector_encode<<<grid_blocks_for(nvec), BT, 0, st>>>(L->shared, L->nbr, l1, l2, l3, nvec, L->vs);
+        k_vector_encode<<<grid_blocks_for(nvec), BT, 0, st>>>(L->shared, L->nbr, l1, l2, l3, nvec, L->vs); GRZ_COUNT_LAUNCH(g);
         LCK(cudaGetLastError());
     } else {
-        k_empty_list<<<1, 1, 0, st>>>(L->vs, L->nbr, L->shared);
+        k_empty_list<<<1, 1, 0, st>>>(L->vs, L->nbr, L->shared); GRZ_COUNT_LAUNCH(g);
         LCK(cudaGetLastError());
     }
     {
@@ -231,14 +231,14 @@ int grz_build_list(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t 
         LCK(cudaStreamSynchronize(st));
         L->vindex_start = fs;
         L->vindex_end = ls;
-        k_vindex_fill<<<grid_blocks_for(vi_count), BT, 0, st>>>(L->vindex, vi_count, fs, ls);
+        k_vindex_fill<<<grid_blocks_for(vi_count), BT, 0, st>>>(L->vindex, vi_count, fs, ls); GRZ_COUNT_LAUNCH(g);
         LCK(cudaGetLastError());
-        k_vindex_heads<<<grid_blocks_for(nvec), BT, 0, st>>>(L->shared, nvec, L->vindex);
+        k_vindex_heads<<<grid_blocks_for(nvec), BT, 0, st>>>(L->shared, nvec, L->vindex); GRZ_COUNT_LAUNCH(g);
         LCK(cudaGetLastError());
         uint32_t* cnt = nullptr;
         LCK(cudaMallocAsync((void**)&cnt, sizeof(uint32_t) * (V + 1), st));
         LCK(cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * (V + 1), st));
-        k_row_counts<<<grid_blocks_for(nvec), BT, 0, st>>>(L->shared, nvec, L->vindex, cnt);
+        k_row_counts<<<grid_blocks_for(nvec), BT, 0, st>>>(L->shared, nvec, L->vindex, cnt); GRZ_COUNT_LAUNCH(g);
         LCK(cudaGetLastError());
         rc = grz_exclusive_sum_u32(g, cnt, L->rowptr, V + 1, nullptr);
         cudaFreeAsync(cnt, st);
@@ -266,11 +266,11 @@ int grz_build_outdegrees(grz_graph* g, const uint64_t* d_pull_pairs, uint64_t E)
     GRZ_CK(g, cudaMemsetAsync(g->degree, 0, sizeof(uint32_t) * (V + 1), st));
     GRZ_CK(g, cudaMemsetAsync(g->outdeg, 0, sizeof(double) * (V + 8), st));
     if (E > 0) {
-        k_degree<<<grid_blocks_for(E), BT, 0, st>>>(d_pull_pairs, E, g->degree);
+        k_degree<<<grid_blocks_for(E), BT, 0, st>>>(d_pull_pairs, E, g->degree); GRZ_COUNT_LAUNCH(g);
         GRZ_CK(g, cudaGetLastError());
     }
     if (V > 0) {
-        k_degree_to_double<<<grid_blocks_for(V), BT, 0, st>>>(g->degree, V, g->outdeg, g->inv_deg);
+        k_degree_to_double<<<grid_blocks_for(V), BT, 0, st>>>(g->degree, V, g->outdeg, g->inv_deg); GRZ_COUNT_LAUNCH(g);
         GRZ_CK(g, cudaGetLastError());
     }
     return GRZ_OK;

@@ -291,7 +291,7 @@ int grz_pr_init_state(grz_graph* g, double damping)
     GRZ_CK(g, cudaMemsetAsync(g->pr_sum, 0, sizeof(u128) * 2 * (blocks_for(g->V) + 1), g->stream));
     GRZ_CK(g, cudaMemsetAsync(g->accum, 0, sizeof(double) * (g->V + 8), g->stream));
     if (g->V) {
-        k_pr_init<<<blocks_for(g->V), PR_THREADS, 0, g->stream>>>(g->outdeg, g->degree, g->V, g->prop, g->accum, g->pr_fx[0], g->pr_sum);
+        k_pr_init<<<blocks_for(g->V), PR_THREADS, 0, g->stream>>>(g->outdeg, g->degree, g->V, g->prop, g->accum, g->pr_fx[0], g->pr_sum); GRZ_COUNT_LAUNCH(g);
         GRZ_CK(g, cudaGetLastError());
     }
     return GRZ_OK;
@@ -302,7 +302,7 @@ static int pr_gather(grz_graph* g, uint64_t first, uint64_t count, const PRConst
     if (count == 0) return GRZ_OK;
     grz_prof_begin(g, GRZ_PROF_PR_GATHER);
     k_pr_gather<<<blocks_for(count), PR_THREADS, 0, g->stream>>>(g->pull.nbr, g->pull.shared, first, count, g->pull.nvec,
-                                                                 g->pr_fx[g->pr_cur], (uint32_t)g->V, g->pr_rowacc, pc);
+                                                                 g->pr_fx[g->pr_cur], (uint32_t)g->V, g->pr_rowacc, pc); GRZ_COUNT_LAUNCH(g);
     grz_prof_end(g);
     return grz_cuda_check(g, cudaGetLastError(), "k_pr_gather");
 }
@@ -326,7 +326,7 @@ int grz_pr_fused_iteration(grz_graph* g, int write_double_props)
     grz_prof_begin(g, GRZ_PROF_PR_APPLY);
     k_pr_apply<<<blocks_for(g->V), PR_THREADS, 0, g->stream>>>(g->pr_rowacc, g->inv_deg, g->degree, g->V, g->pr_K,
                                                                g->pr_sum + (size_t)(k ^ 1) * nparts, g->pr_damping, g->pr_fx[g->pr_cur ^ 1],
-                                                               write_double_props ? g->prop : nullptr);
+                                                               write_double_props ? g->prop : nullptr); GRZ_COUNT_LAUNCH(g);
     grz_prof_end(g);
     GRZ_CK(g, cudaGetLastError());
     g->pr_cur ^= 1;
@@ -346,7 +346,7 @@ int grz_pr_edge_pull(grz_graph* g, uint64_t first, uint64_t count)
     int rc = pr_gather(g, first, count, pc);
     if (rc) return rc;
     if (first + count < g->pull.nvec) return GRZ_OK;
-    k_pr_accum_out<<<blocks_for(g->V), PR_THREADS, 0, g->stream>>>(g->pr_rowacc, g->V, g->accum, g->glob);
+    k_pr_accum_out<<<blocks_for(g->V), PR_THREADS, 0, g->stream>>>(g->pr_rowacc, g->V, g->accum, g->glob); GRZ_COUNT_LAUNCH(g);
     GRZ_CK(g, cudaGetLastError());
     return GRZ_OK;
 }
@@ -362,7 +362,7 @@ int grz_pr_vertex(grz_graph* g, uint64_t first, uint64_t count, double S)
     const double K = fma(G, g->pr_damping, c);
     // the props being gathered are rewritten in place: the boundary path keeps one live copy
     k_pr_vertex<<<blocks_for(count), PR_THREADS, 0, g->stream>>>(g->accum, g->inv_deg, g->prop, g->pr_fx[g->pr_cur],
-                                                                 first, count, g->pr_damping, K);
+                                                                 first, count, g->pr_damping, K); GRZ_COUNT_LAUNCH(g);
     GRZ_CK(g, cudaGetLastError());
     return GRZ_OK;
 }
@@ -371,7 +371,7 @@ int grz_pr_vertex(grz_graph* g, uint64_t first, uint64_t count, double S)
 int grz_pr_props_to_double(grz_graph* g)
 {
     if (g->V == 0) return GRZ_OK;
-    k_fx_to_double<<<blocks_for(g->V), PR_THREADS, 0, g->stream>>>(g->pr_fx[g->pr_cur], g->V, g->prop);
+    k_fx_to_double<<<blocks_for(g->V), PR_THREADS, 0, g->stream>>>(g->pr_fx[g->pr_cur], g->V, g->prop); GRZ_COUNT_LAUNCH(g);
     GRZ_CK(g, cudaGetLastError());
     return GRZ_OK;
 }
@@ -432,9 +432,9 @@ int grz_pr_push_phase(grz_graph* g, uint64_t first_vec, uint64_t count)
     if (count == 0) return GRZ_OK;
     // the pull accumulators double as the push accumulators (zero between uses)
     k_pr_push<<<blocks_for(count), PR_THREADS, 0, g->stream>>>(g->push.nbr, g->push.shared, first_vec, count,
-                                                               g->pr_fx[g->pr_cur], g->pr_rowacc, g->glob);
+                                                               g->pr_fx[g->pr_cur], g->pr_rowacc, g->glob); GRZ_COUNT_LAUNCH(g);
     GRZ_CK(g, cudaGetLastError());
-    k_pr_push_accum_out<<<blocks_for(g->V), PR_THREADS, 0, g->stream>>>(g->pr_rowacc, g->accum, 0, g->V);
+    k_pr_push_accum_out<<<blocks_for(g->V), PR_THREADS, 0, g->stream>>>(g->pr_rowacc, g->accum, 0, g->V); GRZ_COUNT_LAUNCH(g);
     GRZ_CK(g, cudaGetLastError());
     return GRZ_OK;
 }

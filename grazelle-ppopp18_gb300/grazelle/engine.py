@@ -68,6 +68,9 @@ class Graph:
             native.check(n, self.h)
         return [(self.lib.grz_profile_kind_name(kinds[i]).decode(), ms[i]) for i in range(n)]
 
+    def launch_count(self) -> int:
+        return int(self.lib.grz_launch_count(self.h))
+
     # ------------------------------------------------------------------ ingest
     def load_pairs(self, num_vertices: int, pull_pairs, push_pairs=None):
         """Interleaved (src, dst) uint64 pairs in file order.  numpy arrays (host) or raw device pointers (int)."""
@@ -85,6 +88,13 @@ class Graph:
         E = keep1.shape[0] // 2
         self._ck(self.lib.grz_graph_load_pairs(self.h, num_vertices, E, pp, sp))
         self.V, self.E = num_vertices, E
+        return self
+
+    def load_pointers(self, num_vertices: int, num_edges: int, pull_ptr: int, push_ptr: int | None = None):
+        """Edge lists given as raw pointers (pinned host or device memory), 2*E uint64 each."""
+        self._ck(self.lib.grz_graph_load_pairs(self.h, num_vertices, num_edges, C.c_void_p(pull_ptr),
+                                               C.c_void_p(push_ptr) if push_ptr else None))
+        self.V, self.E = num_vertices, num_edges
         return self
 
     def load_device_pairs(self, num_vertices: int, num_edges: int, pull_ptr: int, push_ptr: int | None = None):

@@ -51,6 +51,9 @@ def _tools():
         lib.grz_gen_rmat_raw.argtypes = [C.c_int, C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint64, u64p, u64p]
         lib.grz_gen_er_raw.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64, u64p, u64p]
         lib.grz_radix_sort_u64.argtypes = [u64p, u64p, C.c_uint64, C.c_int]
+        lib.grz_radix_sort_u64_mt.argtypes = [u64p, u64p, C.c_uint64, C.c_int]
+        lib.grz_sym_keys.argtypes = [u64p, u64p, C.c_uint64, u64p]
+        lib.grz_keys_to_pairs.argtypes = [u64p, C.c_uint64, C.c_int, u64p]
         lib.grz_unique_no_loops.restype = C.c_uint64
         lib.grz_unique_no_loops.argtypes = [u64p, C.c_uint64]
         _TOOLS = lib
@@ -68,20 +71,32 @@ class EdgeList:
     num_vertices: int
     src: np.ndarray  # uint64[E]
     dst: np.ndarray  # uint64[E]
+    push_sorted: bool = False  # edges already in (src, dst) order
 
     @property
     def num_edges(self) -> int:
         return int(self.src.shape[0])
 
+    def _sorted_by(self, major: np.ndarray, minor: np.ndarray, major_is_src: bool) -> "EdgeList":
+        if major_is_src and self.push_sorted:
+            return self
+        lib = _tools()
+        if lib is not None and self.num_vertices <= (1 << 32):
+            key = (major.astype(np.uint64) << np.uint64(32)) | minor.astype(np.uint64)
+            tmp = np.empty_like(key)
+            lib.grz_radix_sort_u64_mt(key, tmp, key.shape[0], max(1, 32 + int(max(self.num_vertices - 1, 1)).bit_length()))
+            hi, lo = key >> np.uint64(32), key & np.uint64(0xFFFFFFFF)
+            return EdgeList(self.num_vertices, hi, lo, True) if major_is_src else EdgeList(self.num_vertices, lo, hi)
+        o = np.lexsort((minor, major))
+        return EdgeList(self.num_vertices, self.src[o], self.dst[o], major_is_src)
+
     def pull_order(self) -> "EdgeList":
         """Edges sorted by (dst, src): the ``-pull`` file order."""
-        o = np.lexsort((self.src, self.dst))
-        return EdgeList(self.num_vertices, self.src[o], self.dst[o])
+        return self._sorted_by(self.dst, self.src, False)
 
     def push_order(self) -> "EdgeList":
         """Edges sorted by (src, dst): the ``-push`` file order."""
-        o = np.lexsort((self.dst, self.src))
-        return EdgeList(self.num_vertices, self.src[o], self.dst[o])
+        return self._sorted_by(self.src, self.dst, True)
 
     def pairs(self) -> np.ndarray:
         """Interleaved uint64[2E] (src0, dst0, src1, dst1, ...), the on-disk pair layout."""
@@ -90,6 +105,9 @@ class EdgeList:
         out[1::2] = self.dst
         return out
 
+    def out_degrees_fast(self) -> np.ndarray:
+        return self.out_degrees()
+
     def out_degrees(self) -> np.ndarray:
         return np.bincount(self.src.astype(np.int64), minlength=self.num_vertices).astype(np.uint64)
 
@@ -97,16 +115,21 @@ class EdgeList:
         return np.bincount(self.dst.astype(np.int64), minlength=self.num_vertices).astype(np.uint64)
 
 
+def _dedup_keys(num_vertices: int, key: np.ndarray) -> EdgeList:
+    lib = _tools()
+    tmp = np.empty_like(key)
+    bits = max(1, 32 + int(max(num_vertices - 1, 1)).bit_length())
+    lib.grz_radix_sort_u64_mt(key, tmp, key.shape[0], bits)
+    del tmp
+    n = int(lib.grz_unique_no_loops(key, key.shape[0]))
+    key = key[:n]
+    return EdgeList(num_vertices, key >> np.uint64(32), key & np.uint64(0xFFFFFFFF), True)
+
+
 def _dedup(num_vertices: int, src: np.ndarray, dst: np.ndarray) -> EdgeList:
     lib = _tools()
     if lib is not None and num_vertices <= (1 << 32):
-        key = (src << np.uint64(32)) | dst
-        tmp = np.empty_like(key)
-        bits = max(1, 32 + int(num_vertices - 1).bit_length())
-        lib.grz_radix_sort_u64(key, tmp, key.shape[0], bits)
-        n = int(lib.grz_unique_no_loops(key, key.shape[0]))
-        key = key[:n]
-        return EdgeList(num_vertices, key >> np.uint64(32), key & np.uint64(0xFFFFFFFF))
+        return _dedup_keys(num_vertices, (src << np.uint64(32)) | dst)
     keep = src != dst
     src, dst = src[keep], dst[keep]
     if num_vertices <= (1 << 32):
@@ -117,7 +140,7 @@ def _dedup(num_vertices: int, src: np.ndarray, dst: np.ndarray) -> EdgeList:
 
 
 def rmat(scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19,
-         seed: int = 1, chunk: int = 1 << 24, use_native: bool = True) -> EdgeList:
+         seed: int = 1, chunk: int = 1 << 24, use_native: bool = True, symmetric: bool = False) -> EdgeList:
     """Directed R-MAT graph (Chakrabarti, Zhan & Faloutsos 2004) with per-bit quadrant sampling.
 
     ``edge_factor * 2**scale`` edges are drawn.  At bit level ``i`` (MSB first) the
@@ -136,6 +159,11 @@ def rmat(scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c:
         s = np.empty(m, dtype=np.uint64)
         d = np.empty(m, dtype=np.uint64)
         lib.grz_gen_rmat_raw(scale, m, int(key), int(ta), int(tb), int(tc), s, d)
+        if symmetric:
+            keys = np.empty(2 * m, dtype=np.uint64)
+            lib.grz_sym_keys(s, d, m, keys)
+            del s, d
+            return _dedup_keys(n, keys)
         return _dedup(n, s, d)
     srcs, dsts = [], []
     for lo in range(0, m, chunk):
@@ -156,7 +184,8 @@ def rmat(scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c:
             s |= np.where(qc | qd, bit, np.uint64(0))
         srcs.append(s)
         dsts.append(d)
-    return _dedup(n, np.concatenate(srcs), np.concatenate(dsts))
+    g = _dedup(n, np.concatenate(srcs), np.concatenate(dsts))
+    return symmetrize(g) if symmetric else g
 
 
 def erdos_renyi(num_vertices: int, avg_degree: float, seed: int = 1, use_native: bool = True) -> EdgeList:

@@ -75,6 +75,9 @@ SIGNATURES = {
     "grz_profile_enable": (_I, [_VP, _I]),
     "grz_profile_read": (_I, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_float), _I]),
     "grz_profile_kind_name": (C.c_char_p, [_I]),
+    "grz_launch_count": (C.c_ulonglong, [_VP]),
+    "grz_fixed_point_roundtrip": (_I, [_D, _PD]),
+    "grz_fixed_point_sum": (_I, [_VP, _U64, _PD]),
     # grazelle_phases.h
     "grz_phases_bind": (_I, [_VP, _I]),
     "grz_phases_last_status": (_I, []),

@@ -140,6 +140,15 @@ int grz_frontier_current_vote(grz_graph* g, uint64_t* vote, int* threshold_engin
 int grz_profile_enable(grz_graph* g, int on);
 int grz_profile_read(grz_graph* g, int* kinds, float* ms, int capacity);
 const char* grz_profile_kind_name(int kind);
+/* number of kernels this graph has launched so far (monotonic) */
+unsigned long long grz_launch_count(const grz_graph* g);
+
+/* Host-side diagnostics of the exact accumulation used by PageRank: values are converted
+ * exactly to unsigned 4.124 fixed point, summed as 128-bit integers and rounded once to
+ * double (round to nearest even).  Inputs and the total must stay in [0, 16); a total that
+ * reaches 16 returns GRZ_ERR_RANGE. */
+int grz_fixed_point_roundtrip(double x, double* out);
+int grz_fixed_point_sum(const double* xs, uint64_t n, double* out);
 
 #ifdef __cplusplus
 }

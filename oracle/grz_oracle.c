@@ -651,3 +651,214 @@ uint64_t oracle_bfs_check_tree(const uint64_t* push_pairs, uint64_t E, uint64_t 
     free(off);
     return bad;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Multi-threaded CC / BFS: the CPU baseline on machines where the reference  */
+/* (x86-64 AVX2 only) cannot run.  Same SPMD semantics as the reference:      */
+/* dynamic work units, CAS-min label updates, asynchronous HasInfo updates in */
+/* CC push, unsynchronised parent stores in BFS, strong-frontier skip-ahead   */
+/* through the vertex index (include/phasehelpers.inc:137-213).               */
+/* ------------------------------------------------------------------------- */
+
+static inline int orc_abit(const uint64_t* bm, uint64_t v)
+{
+    return (int)((__atomic_load_n(&bm[v >> 6], __ATOMIC_RELAXED) >> (v & 63)) & 1ull);
+}
+static inline void orc_aset(uint64_t* bm, uint64_t v) { __atomic_fetch_or(&bm[v >> 6], 1ull << (v & 63), __ATOMIC_RELAXED); }
+static inline void orc_aclr(uint64_t* bm, uint64_t v) { __atomic_fetch_and(&bm[v >> 6], ~(1ull << (v & 63)), __ATOMIC_RELAXED); }
+
+static inline double orc_aload(const double* p)
+{
+    uint64_t b = __atomic_load_n((const uint64_t*)p, __ATOMIC_RELAXED);
+    double d;
+    memcpy(&d, &b, 8);
+    return d;
+}
+
+/* CAS-min of a non-negative double label (lock cmpxchg loop, phase_edge_pull_cc.asm:188-202);
+ * returns 1 if this call lowered it */
+static inline int orc_cas_min(double* p, double x)
+{
+    uint64_t* q = (uint64_t*)p;
+    uint64_t old = __atomic_load_n(q, __ATOMIC_RELAXED);
+    for (;;) {
+        double od;
+        memcpy(&od, &old, 8);
+        if (!(x < od)) return 0;
+        uint64_t nb;
+        memcpy(&nb, &x, 8);
+        if (__atomic_compare_exchange_n(q, &old, nb, 1, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) return 1;
+    }
+}
+
+/* next vertex >= v that is set in `bm` and owns vectors (vindex entry without bit 62/63);
+ * returns its first vector, or UINT64_MAX if none (strong frontier search) */
+static uint64_t orc_next_active(const uint64_t* bm, const uint64_t* vindex, uint64_t v, uint64_t words)
+{
+    for (;;) {
+        uint64_t w = v >> 6;
+        if (w >= words) return UINT64_MAX;
+        uint64_t x = __atomic_load_n(&bm[w], __ATOMIC_RELAXED) & (~0ull << (v & 63));
+        while (!x) {
+            if (++w >= words) return UINT64_MAX;
+            x = __atomic_load_n(&bm[w], __ATOMIC_RELAXED);
+        }
+        const uint64_t cand = (w << 6) + (uint64_t)__builtin_ctzll(x);
+        const uint64_t idx = vindex[cand];
+        if (idx & 0x8000000000000000ull) return UINT64_MAX;   /* beyond the last vertex */
+        if (!(idx & 0x4000000000000000ull)) return idx;         /* has vectors */
+        v = cand + 1;
+    }
+}
+
+typedef struct orc_mt_graph {
+    const uint64_t* pull_vec; uint64_t pull_nvec; const uint64_t* pull_index;
+    const uint64_t* push_vec; uint64_t push_nvec; const uint64_t* push_index;
+    const double* outdeg; uint64_t V, E;
+} orc_mt_graph;
+
+/*
+ * Multi-threaded CC or BFS (app 1 / 2) from root 0: the reference's execution_impl_{cc,bfs}
+ * run by `threads` OpenMP threads.  props[V] out (labels / parents as doubles), iter_out[3]
+ * out.  Returns the thread count used.
+ */
+int oracle_frontier_mt(const uint64_t* pull_vec, uint64_t pull_nvec, const uint64_t* pull_index,
+                       const uint64_t* push_vec, uint64_t push_nvec, const uint64_t* push_index,
+                       const double* outdeg, uint64_t V, uint64_t E, int app, int flags, int threads,
+                       double* props, uint64_t* iter_out)
+{
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#else
+    threads = 1;
+#endif
+    const uint64_t words = (V >> 6) + ((V & 63) ? 1 : 0);
+    uint64_t* has = (uint64_t*)calloc(words + 1, sizeof(uint64_t));
+    uint64_t* has_next = (uint64_t*)calloc(words + 1, sizeof(uint64_t));
+    uint64_t* wants = (uint64_t*)calloc(words + 1, sizeof(uint64_t));
+    const int wc = (flags & ORC_WITHOUT_COUNT) != 0, wo = (flags & ORC_WITHOUT_OUTDEG) != 0;
+    uint64_t vote = 0;
+    if (app == 1) {
+        for (uint64_t w = 0; w < words; ++w) has[w] = wants[w] = ~0ull;
+        for (uint64_t v = 0; v < V; ++v) props[v] = (double)v;
+        if (!wo) vote += E;
+        if (!wc) vote += V;
+    } else {
+        for (uint64_t w = 0; w < words; ++w) wants[w] = ~0ull;
+        orc_set(has, 0);
+        orc_clr(wants, 0);
+        for (uint64_t v = 0; v < V; ++v) props[v] = -1.0;
+        if (!wo) vote += (uint64_t)outdeg[0];
+        if (!wc) vote += 1;
+    }
+    const uint64_t units = (uint64_t)threads << 5;
+    uint64_t ctr = 0, npull = 0, npush = 0;
+    for (;;) {
+        ++ctr;
+        const int pull = orc_use_pull(flags, vote, V, E);
+        if (pull) ++npull; else ++npush;
+        uint64_t nv = 0;
+        const uint64_t* vec = pull ? pull_vec : push_vec;
+        const uint64_t nvec = pull ? pull_nvec : push_nvec;
+        const uint64_t* vindex = pull ? pull_index : push_index;
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 1) reduction(+ : nv)
+        for (int64_t uu = 0; uu < (int64_t)units; ++uu) {
+            uint64_t lo, hi;
+            orc_unit_range(nvec, units, (uint64_t)uu, &lo, &hi);
+            if (lo >= hi) continue;
+            if (app == 1 && pull) {
+                /* CC pull: phase_edge_pull_cc.asm, write at each destination change and unit end */
+                uint64_t prev = orc_shared(vec + 4 * lo);
+                double acc = INFINITY;
+                for (uint64_t i = lo; i < hi; ++i) {
+                    const uint64_t* v = vec + 4 * i;
+                    const uint64_t dst = orc_shared(v);
+                    double m = INFINITY;
+                    for (int k = 0; k < 4; ++k)
+                        if (v[k] & ORC_VALID) { const double x = orc_aload(&props[v[k] & ORC_ID48]); m = x < m ? x : m; }
+                    if (prev != dst) {
+                        if (orc_cas_min(&props[prev], acc)) {
+                            orc_aset(has_next, prev);
+                            nv += orc_vote(outdeg, prev, wc, wo);
+                        }
+                        acc = INFINITY;
+                    }
+                    prev = dst;
+                    acc = m < acc ? m : acc;
+                }
+                if (orc_cas_min(&props[prev], acc)) { orc_aset(has_next, prev); nv += orc_vote(outdeg, prev, wc, wo); }
+            } else {
+                /* strong frontier on the shared vertex: HasInfo (push) or WantsInfo (BFS pull) */
+                const uint64_t* strong = pull ? wants : has;
+                uint64_t i = lo;
+                while (i < hi) {
+                    const uint64_t* v = vec + 4 * i;
+                    const uint64_t sh = orc_shared(v);
+                    if (!orc_abit(strong, sh)) {
+                        const uint64_t nx = orc_next_active(strong, vindex, sh + 1, words);
+                        if (nx == UINT64_MAX) break;
+                        i = nx > i ? nx : i + 1;
+                        continue;
+                    }
+                    if (app == 2 && pull) {
+                        /* BFS pull: phase_edge_pull_bfs.asm:104-207 */
+                        int any = 0;
+                        uint64_t best = 0;
+                        for (int k = 0; k < 4; ++k) {
+                            if (!(v[k] & ORC_VALID)) continue;
+                            const uint64_t s = v[k] & ORC_ID48;
+                            if (!orc_abit(has, s)) continue;
+                            if (!any || s > best) best = s;
+                            any = 1;
+                        }
+                        if (any) {
+                            __atomic_store_n((uint64_t*)&props[sh], 0, __ATOMIC_RELAXED);
+                            const double pd = (double)(int64_t)best;
+                            uint64_t pb;
+                            memcpy(&pb, &pd, 8);
+                            __atomic_store_n((uint64_t*)&props[sh], pb, __ATOMIC_RELAXED);
+                            orc_aset(has_next, sh);
+                            orc_aclr(wants, sh);
+                            nv += orc_vote(outdeg, sh, wc, wo);
+                        }
+                    } else if (app == 2) {
+                        /* BFS push: phase_edge_push_bfs.asm:104-198 */
+                        int mark[4];
+                        for (int k = 0; k < 4; ++k) mark[k] = (v[k] & ORC_VALID) && orc_abit(wants, v[k] & ORC_ID48);
+                        const double pd = (double)(int64_t)sh;
+                        uint64_t pb;
+                        memcpy(&pb, &pd, 8);
+                        for (int k = 0; k < 4; ++k) {
+                            if (!mark[k]) continue;
+                            const uint64_t d = v[k] & ORC_ID48;
+                            orc_aclr(wants, d);
+                            orc_aset(has_next, d);
+                            __atomic_store_n((uint64_t*)&props[d], pb, __ATOMIC_RELAXED);
+                            nv += orc_vote(outdeg, d, wc, wo);
+                        }
+                    } else {
+                        /* CC push: phase_edge_push_cc.asm:130-225, asynchronous HasInfo */
+                        const double msg = orc_aload(&props[sh]);
+                        for (int k = 0; k < 4; ++k) {
+                            if (!(v[k] & ORC_VALID)) continue;
+                            const uint64_t d = v[k] & ORC_ID48;
+                            if (orc_cas_min(&props[d], msg)) {
+                                orc_aset(has, d);
+                                orc_aset(has_next, d);
+                                nv += orc_vote(outdeg, d, wc, wo);
+                            }
+                        }
+                    }
+                    ++i;
+                }
+            }
+        }
+        vote = nv;
+        if (vote == 0) break;
+        uint64_t* t = has; has = has_next; has_next = t;
+        memset(has_next, 0, sizeof(uint64_t) * words);
+    }
+    iter_out[0] = ctr; iter_out[1] = npull; iter_out[2] = npush;
+    free(has); free(has_next); free(wants);
+    return threads;
+}

@@ -71,6 +71,9 @@ def lib():
                                 _f64p, _u64p, _u8p, C.c_uint64]
         L.oracle_bfs.argtypes = [_u64p, C.c_uint64, _u64p, C.c_uint64, _f64p, C.c_uint64, C.c_uint64, C.c_int,
                                  _f64p, _u64p, _u8p, C.c_uint64]
+        L.oracle_frontier_mt.restype = C.c_int
+        L.oracle_frontier_mt.argtypes = [_u64p, C.c_uint64, _u64p, _u64p, C.c_uint64, _u64p, _f64p, C.c_uint64, C.c_uint64,
+                                         C.c_int, C.c_int, C.c_int, _f64p, _u64p]
         L.oracle_bfs_levels.argtypes = [_u64p, C.c_uint64, C.c_uint64, C.c_uint64, _i64p]
         L.oracle_bfs_check_tree.restype = C.c_uint64
         L.oracle_bfs_check_tree.argtypes = [_u64p, C.c_uint64, C.c_uint64, C.c_uint64, _i64p, _i64p]
@@ -165,6 +168,16 @@ def bfs(L: Layout, flags: int = 0):
                      np.ascontiguousarray(L.push_vec).reshape(-1), L.push_vec.shape[0],
                      np.ascontiguousarray(L.outdeg), L.V, L.E, flags, parent, it, log, log.shape[0])
     return parent, it, log[:int(it[0])].copy()
+
+
+def frontier_mt(L: Layout, app: int, flags: int = 0, threads: int = 0):
+    """Multi-threaded CC (app 1) or BFS (app 2) with the reference's SPMD semantics; (props, iters, threads)."""
+    props = np.zeros(L.V, dtype=np.float64)
+    it = np.zeros(3, dtype=np.uint64)
+    n = lib().oracle_frontier_mt(np.ascontiguousarray(L.pull_vec).reshape(-1), L.pull_vec.shape[0], L.pull_index,
+                                 np.ascontiguousarray(L.push_vec).reshape(-1), L.push_vec.shape[0], L.push_index,
+                                 np.ascontiguousarray(L.outdeg), L.V, L.E, app, flags, threads, props, it)
+    return props, it, n
 
 
 def bfs_levels(push_pairs: np.ndarray, V: int, root: int = 0) -> np.ndarray:

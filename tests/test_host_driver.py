@@ -1,0 +1,65 @@
+"""The C host driver (grazelle-gb300-{pr,cc,bfs}): command line, exit codes and outputs."""
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from oracle import oracle as O
+
+
+def exe(app):
+    from grazelle import build
+    build.build()
+    return str(build.BUILD / ("grazelle-gb300-" + app))
+
+
+def run(args, **kw):
+    return subprocess.run(args, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=300, **kw)
+
+
+@pytest.mark.parametrize("app", ["pr", "cc", "bfs"])
+def test_exit_codes_without_gpu(app, tmp_path):
+    e = exe(app)
+    assert run([e, "-x"]).returncode == 1            # unknown option (cmdline.c:120-125)
+    assert run([e, "-N", "zero", "-i", "g"]).returncode == 2   # invalid value
+    assert run([e, "-i"]).returncode == 3            # missing value
+    assert run([e, "-h", "x"]).returncode == 4       # extraneous value
+    assert run([e]).returncode == 5                  # missing -i
+    r = run([e, "-i", str(tmp_path / "nope")])
+    assert r.returncode == 255 and "unable to read file" in r.stderr   # graphdata.c:963-967
+    # truncated file: header promises more edges than the file holds
+    base = tmp_path / "trunc"
+    np.array([10, 5, 1, 2], dtype=np.uint64).tofile(str(base) + "-pull")
+    assert run([e, "-i", str(base)]).returncode == 255
+    v = run([e, "-V"])
+    assert v.returncode == 0 and "ppopp18" in v.stdout
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("app", ["pr", "cc", "bfs"])
+def test_driver_output_matches_reference(app, tmp_path):
+    from grazelle import graphgen as gg
+    rec, g = load_golden("rmat10_s12")
+    base = str(tmp_path / "g")
+    gg.write_grazelle(g, base)
+    out = tmp_path / "out.txt"
+    r = run([exe(app), "-i", base, "-N", "16", "-o", str(out)])
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "EXECUTION STATISTICS" in r.stdout
+    vals = np.loadtxt(out)
+    assert vals.shape == (g.num_vertices, 2)
+    np.testing.assert_array_equal(vals[:, 0], np.arange(g.num_vertices))
+    if app == "pr":
+        od = np.where(rec["outdeg"] == 0, g.num_vertices, rec["outdeg"])
+        ranks = rec["pr_n1"] * od
+        np.testing.assert_allclose(vals[:, 1], ranks, rtol=1e-5)   # %.5le in the file
+        assert "PageRank Sum              = 1.0000000000" in r.stdout or "PageRank Sum              = 0.9999999999" in r.stdout
+    elif app == "cc":
+        np.testing.assert_array_equal(vals[:, 1], rec["cc_labels"])
+        assert "Total Iterations" in r.stdout
+    else:
+        np.testing.assert_array_equal(vals[:, 1], rec["bfs_parents"])
+        it = rec["bfs_iters"]
+        assert "Total Iterations          = %d" % it[0] in r.stdout
+        assert "Pull-Based Iterations     = %d" % it[1] in r.stdout

@@ -77,6 +77,8 @@ SIGNATURES = {
     "grz_profile_kind_name": (C.c_char_p, [_I]),
     "grz_launch_count": (C.c_ulonglong, [_VP]),
     "grz_fixed_point_roundtrip": (_I, [_D, _PD]),
+    "grz_pr_step_noalloc": (_I, [_VP, _U64, _U64, _VP, _VP, _D, _VP, _VP]),
+    "grz_pr_step_noalloc_max_vertices": (_U64, []),
     "grz_fixed_point_sum": (_I, [_VP, _U64, _PD]),
     # grazelle_phases.h
     "grz_phases_bind": (_I, [_VP, _I]),

@@ -143,6 +143,35 @@ const char* grz_profile_kind_name(int kind);
 /* number of kernels this graph has launched so far (monotonic) */
 unsigned long long grz_launch_count(const grz_graph* g);
 
+/* -------- allocation-free PageRank step -------- */
+
+/* Largest graph (vertices) that grz_pr_step_noalloc accepts. */
+#define GRZ_NOALLOC_MAX_VERTICES (1u << 18)
+
+/* One PageRank iteration (edge-pull + vertex phase) on caller-owned device arrays, for callers
+ * that cannot allocate device memory while they run: a framework whose own pool owns the
+ * device memory, a latency-bound loop where cudaMalloc/cudaFree would synchronise the device,
+ * or a sandbox that forbids allocation after start-up.  This function has no counterpart in
+ * the reference.  It calls no cudaMalloc, cudaFree or other allocating routine.  Its scratch
+ * (exact per-destination accumulators and per-block partial sums, about 4 MB) lives in a
+ * fixed device array inside this library, held by every GPU that loads it until the process
+ * exits.
+ *   vectors      the reference's 256-bit pull vectors on the device (32-byte aligned), e.g.
+ *                grz_graph_info_t.pull_list_device; num_vectors of them
+ *   props_in     double[V] on the device: rank / outdegree', as the reference stores props
+ *   outdeg       double[V] on the device: outdegree from the -pull list
+ *   props_out    double[V] on the device: the props after one iteration (may not alias props_in)
+ *   stream       cudaStream_t to run on (NULL = the legacy default stream)
+ * Returns GRZ_ERR_RANGE if num_vertices is 0 or above GRZ_NOALLOC_MAX_VERTICES, GRZ_ERR_ARG
+ * for a bad argument, GRZ_ERR_CUDA if a launch fails.
+ * The first call on a device resolves the scratch array's device address (cudaGetSymbolAddress)
+ * for that device, so make that first call before capturing a stream.  Every call shares the
+ * one array and clears the part it needs when it starts, so calls that overlap on the GPU (on
+ * different streams, or from different host threads) race with each other: order them. */
+int grz_pr_step_noalloc(const void* vectors, uint64_t num_vectors, uint64_t num_vertices, const double* props_in,
+                        const double* outdeg, double damping, double* props_out, void* stream);
+uint64_t grz_pr_step_noalloc_max_vertices(void);
+
 /* Host-side diagnostics of the exact accumulation used by PageRank: values are converted
  * exactly to unsigned 4.124 fixed point, summed as 128-bit integers and rounded once to
  * double (round to nearest even).  Inputs and the total must stay in [0, 16); a total that

@@ -18,9 +18,10 @@
 //   * Pull: one thread per vector, a warp-segmented reduction per destination, one atomic per
 //     (warp, destination).  Labels are updated in place, as the reference's CAS loop does, so
 //     a later vector may already see a lowered label.
-//   * Push: HasInfo is compacted into a list of active sources that have out-edges.  Each block
-//     then expands 256 of them, with a block-wide scan over their vector counts, so work per
-//     thread does not depend on source degree.
+//   * Push: HasInfo is compacted, in vertex order, into a list of active sources that have
+//     out-edges, with a scan of their vector counts.  The concatenation of their vector ranges
+//     is expanded in tiles of 1024 vectors over the whole grid, so neither threads nor blocks
+//     wait on high-degree sources.
 //   * Each changed vertex is counted once per iteration: the first setter of its HasInfo* bit
 //     adds 1 + outdeg to the vote.  The reference can count a destination that straddles two
 //     work units twice.  The vote only steers the engine choice.
@@ -152,95 +153,171 @@ __global__ void __launch_bounds__(T) k_bfs_pull(const uint4* __restrict__ nbr, c
 }
 
 // ---------------------------------------------------------------------------------------------
-// frontier compaction: active sources (bit set in `has`) that have out-vectors
+// Push: frontier compaction and edge-balanced expansion.
+//
+// The active sources that have out-vectors are compacted in vertex order, each with the offset
+// of its first vector in the concatenation of their vector ranges.  The expansion then splits
+// that concatenation into tiles of PUSH_TILE vectors spread over the grid, so a hub's vectors
+// are spread over many blocks.  tile_first[t] is the frontier entry that owns the first vector
+// of tile t.  Passes: k_fr_count (per block of bitmap words: sources and vectors),
+// k_fr_scan (one block: exclusive scan of the block totals), k_fr_write (frontier entries,
+// their vector offsets and the tile owners), k_push_expand.
 
-__global__ void __launch_bounds__(T) k_compact(const unsigned long long* __restrict__ has,
-                                               const unsigned long long* __restrict__ nonempty, uint64_t words,
-                                               uint32_t* __restrict__ frontier, uint32_t* __restrict__ nfrontier)
+constexpr uint32_t PUSH_TILE = 1024;
+
+__device__ __forceinline__ uint32_t vec_count(const uint32_t* __restrict__ rowptr, uint32_t u)
 {
-    __shared__ uint32_t warp_tot[T / 32];
-    __shared__ uint32_t base;
-    const uint64_t w = (uint64_t)blockIdx.x * T + threadIdx.x;
-    const unsigned long long bits = (w < words) ? (has[w] & nonempty[w]) : 0ull;
-    const uint32_t cnt = __popcll(bits);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t x = cnt;
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) warp_tot[warp] = x;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t run = 0;
-        for (int k = 0; k < T / 32; ++k) { const uint32_t t = warp_tot[k]; warp_tot[k] = run; run += t; }
-        base = run ? atomicAdd(nfrontier, run) : 0u;
-    }
-    __syncthreads();
-    uint32_t pos = base + warp_tot[warp] + x - cnt;
-    unsigned long long b = bits;
-    while (b) {
-        const int k = __ffsll((long long)b) - 1;
-        b &= b - 1;
-        frontier[pos++] = (uint32_t)(w * 64 + (uint64_t)k);
-    }
+    return rowptr[u + 1] - rowptr[u];
 }
 
-// Expand the compacted frontier: block c handles frontier entries [256c, 256c+256).  A block
-// scan of their vector counts maps each of the block's vectors to its source by a binary search
-// in shared memory.  Grid-stride over chunks, so the frontier size stays on the device.
+// block-wide exclusive scan of two u32 values; returns the block totals through the references
+__device__ __forceinline__ void block_scan2(uint32_t& a, uint32_t& b, uint32_t& tot_a, uint32_t& tot_b, uint32_t* sa,
+                                            uint32_t* sb)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t xa = a, xb = b;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t ya = __shfl_up_sync(0xffffffffu, xa, o);
+        const uint32_t yb = __shfl_up_sync(0xffffffffu, xb, o);
+        if (lane >= o) { xa += ya; xb += yb; }
+    }
+    if (lane == 31) { sa[warp] = xa; sb[warp] = xb; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t ra = 0, rb = 0;
+        for (int k = 0; k < T / 32; ++k) {
+            const uint32_t ta = sa[k], tb = sb[k];
+            sa[k] = ra; sb[k] = rb;
+            ra += ta; rb += tb;
+        }
+        sa[T / 32] = ra; sb[T / 32] = rb;
+    }
+    __syncthreads();
+    a = sa[warp] + xa - a;
+    b = sb[warp] + xb - b;
+    tot_a = sa[T / 32];
+    tot_b = sb[T / 32];
+}
+
+__global__ void __launch_bounds__(T) k_fr_count(const unsigned long long* __restrict__ has,
+                                                const unsigned long long* __restrict__ nonempty, uint64_t words,
+                                                const uint32_t* __restrict__ rowptr, uint32_t* __restrict__ part_n,
+                                                uint32_t* __restrict__ part_vec)
+{
+    __shared__ uint32_t sa[T / 32 + 1], sb[T / 32 + 1];
+    const uint64_t w = (uint64_t)blockIdx.x * T + threadIdx.x;
+    unsigned long long bits = (w < words) ? (has[w] & nonempty[w]) : 0ull;
+    uint32_t n = __popcll(bits), vec = 0;
+    while (bits) {
+        const int k = __ffsll((long long)bits) - 1;
+        bits &= bits - 1;
+        vec += vec_count(rowptr, (uint32_t)(w * 64 + (uint64_t)k));
+    }
+    uint32_t tn, tv;
+    block_scan2(n, vec, tn, tv, sa, sb);
+    if (threadIdx.x == 0) { part_n[blockIdx.x] = tn; part_vec[blockIdx.x] = tv; }
+}
+
+// one block: exclusive scan of the per-block totals in place; counters[0] = sources,
+// counters[2] = vectors
+__global__ void __launch_bounds__(T) k_fr_scan(uint32_t* __restrict__ part_n, uint32_t* __restrict__ part_vec, uint32_t nb,
+                                               uint32_t* __restrict__ counters)
+{
+    __shared__ uint32_t sa[T / 32 + 1], sb[T / 32 + 1];
+    uint32_t carry_n = 0, carry_v = 0;
+    for (uint32_t base = 0; base < nb; base += T) {
+        const uint32_t i = base + threadIdx.x;
+        uint32_t n = i < nb ? part_n[i] : 0u, v = i < nb ? part_vec[i] : 0u;
+        uint32_t tn, tv;
+        block_scan2(n, v, tn, tv, sa, sb);
+        if (i < nb) { part_n[i] = carry_n + n; part_vec[i] = carry_v + v; }
+        carry_n += tn;
+        carry_v += tv;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { counters[0] = carry_n; counters[2] = carry_v; }
+}
+
+// frontier[i] = source, voff[i] = offset of its first vector, vdelta[i] = its first vector's
+// index in the push list minus voff[i] (mod 2^32); tile_first[t] for the tiles that start in
+// its range.  voff[nf] = total vectors.
+__global__ void __launch_bounds__(T) k_fr_write(const unsigned long long* __restrict__ has,
+                                                const unsigned long long* __restrict__ nonempty, uint64_t words,
+                                                const uint32_t* __restrict__ rowptr, const uint32_t* __restrict__ base_n,
+                                                const uint32_t* __restrict__ base_vec, const uint32_t* __restrict__ counters,
+                                                uint32_t* __restrict__ frontier, uint32_t* __restrict__ voff,
+                                                uint32_t* __restrict__ vdelta, uint32_t* __restrict__ tile_first)
+{
+    __shared__ uint32_t sa[T / 32 + 1], sb[T / 32 + 1];
+    const uint64_t w = (uint64_t)blockIdx.x * T + threadIdx.x;
+    const unsigned long long bits0 = (w < words) ? (has[w] & nonempty[w]) : 0ull;
+    unsigned long long bits = bits0;
+    uint32_t n = __popcll(bits), vec = 0;
+    while (bits) {
+        const int k = __ffsll((long long)bits) - 1;
+        bits &= bits - 1;
+        vec += vec_count(rowptr, (uint32_t)(w * 64 + (uint64_t)k));
+    }
+    uint32_t tn, tv;
+    block_scan2(n, vec, tn, tv, sa, sb);
+    uint32_t pos = base_n[blockIdx.x] + n, vo = base_vec[blockIdx.x] + vec;
+    bits = bits0;
+    while (bits) {
+        const int k = __ffsll((long long)bits) - 1;
+        bits &= bits - 1;
+        const uint32_t u = (uint32_t)(w * 64 + (uint64_t)k);
+        const uint32_t r0 = rowptr[u], cnt = rowptr[u + 1] - r0;
+        frontier[pos] = u;
+        voff[pos] = vo;
+        vdelta[pos] = r0 - vo;
+        for (uint64_t t = ((uint64_t)vo + PUSH_TILE - 1) / PUSH_TILE; t * PUSH_TILE < (uint64_t)vo + cnt; ++t) tile_first[t] = pos;
+        ++pos;
+        vo += cnt;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) voff[counters[0]] = counters[2];
+}
+
+// Expand the compacted frontier, one tile of PUSH_TILE vectors at a time (grid-stride over
+// tiles; the totals stay on the device).  The tile's owners are staged in shared memory and
+// each vector finds its owner by a binary search there.
 template <bool IsBfs>
-__global__ void __launch_bounds__(T) k_push_expand(const uint32_t* __restrict__ frontier, const uint32_t* __restrict__ nfrontier,
-                                                   const uint32_t* __restrict__ rowptr, const uint4* __restrict__ nbr,
+__global__ void __launch_bounds__(T) k_push_expand(const uint32_t* __restrict__ frontier, const uint32_t* __restrict__ voff,
+                                                   const uint32_t* __restrict__ vdelta, const uint32_t* __restrict__ tile_first,
+                                                   const uint32_t* __restrict__ counters, const uint4* __restrict__ nbr,
                                                    uint32_t V, uint32_t* __restrict__ label,
                                                    unsigned long long* __restrict__ has_next, const unsigned long long* __restrict__ wants,
                                                    uint32_t* __restrict__ cand32, uint32_t* __restrict__ touched,
                                                    uint32_t* __restrict__ ntouched, VoteCfg vc, unsigned long long* __restrict__ vote)
 {
-    __shared__ uint32_t src[T];
-    __shared__ uint32_t vbase[T];
-    __shared__ uint32_t off[T + 1];
-    __shared__ uint32_t warp_tot[T / 32];
+    __shared__ uint32_t s_src[PUSH_TILE + 1];
+    __shared__ uint32_t s_off[PUSH_TILE + 1];
+    __shared__ uint32_t s_delta[PUSH_TILE + 1];
     __shared__ unsigned long long red[T / 32];
-    const uint32_t nf = *nfrontier;
-    const uint32_t nchunks = (nf + T - 1) / T;
+    const uint32_t nf = counters[0], total = counters[2];
+    const uint32_t ntiles = (total + PUSH_TILE - 1) / PUSH_TILE;
     unsigned long long my_vote = 0;
-    for (uint32_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
-        const uint32_t idx = c * T + threadIdx.x;
-        uint32_t cnt = 0;
-        if (idx < nf) {
-            const uint32_t u = frontier[idx];
-            src[threadIdx.x] = u;
-            vbase[threadIdx.x] = rowptr[u];
-            cnt = rowptr[u + 1] - rowptr[u];
-        }
-        // block exclusive scan of cnt
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        uint32_t x = cnt;
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        if (lane == 31) warp_tot[warp] = x;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            uint32_t run = 0;
-            for (int k = 0; k < T / 32; ++k) { const uint32_t t = warp_tot[k]; warp_tot[k] = run; run += t; }
-            off[T] = run;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint32_t first = tile_first[tile];
+        const uint32_t t0 = tile * PUSH_TILE;
+        const uint32_t tend = min(total, t0 + PUSH_TILE);
+        // entries first .. first+nw-1 own every vector of the tile (each owns at least one)
+        const uint32_t nw = min(PUSH_TILE, nf - first);
+        for (uint32_t i = threadIdx.x; i <= nw; i += T) {
+            s_off[i] = voff[first + i];
+            if (i < nw) {
+                s_src[i] = frontier[first + i];
+                s_delta[i] = vdelta[first + i];
+            }
         }
         __syncthreads();
-        off[threadIdx.x] = warp_tot[warp] + x - cnt;
-        __syncthreads();
-        const uint32_t total = off[T];
-        const int nent = (int)min((uint32_t)T, nf - c * T);
-        for (uint32_t t = threadIdx.x; t < total; t += T) {
-            int lo = 0, hi = nent - 1;  // last entry with off <= t
+        for (uint32_t gv = t0 + threadIdx.x; gv < tend; gv += T) {
+            int lo = 0, hi = (int)nw - 1;  // last entry with s_off <= gv
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
-                if (off[mid] <= t) lo = mid; else hi = mid - 1;
+                if (s_off[mid] <= gv) lo = mid; else hi = mid - 1;
             }
-            const uint32_t u = src[lo];
-            const uint4 s = __ldcs(nbr + vbase[lo] + (t - off[lo]));
+            const uint32_t u = s_src[lo];
+            const uint4 s = __ldcs(nbr + (uint32_t)(gv + s_delta[lo]));
             const uint32_t ids[4] = { s.x, s.y, s.z, s.w };
             if (IsBfs) {
 #pragma unroll
@@ -375,6 +452,10 @@ static int ensure_frontier_state(grz_graph* g)
     GRZ_CK(g, cudaMalloc((void**)&f.wants, sizeof(unsigned long long) * W));
     GRZ_CK(g, cudaMalloc((void**)&f.nonempty_push, sizeof(unsigned long long) * W));
     GRZ_CK(g, cudaMalloc((void**)&f.frontier, sizeof(uint32_t) * (V + 1)));
+    GRZ_CK(g, cudaMalloc((void**)&f.voff, sizeof(uint32_t) * (V + 1)));
+    GRZ_CK(g, cudaMalloc((void**)&f.vdelta, sizeof(uint32_t) * (V + 1)));
+    GRZ_CK(g, cudaMalloc((void**)&f.tile_first, sizeof(uint32_t) * (g->push.nvec / PUSH_TILE + 2)));
+    GRZ_CK(g, cudaMalloc((void**)&f.fr_part, sizeof(uint32_t) * 2 * blocks_for(W)));
     GRZ_CK(g, cudaMalloc((void**)&f.touched, sizeof(uint32_t) * (V + 1)));
     GRZ_CK(g, cudaMalloc((void**)&f.cand64, sizeof(unsigned long long) * (V + 1)));
     GRZ_CK(g, cudaMalloc((void**)&f.cand32, sizeof(uint32_t) * (V + 1)));
@@ -412,6 +493,8 @@ int grz_frontier_init(grz_graph* g, int app, int flags, uint32_t root)
     f.root = root;
     f.iter = 0;
     f.npull = f.npush = 0;
+    f.last_engine = 1;
+    f.next_pull = 1;
     cudaStream_t st = g->stream;
     if (app == GRZ_APP_CONNECTED_COMPONENTS) {
         k_cc_init<<<blocks_for(V + 1), T, 0, st>>>(f.label, V); GRZ_COUNT_LAUNCH(g);
@@ -484,16 +567,20 @@ static int edge_phase(grz_graph* g, int pull, uint64_t first, uint64_t count)
     } else {
         if (!g->push.nbr) return grz_set_error(g, GRZ_ERR_STATE, "push list not loaded");
         grz_prof_begin(g, bfs ? GRZ_PROF_BFS_PUSH : GRZ_PROF_CC_PUSH);
-        k_compact<<<blocks_for(W), T, 0, st>>>(f.has, f.nonempty_push, W, f.frontier, f.counters + 0); GRZ_COUNT_LAUNCH(g);
+        const unsigned nbw = blocks_for(W);
+        k_fr_count<<<nbw, T, 0, st>>>(f.has, f.nonempty_push, W, g->push.rowptr, f.fr_part, f.fr_part + nbw); GRZ_COUNT_LAUNCH(g);
+        k_fr_scan<<<1, T, 0, st>>>(f.fr_part, f.fr_part + nbw, nbw, f.counters); GRZ_COUNT_LAUNCH(g);
+        k_fr_write<<<nbw, T, 0, st>>>(f.has, f.nonempty_push, W, g->push.rowptr, f.fr_part, f.fr_part + nbw, f.counters,
+                                      f.frontier, f.voff, f.vdelta, f.tile_first); GRZ_COUNT_LAUNCH(g);
         const unsigned grid = (unsigned)g->num_sms * 8;
         if (bfs) {
-            k_push_expand<true><<<grid, T, 0, st>>>(f.frontier, f.counters + 0, g->push.rowptr, g->push.nbr, V, f.label, f.has_next,
-                                                    f.wants, f.cand32, f.touched, f.counters + 1, vc, f.vote); GRZ_COUNT_LAUNCH(g);
+            k_push_expand<true><<<grid, T, 0, st>>>(f.frontier, f.voff, f.vdelta, f.tile_first, f.counters, g->push.nbr, V, f.label,
+                                                    f.has_next, f.wants, f.cand32, f.touched, f.counters + 1, vc, f.vote); GRZ_COUNT_LAUNCH(g);
             k_bfs_visit<false><<<g->num_sms * 4, T, 0, st>>>(f.touched, f.counters + 1, f.cand64, f.cand32, f.label, f.level,
                                                              f.iter, f.wants, f.has_next, vc, f.vote); GRZ_COUNT_LAUNCH(g);
         } else {
-            k_push_expand<false><<<grid, T, 0, st>>>(f.frontier, f.counters + 0, g->push.rowptr, g->push.nbr, V, f.label, f.has_next,
-                                                     f.wants, f.cand32, f.touched, f.counters + 1, vc, f.vote); GRZ_COUNT_LAUNCH(g);
+            k_push_expand<false><<<grid, T, 0, st>>>(f.frontier, f.voff, f.vdelta, f.tile_first, f.counters, g->push.nbr, V, f.label,
+                                                     f.has_next, f.wants, f.cand32, f.touched, f.counters + 1, vc, f.vote); GRZ_COUNT_LAUNCH(g);
         }
         grz_prof_end(g);
     }
@@ -541,16 +628,36 @@ int grz_bfs_phase(grz_graph* g, int pull, uint64_t first_vec, uint64_t count)
 int grz_frontier_step(grz_graph* g, int engine, int* engine_out, uint64_t* vote_out)
 {
     grz_frontier_state& f = g->fr;
-    const int pull = engine >= 0 ? engine : grz_engine_threshold(g, f.vote_host);
+    const bool learned = f.policy == GRZ_POLICY_LEARNED && f.mlp;
+    int rc;
+    if (engine < 0 && learned && f.iter == 0) {
+        // first iteration: decide from the initial frontier and the initial vote
+        uint64_t v0 = 0;
+        rc = grz_switch_decide(g, f.has, f.vote_host, 1, &v0, &f.next_pull, f.last_features);
+        if (rc) return rc;
+    }
+    const int pull = engine >= 0 ? engine : (learned ? f.next_pull : grz_engine_threshold(g, f.vote_host));
     if (engine_out) *engine_out = pull;
     GRZ_CK(g, cudaMemsetAsync(f.vote, 0, sizeof(unsigned long long) * GRZ_VOTE_SLOTS * GRZ_VOTE_STRIDE, g->stream));
     f.iter++;
-    int rc = edge_phase(g, pull, 0, pull ? g->pull.nvec : g->push.nvec);
+    if (f.time_edges) GRZ_CK(g, cudaEventRecord(f.ev[0], g->stream));
+    rc = edge_phase(g, pull, 0, pull ? g->pull.nvec : g->push.nvec);
     if (rc) return rc;
+    if (f.time_edges) GRZ_CK(g, cudaEventRecord(f.ev[1], g->stream));
     if (pull) f.npull++; else f.npush++;
+    f.last_engine = pull;
     uint64_t v = 0;
-    rc = grz_read_vote(g, &v);
+    if (learned) {
+        // the vote and the next engine in one read-back; the next frontier is HasInfo*
+        rc = grz_switch_decide(g, f.has_next, ~0ull, f.iter + 1, &v, &f.next_pull, f.last_features);
+    } else {
+        rc = grz_read_vote(g, &v);
+    }
     if (rc) return rc;
+    if (f.time_edges) {
+        GRZ_CK(g, cudaEventSynchronize(f.ev[1]));
+        GRZ_CK(g, cudaEventElapsedTime(&f.last_edge_ms, f.ev[0], f.ev[1]));
+    }
     f.vote_host = v;
     if (vote_out) *vote_out = v;
     if (v == 0) return 0;
@@ -558,12 +665,22 @@ int grz_frontier_step(grz_graph* g, int engine, int* engine_out, uint64_t* vote_
     return rc ? rc : 1;
 }
 
+// the pinned host buffer the per-iteration read-backs go through
+int grz_frontier_mail(grz_graph* g)
+{
+    if (!g->fr.mail) GRZ_CK(g, cudaMallocHost(&g->fr.mail, sizeof(unsigned long long) * GRZ_VOTE_SLOTS * GRZ_VOTE_STRIDE));
+    return GRZ_OK;
+}
+
 // sum of the vote slots (synchronises the stream)
 int grz_read_vote(grz_graph* g, uint64_t* out)
 {
-    unsigned long long slots[GRZ_VOTE_SLOTS * GRZ_VOTE_STRIDE];
-    GRZ_CK(g, cudaMemcpyAsync(slots, g->fr.vote, sizeof(slots), cudaMemcpyDeviceToHost, g->stream));
+    const int rc = grz_frontier_mail(g);
+    if (rc) return rc;
+    const size_t bytes = sizeof(unsigned long long) * GRZ_VOTE_SLOTS * GRZ_VOTE_STRIDE;
+    GRZ_CK(g, cudaMemcpyAsync(g->fr.mail, g->fr.vote, bytes, cudaMemcpyDeviceToHost, g->stream));
     GRZ_CK(g, cudaStreamSynchronize(g->stream));
+    const unsigned long long* slots = (const unsigned long long*)g->fr.mail;
     uint64_t v = 0;
     for (int i = 0; i < GRZ_VOTE_SLOTS; ++i) v += slots[i * GRZ_VOTE_STRIDE];
     *out = v;
@@ -582,8 +699,15 @@ int grz_frontier_props(grz_graph* g)
 void grz_frontier_free(grz_graph* g)
 {
     grz_frontier_state& f = g->fr;
-    void* ptrs[] = { f.label, f.level, f.has, f.has_next, f.wants, f.nonempty_push, f.frontier, f.touched, f.cand64, f.cand32,
-                     f.counters, f.vote };
+    void* ptrs[] = { f.label, f.level, f.has, f.has_next, f.wants, f.nonempty_push, f.frontier, f.voff, f.vdelta, f.tile_first,
+                     f.fr_part, f.touched, f.cand64, f.cand32,
+                     f.counters, f.vote, f.sw_out, f.snap };
     for (void* p : ptrs) cudaFree(p);
+    if (f.ev[0]) { cudaEventDestroy(f.ev[0]); cudaEventDestroy(f.ev[1]); }
+    if (f.mail) cudaFreeHost(f.mail);
+    grz_mlp* keep_mlp = f.mlp;
+    const int keep_policy = f.policy;
     memset(&f, 0, sizeof(f));
+    f.mlp = keep_mlp;
+    f.policy = keep_policy;
 }

@@ -195,6 +195,14 @@ struct grz_prof;
 #define GRZ_VOTE_SLOTS 64
 #define GRZ_VOTE_STRIDE 16
 
+// learned switch (grz_switch.cu)
+#define GRZ_MLP_FEATURES 12
+#define GRZ_MLP_HIDDEN 32
+#define GRZ_MLP_PARAMS 1505  // 32*12 + 32 + 32*32 + 32 + 32 + 1
+#define GRZ_POLICY_THRESHOLD 0
+#define GRZ_POLICY_LEARNED 1
+struct grz_mlp;
+
 // CC / BFS state (grz_ccbfs.cu)
 struct grz_frontier_state {
     int app, flags;
@@ -207,11 +215,30 @@ struct grz_frontier_state {
     unsigned long long* wants;       // WantsInfo
     unsigned long long* nonempty_push;  // vertices with out-vectors
     uint32_t* frontier;              // compacted active sources
+    uint32_t* voff;                  // push: offset of each source's first vector among the frontier's
+    uint32_t* vdelta;                // push: first vector index in the list minus voff (mod 2^32)
+    uint32_t* tile_first;            // push: frontier entry owning the first vector of each tile
+    uint32_t* fr_part;               // push: per-block source and vector totals (scanned)
     uint32_t* touched;               // BFS destinations reached in this phase
     unsigned long long* cand64;      // BFS pull: (vector index, ~source) per destination
     uint32_t* cand32;                // BFS push: smallest source per destination
     uint32_t* counters;              // [0] frontier size, [1] touched count
     unsigned long long* vote;        // GRZ_VOTE_SLOTS * GRZ_VOTE_STRIDE
+    // engine policy
+    int policy;                      // GRZ_POLICY_*
+    grz_mlp* mlp;
+    int next_pull;                   // learned decision for the next iteration
+    int last_engine;
+    float last_features[GRZ_MLP_FEATURES];
+    void* sw_out;                    // device: vote, decision, counts, ticket, features
+    void* mail;                      // pinned host: read-back of the vote slots or of sw_out
+    float last_edge_ms;              // edge-phase time of the last step when timing is on
+    int time_edges;
+    cudaEvent_t ev[2];
+    // snapshot for timing both engines from one state
+    void* snap;
+    uint64_t snap_bytes;
+    uint64_t snap_scalars[8];
 };
 
 struct grz_graph {
@@ -241,6 +268,8 @@ struct grz_graph {
     u128* glob;           // u128[GRZ_SUM_SLOTS] device
     int app;              // 0 PR, 1 CC, 2 BFS
     int num_sms;
+    uint32_t max_degree;
+    int max_degree_known;
     grz_frontier_state fr;
     grz_prof* prof;       // kernel timing (null unless enabled)
     unsigned long long nlaunch;  // kernels launched by this graph (grz_launch_count)
@@ -307,6 +336,11 @@ int grz_frontier_vertex_phase(grz_graph* g, uint64_t first, uint64_t count);
 int grz_frontier_props(grz_graph* g);
 int grz_engine_threshold(const grz_graph* g, uint64_t vote);
 int grz_read_vote(grz_graph* g, uint64_t* out);
+int grz_frontier_mail(grz_graph* g);
+// learned switch: features of a state + the policy's decision; frontier = HasInfo of the
+// iteration the decision is for; vote_override = ~0 to read the vote slots
+int grz_switch_decide(grz_graph* g, const unsigned long long* frontier, uint64_t vote_override, uint32_t iter,
+                      uint64_t* vote, int* next_pull, float* features);
 void grz_frontier_free(grz_graph* g);
 
 // layout (grz_layout.cu)

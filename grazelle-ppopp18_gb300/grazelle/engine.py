@@ -172,6 +172,13 @@ class Graph:
         self._ck(self.lib.grz_read_levels(self.h, _ptr(lv), lv.shape[0]))
         return (par, lv, st) if stats else (par, lv)
 
+    def set_policy(self, policy: int, switch=None):
+        """Engine choice for CC/BFS runs: native.POLICY_THRESHOLD (the reference's rule) or
+        native.POLICY_LEARNED with a grazelle.switch.Switch."""
+        self._ck(self.lib.grz_frontier_set_policy(self.h, policy, switch.h if switch is not None else None))
+        self._switch = switch  # keeps the network alive while the graph refers to it
+        return self
+
     def frontier_begin(self, app: int, root: int = 0, flags: int = 0):
         self._ck(self.lib.grz_frontier_begin(self.h, app, root, flags))
         return self

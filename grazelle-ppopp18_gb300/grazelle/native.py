@@ -27,6 +27,8 @@ class GrzError(RuntimeError):
 
 
 FORCE_PULL, FORCE_PUSH, WITHOUT_COUNT, WITHOUT_OUTDEG = 1, 2, 4, 8
+MLP_FEATURES, MLP_HIDDEN, MLP_PARAMS = 12, 32, 1505
+POLICY_THRESHOLD, POLICY_LEARNED = 0, 1
 
 
 class RunStats(C.Structure):
@@ -72,6 +74,19 @@ SIGNATURES = {
     "grz_frontier_begin": (_I, [_VP, _I, _U32, _I]),
     "grz_frontier_next": (_I, [_VP, _I, C.POINTER(C.c_int), C.POINTER(C.c_uint64)]),
     "grz_frontier_current_vote": (_I, [_VP, C.POINTER(C.c_uint64), C.POINTER(C.c_int)]),
+    "grz_mlp_create": (_I, [C.POINTER(_VP), _I, _U64]),
+    "grz_mlp_destroy": (None, [_VP]),
+    "grz_mlp_get_params": (_I, [_VP, _VP, _U64]),
+    "grz_mlp_set_params": (_I, [_VP, _VP, _U64]),
+    "grz_mlp_gradients": (_I, [_VP, _VP, _VP, _VP, _U64, _VP, C.POINTER(C.c_float)]),
+    "grz_mlp_train": (_I, [_VP, _VP, _VP, _VP, _U64, _U32, C.c_float, C.POINTER(C.c_float)]),
+    "grz_mlp_predict": (_I, [_VP, _VP, _U64, _VP]),
+    "grz_frontier_set_policy": (_I, [_VP, _I, _VP]),
+    "grz_frontier_features": (_I, [_VP, _VP, _U64, C.POINTER(C.c_int)]),
+    "grz_frontier_last_features": (_I, [_VP, _VP, _U64]),
+    "grz_frontier_snapshot": (_I, [_VP]),
+    "grz_frontier_restore": (_I, [_VP]),
+    "grz_frontier_next_timed": (_I, [_VP, _I, C.POINTER(C.c_int), C.POINTER(C.c_uint64), C.POINTER(C.c_float)]),
     "grz_profile_enable": (_I, [_VP, _I]),
     "grz_profile_read": (_I, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_float), _I]),
     "grz_profile_kind_name": (C.c_char_p, [_I]),

@@ -133,6 +133,40 @@ int grz_frontier_next(grz_graph* g, int engine, int* engine_used, uint64_t* vote
 /* the vote that decides the next iteration and the heuristic's engine for it */
 int grz_frontier_current_vote(grz_graph* g, uint64_t* vote, int* threshold_engine);
 
+/* -------- learned push/pull switch -------- */
+
+/* The reference chooses the engine with a threshold on the vote (pull iff vote > E/5,
+ * source/execution_bfs.c:146-168); that stays the default policy.  GRZ_POLICY_LEARNED asks a
+ * small MLP (GRZ_MLP_FEATURES -> 32 -> 32 -> 1, FP32, hand-written CUDA kernels) before each
+ * iteration whether pull will be faster.  Labels and levels do not depend on the choice. */
+#define GRZ_MLP_FEATURES 12
+#define GRZ_MLP_HIDDEN 32
+#define GRZ_MLP_PARAMS 1505
+#define GRZ_POLICY_THRESHOLD 0
+#define GRZ_POLICY_LEARNED 1
+
+typedef struct grz_mlp grz_mlp;
+int grz_mlp_create(grz_mlp** out, int device, uint64_t seed);
+void grz_mlp_destroy(grz_mlp* n);
+int grz_mlp_get_params(grz_mlp* n, float* host_params, uint64_t capacity);
+int grz_mlp_set_params(grz_mlp* n, const float* host_params, uint64_t count);
+/* X: count x GRZ_MLP_FEATURES, Y: 1 if pull was faster, W: per-sample weight (e.g. |t_pull - t_push|);
+ * loss = mean of W * BCE(logit, Y) */
+int grz_mlp_gradients(grz_mlp* n, const float* X, const float* Y, const float* W, uint64_t count, float* host_grads,
+                      float* loss);
+int grz_mlp_train(grz_mlp* n, const float* X, const float* Y, const float* W, uint64_t count, uint32_t epochs, float lr,
+                  float* final_loss);
+int grz_mlp_predict(grz_mlp* n, const float* X, uint64_t count, float* host_logits);
+
+int grz_frontier_set_policy(grz_graph* g, int policy, grz_mlp* mlp);
+/* features of the state the next iteration starts from; *policy_choice = the current policy's engine */
+int grz_frontier_features(grz_graph* g, float* host_features, uint64_t capacity, int* policy_choice);
+int grz_frontier_last_features(grz_graph* g, float* host_features, uint64_t capacity);
+/* time both engines from one state: snapshot, run one, restore, run the other */
+int grz_frontier_snapshot(grz_graph* g);
+int grz_frontier_restore(grz_graph* g);
+int grz_frontier_next_timed(grz_graph* g, int engine, int* engine_used, uint64_t* vote, float* edge_ms);
+
 /* Kernel profiling: when enabled, every launch is bracketed by a CUDA event pair on the graph's
  * stream (the GPU form of the reference's EXPERIMENT_ITERATION_PROFILE, source/main.c:43-55).
  * grz_profile_read synchronises, returns up to `capacity` (kind, milliseconds) records in launch

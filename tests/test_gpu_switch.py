@@ -1,0 +1,166 @@
+"""The learned push/pull switch: GPU training kernels against the FP64 oracle, decisions on the
+device against the network's own predictions, identical results under any policy, and the gain
+of a trained network over the reference's threshold rule.
+
+The reference's rule (pull iff vote > E/5, source/execution_bfs.c:146-168,
+source/execution_cc.c:120-142) is the yardstick.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+from oracle import mlp as M
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def synthetic(n, seed):
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(0, 1, (n, M.F)).astype(np.float32)
+    Y = (X[:, 1] + 0.5 * X[:, 2] > 0.7).astype(np.float32)
+    W = rng.uniform(0.1, 2.0, n).astype(np.float32)
+    return X, Y, W
+
+
+def test_params_roundtrip_and_bad_args():
+    from grazelle import native
+    from grazelle.switch import Switch
+    net = Switch(0, seed=5)
+    p = net.params()
+    assert p.shape == (M.NP,) and np.isfinite(p).all() and np.abs(p).max() > 0
+    q = np.arange(M.NP, dtype=np.float32) * 1e-3
+    net.set_params(q)
+    np.testing.assert_array_equal(net.params(), q)
+    with pytest.raises(native.GrzError):
+        net.set_params(q[:-1])
+
+
+@pytest.mark.parametrize("n, seed", [(37, 1), (1000, 2), (5000, 3)])
+def test_gradients_match_fp64_oracle(n, seed):
+    from grazelle.switch import Switch
+    net = Switch(0, seed=seed)
+    X, Y, W = synthetic(n, seed)
+    net.train(X, Y, W, epochs=20, lr=3e-3)  # move off the initial point so every ReLU region shows up
+    p = net.params()
+    loss, g = net.gradients(X, Y, W)
+    loss64, g64 = M.loss_and_grad(p, X, Y, W)
+    # FP32 accumulation on the GPU against FP64: relative to the largest gradient component
+    assert abs(loss - loss64) <= 1e-5 * max(1.0, abs(loss64))
+    assert np.max(np.abs(g - g64)) <= 2e-5 * np.max(np.abs(g64))
+    z = net.predict(X)
+    z64, _ = M.forward(p, X)
+    assert np.max(np.abs(z - z64)) <= 1e-5 * (1.0 + np.max(np.abs(z64)))
+
+
+def test_training_lowers_loss():
+    from grazelle.switch import Switch
+    net = Switch(0, seed=7)
+    X, Y, W = synthetic(4096, 9)
+    loss0, _ = net.gradients(X, Y, W)
+    loss = net.train(X, Y, W, epochs=400, lr=3e-3)
+    assert loss < 0.3 * loss0
+    z = net.predict(X)
+    assert np.mean((z > 0) == (Y > 0.5)) > 0.95
+
+
+def gpu_graph(g):
+    from grazelle.engine import Graph
+    G = Graph(0)
+    G.load_pairs(g.num_vertices, g.pull_order().pairs(), g.push_order().pairs())
+    return G
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_learned_policy_gives_reference_results(name):
+    """Any network, trained or not, only changes the engine sequence: CC labels and BFS levels
+    stay bit-exact and BFS parents stay a legal BFS tree."""
+    from grazelle import native
+    from grazelle.switch import Switch
+    rec, g = load_golden(name)
+    push = g.push_order().pairs()
+    ref_lv = O.bfs_levels(push, g.num_vertices, 0)
+    with gpu_graph(g) as G:
+        for seed in (1, 2, 3, 4):
+            net = Switch(0, seed=seed)
+            G.set_policy(native.POLICY_LEARNED, net)
+            lab, st = G.connected_components(stats=True)
+            np.testing.assert_array_equal(lab, rec["cc_labels"])
+            par, lv, st2 = G.bfs(0, stats=True)
+            np.testing.assert_array_equal(lv, ref_lv)
+            assert O.bfs_check_tree(push, g.num_vertices, 0, lv, par.astype(np.int64)) == 0
+            assert st.iterations == st.pull_iterations + st.push_iterations
+            assert st2.iterations == st2.pull_iterations + st2.push_iterations
+            G.set_policy(native.POLICY_THRESHOLD)
+
+
+def test_device_decision_equals_network_prediction():
+    """The decision kernel's forward pass has the training kernel's operation order, so its
+    choice is the sign of grz_mlp_predict on the same features."""
+    from grazelle import graphgen as gg
+    from grazelle import native
+    from grazelle import switch as sw
+    g = gg.rmat(15, seed=21)
+    with gpu_graph(g) as G:
+        for seed in (1, 2, 3):
+            net = sw.Switch(0, seed=seed)
+            G.set_policy(native.POLICY_LEARNED, net)
+            for app, root in ((native.APP_BREADTH_FIRST_SEARCH, 3), (native.APP_CONNECTED_COMPONENTS, 0)):
+                G.frontier_begin(app, root)
+                for _ in range(100):
+                    f, choice = sw._features(G)
+                    assert np.isfinite(f).all()
+                    assert choice == int(net.predict(f[None, :])[0] > 0)
+                    running, used, _ = G.frontier_next()
+                    assert used == choice
+                    if not running:
+                        break
+            G.set_policy(native.POLICY_THRESHOLD)
+
+
+def test_snapshot_restore_replays_an_iteration():
+    """Timing both engines from one state needs an exact restore: pull and push from the same
+    snapshot leave the same BFS frontier and levels."""
+    from grazelle import graphgen as gg
+    from grazelle import native
+    from grazelle import switch as sw
+    g = gg.rmat(14, seed=4)
+    with gpu_graph(g) as G:
+        G.frontier_begin(native.APP_BREADTH_FIRST_SEARCH, 1)
+        for _ in range(3):
+            G.frontier_next()
+        G.lib.grz_frontier_snapshot(G.h)
+        run_a, _ = sw._step_timed(G, 1)
+        lv_a = G.levels()
+        G.lib.grz_frontier_restore(G.h)
+        run_b, _ = sw._step_timed(G, 0)
+        lv_b = G.levels()
+        assert run_a == run_b
+        np.testing.assert_array_equal(lv_a, lv_b)
+
+
+def test_trained_switch_beats_threshold():
+    """Trained on per-iteration timings from seeded R-MAT and Erdos-Renyi graphs, evaluated on
+    held-out graphs.  Edge-phase time summed over the iterations along each run: the learned
+    choices must beat the threshold's overall and come within 15% of the best choice per
+    iteration (the regret bound).  Results are identical under both policies."""
+    from grazelle import graphgen as gg
+    from grazelle import switch as sw
+    train_graphs = [("rmat17", gg.rmat(17, seed=201)), ("rmat19", gg.rmat(19, seed=202)),
+                    ("rmat20", gg.rmat(20, seed=203)), ("er18_d8", gg.erdos_renyi(1 << 18, 8, seed=204)),
+                    ("er19_d32", gg.erdos_renyi(1 << 19, 32, seed=205))]
+    net, data = sw.train(0, seed=3, graphs=train_graphs, roots_per_graph=4)
+    X, y, w = data.labels()
+    assert np.mean((net.predict(X) > 0) == (y > 0.5)) > 0.8
+    held = [("rmat20b", gg.rmat(20, seed=301)), ("rmat21sym", gg.rmat(21, seed=302, symmetric=True)),
+            ("er19_d16", gg.erdos_renyi(1 << 19, 16, seed=303))]
+    report = sw.evaluate(net, 0, graphs=held, roots_per_graph=4)
+    thr = sum(r["edge"]["threshold_ms"] for r in report.values())
+    learned = sum(r["edge"]["learned_ms"] for r in report.values())
+    best = sum(r["edge"]["best_ms"] for r in report.values())
+    print("edge ms: threshold %.3f learned %.3f best %.3f" % (thr, learned, best))
+    for name, r in report.items():
+        print(name, r["edge"], r["bfs"]["threshold_ms"], r["bfs"]["learned_ms"])
+        assert r["bfs"]["identical_results"] and r["cc"]["identical_results"], name
+    assert learned <= thr
+    assert learned <= 1.15 * best

@@ -72,6 +72,7 @@ static void free_graph_data(grz_graph* g)
     g->pr_fx[0] = g->pr_fx[1] = nullptr; g->pr_sum = nullptr; g->pr_K = nullptr; g->pr_rowacc = nullptr;
     g->prop = nullptr; g->accum = nullptr; g->glob = nullptr; g->scratch = nullptr;
     g->scratch_bytes = 0;
+    g->max_degree_known = 0;
     g->V = g->E = 0;
 }
 
@@ -433,22 +434,32 @@ extern "C" int grz_read_props(grz_graph* g, double* host, uint64_t cap)
 // ---------------------------------------------------------------------------------------------
 // Connected Components and BFS
 
+// One CC/BFS run to convergence.  By default the whole loop is one CUDA graph launch
+// (grz_frontier_run_graph); GRZ_FLAG_HOST_LOOP, profiling, or a graph without both lists run
+// it with one host round trip per iteration (grz_frontier_step).  Both give the same
+// iterations, engines and results.
 static int frontier_run(grz_graph* g, int app, uint32_t root, int flags, grz_run_stats_t* stats)
 {
     if (!g) return GRZ_ERR_ARG;
     GRZ_CK(g, cudaSetDevice(g->device));
     g->app = app;
+    const bool graph = !(flags & GRZ_FLAG_HOST_LOOP) && !g->prof && g->pull.nvec && g->push.nvec;
+    if (graph) grz_frontier_run_prepare(g);
     int rc = grz_frontier_init(g, app, flags, root);
     if (rc) return rc;
     cudaEvent_t e0, e1;
     GRZ_CK(g, cudaEventCreate(&e0));
     GRZ_CK(g, cudaEventCreate(&e1));
     cudaEventRecord(e0, g->stream);
-    for (;;) {
-        int engine = -1;
-        uint64_t vote = 0;
-        rc = grz_frontier_step(g, -1, &engine, &vote);
-        if (rc <= 0) break;
+    if (graph) {
+        rc = grz_frontier_run_graph(g, nullptr);
+    } else {
+        for (;;) {
+            int engine = -1;
+            uint64_t vote = 0;
+            rc = grz_frontier_step(g, -1, &engine, &vote);
+            if (rc <= 0) break;
+        }
     }
     cudaEventRecord(e1, g->stream);
     if (rc == 0) rc = grz_cuda_check(g, cudaEventSynchronize(e1), "run");

@@ -31,6 +31,8 @@
 //     A vertex's BFS level is the iteration that visits it, so levels are exact by construction.
 #include <string.h>
 
+#include <algorithm>
+
 #include "grz_internal.cuh"
 
 namespace {
@@ -353,12 +355,14 @@ __global__ void __launch_bounds__(T) k_push_expand(const uint32_t* __restrict__ 
 template <bool FromPull>
 __global__ void __launch_bounds__(T) k_bfs_visit(const uint32_t* __restrict__ touched, const uint32_t* __restrict__ ntouched,
                                                  unsigned long long* __restrict__ cand64, uint32_t* __restrict__ cand32,
-                                                 uint32_t* __restrict__ parent, uint32_t* __restrict__ level, uint32_t iter,
+                                                 uint32_t* __restrict__ parent, uint32_t* __restrict__ level, uint32_t iter_host,
+                                                 const uint32_t* __restrict__ iter_dev,
                                                  unsigned long long* __restrict__ wants, unsigned long long* __restrict__ has_next,
                                                  VoteCfg vc, unsigned long long* __restrict__ vote)
 {
     __shared__ unsigned long long red[T / 32];
     const uint32_t n = *ntouched;
+    const uint32_t iter = iter_dev ? *iter_dev : iter_host;
     unsigned long long my_vote = 0;
     for (uint32_t i = blockIdx.x * T + threadIdx.x; i < n; i += gridDim.x * T) {
         const uint32_t d = touched[i];
@@ -559,7 +563,7 @@ static int edge_phase(grz_graph* g, int pull, uint64_t first, uint64_t count)
             k_bfs_pull<<<blocks_for(count), T, 0, st>>>(g->pull.nbr, g->pull.shared, first, count, V, f.has, f.wants, f.cand64,
                                                        f.touched, f.counters + 1); GRZ_COUNT_LAUNCH(g);
             k_bfs_visit<true><<<g->num_sms * 4, T, 0, st>>>(f.touched, f.counters + 1, f.cand64, f.cand32, f.label, f.level,
-                                                            f.iter, f.wants, f.has_next, vc, f.vote); GRZ_COUNT_LAUNCH(g);
+                                                            f.iter, f.level_dev, f.wants, f.has_next, vc, f.vote); GRZ_COUNT_LAUNCH(g);
         } else {
             k_cc_pull<<<blocks_for(count), T, 0, st>>>(g->pull.nbr, g->pull.shared, first, count, V, f.label, f.has_next, vc, f.vote); GRZ_COUNT_LAUNCH(g);
         }
@@ -577,7 +581,7 @@ static int edge_phase(grz_graph* g, int pull, uint64_t first, uint64_t count)
             k_push_expand<true><<<grid, T, 0, st>>>(f.frontier, f.voff, f.vdelta, f.tile_first, f.counters, g->push.nbr, V, f.label,
                                                     f.has_next, f.wants, f.cand32, f.touched, f.counters + 1, vc, f.vote); GRZ_COUNT_LAUNCH(g);
             k_bfs_visit<false><<<g->num_sms * 4, T, 0, st>>>(f.touched, f.counters + 1, f.cand64, f.cand32, f.label, f.level,
-                                                             f.iter, f.wants, f.has_next, vc, f.vote); GRZ_COUNT_LAUNCH(g);
+                                                             f.iter, f.level_dev, f.wants, f.has_next, vc, f.vote); GRZ_COUNT_LAUNCH(g);
         } else {
             k_push_expand<false><<<grid, T, 0, st>>>(f.frontier, f.voff, f.vdelta, f.tile_first, f.counters, g->push.nbr, V, f.label,
                                                      f.has_next, f.wants, f.cand32, f.touched, f.counters + 1, vc, f.vote); GRZ_COUNT_LAUNCH(g);
@@ -636,7 +640,8 @@ int grz_frontier_step(grz_graph* g, int engine, int* engine_out, uint64_t* vote_
         rc = grz_switch_decide(g, f.has, f.vote_host, 1, &v0, &f.next_pull, f.last_features);
         if (rc) return rc;
     }
-    const int pull = engine >= 0 ? engine : (learned ? f.next_pull : grz_engine_threshold(g, f.vote_host));
+    const bool forced = (f.flags & (GRZ_FLAG_FORCE_PULL | GRZ_FLAG_FORCE_PUSH)) != 0;
+    const int pull = engine >= 0 ? engine : ((learned && !forced) ? f.next_pull : grz_engine_threshold(g, f.vote_host));
     if (engine_out) *engine_out = pull;
     GRZ_CK(g, cudaMemsetAsync(f.vote, 0, sizeof(unsigned long long) * GRZ_VOTE_SLOTS * GRZ_VOTE_STRIDE, g->stream));
     f.iter++;
@@ -705,9 +710,215 @@ void grz_frontier_free(grz_graph* g)
     for (void* p : ptrs) cudaFree(p);
     if (f.ev[0]) { cudaEventDestroy(f.ev[0]); cudaEventDestroy(f.ev[1]); }
     if (f.mail) cudaFreeHost(f.mail);
+    if (f.run_exec) cudaGraphExecDestroy(f.run_exec);
+    cudaFree(f.ctl);
     grz_mlp* keep_mlp = f.mlp;
     const int keep_policy = f.policy;
     memset(&f, 0, sizeof(f));
     f.mlp = keep_mlp;
     f.policy = keep_policy;
+}
+
+// ---------------------------------------------------------------------------------------------
+// A whole CC/BFS run as one CUDA graph.
+//
+//   k_run_decide (initial: sets pull0/push0)  ->  WHILE (loop) {
+//       IF (pull0) { pull edge phase, even roles }   IF (push0) { push edge phase, even roles }
+//       k_run_decide (next HasInfo = B, clears A; sets pull1/push1, loop)
+//       IF (pull1) { pull edge phase, odd roles }    IF (push1) { push edge phase, odd roles }
+//       k_run_decide (next HasInfo = A, clears B; sets pull0/push0, loop)
+//   }
+//
+// Even iterations read HasInfo from buffer A and write HasInfo* into B; odd ones the reverse,
+// which is the reference's pointer swap (source/execution_cc.c:245-250) without a host step.
+// The decision kernel sets the conditional handles, so the engine choice, the convergence test
+// and the iteration count never leave the device: one launch, one read-back of the control
+// block.  The iterations, engines and results are those of the host loop (grz_frontier_step).
+
+static int capture_begin(grz_graph* g, cudaStream_t cs, cudaGraph_t graph, const cudaGraphNode_t* deps, size_t ndeps)
+{
+    GRZ_CK(g, cudaStreamBeginCaptureToGraph(cs, graph, deps, nullptr, ndeps, cudaStreamCaptureModeThreadLocal));
+    return GRZ_OK;
+}
+
+// ends a capture into an existing graph; *sink = the captured work's last node
+static int capture_end(grz_graph* g, cudaStream_t cs, cudaGraphNode_t* sink)
+{
+    cudaStreamCaptureStatus st;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t n = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(cs, &st, nullptr, nullptr, &deps, nullptr, &n);
+    cudaGraphNode_t last = (e == cudaSuccess && n == 1) ? deps[0] : nullptr;
+    cudaGraph_t out = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(cs, &out);
+    if (e != cudaSuccess) return grz_cuda_check(g, e, "capture info");
+    if (e2 != cudaSuccess) return grz_cuda_check(g, e2, "end capture");
+    if (sink) {
+        if (!last) return grz_set_error(g, GRZ_ERR_STATE, "captured work does not end in one node");
+        *sink = last;
+    }
+    return GRZ_OK;
+}
+
+static int add_conditional(grz_graph* g, cudaGraph_t graph, const cudaGraphNode_t* deps, size_t ndeps, cudaGraphConditionalHandle h,
+                           cudaGraphConditionalNodeType type, cudaGraphNode_t* node, cudaGraph_t* body)
+{
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = type;
+    p.conditional.size = 1;
+    GRZ_CK(g, cudaGraphAddNode(node, graph, deps, nullptr, ndeps, &p));
+    *body = p.conditional.phGraph_out[0];
+    return GRZ_OK;
+}
+
+static int build_run_graph(grz_graph* g)
+{
+    grz_frontier_state& f = g->fr;
+    if (f.run_exec) {
+        cudaGraphExecDestroy(f.run_exec);
+        f.run_exec = nullptr;
+    }
+    unsigned long long* A = f.has;
+    unsigned long long* B = f.has_next;
+    cudaStream_t user = g->stream;
+    cudaStream_t cs = nullptr;
+    GRZ_CK(g, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t top = nullptr;
+    int rc = grz_cuda_check(g, cudaGraphCreate(&top, 0), "graph create");
+    // one handle per conditional node: the loop, and pull / push for the even and odd halves
+    cudaGraphConditionalHandle hloop = 0, hpull[2] = { 0, 0 }, hpush[2] = { 0, 0 };
+    if (!rc) rc = grz_cuda_check(g, cudaGraphConditionalHandleCreate(&hloop, top, 1, cudaGraphCondAssignDefault), "handle");
+    for (int p = 0; p < 2 && !rc; ++p) {
+        rc = grz_cuda_check(g, cudaGraphConditionalHandleCreate(&hpull[p], top, 0, cudaGraphCondAssignDefault), "handle");
+        if (!rc) rc = grz_cuda_check(g, cudaGraphConditionalHandleCreate(&hpush[p], top, 0, cudaGraphCondAssignDefault), "handle");
+    }
+    g->stream = cs;
+    f.level_dev = &f.ctl->level;
+    cudaGraphNode_t n0 = nullptr, wnode = nullptr;
+    cudaGraph_t body = nullptr;
+    if (!rc) rc = capture_begin(g, cs, top, nullptr, 0);
+    if (!rc) {
+        rc = grz_switch_launch_run_decide(g, A, nullptr, 1, hloop, hpull[0], hpush[0]);
+        const int rc2 = capture_end(g, cs, &n0);
+        if (!rc) rc = rc2;
+    }
+    if (!rc) rc = add_conditional(g, top, &n0, 1, hloop, cudaGraphCondTypeWhile, &wnode, &body);
+    cudaGraphNode_t prev = nullptr;
+    for (int parity = 0; parity < 2 && !rc; ++parity) {
+        f.has = parity ? B : A;
+        f.has_next = parity ? A : B;
+        cudaGraphNode_t npull = nullptr, npush = nullptr, ndec = nullptr;
+        cudaGraph_t bpull = nullptr, bpush = nullptr;
+        rc = add_conditional(g, body, prev ? &prev : nullptr, prev ? 1 : 0, hpull[parity], cudaGraphCondTypeIf, &npull, &bpull);
+        if (!rc) rc = capture_begin(g, cs, bpull, nullptr, 0);
+        if (!rc) {
+            rc = edge_phase(g, 1, 0, g->pull.nvec);
+            const int rc2 = capture_end(g, cs, nullptr);
+            if (!rc) rc = rc2;
+        }
+        if (!rc) rc = add_conditional(g, body, &npull, 1, hpush[parity], cudaGraphCondTypeIf, &npush, &bpush);
+        if (!rc) rc = capture_begin(g, cs, bpush, nullptr, 0);
+        if (!rc) {
+            rc = edge_phase(g, 0, 0, g->push.nvec);
+            const int rc2 = capture_end(g, cs, nullptr);
+            if (!rc) rc = rc2;
+        }
+        if (!rc) rc = capture_begin(g, cs, body, &npush, 1);
+        if (!rc) {
+            // decides the other half's engine
+            rc = grz_switch_launch_run_decide(g, f.has_next, f.has, 0, hloop, hpull[1 - parity], hpush[1 - parity]);
+            const int rc2 = capture_end(g, cs, &ndec);
+            if (!rc) rc = rc2;
+        }
+        prev = ndec;
+    }
+    f.has = A;
+    f.has_next = B;
+    f.level_dev = nullptr;
+    g->stream = user;
+    if (!rc) rc = grz_cuda_check(g, cudaGraphInstantiate(&f.run_exec, top, 0), "graph instantiate");
+    if (top) cudaGraphDestroy(top);
+    cudaStreamDestroy(cs);
+    if (rc) {
+        f.run_exec = nullptr;
+        return rc;
+    }
+    f.run_bm[0] = A;
+    f.run_bm[1] = B;
+    f.run_key[0] = f.app;
+    f.run_key[1] = f.flags;
+    return GRZ_OK;
+}
+
+// Before grz_frontier_init: puts the HasInfo buffers back in the roles the cached graph has.
+void grz_frontier_run_prepare(grz_graph* g)
+{
+    grz_frontier_state& f = g->fr;
+    if (f.run_exec && f.has == f.run_bm[1] && f.has_next == f.run_bm[0]) {
+        f.has = f.run_bm[0];
+        f.has_next = f.run_bm[1];
+    }
+}
+
+// Runs the initialised CC/BFS state to convergence with one graph launch.  *launches: kernels
+// the graph ran.
+int grz_frontier_run_graph(grz_graph* g, uint64_t* launches)
+{
+    grz_frontier_state& f = g->fr;
+    if (!f.label) return grz_set_error(g, GRZ_ERR_STATE, "frontier state not initialised");
+    if (!g->pull.nbr || !g->push.nbr || !g->pull.nvec || !g->push.nvec)
+        return grz_set_error(g, GRZ_ERR_STATE, "the graph run needs both edge lists");
+    int rc = grz_frontier_mail(g);
+    if (rc) return rc;
+    if (!f.ctl) {
+        GRZ_CK(g, cudaMalloc((void**)&f.ctl, sizeof(grz_runctl)));
+    }
+    rc = grz_switch_max_degree(g);
+    if (rc) return rc;
+    const bool same = f.run_exec && f.run_bm[0] == f.has && f.run_bm[1] == f.has_next && f.run_key[0] == f.app &&
+                      f.run_key[1] == f.flags;
+    if (!same) {
+        rc = build_run_graph(g);
+        if (rc) return rc;
+    }
+    grz_runctl c;
+    memset(&c, 0, sizeof(c));
+    c.running = 1;
+    c.level = f.iter + 1;
+    c.last_engine = (uint32_t)f.last_engine;
+    c.vote = f.vote_host;
+    c.max_level = (uint32_t)std::min<uint64_t>(g->V + 2, 0xfffffff0ull) + f.iter;
+    c.limit_ns = 300ull * 1000000000ull;
+    grz_switch_policy_ctl(g, &c);
+    memcpy(f.mail, &c, sizeof(c));
+    GRZ_CK(g, cudaMemcpyAsync(f.ctl, f.mail, sizeof(c), cudaMemcpyHostToDevice, g->stream));
+    GRZ_CK(g, cudaMemsetAsync(f.vote, 0, sizeof(unsigned long long) * GRZ_VOTE_SLOTS * GRZ_VOTE_STRIDE, g->stream));
+    GRZ_CK(g, cudaGraphLaunch(f.run_exec, g->stream));
+    GRZ_CK(g, cudaMemcpyAsync(f.mail, f.ctl, sizeof(c), cudaMemcpyDeviceToHost, g->stream));
+    GRZ_CK(g, cudaStreamSynchronize(g->stream));
+    memcpy(&c, f.mail, sizeof(c));
+    if (c.overrun == 1) return grz_set_error(g, GRZ_ERR_STATE, "no convergence within %u iterations", c.max_level);
+    if (c.overrun) return grz_set_error(g, GRZ_ERR_STATE, "run stopped by its time bound");
+    const uint32_t n = c.npull + c.npush;
+    f.iter += n;
+    f.npull += c.npull;
+    f.npush += c.npush;
+    f.vote_host = c.vote;
+    f.last_engine = (int)c.last_engine;
+    f.next_pull = (int)c.engine;
+    memcpy(f.last_features, c.features, sizeof(f.last_features));
+    // iteration k (1-based within the launch) read HasInfo from A when k is odd
+    if (n % 2 == 0 && n > 0) {
+        unsigned long long* t = f.has;
+        f.has = f.has_next;
+        f.has_next = t;
+    }
+    const bool bfs = f.app == GRZ_APP_BREADTH_FIRST_SEARCH;
+    const uint64_t per_pull = bfs ? 2 : 1, per_push = bfs ? 5 : 4;
+    uint64_t k = 1 + n + (uint64_t)c.npull * per_pull + (uint64_t)c.npush * per_push + (n % 2);
+    g->nlaunch += k;
+    if (launches) *launches = k;
+    return GRZ_OK;
 }

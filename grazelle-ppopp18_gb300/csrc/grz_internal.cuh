@@ -190,6 +190,7 @@ struct grz_prof;
 #define GRZ_FLAG_FORCE_PUSH 2       // EXPERIMENT_EDGE_FORCE_PUSH
 #define GRZ_FLAG_WITHOUT_COUNT 4    // EXPERIMENT_THRESHOLD_WITHOUT_COUNT
 #define GRZ_FLAG_WITHOUT_OUTDEG 8   // EXPERIMENT_THRESHOLD_WITHOUT_OUTDEGREES
+#define GRZ_FLAG_HOST_LOOP 16       // run the iteration loop on the host
 
 // the vote is added into GRZ_VOTE_SLOTS counters, 128 bytes apart (block mod slots)
 #define GRZ_VOTE_SLOTS 64
@@ -202,6 +203,30 @@ struct grz_prof;
 #define GRZ_POLICY_THRESHOLD 0
 #define GRZ_POLICY_LEARNED 1
 struct grz_mlp;
+
+// Device control block of a CC/BFS run executed as one CUDA graph (grz_ccbfs.cu): the
+// decision kernel at the end of each iteration updates it and sets the graph's conditional
+// handles.  The host writes it before the launch and reads it after.
+struct grz_runctl {
+    unsigned long long vote;         // vote of the last iteration
+    unsigned long long cnt_f;        // popcount accumulators of the decision kernel (zero between uses)
+    unsigned long long cnt_u;
+    unsigned long long ticket;       // last-block ticket of the decision kernel (zero between uses)
+    uint32_t running;                // 1 until an iteration ends with vote 0
+    uint32_t engine;                 // engine of the iteration about to run: 1 pull, 0 push
+    uint32_t level;                  // number of the iteration about to run (1-based) = BFS level
+    uint32_t npull, npush;
+    uint32_t last_engine;
+    uint32_t max_level;              // iteration bound: the run stops with `overrun` = 1 beyond it
+    uint32_t overrun;                // 2: stopped by the time bound
+    unsigned long long t0_ns;        // %globaltimer at the initial decision
+    unsigned long long limit_ns;     // time bound of the run
+    // the engine policy, read at run time so that one captured graph serves every policy
+    const float* params;             // MLP parameters (learned policy) or null
+    double threshold;                // vote threshold (E/5 or V/2)
+    int32_t force;                   // 1 pull, 0 push, -1 the policy decides
+    float features[GRZ_MLP_FEATURES];
+};
 
 // CC / BFS state (grz_ccbfs.cu)
 struct grz_frontier_state {
@@ -235,6 +260,12 @@ struct grz_frontier_state {
     float last_edge_ms;              // edge-phase time of the last step when timing is on
     int time_edges;
     cudaEvent_t ev[2];
+    // the run as one CUDA graph (WHILE over two iterations with IF nodes per engine)
+    grz_runctl* ctl;                 // device
+    const uint32_t* level_dev;       // set while capturing: BFS level read from ctl->level
+    cudaGraphExec_t run_exec;
+    unsigned long long* run_bm[2];   // the HasInfo buffers in the graph's even-iteration roles
+    int run_key[2];                  // app, flags of the captured graph
     // snapshot for timing both engines from one state
     void* snap;
     uint64_t snap_bytes;
@@ -337,6 +368,12 @@ int grz_frontier_props(grz_graph* g);
 int grz_engine_threshold(const grz_graph* g, uint64_t vote);
 int grz_read_vote(grz_graph* g, uint64_t* out);
 int grz_frontier_mail(grz_graph* g);
+int grz_frontier_run_graph(grz_graph* g, uint64_t* launches);
+void grz_frontier_run_prepare(grz_graph* g);
+int grz_switch_max_degree(grz_graph* g);
+void grz_switch_policy_ctl(grz_graph* g, grz_runctl* c);
+int grz_switch_launch_run_decide(grz_graph* g, const unsigned long long* next_frontier, unsigned long long* clear_bm, int initial,
+                                 unsigned long long hloop, unsigned long long hpull, unsigned long long hpush);
 // learned switch: features of a state + the policy's decision; frontier = HasInfo of the
 // iteration the decision is for; vote_override = ~0 to read the vote slots
 int grz_switch_decide(grz_graph* g, const unsigned long long* frontier, uint64_t vote_override, uint32_t iter,

@@ -78,6 +78,26 @@ struct FeatIn {
 // ticket, then NF floats.  Words 2-4 are zero between calls.
 constexpr int SW_U64 = 5;
 
+// MLP forward pass of one sample by one warp, lane j computing hidden unit j.  Same operation
+// order as mlp_forward, so the logit equals grz_mlp_predict's.  f: NF features, h: NH scratch
+// (both shared); every lane returns the logit.
+__device__ float mlp_logit_warp(const float* params, const float* f, float* h, int lane)
+{
+    float s = params[OFF_B1 + lane];
+    for (int k = 0; k < NF; ++k) s = fmaf(params[OFF_W1 + lane * NF + k], f[k], s);
+    h[lane] = relu(s);
+    __syncwarp();
+    s = params[OFF_B2 + lane];
+    for (int k = 0; k < NH; ++k) s = fmaf(params[OFF_W2 + lane * NH + k], h[k], s);
+    __syncwarp();
+    h[lane] = relu(s);
+    __syncwarp();
+    float z = params[OFF_B3];
+    for (int k = 0; k < NH; ++k) z = fmaf(params[OFF_W3 + k], h[k], z);
+    __syncwarp();
+    return z;
+}
+
 // feature k of the state (lane k computes it)
 __device__ float feature(int k, const FeatIn& in, float F, float U, float vote)
 {
@@ -110,6 +130,7 @@ __global__ void __launch_bounds__(T) k_features_decide(FeatIn in, const float* _
     __shared__ bool s_last;
     __shared__ float f[NF];
     __shared__ float h[NH];
+    __shared__ float sp[NP];
     unsigned pf = 0, pw = 0;
     for (uint64_t w = (uint64_t)blockIdx.x * T + threadIdx.x; w < in.words; w += (uint64_t)gridDim.x * T) {
         pf += __popcll(in.frontier[w]);
@@ -143,18 +164,9 @@ __global__ void __launch_bounds__(T) k_features_decide(FeatIn in, const float* _
     __syncwarp();
     int pull;
     if (use_mlp) {
-        float s = params[OFF_B1 + lane];
-        for (int k = 0; k < NF; ++k) s = fmaf(params[OFF_W1 + lane * NF + k], f[k], s);
-        h[lane] = relu(s);
+        for (int i = lane; i < NP; i += 32) sp[i] = params[i];  // coalesced, then the forward from shared memory
         __syncwarp();
-        s = params[OFF_B2 + lane];
-        for (int k = 0; k < NH; ++k) s = fmaf(params[OFF_W2 + lane * NH + k], h[k], s);
-        __syncwarp();
-        h[lane] = relu(s);
-        __syncwarp();
-        float z = params[OFF_B3];
-        for (int k = 0; k < NH; ++k) z = fmaf(params[OFF_W3 + k], h[k], z);
-        pull = z > 0.f ? 1 : 0;
+        pull = mlp_logit_warp(sp, f, h, lane) > 0.f ? 1 : 0;
     } else {
         pull = (double)vote > threshold ? 1 : 0;
     }
@@ -165,6 +177,117 @@ __global__ void __launch_bounds__(T) k_features_decide(FeatIn in, const float* _
         out[2] = 0;
         out[3] = 0;
         out[4] = 0;
+    }
+}
+
+// The decision at the end of an iteration of a CC/BFS run executed as one CUDA graph.
+// Grid-wide: popcounts of the next frontier and WantsInfo; clears the old HasInfo (the
+// reference's vertex phase after the pointer swap, source/phase_vertex_cc.asm:37-46).  The
+// last block: the vote (sum of the slots, which it re-zeroes), convergence (vote 0), the
+// iteration bound, the run statistics, the next engine (forced, threshold or MLP), and the
+// graph's conditional handles: hpull / hpush select the next iteration's engine body, hloop
+// keeps the WHILE node going.  `initial`: the decision before the first iteration, from the
+// starting vote; no statistics, no clearing.
+struct RunIn {
+    FeatIn feat;                        // frontier = the next HasInfo
+    unsigned long long* vote_slots;     // read and re-zeroed
+    unsigned long long* clear_bm;       // old HasInfo (null when initial)
+    int initial;
+};
+
+__global__ void __launch_bounds__(T) k_run_decide(RunIn in, grz_runctl* __restrict__ ctl, cudaGraphConditionalHandle hloop,
+                                                  cudaGraphConditionalHandle hpull, cudaGraphConditionalHandle hpush)
+{
+    __shared__ unsigned s_pf[T / 32], s_pw[T / 32];
+    __shared__ bool s_last;
+    __shared__ float f[NF];
+    __shared__ float h[NH];
+    __shared__ float sp[NP];
+    if (!in.initial && !*(volatile uint32_t*)&ctl->running) return;
+    const FeatIn& fi = in.feat;
+    unsigned pf = 0, pw = 0;
+    for (uint64_t w = (uint64_t)blockIdx.x * T + threadIdx.x; w < fi.words; w += (uint64_t)gridDim.x * T) {
+        pf += __popcll(fi.frontier[w]);
+        if (fi.app_bfs) pw += __popcll(fi.wants[w]);
+        if (in.clear_bm) in.clear_bm[w] = 0ull;
+    }
+    pf = __reduce_add_sync(0xffffffffu, pf);
+    pw = __reduce_add_sync(0xffffffffu, pw);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) { s_pf[warp] = pf; s_pw[warp] = pw; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long bf = 0, bw = 0;
+        for (int i = 0; i < T / 32; ++i) { bf += s_pf[i]; bw += s_pw[i]; }
+        if (bf) atomicAdd(&ctl->cnt_f, bf);
+        if (bw) atomicAdd(&ctl->cnt_u, bw);
+        __threadfence();
+        s_last = atomicAdd(&ctl->ticket, 1ull) == (unsigned long long)(gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last || warp != 0) return;
+    __threadfence();
+    const unsigned long long F = *(volatile unsigned long long*)&ctl->cnt_f;
+    const unsigned long long U = *(volatile unsigned long long*)&ctl->cnt_u;
+    unsigned long long vote = ctl->vote;  // initial: the starting vote, written by the host
+    if (!in.initial) {
+        unsigned long long* a = in.vote_slots + lane * GRZ_VOTE_STRIDE;
+        unsigned long long* b = in.vote_slots + (lane + 32) * GRZ_VOTE_STRIDE;
+        unsigned long long vs = *(volatile unsigned long long*)a + *(volatile unsigned long long*)b;
+        *a = 0ull;
+        *b = 0ull;
+        for (int o = 16; o > 0; o >>= 1) vs += __shfl_down_sync(0xffffffffu, vs, o);
+        vote = __shfl_sync(0xffffffffu, vs, 0);
+    }
+    uint32_t level = ctl->level;
+    const uint32_t ran = ctl->engine;
+    uint32_t last_engine = ctl->last_engine;
+    uint32_t running = 1, overrun = 0;
+    unsigned long long now;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+    if (!in.initial) {
+        last_engine = ran;
+        running = vote != 0ull;
+        if (running) {
+            ++level;
+            if (level > ctl->max_level) { running = 0; overrun = 1; }
+            if (now - ctl->t0_ns > ctl->limit_ns) { running = 0; overrun = 2; }
+        }
+    }
+    FeatIn fe = fi;
+    fe.iter = level;
+    fe.last_engine = (int)last_engine;
+    if (lane < NF) f[lane] = feature(lane, fe, (float)F, (float)U, (float)vote);
+    __syncwarp();
+    int pull;
+    const float* params = ctl->params;
+    if (ctl->force >= 0) {
+        pull = ctl->force;
+    } else if (params) {
+        for (int i = lane; i < NP; i += 32) sp[i] = params[i];  // coalesced, then the forward from shared memory
+        __syncwarp();
+        pull = mlp_logit_warp(sp, f, h, lane) > 0.f ? 1 : 0;
+    } else {
+        pull = (double)vote > ctl->threshold ? 1 : 0;
+    }
+    if (lane < NF) ctl->features[lane] = f[lane];
+    if (lane == 0) {
+        if (!in.initial) {
+            if (ran) ctl->npull += 1; else ctl->npush += 1;
+        }
+        if (in.initial) ctl->t0_ns = now;
+        ctl->vote = vote;
+        ctl->running = running;
+        ctl->engine = (uint32_t)pull;
+        ctl->level = level;
+        ctl->last_engine = last_engine;
+        ctl->overrun |= overrun;
+        ctl->cnt_f = 0ull;
+        ctl->cnt_u = 0ull;
+        ctl->ticket = 0ull;
+        cudaGraphSetConditional(hpull, running && pull ? 1u : 0u);
+        cudaGraphSetConditional(hpush, running && !pull ? 1u : 0u);
+        cudaGraphSetConditional(hloop, running);
     }
 }
 
@@ -380,6 +503,37 @@ extern "C" int grz_mlp_train(grz_mlp* n, const float* X, const float* Y, const f
 // ---------------------------------------------------------------------------------------------
 // engine policy inside the CC/BFS step
 
+__global__ void __launch_bounds__(T) k_max_u32(const uint32_t* __restrict__ a, uint64_t n, unsigned* __restrict__ out)
+{
+    unsigned m = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * T + threadIdx.x; i < n; i += (uint64_t)gridDim.x * T) m = max(m, a[i]);
+    m = __reduce_max_sync(0xffffffffu, m);
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
+// the largest degree (a feature), computed once per loaded graph
+int grz_switch_max_degree(grz_graph* g)
+{
+    if (g->max_degree_known) return GRZ_OK;
+    int rc = grz_frontier_mail(g);
+    if (rc) return rc;
+    unsigned* d = nullptr;
+    GRZ_CK(g, cudaMallocAsync((void**)&d, sizeof(unsigned), g->stream));
+    cudaError_t e = cudaMemsetAsync(d, 0, sizeof(unsigned), g->stream);
+    if (e == cudaSuccess && g->V) {
+        const unsigned grid = (unsigned)std::min<uint64_t>((g->V + T - 1) / T, (uint64_t)g->num_sms * 4);
+        k_max_u32<<<grid, T, 0, g->stream>>>(g->degree, g->V, d); GRZ_COUNT_LAUNCH(g);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(g->fr.mail, d, sizeof(unsigned), cudaMemcpyDeviceToHost, g->stream);
+    cudaFreeAsync(d, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) return grz_cuda_check(g, e, "max degree");
+    g->max_degree = *(const unsigned*)g->fr.mail;
+    g->max_degree_known = 1;
+    return GRZ_OK;
+}
+
 int grz_switch_decide(grz_graph* g, const unsigned long long* frontier, uint64_t vote_override, uint32_t iter,
                       uint64_t* vote, int* next_pull, float* features)
 {
@@ -389,18 +543,8 @@ int grz_switch_decide(grz_graph* g, const unsigned long long* frontier, uint64_t
         GRZ_CK(g, cudaMemsetAsync(f.sw_out, 0, sizeof(unsigned long long) * SW_U64, g->stream));
     }
     int rc = grz_frontier_mail(g);
+    if (!rc) rc = grz_switch_max_degree(g);
     if (rc) return rc;
-    if (!g->max_degree_known) {
-        uint32_t* tmp = (uint32_t*)malloc(sizeof(uint32_t) * (g->V ? g->V : 1));
-        if (!tmp) return GRZ_ERR_NOMEM;
-        cudaError_t e = cudaMemcpy(tmp, g->degree, sizeof(uint32_t) * g->V, cudaMemcpyDeviceToHost);
-        if (e != cudaSuccess) { free(tmp); return grz_cuda_check(g, e, "degrees"); }
-        uint32_t mx = 0;
-        for (uint64_t v = 0; v < g->V; ++v) mx = tmp[v] > mx ? tmp[v] : mx;
-        free(tmp);
-        g->max_degree = mx;
-        g->max_degree_known = 1;
-    }
     FeatIn in;
     in.frontier = frontier;
     in.vote_override = vote_override;
@@ -429,6 +573,31 @@ int grz_switch_decide(grz_graph* g, const unsigned long long* frontier, uint64_t
     *next_pull = (int)o[1];
     if (features) memcpy(features, host + sizeof(o), sizeof(float) * NF);
     return GRZ_OK;
+}
+
+// Launches k_run_decide on the graph's stream (called while capturing the run graph).  The
+// policy is not captured: the host writes it into the control block before each launch.
+int grz_switch_launch_run_decide(grz_graph* g, const unsigned long long* next_frontier, unsigned long long* clear_bm, int initial,
+                                 unsigned long long hloop, unsigned long long hpull, unsigned long long hpush)
+{
+    grz_frontier_state& f = g->fr;
+    RunIn in;
+    memset(&in, 0, sizeof(in));
+    in.feat.frontier = next_frontier;
+    in.feat.vote_override = 0;
+    in.feat.wants = f.wants;
+    in.feat.vote_slots = f.vote;
+    in.feat.words = (g->V >> 6) + 2;
+    in.feat.V = (double)(g->V ? g->V : 1);
+    in.feat.E = (double)(g->E ? g->E : 1);
+    in.feat.max_degree = (double)g->max_degree;
+    in.feat.app_bfs = f.app == GRZ_APP_BREADTH_FIRST_SEARCH;
+    in.vote_slots = f.vote;
+    in.clear_bm = clear_bm;
+    in.initial = initial;
+    const unsigned grid = (unsigned)std::min<uint64_t>((in.feat.words + T - 1) / T, (uint64_t)g->num_sms * 2);
+    k_run_decide<<<grid, T, 0, g->stream>>>(in, f.ctl, hloop, hpull, hpush);
+    return grz_cuda_check(g, cudaGetLastError(), "run decision");
 }
 
 extern "C" int grz_frontier_set_policy(grz_graph* g, int policy, grz_mlp* mlp)
@@ -518,4 +687,13 @@ extern "C" int grz_frontier_next_timed(grz_graph* g, int engine, int* engine_use
     f.time_edges = 0;
     if (rc >= 0 && edge_ms) *edge_ms = f.last_edge_ms;
     return rc;
+}
+
+// the policy fields of the run control block for the current frontier state
+void grz_switch_policy_ctl(grz_graph* g, grz_runctl* c)
+{
+    const grz_frontier_state& f = g->fr;
+    c->force = (f.flags & GRZ_FLAG_FORCE_PULL) ? 1 : ((f.flags & GRZ_FLAG_FORCE_PUSH) ? 0 : -1);
+    c->params = (f.policy == GRZ_POLICY_LEARNED && f.mlp) ? f.mlp->params : nullptr;
+    c->threshold = (f.flags & GRZ_FLAG_WITHOUT_OUTDEG) ? (double)(g->V / 2) : (double)(g->E / 5);
 }

@@ -27,6 +27,7 @@ class GrzError(RuntimeError):
 
 
 FORCE_PULL, FORCE_PUSH, WITHOUT_COUNT, WITHOUT_OUTDEG = 1, 2, 4, 8
+FLAG_HOST_LOOP = 16  # grz_cc_run / grz_bfs_run: host round trip per iteration instead of one CUDA graph
 MLP_FEATURES, MLP_HIDDEN, MLP_PARAMS = 12, 32, 1505
 POLICY_THRESHOLD, POLICY_LEARNED = 0, 1
 

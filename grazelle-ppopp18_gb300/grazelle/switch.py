@@ -213,6 +213,7 @@ def compare_runs(G: Graph, app: int, roots, net: Switch, repeats: int = 1) -> di
     it_thr, it_mlp = [], []
     for r in roots:
         run_time(G, app, r, native.POLICY_THRESHOLD, None)
+        run_time(G, app, r, native.POLICY_LEARNED, net)
         for _ in range(repeats):
             t, it = run_time(G, app, r, native.POLICY_THRESHOLD, None)
             thr += t

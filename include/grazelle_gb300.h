@@ -110,6 +110,7 @@ int grz_pr_time_iterations(grz_graph* g, uint32_t iterations, float* ms_out);
 #define GRZ_FLAG_FORCE_PUSH 2       /* EXPERIMENT_EDGE_FORCE_PUSH */
 #define GRZ_FLAG_WITHOUT_COUNT 4    /* EXPERIMENT_THRESHOLD_WITHOUT_COUNT */
 #define GRZ_FLAG_WITHOUT_OUTDEG 8   /* EXPERIMENT_THRESHOLD_WITHOUT_OUTDEGREES */
+#define GRZ_FLAG_HOST_LOOP 16       /* grz_cc_run / grz_bfs_run: one host round trip per iteration instead of one CUDA graph launch per run */
 
 typedef struct grz_run_stats_t {
     uint32_t iterations;        /* total_iterations_executed */

@@ -144,3 +144,58 @@ def test_phase_api_cc_and_bfs_drivers():
                 vertex_phase(0, info.num_vertices, None)
             assert lib.grz_phases_last_status() == 0
             np.testing.assert_array_equal(G.props(), ref)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_graph_run_equals_host_loop(name):
+    """grz_cc_run / grz_bfs_run execute the whole loop as one CUDA graph (engine choice and
+    convergence on the device).  GRZ_FLAG_HOST_LOOP runs the same loop with a host round trip
+    per iteration.  Both must give the same results for every engine flag set and for the
+    learned policy, and BFS (level-synchronous) the same iterations and engine counts."""
+    from grazelle import native
+    from grazelle.switch import Switch
+    rec, g = load_golden(name)
+    with gpu_graph(g) as G:
+        for policy in ("threshold", "learned"):
+            if policy == "learned":
+                G.set_policy(native.POLICY_LEARNED, Switch(0, seed=11))
+            for _, flags in CC_VARIANTS:
+                a, sa = G.connected_components(flags, stats=True)
+                b, sb = G.connected_components(flags | native.FLAG_HOST_LOOP, stats=True)
+                np.testing.assert_array_equal(a, b)
+                np.testing.assert_array_equal(a, rec["cc_labels"])
+                # CC updates labels in place (asynchronous, as the reference's CAS loop), so the
+                # number of iterations may differ between runs; the labels may not
+                for s_ in (sa, sb):
+                    assert s_.iterations == s_.pull_iterations + s_.push_iterations
+                    assert s_.iterations >= 1
+            for _, flags in BFS_VARIANTS:
+                for root in (0, g.num_vertices // 3):
+                    pa, la, sa = G.bfs(root, flags, stats=True)
+                    pb, lb, sb = G.bfs(root, flags | native.FLAG_HOST_LOOP, stats=True)
+                    np.testing.assert_array_equal(la, lb)
+                    np.testing.assert_array_equal(pa, pb)
+                    assert (sa.iterations, sa.pull_iterations, sa.push_iterations) == \
+                        (sb.iterations, sb.pull_iterations, sb.push_iterations), (policy, flags, root)
+        G.set_policy(native.POLICY_THRESHOLD)
+
+
+def test_graph_run_repeated_and_alternating():
+    """The cached run graph survives alternating apps, roots and loops on one graph."""
+    from grazelle import graphgen as gg, native
+    g = gg.rmat(16, seed=77)
+    push = g.push_order().pairs()
+    with gpu_graph(g) as G:
+        for k in range(3):
+            for root in (1, 100, 5000):
+                _, lv, st = G.bfs(root, stats=True)
+                np.testing.assert_array_equal(lv, O.bfs_levels(push, g.num_vertices, root))
+                _, lv2, st2 = G.bfs(root, native.FLAG_HOST_LOOP, stats=True)
+                np.testing.assert_array_equal(lv2, lv)
+                assert st.iterations == st2.iterations
+            lab = G.connected_components()
+            lab2 = G.connected_components(native.FLAG_HOST_LOOP)
+            np.testing.assert_array_equal(lab, lab2)
+        before = G.launch_count()
+        G.bfs(1)
+        assert G.launch_count() > before

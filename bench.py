@@ -218,23 +218,23 @@ def run_native(a):
     # one step of the workload, graph resident; returns (teps units, iterations)
     roots = pick_roots(g, 8) if wl == "bfs" else []
 
+    # (results stay on the device; the e2e loop below reads them back)
     def step(i):
         if wl == "cc":
-            _, st = G.connected_components(stats=True)
+            st = G.cc_run()
             return E * st.iterations, st.iterations
         if wl == "pr":
             G.pr_init(0.875).pr_iterate(16)
             G.sync()
             return E * 16, 16
         root = roots[i % len(roots)]
-        par, lv, st = G.bfs(root, stats=True)
-        reached = lv >= 0
-        return int(g.out_degrees()[reached].sum()), st.iterations
+        st = G.bfs_run(root)
+        _, reached_edges, _ = G.digest()
+        return reached_edges, st.iterations
 
     for i in range(a.warmup):
         step(i)
     barrier()
-    G.profile(True)
     l0 = G.launch_count()
     units = 0
     iters = 0
@@ -245,10 +245,18 @@ def run_native(a):
                 units += u
                 iters += it
     launches = G.launch_count() - l0
-    recs = G.profile_read()
-    G.profile(False)
     ms = max_over_ranks(tm.ms)
     value = world * units / (ms * 1e-3) / 1e9
+
+    # Per-kernel CUDA-event durations for the roofline: the same K steps once more with kernel
+    # profiling on.  The event pairs need host-launched kernels, so CC/BFS run their host loop
+    # here (the same kernels as the graph the headline region launches).
+    G.profile(True)
+    with Timer(torch, stream) as tprof:
+        for i in range(a.steps):
+            step(i)
+    recs = G.profile_read()
+    G.profile(False)
     ks = kernel_stats(recs)
     dominant = max(ks.items(), key=lambda kv: kv[1]["total_ms"])[0] if ks else None
 
@@ -263,6 +271,8 @@ def run_native(a):
             roof = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": hbm, "peak_kind": hbm_kind,
                     "unit": "GB/s", "frac": round(achieved / hbm, 4), "algorithmic_bytes": alg[dominant],
                     "mean_launch_ms": round(ks[dominant]["mean_ms"], 4),
+                    "share_of_profiled_pass": round(ks[dominant]["total_ms"] / tprof.ms, 4),
+                    "region": "profiled pass of the same %d steps" % a.steps,
                     "traffic": profile_traffic(dominant, "%s%d" % (wl, scale))}
 
     # end to end through the C ABI from pinned host buffers
@@ -310,42 +320,51 @@ def run_native(a):
 
 
 def extra_apps(a, G_cc, g_cc, torch, stream, hbm, hbm_kind):
-    """PageRank on R-MAT 20 (16 pull iterations) and BFS from 8 roots on the CC graph."""
+    """CC under the learned switch on the headline graph, the BFS switch study (directed R-MAT
+    26, 64 roots, threshold vs learned), and PageRank on R-MAT 20 (16 pull iterations)."""
+    from grazelle import native
+    from grazelle import switch as sw
     from grazelle.engine import Graph
     out = {}
-    # BFS on the CC graph
-    roots = pick_roots(g_cc, 8)
-    deg = g_cc.out_degrees()
-    for r in roots[:2]:
-        G_cc.bfs(r)
-    G_cc.profile(True)
-    teps = 0
-    dev_ms = 0.0
-    iters = []
-    for r in roots:
-        _, lv, st = G_cc.bfs(r, stats=True)  # st.ms: device time of the run (CUDA events); readback excluded
-        teps += int(deg[lv >= 0].sum())
-        dev_ms += st.ms
-        iters.append((st.iterations, st.pull_iterations, st.push_iterations))
-    recs = kernel_stats(G_cc.profile_read())
-    G_cc.profile(False)
-    out["bfs"] = {"workload": "bfs-rmat%d-sym, %d roots" % (int(np.log2(g_cc.num_vertices)), len(roots)),
-                  "gteps": round(teps / (dev_ms * 1e-3) / 1e9, 3), "ms_per_root": round(dev_ms / len(roots), 3),
-                  "iterations_pull_push": iters,
-                  "kernels_us": {k: round(v["mean_ms"] * 1e3, 2) for k, v in recs.items()}}
+    dev = torch.cuda.current_device()
+    net = sw.pretrained(dev)
+    # CC on the headline graph under both policies (device time per run, identical labels)
+    cc = {}
+    for name, policy, mlp in (("threshold", native.POLICY_THRESHOLD, None), ("learned", native.POLICY_LEARNED, net)):
+        G_cc.set_policy(policy, mlp)
+        G_cc.cc_run()
+        tot, digs = 0.0, set()
+        for _ in range(max(1, a.steps)):
+            st = G_cc.cc_run()
+            tot += st.ms
+            digs.add(G_cc.digest())
+        cc[name] = {"ms_per_run": round(tot / max(1, a.steps), 3), "iterations_pull_push": [st.iterations, st.pull_iterations,
+                                                                                           st.push_iterations]}
+        cc[name]["digest"] = sorted(digs)
+    G_cc.set_policy(native.POLICY_THRESHOLD)
+    cc["identical_labels"] = cc["threshold"]["digest"] == cc["learned"]["digest"]
+    for k in ("threshold", "learned"):
+        cc[k].pop("digest")
+    cc["learned_speedup"] = round(cc["threshold"]["ms_per_run"] / cc["learned"]["ms_per_run"], 4)
+    out["cc_switch"] = cc
+    if a.bfs_scale:
+        out["bfs_switch"] = bfs_switch_study(a, torch, stream, net, dev)
     # PageRank
     g, pull, push = make_graph("pr", 20, a.seed)
     V, E = g.num_vertices, g.num_edges
     with Graph(torch.cuda.current_device(), stream=stream.cuda_stream) as G:
         G.load_pairs(V, pull, push)
         G.pr_init(0.875).pr_iterate(16)
-        G.profile(True)
+        n = max(1, a.steps // 2)
         with Timer(torch, stream) as tp:
-            for _ in range(max(1, a.steps // 2)):
+            for _ in range(n):
                 G.pr_init(0.875).pr_iterate(16)
+        G.profile(True)
+        for _ in range(n):
+            G.pr_init(0.875).pr_iterate(16)
+        G.sync()
         ks = kernel_stats(G.profile_read())
         G.profile(False)
-        n = max(1, a.steps // 2)
         alg = 8 * E + 16 * V
         gm = ks.get("pr_gather", {}).get("mean_ms", 0)
         it_ms = tp.ms / (16 * n)
@@ -357,6 +376,54 @@ def extra_apps(a, G_cc, g_cc, torch, stream, hbm, hbm_kind):
                            "kernels_us": {k: round(v["mean_ms"] * 1e3, 2) for k, v in ks.items()},
                            "gather_roofline_frac": round(alg / (gm * 1e-3) / 1e9 / hbm, 4) if gm else None}
     return out
+
+
+def bfs_switch_study(a, torch, stream, net, dev):
+    """BFS on a directed R-MAT (default scale 26, edge factor 16) from 64 seeded non-isolated
+    roots under the threshold rule and the learned switch: GTEPS from the device time of each
+    run, identical levels checked by an on-device digest, and the edge-phase regret of both
+    policies against the best engine per iteration on 4 of the roots."""
+    from grazelle import graphgen as gg
+    from grazelle import native
+    from grazelle import switch as sw
+    from grazelle.engine import Graph
+    t0 = time.time()
+    g = gg.rmat(a.bfs_scale, 16, seed=a.seed + 26)
+    V, E = g.num_vertices, g.num_edges
+    roots = pick_roots(g, 64, seed=a.seed + 64)
+    log("bfs graph: scale %d V=%d E=%d (%.1fs)" % (a.bfs_scale, V, E, time.time() - t0))
+    res = {"workload": "bfs-rmat%d (directed), %d roots" % (a.bfs_scale, len(roots)), "V": V, "E": E}
+    with Graph(dev, stream=stream.cuda_stream) as G:
+        G.load_pairs(V, g.pull_order().pairs(), g.push_order().pairs())
+        del g
+        digests = {}
+        for name, policy, mlp in (("threshold", native.POLICY_THRESHOLD, None), ("learned", native.POLICY_LEARNED, net)):
+            G.set_policy(policy, mlp)
+            for r in roots[:3]:
+                G.bfs_run(r)
+            ms, teps, npull, npush, dg = 0.0, 0, 0, 0, []
+            for r in roots:
+                st = G.bfs_run(r)
+                reached, edges, h = G.digest()
+                ms += st.ms
+                teps += edges
+                npull += st.pull_iterations
+                npush += st.push_iterations
+                dg.append((reached, edges, h))
+            digests[name] = dg
+            res[name] = {"ms_total": round(ms, 3), "ms_per_root": round(ms / len(roots), 4),
+                         "gteps": round(teps / (ms * 1e-3) / 1e9, 3), "pull_iterations": npull, "push_iterations": npush}
+        G.set_policy(native.POLICY_THRESHOLD)
+        res["identical_levels"] = digests["threshold"] == digests["learned"]
+        res["learned_speedup"] = round(res["threshold"]["ms_total"] / res["learned"]["ms_total"], 4)
+        d = sw.Samples()
+        d.extend(sw.collect(G, native.APP_BREADTH_FIRST_SEARCH, roots[:4]))
+        e = sw.edge_totals(d, net)
+        res["edge_phase_regret_4_roots"] = {"threshold_ms": round(e["threshold_ms"], 4), "learned_ms": round(e["learned_ms"], 4),
+                                            "best_per_iteration_ms": round(e["best_ms"], 4), "iterations": e["iterations"],
+                                            "learned_regret": round(e["learned_ms"] / e["best_ms"] - 1, 4),
+                                            "threshold_regret": round(e["threshold_ms"] / e["best_ms"] - 1, 4)}
+    return res
 
 
 # ---------------------------------------------------------------------------------------------- CPU
@@ -431,6 +498,7 @@ def main():
     ap.add_argument("--scale", type=int, default=0)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-apps", action="store_true")
+    ap.add_argument("--bfs-scale", type=int, default=26, help="R-MAT scale of the BFS switch study (0: skip)")
     ap.add_argument("--no-cpu", action="store_true")
     a = ap.parse_args()
     if a.warmup < 3:

@@ -58,6 +58,7 @@ static void free_list(grz_list* L)
     cudaFree(L->nbr);
     cudaFree(L->shared);
     cudaFree(L->rowptr);
+    cudaFree(L->hub_vid);
     memset(L, 0, sizeof(*L));
 }
 
@@ -96,6 +97,10 @@ extern "C" int grz_graph_create(grz_graph** out, int device, void* stream)
     grz_graph* g = (grz_graph*)calloc(1, sizeof(grz_graph));
     if (!g) return GRZ_ERR_NOMEM;
     g->device = device;
+    g->tune.hub_max = 0;      // measured: the label gathers are bound by the L1/L2 path of non-hub lanes
+    g->tune.cc_cache = 16384;
+    g->tune.cc_threads = 512;
+    g->tune.cc_grid = 0;
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e != cudaSuccess) {
@@ -256,6 +261,7 @@ extern "C" int grz_graph_load_pairs(grz_graph* g, uint64_t V, uint64_t E, const 
         }
         rc = grz_build_list(g, which == 0 ? &g->pull : &g->push, dp, E, which == 0 ? 1 : 0);
         if (rc == GRZ_OK && which == 0) rc = grz_build_outdegrees(g, dp, E);
+        if (rc == GRZ_OK && which == 0) rc = grz_build_hubs(g, &g->pull, g->tune.hub_max);
         if (rc == GRZ_OK) rc = grz_cuda_check(g, cudaStreamSynchronize(st), "layout build");
     }
     if (dpairs) cudaFree(dpairs);
@@ -521,6 +527,50 @@ extern "C" int grz_read_levels(grz_graph* g, int64_t* host, uint64_t cap)
         for (uint64_t v = 0; v < g->V; ++v) host[v] = tmp[v] == 0xffffffffu ? -1 : (int64_t)tmp[v];
     free(tmp);
     return grz_cuda_check(g, e, "read levels");
+}
+
+extern "C" int grz_result_digest(grz_graph* g, uint64_t* out3)
+{
+    if (!g || !out3) return GRZ_ERR_ARG;
+    return grz_frontier_digest(g, out3);
+}
+
+extern "C" int grz_tune_set(grz_graph* g, int param, int64_t value)
+{
+    if (!g || value < 0) return GRZ_ERR_ARG;
+    switch (param) {
+    case GRZ_TUNE_HUBS:
+        if (value > (int64_t)GRZ_HUB_MAX) return grz_set_error(g, GRZ_ERR_RANGE, "at most %u hubs", GRZ_HUB_MAX);
+        g->tune.hub_max = (uint32_t)value;
+        return GRZ_OK;
+    case GRZ_TUNE_CC_CACHE:
+        if (value > (int64_t)GRZ_HUB_MAX) return grz_set_error(g, GRZ_ERR_RANGE, "at most %u cached hubs", GRZ_HUB_MAX);
+        g->tune.cc_cache = (uint32_t)value;
+        return GRZ_OK;
+    case GRZ_TUNE_CC_THREADS:
+        if (value != 256 && value != 512 && value != 1024) return grz_set_error(g, GRZ_ERR_ARG, "threads must be 256, 512 or 1024");
+        g->tune.cc_threads = (uint32_t)value;
+        return GRZ_OK;
+    case GRZ_TUNE_CC_GRID:
+        if (value > (1 << 20)) return GRZ_ERR_RANGE;
+        g->tune.cc_grid = (uint32_t)value;
+        return GRZ_OK;
+    default:
+        return grz_set_error(g, GRZ_ERR_ARG, "unknown tuning parameter %d", param);
+    }
+}
+
+extern "C" int grz_tune_get(const grz_graph* g, int param, int64_t* value)
+{
+    if (!g || !value) return GRZ_ERR_ARG;
+    switch (param) {
+    case GRZ_TUNE_HUBS: *value = g->tune.hub_max; return GRZ_OK;
+    case GRZ_TUNE_CC_CACHE: *value = g->tune.cc_cache; return GRZ_OK;
+    case GRZ_TUNE_CC_THREADS: *value = g->tune.cc_threads; return GRZ_OK;
+    case GRZ_TUNE_CC_GRID: *value = g->tune.cc_grid; return GRZ_OK;
+    case GRZ_TUNE_HUBS_LOADED: *value = g->pull.nhub; return GRZ_OK;
+    default: return GRZ_ERR_ARG;
+    }
 }
 
 extern "C" unsigned long long grz_launch_count(const grz_graph* g) { return g ? g->nlaunch : 0ull; }

@@ -82,42 +82,73 @@ struct VoteCfg {
 // ---------------------------------------------------------------------------------------------
 // CC pull
 
-__global__ void __launch_bounds__(T) k_cc_pull(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv, uint64_t first,
-                                               uint64_t nvec, uint32_t V, uint32_t* __restrict__ label,
-                                               unsigned long long* __restrict__ has_next, VoteCfg vc,
-                                               unsigned long long* __restrict__ vote)
+// Persistent, BT threads per block, one thread per vector per tile of BT vectors.  The labels
+// of the first `ncache` hub slots are copied into shared memory when the block starts; lanes
+// that name them read shared memory instead of gathering through L1 (in a power-law graph most
+// lanes).  Those copies may fall behind the in-place updates of this phase, which the
+// reference's asynchronous CAS loop allows as well: a label only ever decreases, every value
+// read is one the source really had, and an iteration that changes nothing is still a fixpoint.
+template <int BT>
+__global__ void __launch_bounds__(BT) k_cc_pull(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv, uint64_t first,
+                                                uint64_t nvec, uint32_t V, uint32_t* __restrict__ label,
+                                                const uint32_t* __restrict__ hub_vid, uint32_t nhub, uint32_t ncache,
+                                                unsigned long long* __restrict__ has_next, VoteCfg vc,
+                                                unsigned long long* __restrict__ vote)
 {
-    __shared__ unsigned long long red[T / 32];
-    const uint64_t i = (uint64_t)blockIdx.x * T + threadIdx.x;
-    const uint64_t v = first + i;
+    extern __shared__ uint32_t s_hub[];
+    __shared__ unsigned long long red[BT / 32];
+    for (uint32_t k = threadIdx.x; k < ncache; k += BT) s_hub[k] = label[__ldg(hub_vid + k)];
+    __syncthreads();
     const int lane = threadIdx.x & 31;
-    const bool live = i < nvec;
-    uint32_t key = INF, m = INF;
-    if (live) {
-        const uint4 s = __ldcs(nbr + v);
-        key = __ldcs(dstv + v);
-        // labels change in place during the phase: plain (coherent) loads, not the read-only path
-        const uint32_t a = label[min(s.x, V)], b = label[min(s.y, V)], c = label[min(s.z, V)], d = label[min(s.w, V)];
-        m = min(min(a, b), min(c, d));
-    }
-    const uint32_t prevkey = __shfl_up_sync(0xffffffffu, key, 1);
-    const uint32_t nextkey = __shfl_down_sync(0xffffffffu, key, 1);
-    const bool head = lane == 0 || key != prevkey;
-    const bool tail = lane == 31 || key != nextkey;
-    const unsigned heads = __ballot_sync(0xffffffffu, head);
-    const int segstart = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
-    const int maxlen = __reduce_max_sync(0xffffffffu, (unsigned)(lane - segstart + 1));
-    for (int off = 1; off < maxlen; off <<= 1) {
-        const uint32_t o = __shfl_up_sync(0xffffffffu, m, off);
-        if (lane - off >= segstart) m = min(m, o);
-    }
     unsigned long long my_vote = 0;
-    if (live && tail && m != INF && m < label[key]) {
-        const uint32_t old = atomicMin(label + key, m);
-        if (m < old && bit_set_first(has_next, key)) my_vote = vc.of(key);
+    const uint64_t ntiles = (nvec + BT - 1) / BT;
+    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const uint64_t i = t * BT + threadIdx.x;
+        const uint64_t v = first + i;
+        const bool live = i < nvec;
+        uint32_t key = INF, m = INF;
+        if (live) {
+            const uint4 s = __ldcs(nbr + v);
+            key = __ldcs(dstv + v);
+            const uint32_t x[4] = { s.x, s.y, s.z, s.w };
+            uint32_t val[4];
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                const uint32_t sl = x[l] - GRZ_HUB_BASE;
+                if (sl < ncache) {
+                    val[l] = s_hub[sl];
+                } else {
+                    // labels change in place during the phase: plain (coherent) loads
+                    const uint32_t id = sl < nhub ? __ldg(hub_vid + sl) : min(x[l], V);
+                    val[l] = label[id];
+                }
+            }
+            m = min(min(val[0], val[1]), min(val[2], val[3]));
+        }
+        const uint32_t prevkey = __shfl_up_sync(0xffffffffu, key, 1);
+        const uint32_t nextkey = __shfl_down_sync(0xffffffffu, key, 1);
+        const bool head = lane == 0 || key != prevkey;
+        const bool tail = lane == 31 || key != nextkey;
+        const unsigned heads = __ballot_sync(0xffffffffu, head);
+        const int segstart = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+        const int maxlen = __reduce_max_sync(0xffffffffu, (unsigned)(lane - segstart + 1));
+        for (int off = 1; off < maxlen; off <<= 1) {
+            const uint32_t o = __shfl_up_sync(0xffffffffu, m, off);
+            if (lane - off >= segstart) m = min(m, o);
+        }
+        if (live && tail && m != INF && m < label[key]) {
+            const uint32_t old = atomicMin(label + key, m);
+            if (m < old && bit_set_first(has_next, key)) my_vote += vc.of(key);
+        }
     }
-    my_vote = block_sum_u64(my_vote, red);
-    if (threadIdx.x == 0) vote_add(vote, my_vote);
+    for (int o = 16; o > 0; o >>= 1) my_vote += __shfl_down_sync(0xffffffffu, my_vote, o);
+    if (lane == 0) red[threadIdx.x >> 5] = my_vote;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        unsigned long long x = threadIdx.x < BT / 32 ? red[threadIdx.x] : 0ull;
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (threadIdx.x == 0) vote_add(vote, x);
+    }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -127,7 +158,7 @@ __global__ void __launch_bounds__(T) k_bfs_pull(const uint4* __restrict__ nbr, c
                                                 uint64_t nvec, uint32_t V, const unsigned long long* __restrict__ has,
                                                 const unsigned long long* __restrict__ wants,
                                                 unsigned long long* __restrict__ cand, uint32_t* __restrict__ touched,
-                                                uint32_t* __restrict__ ntouched)
+                                                uint32_t* __restrict__ ntouched, const uint32_t* __restrict__ hub_vid, uint32_t nhub)
 {
     const uint64_t i = (uint64_t)blockIdx.x * T + threadIdx.x;
     const uint64_t v = first + i;
@@ -135,7 +166,8 @@ __global__ void __launch_bounds__(T) k_bfs_pull(const uint4* __restrict__ nbr, c
     const uint32_t key = __ldcs(dstv + v);
     if (!bit_of(wants, key)) return;  // strong check: destination already visited
     const uint4 s = __ldcs(nbr + v);
-    const uint32_t ids[4] = { s.x, s.y, s.z, s.w };
+    const uint32_t ids[4] = { grz_hub_decode(s.x, hub_vid, nhub), grz_hub_decode(s.y, hub_vid, nhub),
+                              grz_hub_decode(s.z, hub_vid, nhub), grz_hub_decode(s.w, hub_vid, nhub) };
     uint32_t best = 0;
     bool any = false;
 #pragma unroll
@@ -544,6 +576,52 @@ int grz_engine_threshold(const grz_graph* g, uint64_t vote)
     return vote > thr ? 1 : 0;
 }
 
+// Shared-memory opt-in and resident blocks per SM of the CC pull kernel, per device and block size.
+template <int BT>
+static int cc_pull_config(grz_graph* g, size_t smem, int* resident)
+{
+    static int configured[64] = {};
+    const int bit = BT == 256 ? 1 : (BT == 512 ? 2 : 4);
+    if (g->device < 0 || g->device >= 64) return GRZ_ERR_ARG;
+    if (!(configured[g->device] & bit)) {
+        cudaFuncAttributes fa;
+        int optin = 0;
+        GRZ_CK(g, cudaFuncGetAttributes(&fa, k_cc_pull<BT>));
+        GRZ_CK(g, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, g->device));
+        GRZ_CK(g, cudaFuncSetAttribute(k_cc_pull<BT>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+        configured[g->device] |= bit;
+    }
+    GRZ_CK(g, cudaOccupancyMaxActiveBlocksPerMultiprocessor(resident, k_cc_pull<BT>, BT, smem));
+    if (*resident < 1) return grz_set_error(g, GRZ_ERR_ARG, "CC pull: %d threads with %zu bytes of shared memory do not fit", BT, smem);
+    return GRZ_OK;
+}
+
+template <int BT>
+static int launch_cc_pull_bt(grz_graph* g, uint64_t first, uint64_t count, const VoteCfg& vc)
+{
+    grz_frontier_state& f = g->fr;
+    const uint32_t ncache = std::min<uint32_t>(g->tune.cc_cache, g->pull.nhub);
+    const size_t smem = sizeof(uint32_t) * ncache;
+    int resident = 0;
+    int rc = cc_pull_config<BT>(g, smem, &resident);
+    if (rc) return rc;
+    const uint64_t tiles = (count + BT - 1) / BT;
+    uint64_t grid = g->tune.cc_grid ? g->tune.cc_grid : (uint64_t)g->num_sms * resident;
+    grid = std::max<uint64_t>(1, std::min<uint64_t>(grid, tiles));
+    k_cc_pull<BT><<<(unsigned)grid, BT, smem, g->stream>>>(g->pull.nbr, g->pull.shared, first, count, (uint32_t)g->V, f.label,
+                                                          g->pull.hub_vid, g->pull.nhub, ncache, f.has_next, vc, f.vote); GRZ_COUNT_LAUNCH(g);
+    return GRZ_OK;
+}
+
+static int launch_cc_pull(grz_graph* g, uint64_t first, uint64_t count, const VoteCfg& vc)
+{
+    switch (g->tune.cc_threads) {
+    case 256: return launch_cc_pull_bt<256>(g, first, count, vc);
+    case 1024: return launch_cc_pull_bt<1024>(g, first, count, vc);
+    default: return launch_cc_pull_bt<512>(g, first, count, vc);
+    }
+}
+
 // One edge phase on a vector range of the pull (pull=1) or push list.  Leaves the vote of the
 // phase in fr.vote[0] on the device.  The push engine always expands the whole compacted frontier.
 static int edge_phase(grz_graph* g, int pull, uint64_t first, uint64_t count)
@@ -561,11 +639,12 @@ static int edge_phase(grz_graph* g, int pull, uint64_t first, uint64_t count)
         grz_prof_begin(g, bfs ? GRZ_PROF_BFS_PULL : GRZ_PROF_CC_PULL);
         if (bfs) {
             k_bfs_pull<<<blocks_for(count), T, 0, st>>>(g->pull.nbr, g->pull.shared, first, count, V, f.has, f.wants, f.cand64,
-                                                       f.touched, f.counters + 1); GRZ_COUNT_LAUNCH(g);
+                                                       f.touched, f.counters + 1, g->pull.hub_vid, g->pull.nhub); GRZ_COUNT_LAUNCH(g);
             k_bfs_visit<true><<<g->num_sms * 4, T, 0, st>>>(f.touched, f.counters + 1, f.cand64, f.cand32, f.label, f.level,
                                                             f.iter, f.level_dev, f.wants, f.has_next, vc, f.vote); GRZ_COUNT_LAUNCH(g);
         } else {
-            k_cc_pull<<<blocks_for(count), T, 0, st>>>(g->pull.nbr, g->pull.shared, first, count, V, f.label, f.has_next, vc, f.vote); GRZ_COUNT_LAUNCH(g);
+            int rc = launch_cc_pull(g, first, count, vc);
+            if (rc) return rc;
         }
         grz_prof_end(g);
     } else {
@@ -689,6 +768,58 @@ int grz_read_vote(grz_graph* g, uint64_t* out)
     uint64_t v = 0;
     for (int i = 0; i < GRZ_VOTE_SLOTS; ++i) v += slots[i * GRZ_VOTE_STRIDE];
     *out = v;
+    return GRZ_OK;
+}
+
+// digest of a CC/BFS result: out[0] = reached vertices (BFS: level set; CC: label == own id,
+// i.e. components), out[1] = sum of out-degrees of the reached vertices (BFS), out[2] = an
+// order-independent checksum of the labels and levels: sum over v of (value(v) + 1) * odd(v)
+// mod 2^64, where value is the BFS level or the CC label (unreached = 2^32 - 1)
+__global__ void __launch_bounds__(T) k_digest(const uint32_t* __restrict__ label, const uint32_t* __restrict__ level,
+                                              const uint32_t* __restrict__ degree, uint64_t V, int bfs,
+                                              unsigned long long* __restrict__ out)
+{
+    unsigned long long r = 0, e = 0, h = 0;
+    for (uint64_t v = (uint64_t)blockIdx.x * T + threadIdx.x; v < V; v += (uint64_t)gridDim.x * T) {
+        const uint32_t x = bfs ? level[v] : label[v];
+        const bool reached = bfs ? x != INF : x == (uint32_t)v;
+        if (reached) {
+            r += 1;
+            if (bfs) e += degree[v];
+        }
+        h += ((unsigned long long)x + 1ull) * ((v * 0x9E3779B97F4A7C15ull) | 1ull);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        r += __shfl_down_sync(0xffffffffu, r, o);
+        e += __shfl_down_sync(0xffffffffu, e, o);
+        h += __shfl_down_sync(0xffffffffu, h, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out + 0, r);
+        atomicAdd(out + 1, e);
+        atomicAdd(out + 2, h);
+    }
+}
+
+int grz_frontier_digest(grz_graph* g, uint64_t* out3)
+{
+    grz_frontier_state& f = g->fr;
+    if (!f.label) return grz_set_error(g, GRZ_ERR_STATE, "no CC/BFS result");
+    int rc = grz_frontier_mail(g);
+    if (rc) return rc;
+    unsigned long long* d = nullptr;
+    GRZ_CK(g, cudaMallocAsync((void**)&d, 3 * sizeof(unsigned long long), g->stream));
+    cudaError_t e = cudaMemsetAsync(d, 0, 3 * sizeof(unsigned long long), g->stream);
+    if (e == cudaSuccess && g->V) {
+        const unsigned grid = (unsigned)std::min<uint64_t>(blocks_for(g->V), (uint64_t)g->num_sms * 8);
+        k_digest<<<grid, T, 0, g->stream>>>(f.label, f.level, g->degree, g->V, f.app == GRZ_APP_BREADTH_FIRST_SEARCH, d); GRZ_COUNT_LAUNCH(g);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(f.mail, d, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, g->stream);
+    cudaFreeAsync(d, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) return grz_cuda_check(g, e, "digest");
+    memcpy(out3, f.mail, 3 * sizeof(uint64_t));
     return GRZ_OK;
 }
 
@@ -849,6 +980,7 @@ static int build_run_graph(grz_graph* g)
     f.run_bm[1] = B;
     f.run_key[0] = f.app;
     f.run_key[1] = f.flags;
+    f.run_tune = g->tune;
     return GRZ_OK;
 }
 
@@ -878,9 +1010,13 @@ int grz_frontier_run_graph(grz_graph* g, uint64_t* launches)
     rc = grz_switch_max_degree(g);
     if (rc) return rc;
     const bool same = f.run_exec && f.run_bm[0] == f.has && f.run_bm[1] == f.has_next && f.run_key[0] == f.app &&
-                      f.run_key[1] == f.flags;
+                      f.run_key[1] == f.flags && !memcmp(&f.run_tune, &g->tune, sizeof(g->tune));
     if (!same) {
-        rc = build_run_graph(g);
+        int resident = 0;
+        const size_t smem = sizeof(uint32_t) * std::min<uint32_t>(g->tune.cc_cache, g->pull.nhub);
+        rc = g->tune.cc_threads == 256 ? cc_pull_config<256>(g, smem, &resident)
+             : (g->tune.cc_threads == 1024 ? cc_pull_config<1024>(g, smem, &resident) : cc_pull_config<512>(g, smem, &resident));
+        if (!rc) rc = build_run_graph(g);
         if (rc) return rc;
     }
     grz_runctl c;

@@ -178,10 +178,26 @@ struct grz_list {
     uint64_t* vindex;       // uint64[V+64]
     uint64_t vindex_start;  // first shared vertex with vectors
     uint64_t vindex_end;    // last shared vertex with vectors
-    uint4* nbr;             // uint4[nvec]
+    uint4* nbr;             // uint4[nvec]; pull list: hub sources encoded as GRZ_HUB_BASE + slot
     uint32_t* shared;       // uint32[nvec]
     uint32_t* rowptr;       // uint32[V+1]
+    uint32_t* hub_vid;      // pull list: vertex of each hub slot, slots by out-degree, highest first
+    uint32_t nhub;
 };
+
+// Hub sources of the pull list.  In power-law graphs a few thousand vertices are the source of
+// most edges.  The device pull list stores such a source as GRZ_HUB_BASE + slot, so the pull
+// kernels can serve it from a copy of the hubs' values in shared memory instead of a gather
+// through L1.  Invalid lanes stay GRZ_INVALID_ID; other sources are plain IDs (< V < 2^31).
+#define GRZ_HUB_BASE 0x80000000u
+#define GRZ_HUB_MAX 49152u
+
+// the vertex a pull-list neighbour field names (GRZ_INVALID_ID stays invalid)
+__device__ __forceinline__ uint32_t grz_hub_decode(uint32_t x, const uint32_t* __restrict__ hub_vid, uint32_t nhub)
+{
+    const uint32_t sl = x - GRZ_HUB_BASE;
+    return sl < nhub ? __ldg(hub_vid + sl) : x;
+}
 
 struct grz_prof;
 
@@ -203,6 +219,20 @@ struct grz_prof;
 #define GRZ_POLICY_THRESHOLD 0
 #define GRZ_POLICY_LEARNED 1
 struct grz_mlp;
+
+#define GRZ_TUNE_HUBS 0
+#define GRZ_TUNE_CC_CACHE 1
+#define GRZ_TUNE_CC_THREADS 2
+#define GRZ_TUNE_CC_GRID 3
+#define GRZ_TUNE_HUBS_LOADED 100
+
+// kernel shapes chosen per graph (grz_tune_set; the autotuner searches them)
+struct grz_tuning {
+    uint32_t hub_max;      // hub sources encoded when a graph is loaded (0: none)
+    uint32_t cc_cache;     // hub labels the CC pull kernel keeps in shared memory
+    uint32_t cc_threads;   // threads per block of the CC pull kernel (256, 512, 1024)
+    uint32_t cc_grid;      // blocks of the persistent CC pull kernel (0: SMs x resident blocks)
+};
 
 // Device control block of a CC/BFS run executed as one CUDA graph (grz_ccbfs.cu): the
 // decision kernel at the end of each iteration updates it and sets the graph's conditional
@@ -266,6 +296,7 @@ struct grz_frontier_state {
     cudaGraphExec_t run_exec;
     unsigned long long* run_bm[2];   // the HasInfo buffers in the graph's even-iteration roles
     int run_key[2];                  // app, flags of the captured graph
+    grz_tuning run_tune;             // kernel shapes of the captured graph
     // snapshot for timing both engines from one state
     void* snap;
     uint64_t snap_bytes;
@@ -304,6 +335,7 @@ struct grz_graph {
     grz_frontier_state fr;
     grz_prof* prof;       // kernel timing (null unless enabled)
     unsigned long long nlaunch;  // kernels launched by this graph (grz_launch_count)
+    grz_tuning tune;
     char err[256];
 };
 
@@ -370,6 +402,7 @@ int grz_read_vote(grz_graph* g, uint64_t* out);
 int grz_frontier_mail(grz_graph* g);
 int grz_frontier_run_graph(grz_graph* g, uint64_t* launches);
 void grz_frontier_run_prepare(grz_graph* g);
+int grz_frontier_digest(grz_graph* g, uint64_t* out3);
 int grz_switch_max_degree(grz_graph* g);
 void grz_switch_policy_ctl(grz_graph* g, grz_runctl* c);
 int grz_switch_launch_run_decide(grz_graph* g, const unsigned long long* next_frontier, unsigned long long* clear_bm, int initial,
@@ -382,6 +415,7 @@ void grz_frontier_free(grz_graph* g);
 
 // layout (grz_layout.cu)
 int grz_build_list(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t E, int shared_is_dst);
+int grz_build_hubs(grz_graph* g, grz_list* L, uint32_t max_hubs);
 int grz_build_outdegrees(grz_graph* g, const uint64_t* d_pull_pairs, uint64_t E);
 
 // scans (grz_scan.cu): exclusive sum of uint32 into uint32 (n < 2^32), inclusive max of uint32

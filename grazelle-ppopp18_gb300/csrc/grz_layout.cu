@@ -12,6 +12,9 @@
 // Edge e starts a new vector when it starts a run of its shared vertex or when its position in
 // the run is a multiple of 4 (the stash flushes on a change of shared vertex or when full), so
 // vector numbers come from a scan over those flags, and a lane is (position in run) mod 4.
+#include <algorithm>
+#include <vector>
+
 #include "grz_internal.cuh"
 
 namespace {
@@ -274,4 +277,135 @@ int grz_build_outdegrees(grz_graph* g, const uint64_t* d_pull_pairs, uint64_t E)
         GRZ_CK(g, cudaGetLastError());
     }
     return GRZ_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Hub sources of the pull list (see GRZ_HUB_BASE).  The hubs are the vertices with the highest
+// out-degree (number of pull-list lanes that name them).  Selection: a histogram of
+// min(degree, HUB_BINS - 1) gives the smallest degree bin above which at most max_hubs
+// vertices lie; those candidates are compacted in ID order, sorted on the host by (degree
+// descending, ID) and cut to max_hubs; the list's neighbour fields are then rewritten.
+
+namespace {
+
+constexpr uint32_t HUB_BINS = 8192;
+
+__global__ void __launch_bounds__(BT) k_deg_hist(const uint32_t* __restrict__ degree, uint64_t V, uint32_t* __restrict__ hist)
+{
+    __shared__ uint32_t h[HUB_BINS];
+    for (uint32_t i = threadIdx.x; i < HUB_BINS; i += BT) h[i] = 0;
+    __syncthreads();
+    for (uint64_t v = (uint64_t)blockIdx.x * BT + threadIdx.x; v < V; v += (uint64_t)gridDim.x * BT)
+        atomicAdd(&h[min(degree[v], HUB_BINS - 1)], 1u);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < HUB_BINS; i += BT)
+        if (h[i]) atomicAdd(hist + i, h[i]);
+}
+
+__global__ void k_hub_flags(const uint32_t* __restrict__ degree, uint64_t V, uint32_t tbin, uint32_t* __restrict__ flags)
+{
+    const uint64_t v = (uint64_t)blockIdx.x * BT + threadIdx.x;
+    if (v < V) flags[v] = min(degree[v], HUB_BINS - 1) > tbin ? 1u : 0u;
+}
+
+__global__ void k_hub_compact(const uint32_t* __restrict__ flags, const uint32_t* __restrict__ pos, uint64_t V,
+                              const uint32_t* __restrict__ degree, uint32_t* __restrict__ cand, uint32_t* __restrict__ cand_deg)
+{
+    const uint64_t v = (uint64_t)blockIdx.x * BT + threadIdx.x;
+    if (v < V && flags[v]) {
+        cand[pos[v]] = (uint32_t)v;
+        cand_deg[pos[v]] = degree[v];
+    }
+}
+
+__global__ void k_hub_slots(const uint32_t* __restrict__ hub_vid, uint32_t nhub, uint32_t* __restrict__ slot_of)
+{
+    const uint32_t i = blockIdx.x * BT + threadIdx.x;
+    if (i < nhub) slot_of[hub_vid[i]] = i;
+}
+
+__global__ void k_hub_encode(uint4* __restrict__ nbr, uint64_t nvec, const uint32_t* __restrict__ slot_of, uint32_t V)
+{
+    const uint64_t v = (uint64_t)blockIdx.x * BT + threadIdx.x;
+    if (v >= nvec) return;
+    uint4 s = nbr[v];
+    uint32_t* f[4] = { &s.x, &s.y, &s.z, &s.w };
+    bool any = false;
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+        const uint32_t x = *f[l];
+        if (x < V) {
+            const uint32_t sl = slot_of[x];
+            if (sl != GRZ_INVALID_ID) { *f[l] = GRZ_HUB_BASE + sl; any = true; }
+        }
+    }
+    if (any) nbr[v] = s;
+}
+
+}  // namespace
+
+int grz_build_hubs(grz_graph* g, grz_list* L, uint32_t max_hubs)
+{
+    const uint64_t V = g->V;
+    cudaStream_t st = g->stream;
+    L->nhub = 0;
+    if (max_hubs > GRZ_HUB_MAX) max_hubs = GRZ_HUB_MAX;
+    if (max_hubs == 0 || V == 0 || V >= GRZ_HUB_BASE || !L->nbr || L->nvec == 0) return GRZ_OK;
+    int rc = GRZ_OK;
+    uint32_t *hist = nullptr, *flags = nullptr, *pos = nullptr, *tot = nullptr, *cand = nullptr, *cdeg = nullptr, *slot_of = nullptr;
+    std::vector<uint32_t> h(HUB_BINS);
+#define HCK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { rc = grz_cuda_check(g, e_, #x); goto done; } } while (0)
+    {
+        HCK(cudaMallocAsync((void**)&hist, sizeof(uint32_t) * HUB_BINS, st));
+        HCK(cudaMemsetAsync(hist, 0, sizeof(uint32_t) * HUB_BINS, st));
+        const unsigned grid = (unsigned)std::min<uint64_t>(grid_blocks_for(V), (uint64_t)g->num_sms * 4);
+        k_deg_hist<<<grid, BT, 0, st>>>(g->degree, V, hist); GRZ_COUNT_LAUNCH(g);
+        HCK(cudaGetLastError());
+        HCK(cudaMemcpyAsync(h.data(), hist, sizeof(uint32_t) * HUB_BINS, cudaMemcpyDeviceToHost, st));
+        HCK(cudaStreamSynchronize(st));
+        // smallest tbin >= 1 with count(bin > tbin) <= max_hubs; a hub has degree >= 2
+        uint64_t above = 0;
+        uint32_t tbin = HUB_BINS - 1;
+        while (tbin > 1 && above + h[tbin] <= max_hubs) above += h[tbin--];
+        if (tbin == HUB_BINS - 1) tbin = HUB_BINS - 2;  // more top-bin vertices than slots: sort them all
+        HCK(cudaMallocAsync((void**)&flags, sizeof(uint32_t) * V, st));
+        HCK(cudaMallocAsync((void**)&pos, sizeof(uint32_t) * V, st));
+        HCK(cudaMallocAsync((void**)&tot, sizeof(uint32_t), st));
+        k_hub_flags<<<grid_blocks_for(V), BT, 0, st>>>(g->degree, V, tbin, flags); GRZ_COUNT_LAUNCH(g);
+        HCK(cudaGetLastError());
+        rc = grz_exclusive_sum_u32(g, flags, pos, V, tot);
+        if (rc) goto done;
+        uint32_t ncand = 0;
+        HCK(cudaMemcpyAsync(&ncand, tot, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        HCK(cudaStreamSynchronize(st));
+        if (ncand == 0) goto done;
+        HCK(cudaMallocAsync((void**)&cand, sizeof(uint32_t) * ncand, st));
+        HCK(cudaMallocAsync((void**)&cdeg, sizeof(uint32_t) * ncand, st));
+        k_hub_compact<<<grid_blocks_for(V), BT, 0, st>>>(flags, pos, V, g->degree, cand, cdeg); GRZ_COUNT_LAUNCH(g);
+        HCK(cudaGetLastError());
+        std::vector<uint32_t> hc(ncand), hd(ncand);
+        HCK(cudaMemcpyAsync(hc.data(), cand, sizeof(uint32_t) * ncand, cudaMemcpyDeviceToHost, st));
+        HCK(cudaMemcpyAsync(hd.data(), cdeg, sizeof(uint32_t) * ncand, cudaMemcpyDeviceToHost, st));
+        HCK(cudaStreamSynchronize(st));
+        std::vector<uint32_t> order(ncand);
+        for (uint32_t i = 0; i < ncand; ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return hd[a] > hd[b]; });
+        const uint32_t nhub = std::min<uint32_t>(ncand, max_hubs);
+        std::vector<uint32_t> vid(nhub);
+        for (uint32_t i = 0; i < nhub; ++i) vid[i] = hc[order[i]];
+        HCK(cudaMalloc((void**)&L->hub_vid, sizeof(uint32_t) * nhub));
+        HCK(cudaMemcpyAsync(L->hub_vid, vid.data(), sizeof(uint32_t) * nhub, cudaMemcpyHostToDevice, st));
+        HCK(cudaMallocAsync((void**)&slot_of, sizeof(uint32_t) * V, st));
+        HCK(cudaMemsetAsync(slot_of, 0xff, sizeof(uint32_t) * V, st));
+        k_hub_slots<<<grid_blocks_for(nhub), BT, 0, st>>>(L->hub_vid, nhub, slot_of); GRZ_COUNT_LAUNCH(g);
+        k_hub_encode<<<grid_blocks_for(L->nvec), BT, 0, st>>>(L->nbr, L->nvec, slot_of, (uint32_t)V); GRZ_COUNT_LAUNCH(g);
+        HCK(cudaGetLastError());
+        HCK(cudaStreamSynchronize(st));
+        L->nhub = nhub;
+    }
+done:
+#undef HCK
+    for (uint32_t* p : { hist, flags, pos, tot, cand, cdeg, slot_of })
+        if (p) cudaFreeAsync(p, st);
+    return rc;
 }

@@ -25,6 +25,8 @@
 //     per vertex instead of three plus a division, on a part whose FP64 rate is low.
 #include <string.h>
 
+#include <algorithm>
+
 #include "grz_internal.cuh"
 
 namespace {
@@ -69,7 +71,7 @@ __device__ __forceinline__ u128 block_reduce_u128(u128 s, u128* red);
 __global__ void __launch_bounds__(PR_THREADS) k_pr_gather(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv,
                                                           uint64_t first, uint64_t nvec, uint64_t list_nvec,
                                                           const u128* __restrict__ prop_fx, uint32_t V, u128* __restrict__ rowacc,
-                                                          const PRConst pc)
+                                                          const uint32_t* __restrict__ hub_vid, uint32_t nhub, const PRConst pc)
 {
     constexpr int NW = PR_THREADS / 32;
     __shared__ uint32_t s_key[2][NW];
@@ -85,74 +87,78 @@ __global__ void __launch_bounds__(PR_THREADS) k_pr_gather(const uint4* __restric
         if (threadIdx.x == 0) *pc.K_out = __fma_rn((1.0 - fx_to_double(S)) / pc.nverts, pc.damping, pc.c);
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane < 2) s_flag[lane][warp] = 0;
-    const uint64_t i = (uint64_t)blockIdx.x * PR_THREADS + threadIdx.x;
-    const uint64_t v = first + i;
-    const bool live = i < nvec;
-    uint32_t key = 0xffffffffu;
-    u128 val = u128_zero();
-    if (live) {
-        const uint4 s = __ldcs(nbr + v);
-        key = __ldcs(dstv + v);
-        const u128 g0 = ld_fx(prop_fx, min(s.x, V));
-        const u128 g1 = ld_fx(prop_fx, min(s.y, V));
-        const u128 g2 = ld_fx(prop_fx, min(s.z, V));
-        const u128 g3 = ld_fx(prop_fx, min(s.w, V));
-        val = u128_add(u128_add(g2, g3), u128_add(g0, g1));
-    }
-    uint32_t prevkey = __shfl_up_sync(0xffffffffu, key, 1);
-    uint32_t nextkey = __shfl_down_sync(0xffffffffu, key, 1);
-    // neighbours across the warp edge come from the whole list, so a destination cut by the edge of
-    // a caller's vector range is also added atomically, from both sides
-    if (lane == 0) prevkey = (live && v > 0) ? __ldg(dstv + v - 1) : 0xfffffffeu;
-    if (lane == 31) nextkey = (live && v + 1 < list_nvec) ? __ldg(dstv + v + 1) : 0xfffffffeu;
-    const bool head = key != prevkey;  // the previous vector has another destination
-    const bool tail = key != nextkey;  // the next vector has another destination
-    const unsigned real_heads = __ballot_sync(0xffffffffu, head);
-    const unsigned seg_heads = real_heads | 1u;  // warp-local segments
-    const int segstart = 31 - __clz(seg_heads & (0xffffffffu >> (31 - lane)));
-    const int maxlen = __reduce_max_sync(0xffffffffu, (unsigned)(lane - segstart + 1));
-    for (int off = 1; off < maxlen; off <<= 1) {
-        const u128 o = u128_shfl_up(val, off);
-        if (lane - off >= segstart) val = u128_add(val, o);
-    }
-    __syncwarp();
-    if (live && (tail || lane == 31)) {
-        const bool head_real = (real_heads >> segstart) & 1u;
-        if (tail && head_real) {
-            // every vector of this destination is in this warp
-            __stcg(reinterpret_cast<ulonglong2*>(rowacc) + key, make_ulonglong2(val.lo, val.hi));
-        } else {
-            // open on the left (slot 0) or on the right only (slot 1): combined across the block below
-            const int slot = (segstart == 0 && !head_real) ? 0 : 1;
-            s_key[slot][warp] = key;
-            s_sum[slot][warp] = val;
-            s_flag[slot][warp] = 1u | (head_real ? 2u : 0u) | (tail ? 4u : 0u);
+    const uint64_t ntiles = (nvec + PR_THREADS - 1) / PR_THREADS;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        if (lane < 2) s_flag[lane][warp] = 0;
+        const uint64_t i = tile * PR_THREADS + threadIdx.x;
+        const uint64_t v = first + i;
+        const bool live = i < nvec;
+        uint32_t key = 0xffffffffu;
+        u128 val = u128_zero();
+        if (live) {
+            const uint4 s = __ldcs(nbr + v);
+            key = __ldcs(dstv + v);
+            const u128 g0 = ld_fx(prop_fx, min(grz_hub_decode(s.x, hub_vid, nhub), V));
+            const u128 g1 = ld_fx(prop_fx, min(grz_hub_decode(s.y, hub_vid, nhub), V));
+            const u128 g2 = ld_fx(prop_fx, min(grz_hub_decode(s.z, hub_vid, nhub), V));
+            const u128 g3 = ld_fx(prop_fx, min(grz_hub_decode(s.w, hub_vid, nhub), V));
+            val = u128_add(u128_add(g2, g3), u128_add(g0, g1));
         }
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        // Walk the warps' open pieces in order.  A destination that starts and ends inside the
-        // block is stored once.  Only destinations that cross the block edge (at most the first
-        // and the last) are added to global memory atomically.
-        bool open = false, open_head = false;
-        uint32_t ok = 0;
-        u128 os = u128_zero();
-        for (int w = 0; w < NW; ++w) {
-            const uint32_t f0 = s_flag[0][w];
-            if (f0 & 1u) {
-                if (!open) { open = true; open_head = false; ok = s_key[0][w]; os = u128_zero(); }
-                os = u128_add(os, s_sum[0][w]);
-                if (f0 & 4u) {
-                    if (open_head) __stcg(reinterpret_cast<ulonglong2*>(rowacc) + ok, make_ulonglong2(os.lo, os.hi));
-                    else if (os.lo | os.hi) u128_atomic_add(rowacc + ok, os);
-                    open = false;
-                }
+        uint32_t prevkey = __shfl_up_sync(0xffffffffu, key, 1);
+        uint32_t nextkey = __shfl_down_sync(0xffffffffu, key, 1);
+        // neighbours across the warp edge come from the whole list, so a destination cut by the edge of
+        // a caller's vector range is also added atomically, from both sides
+        if (lane == 0) prevkey = (live && v > 0) ? __ldg(dstv + v - 1) : 0xfffffffeu;
+        if (lane == 31) nextkey = (live && v + 1 < list_nvec) ? __ldg(dstv + v + 1) : 0xfffffffeu;
+        const bool head = key != prevkey;  // the previous vector has another destination
+        const bool tail = key != nextkey;  // the next vector has another destination
+        const unsigned real_heads = __ballot_sync(0xffffffffu, head);
+        const unsigned seg_heads = real_heads | 1u;  // warp-local segments
+        const int segstart = 31 - __clz(seg_heads & (0xffffffffu >> (31 - lane)));
+        const int maxlen = __reduce_max_sync(0xffffffffu, (unsigned)(lane - segstart + 1));
+        for (int off = 1; off < maxlen; off <<= 1) {
+            const u128 o = u128_shfl_up(val, off);
+            if (lane - off >= segstart) val = u128_add(val, o);
+        }
+        __syncwarp();
+        if (live && (tail || lane == 31)) {
+            const bool head_real = (real_heads >> segstart) & 1u;
+            if (tail && head_real) {
+                // every vector of this destination is in this warp
+                __stcg(reinterpret_cast<ulonglong2*>(rowacc) + key, make_ulonglong2(val.lo, val.hi));
+            } else {
+                // open on the left (slot 0) or on the right only (slot 1): combined across the block below
+                const int slot = (segstart == 0 && !head_real) ? 0 : 1;
+                s_key[slot][warp] = key;
+                s_sum[slot][warp] = val;
+                s_flag[slot][warp] = 1u | (head_real ? 2u : 0u) | (tail ? 4u : 0u);
             }
-            const uint32_t f1 = s_flag[1][w];
-            if (f1 & 1u) { open = true; open_head = (f1 & 2u) != 0; ok = s_key[1][w]; os = s_sum[1][w]; }
         }
-        if (open && (os.lo | os.hi)) u128_atomic_add(rowacc + ok, os);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            // Walk the warps' open pieces in order.  A destination that starts and ends inside the
+            // block is stored once.  Only destinations that cross the block edge (at most the first
+            // and the last) are added to global memory atomically.
+            bool open = false, open_head = false;
+            uint32_t ok = 0;
+            u128 os = u128_zero();
+            for (int w = 0; w < NW; ++w) {
+                const uint32_t f0 = s_flag[0][w];
+                if (f0 & 1u) {
+                    if (!open) { open = true; open_head = false; ok = s_key[0][w]; os = u128_zero(); }
+                    os = u128_add(os, s_sum[0][w]);
+                    if (f0 & 4u) {
+                        if (open_head) __stcg(reinterpret_cast<ulonglong2*>(rowacc) + ok, make_ulonglong2(os.lo, os.hi));
+                        else if (os.lo | os.hi) u128_atomic_add(rowacc + ok, os);
+                        open = false;
+                    }
+                }
+                const uint32_t f1 = s_flag[1][w];
+                if (f1 & 1u) { open = true; open_head = (f1 & 2u) != 0; ok = s_key[1][w]; os = s_sum[1][w]; }
+            }
+            if (open && (os.lo | os.hi)) u128_atomic_add(rowacc + ok, os);
+        }
+        __syncthreads();  // the walk has read this tile's pieces
     }
 }
 
@@ -297,12 +303,30 @@ int grz_pr_init_state(grz_graph* g, double damping)
     return GRZ_OK;
 }
 
+// resident blocks per SM of the gather kernel (its grid is persistent: SMs x resident)
+static int pr_gather_resident(grz_graph* g)
+{
+    static int resident[64] = {};
+    if (g->device < 0 || g->device >= 64) return 1;
+    if (!resident[g->device]) {
+        int r = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_pr_gather, PR_THREADS, 0) != cudaSuccess || r < 1) {
+            cudaGetLastError();
+            r = 1;
+        }
+        resident[g->device] = r;
+    }
+    return resident[g->device];
+}
+
 static int pr_gather(grz_graph* g, uint64_t first, uint64_t count, const PRConst& pc)
 {
     if (count == 0) return GRZ_OK;
+    const uint64_t grid = std::min<uint64_t>(blocks_for(count), (uint64_t)g->num_sms * pr_gather_resident(g));
     grz_prof_begin(g, GRZ_PROF_PR_GATHER);
-    k_pr_gather<<<blocks_for(count), PR_THREADS, 0, g->stream>>>(g->pull.nbr, g->pull.shared, first, count, g->pull.nvec,
-                                                                 g->pr_fx[g->pr_cur], (uint32_t)g->V, g->pr_rowacc, pc); GRZ_COUNT_LAUNCH(g);
+    k_pr_gather<<<(unsigned)grid, PR_THREADS, 0, g->stream>>>(g->pull.nbr, g->pull.shared, first, count, g->pull.nvec,
+                                                                 g->pr_fx[g->pr_cur], (uint32_t)g->V, g->pr_rowacc, g->pull.hub_vid,
+                                                                 g->pull.nhub, pc); GRZ_COUNT_LAUNCH(g);
     grz_prof_end(g);
     return grz_cuda_check(g, cudaGetLastError(), "k_pr_gather");
 }

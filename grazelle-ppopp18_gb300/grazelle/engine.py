@@ -68,6 +68,24 @@ class Graph:
             native.check(n, self.h)
         return [(self.lib.grz_profile_kind_name(kinds[i]).decode(), ms[i]) for i in range(n)]
 
+    def tune(self, **kw):
+        """Set kernel shapes: hubs=, cc_cache=, cc_threads=, cc_grid= (results never depend on them;
+        hubs takes effect at the next load)."""
+        keys = {"hubs": native.TUNE_HUBS, "cc_cache": native.TUNE_CC_CACHE, "cc_threads": native.TUNE_CC_THREADS,
+                "cc_grid": native.TUNE_CC_GRID}
+        for k, v in kw.items():
+            self._ck(self.lib.grz_tune_set(self.h, keys[k], int(v)))
+        return self
+
+    def tuning(self) -> dict:
+        out = {}
+        for k, p in (("hubs", native.TUNE_HUBS), ("cc_cache", native.TUNE_CC_CACHE), ("cc_threads", native.TUNE_CC_THREADS),
+                     ("cc_grid", native.TUNE_CC_GRID), ("hubs_loaded", native.TUNE_HUBS_LOADED)):
+            v = C.c_int64()
+            self._ck(self.lib.grz_tune_get(self.h, p, C.byref(v)))
+            out[k] = v.value
+        return out
+
     def launch_count(self) -> int:
         return int(self.lib.grz_launch_count(self.h))
 
@@ -163,6 +181,18 @@ class Graph:
         lab = self.props()
         return (lab, st) if stats else lab
 
+    def cc_run(self, flags: int = 0) -> native.RunStats:
+        """CC to convergence without reading the labels back."""
+        st = native.RunStats()
+        self._ck(self.lib.grz_cc_run(self.h, flags, C.byref(st)))
+        return st
+
+    def bfs_run(self, root: int = 0, flags: int = 0) -> native.RunStats:
+        """BFS from `root` without reading the result back (see digest / levels / props)."""
+        st = native.RunStats()
+        self._ck(self.lib.grz_bfs_run(self.h, root, flags, C.byref(st)))
+        return st
+
     def bfs(self, root: int = 0, flags: int = 0, stats: bool = False):
         """(parents float64 with -1 for unvisited/root, levels int64 with -1 for unreached)."""
         st = native.RunStats()
@@ -197,6 +227,13 @@ class Graph:
         e = C.c_int()
         self._ck(self.lib.grz_frontier_current_vote(self.h, C.byref(v), C.byref(e)))
         return v.value, e.value
+
+    def digest(self):
+        """(reached vertices or CC components, reached out-edges, checksum of levels/labels),
+        computed on the device."""
+        out = np.zeros(3, dtype=np.uint64)
+        self._ck(self.lib.grz_result_digest(self.h, _ptr(out)))
+        return int(out[0]), int(out[1]), int(out[2])
 
     def levels(self) -> np.ndarray:
         lv = np.zeros(self.V, dtype=np.int64)

@@ -27,6 +27,7 @@ class GrzError(RuntimeError):
 
 
 FORCE_PULL, FORCE_PUSH, WITHOUT_COUNT, WITHOUT_OUTDEG = 1, 2, 4, 8
+TUNE_HUBS, TUNE_CC_CACHE, TUNE_CC_THREADS, TUNE_CC_GRID, TUNE_HUBS_LOADED = 0, 1, 2, 3, 100
 FLAG_HOST_LOOP = 16  # grz_cc_run / grz_bfs_run: host round trip per iteration instead of one CUDA graph
 MLP_FEATURES, MLP_HIDDEN, MLP_PARAMS = 12, 32, 1505
 POLICY_THRESHOLD, POLICY_LEARNED = 0, 1
@@ -72,6 +73,9 @@ SIGNATURES = {
     "grz_cc_run": (_I, [_VP, _I, _VP]),
     "grz_bfs_run": (_I, [_VP, _U32, _I, _VP]),
     "grz_read_levels": (_I, [_VP, _VP, _U64]),
+    "grz_result_digest": (_I, [_VP, _VP]),
+    "grz_tune_set": (_I, [_VP, _I, C.c_int64]),
+    "grz_tune_get": (_I, [_VP, _I, _VP]),
     "grz_frontier_begin": (_I, [_VP, _I, _U32, _I]),
     "grz_frontier_next": (_I, [_VP, _I, C.POINTER(C.c_int), C.POINTER(C.c_uint64)]),
     "grz_frontier_current_vote": (_I, [_VP, C.POINTER(C.c_uint64), C.POINTER(C.c_int)]),

@@ -125,6 +125,22 @@ int grz_cc_run(grz_graph* g, int flags, grz_run_stats_t* stats);
  * grz_read_props (-1 = unvisited or root), levels via grz_read_levels */
 int grz_bfs_run(grz_graph* g, uint32_t root, int flags, grz_run_stats_t* stats);
 int grz_read_levels(grz_graph* g, int64_t* host_levels, uint64_t capacity);
+/* -------- kernel shapes (no counterpart in the reference) --------
+ * Per-graph tuning knobs; the defaults are sound, the autotuner (grazelle/autotune.py) searches
+ * them.  Results never depend on them. */
+#define GRZ_TUNE_HUBS 0         /* hub sources encoded in the pull list at the next load (0..49152; 0 = none) */
+#define GRZ_TUNE_CC_CACHE 1     /* hub labels the CC pull kernel keeps in shared memory (<= 49152) */
+#define GRZ_TUNE_CC_THREADS 2   /* threads per block of the CC pull kernel: 256, 512 or 1024 */
+#define GRZ_TUNE_CC_GRID 3      /* blocks of the persistent CC pull kernel (0 = SMs x resident blocks) */
+#define GRZ_TUNE_HUBS_LOADED 100 /* read-only: hubs encoded in the loaded pull list */
+int grz_tune_set(grz_graph* g, int param, int64_t value);
+int grz_tune_get(const grz_graph* g, int param, int64_t* value);
+
+/* Digest of the last CC/BFS result without reading it back (no counterpart in the reference):
+ * out[0] = reached vertices (BFS) or components (CC: vertices whose label is their own ID),
+ * out[1] = sum of the reached vertices' out-degrees (BFS; the TEPS numerator),
+ * out[2] = order-independent checksum of the levels (BFS) or labels (CC). */
+int grz_result_digest(grz_graph* g, uint64_t out[3]);
 
 /* Step-wise driver for callers that choose the engine themselves (the learned switch):
  * begin, then call next until it returns 0 (converged); engine 1 = pull, 0 = push, -1 = the

@@ -199,3 +199,58 @@ def test_graph_run_repeated_and_alternating():
         before = G.launch_count()
         G.bfs(1)
         assert G.launch_count() > before
+
+
+def _digest_np(values_u32, degree, bfs):
+    V = values_u32.shape[0]
+    v = np.arange(V, dtype=np.uint64)
+    odd = (v * np.uint64(0x9E3779B97F4A7C15)) | np.uint64(1)
+    with np.errstate(over="ignore"):
+        h = int(np.sum((values_u32.astype(np.uint64) + np.uint64(1)) * odd, dtype=np.uint64))
+    if bfs:
+        reached = values_u32 != 0xffffffff
+        return int(reached.sum()), int(degree[reached].sum()), h
+    return int((values_u32 == np.arange(V)).sum()), 0, h
+
+
+@pytest.mark.parametrize("name", ["rmat10_s12", "rmat12_s13", "isolated_root70"])
+def test_result_digest(name):
+    rec, g = load_golden(name)
+    deg = g.out_degrees().astype(np.int64)
+    with gpu_graph(g) as G:
+        par, lv = G.bfs(0)
+        lv32 = np.where(lv < 0, 0xffffffff, lv).astype(np.uint32)
+        assert G.digest() == _digest_np(lv32, deg, True)
+        lab = G.connected_components()
+        assert G.digest() == _digest_np(lab.astype(np.uint32), deg, False)
+
+
+@pytest.mark.parametrize("name", ["rmat12_s13", "rmat10_sym_s21", "star_chain1001"])
+def test_hub_encoding_and_kernel_shapes_do_not_change_results(name):
+    """Hub sources (the pull list's high out-degree vertices served from shared memory) and the
+    CC kernel's block size, cache size and grid change only speed: CC labels, BFS parents and
+    levels, and PageRank props stay identical."""
+    from grazelle.engine import Graph
+    rec, g = load_golden(name)
+    ref_lab = rec["cc_labels"]
+    results = []
+    for hubs, cache, threads, grid in ((0, 0, 512, 0), (49152, 49152, 1024, 0), (49152, 24576, 512, 0),
+                                       (16, 8, 256, 3), (49152, 0, 256, 0), (4, 4, 512, 1)):
+        with Graph(0) as G:
+            G.tune(hubs=hubs, cc_cache=cache, cc_threads=threads, cc_grid=grid)
+            G.load_pairs(g.num_vertices, g.pull_order().pairs(), g.push_order().pairs())
+            t = G.tuning()
+            assert t["hubs_loaded"] <= hubs
+            if hubs == 0:
+                assert t["hubs_loaded"] == 0
+            lab = G.connected_components()
+            lab2 = G.connected_components(O.FORCE_PULL)
+            np.testing.assert_array_equal(lab, ref_lab)
+            np.testing.assert_array_equal(lab2, rec["cc_pull_labels"])
+            par, lv = G.bfs(0, O.FORCE_PULL)
+            pr = G.pagerank(4)
+            results.append((par, lv, pr))
+    for par, lv, pr in results[1:]:
+        np.testing.assert_array_equal(par, results[0][0])
+        np.testing.assert_array_equal(lv, results[0][1])
+        np.testing.assert_array_equal(pr, results[0][2])

@@ -197,7 +197,9 @@ extern "C" int grz_profile_read(grz_graph* g, int* kinds, float* ms, int capacit
 extern "C" const char* grz_profile_kind_name(int kind)
 {
     static const char* names[] = { "none", "pr_gather", "pr_apply", "pr_push", "pr_vertex", "cc_pull", "cc_push",
-                                   "bfs_pull", "bfs_push", "frontier", "vertex", "iteration", "mlp", "batch" };
+                                   "bfs_pull", "bfs_push", "frontier", "vertex", "iteration", "mlp", "batch",
+                                   "bfs_visit", "push_compact" };
+    static_assert(sizeof(names) / sizeof(names[0]) == GRZ_PROF_KINDS, "kind names");
     return (kind > 0 && kind < GRZ_PROF_KINDS) ? names[kind] : "none";
 }
 

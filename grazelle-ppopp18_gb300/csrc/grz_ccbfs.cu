@@ -39,6 +39,10 @@ namespace {
 
 constexpr int T = 256;
 constexpr uint32_t INF = 0xffffffffu;
+// BFS visit: sweep all vertices instead of the touched list when more than V / this were touched
+constexpr uint64_t VISIT_DENSE_RATIO = 128;
+// tiles of T vectors per step of the BFS pull kernel
+constexpr int BFS_PULL_TILES = 4;
 
 unsigned blocks_for(uint64_t n) { return (unsigned)((n + T - 1) / T); }
 
@@ -68,6 +72,20 @@ __device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long x
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
     }
     return x;
+}
+
+// Appends `val` to list[] for the lanes with `pred`, one atomicAdd per warp.  All 32 lanes must
+// call it together (the callers' loops are warp-uniform).
+__device__ __forceinline__ void warp_append(bool pred, uint32_t val, uint32_t* __restrict__ list, uint32_t* __restrict__ count)
+{
+    const unsigned m = __ballot_sync(0xffffffffu, pred);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (pred) list[base + __popc(m & ((1u << lane) - 1u))] = val;
 }
 
 struct VoteCfg {
@@ -154,35 +172,75 @@ __global__ void __launch_bounds__(BT) k_cc_pull(const uint4* __restrict__ nbr, c
 // ---------------------------------------------------------------------------------------------
 // BFS pull
 
+// BFS pull (phase_edge_pull_bfs.asm:53-211), persistent over tiles of T vectors.  For a
+// wanted destination, a vector's candidate is (vector index, ~largest HasInfo source); the
+// smallest candidate per destination wins: the reference's parent rule (the largest frontier
+// source of the first vector that has one).  Vectors of one destination are reduced within
+// the warp first, so only one atomicMin per (warp, destination) reaches memory.
 __global__ void __launch_bounds__(T) k_bfs_pull(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv, uint64_t first,
                                                 uint64_t nvec, uint32_t V, const unsigned long long* __restrict__ has,
                                                 const unsigned long long* __restrict__ wants,
                                                 unsigned long long* __restrict__ cand, uint32_t* __restrict__ touched,
-                                                uint32_t* __restrict__ ntouched, const uint32_t* __restrict__ hub_vid, uint32_t nhub)
+                                                uint32_t* __restrict__ ntouched, const uint32_t* __restrict__ hub_vid, uint32_t nhub,
+                                                unsigned long long* __restrict__ has_next)
 {
-    const uint64_t i = (uint64_t)blockIdx.x * T + threadIdx.x;
-    const uint64_t v = first + i;
-    if (i >= nvec) return;
-    const uint32_t key = __ldcs(dstv + v);
-    if (!bit_of(wants, key)) return;  // strong check: destination already visited
-    const uint4 s = __ldcs(nbr + v);
-    const uint32_t ids[4] = { grz_hub_decode(s.x, hub_vid, nhub), grz_hub_decode(s.y, hub_vid, nhub),
-                              grz_hub_decode(s.z, hub_vid, nhub), grz_hub_decode(s.w, hub_vid, nhub) };
-    uint32_t best = 0;
-    bool any = false;
+    // U tiles per step: their destination loads, then their WantsInfo loads, are issued together
+    // (enough bytes in flight per SM to cover DRAM latency);
+    // late in a BFS most destinations are visited and a warp without a wanted one skips its tile
+    constexpr int U = BFS_PULL_TILES;
+    const int lane = threadIdx.x & 31;
+    const uint64_t ntiles = (nvec + T - 1) / T;
+    for (uint64_t t0 = (uint64_t)blockIdx.x * U; t0 < ntiles; t0 += (uint64_t)gridDim.x * U) {
+        uint32_t keys[U];
+        bool want[U];
 #pragma unroll
-    for (int l = 0; l < 4; ++l) {
-        const uint32_t id = ids[l];
-        if (id < V && bit_of(has, id)) {  // weak check on the source
-            best = any ? max(best, id) : id;
-            any = true;
+        for (int j = 0; j < U; ++j) {
+            const uint64_t i = (t0 + j) * T + threadIdx.x;
+            keys[j] = i < nvec ? __ldcs(dstv + first + i) : INF;
         }
-    }
-    if (!any) return;
-    const unsigned long long k = ((unsigned long long)v << 32) | (unsigned long long)(~best);
-    if (k < cand[key]) {
-        const unsigned long long old = atomicMin(cand + key, k);
-        if (old == ~0ull) touched[atomicAdd(ntouched, 1u)] = key;
+#pragma unroll
+        for (int j = 0; j < U; ++j) want[j] = keys[j] != INF && bit_of(wants, keys[j]);  // strong check
+#pragma unroll
+        for (int j = 0; j < U; ++j) {
+            if (!__ballot_sync(0xffffffffu, want[j])) continue;  // warp-uniform
+            const uint64_t v = first + (t0 + j) * T + threadIdx.x;
+            const uint32_t key = keys[j];
+            unsigned long long k = ~0ull;
+            if (want[j]) {
+                const uint4 s = __ldcs(nbr + v);
+                const uint32_t ids[4] = { grz_hub_decode(s.x, hub_vid, nhub), grz_hub_decode(s.y, hub_vid, nhub),
+                                          grz_hub_decode(s.z, hub_vid, nhub), grz_hub_decode(s.w, hub_vid, nhub) };
+                uint32_t best = 0;
+                bool any = false;
+#pragma unroll
+                for (int l = 0; l < 4; ++l) {
+                    const uint32_t id = ids[l];
+                    if (id < V && bit_of(has, id)) {  // weak check on the source
+                        best = any ? max(best, id) : id;
+                        any = true;
+                    }
+                }
+                if (any) k = ((unsigned long long)v << 32) | (unsigned long long)(~best);
+            }
+            // segmented min of k over runs of equal keys within the warp
+            const uint32_t prevkey = __shfl_up_sync(0xffffffffu, key, 1);
+            const uint32_t nextkey = __shfl_down_sync(0xffffffffu, key, 1);
+            const bool head = lane == 0 || key != prevkey;
+            const bool tail = lane == 31 || key != nextkey;
+            const unsigned heads = __ballot_sync(0xffffffffu, head);
+            const int segstart = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+            const int maxlen = __reduce_max_sync(0xffffffffu, (unsigned)(lane - segstart + 1));
+            for (int off = 1; off < maxlen; off <<= 1) {
+                const unsigned long long o = __shfl_up_sync(0xffffffffu, k, off);
+                if (lane - off >= segstart) k = min(k, o);
+            }
+            bool first_touch = false;
+            if (tail && k != ~0ull && k < cand[key]) {
+                first_touch = atomicMin(cand + key, k) == ~0ull;
+                if (first_touch) atomicOr(has_next + (key >> 6), 1ull << (key & 63));
+            }
+            warp_append(first_touch, key, touched, ntouched);
+        }
     }
 }
 
@@ -344,25 +402,33 @@ __global__ void __launch_bounds__(T) k_push_expand(const uint32_t* __restrict__ 
             }
         }
         __syncthreads();
-        for (uint32_t gv = t0 + threadIdx.x; gv < tend; gv += T) {
-            int lo = 0, hi = (int)nw - 1;  // last entry with s_off <= gv
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (s_off[mid] <= gv) lo = mid; else hi = mid - 1;
+        for (uint32_t base = t0; base < tend; base += T) {  // warp-uniform trip count
+            const uint32_t gv = base + threadIdx.x;
+            const bool live = gv < tend;
+            uint32_t u = 0;
+            uint4 s = make_uint4(INF, INF, INF, INF);
+            if (live) {
+                int lo = 0, hi = (int)nw - 1;  // last entry with s_off <= gv
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (s_off[mid] <= gv) lo = mid; else hi = mid - 1;
+                }
+                u = s_src[lo];
+                s = __ldcs(nbr + (uint32_t)(gv + s_delta[lo]));
             }
-            const uint32_t u = s_src[lo];
-            const uint4 s = __ldcs(nbr + (uint32_t)(gv + s_delta[lo]));
             const uint32_t ids[4] = { s.x, s.y, s.z, s.w };
             if (IsBfs) {
 #pragma unroll
                 for (int l = 0; l < 4; ++l) {
                     const uint32_t d = ids[l];
+                    bool first_touch = false;
                     if (d < V && bit_of(wants, d) && u < cand32[d]) {
-                        const uint32_t old = atomicMin(cand32 + d, u);
-                        if (old == INF) touched[atomicAdd(ntouched, 1u)] = d;
+                        first_touch = atomicMin(cand32 + d, u) == INF;
+                        if (first_touch) atomicOr(has_next + (d >> 6), 1ull << (d & 63));
                     }
+                    warp_append(first_touch, d, touched, ntouched);
                 }
-            } else {
+            } else if (live) {
                 const uint32_t msg = label[u];
 #pragma unroll
                 for (int l = 0; l < 4; ++l) {
@@ -389,15 +455,14 @@ __global__ void __launch_bounds__(T) k_bfs_visit(const uint32_t* __restrict__ to
                                                  unsigned long long* __restrict__ cand64, uint32_t* __restrict__ cand32,
                                                  uint32_t* __restrict__ parent, uint32_t* __restrict__ level, uint32_t iter_host,
                                                  const uint32_t* __restrict__ iter_dev,
-                                                 unsigned long long* __restrict__ wants, unsigned long long* __restrict__ has_next,
-                                                 VoteCfg vc, unsigned long long* __restrict__ vote)
+                                                 unsigned long long* __restrict__ wants, const unsigned long long* __restrict__ has_next,
+                                                 VoteCfg vc, unsigned long long* __restrict__ vote, uint32_t V)
 {
     __shared__ unsigned long long red[T / 32];
     const uint32_t n = *ntouched;
     const uint32_t iter = iter_dev ? *iter_dev : iter_host;
     unsigned long long my_vote = 0;
-    for (uint32_t i = blockIdx.x * T + threadIdx.x; i < n; i += gridDim.x * T) {
-        const uint32_t d = touched[i];
+    auto visit = [&](uint32_t d) {
         uint32_t p;
         if (FromPull) {
             p = ~(uint32_t)(cand64[d] & 0xffffffffull);
@@ -408,9 +473,56 @@ __global__ void __launch_bounds__(T) k_bfs_visit(const uint32_t* __restrict__ to
         }
         parent[d] = p;
         level[d] = iter;
-        atomicAnd(wants + (d >> 6), ~(1ull << (d & 63)));
-        atomicOr(has_next + (d >> 6), 1ull << (d & 63));
         my_vote += vc.of(d);
+    };
+    if ((uint64_t)n * VISIT_DENSE_RATIO <= V) {
+        // few: the touched list (first-touch order)
+        for (uint32_t i = blockIdx.x * T + threadIdx.x; i < n; i += gridDim.x * T) {
+            const uint32_t d = touched[i];
+            visit(d);
+            atomicAnd(wants + (d >> 6), ~(1ull << (d & 63)));
+        }
+    } else {
+        // many: every vertex, in ID order, 4 per thread per step with the loads of the 4 issued
+        // together (coalesced, no per-thread dependence chains).  A vertex was touched in this
+        // call when its HasInfo* bit is set (at first touch) and its WantsInfo bit still is (a
+        // caller's earlier vector range of this iteration visited and cleared its own).  Each
+        // vertex is read and written by one thread only, so cand and degree go through the
+        // read-only path.
+        constexpr int U = 4;
+        const uint32_t lane = threadIdx.x & 31;
+        for (uint64_t base = (uint64_t)blockIdx.x * T * U; base < V; base += (uint64_t)gridDim.x * T * U) {  // warp-uniform
+            uint32_t d[U];
+            bool hit[U];
+#pragma unroll
+            for (int j = 0; j < U; ++j) {
+                d[j] = (uint32_t)(base + (uint64_t)j * T + threadIdx.x);
+                hit[j] = d[j] < V && (((has_next[d[j] >> 6] & wants[d[j] >> 6]) >> (d[j] & 63)) & 1ull);
+            }
+            uint32_t p[U], deg[U];
+#pragma unroll
+            for (int j = 0; j < U; ++j) {
+                if (hit[j]) {
+                    p[j] = FromPull ? ~(uint32_t)(__ldg(cand64 + d[j]) & 0xffffffffull) : __ldg(cand32 + d[j]);
+                    deg[j] = __ldg(vc.degree + d[j]);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < U; ++j) {
+                if (hit[j]) {
+                    if (FromPull) cand64[d[j]] = ~0ull; else cand32[d[j]] = INF;
+                    parent[d[j]] = p[j];
+                    level[d[j]] = iter;
+                    my_vote += (vc.without_count ? 0ull : 1ull) + (vc.without_outdeg ? 0ull : (unsigned long long)deg[j]);
+                }
+                // the warp's 32 vertices lie in one 64-bit word: one atomicAnd clears their WantsInfo bits
+                const unsigned m = __ballot_sync(0xffffffffu, hit[j]);
+                if (m && lane == (uint32_t)(__ffs(m) - 1)) {
+                    const uint32_t d0 = d[j] - lane;
+                    atomicAnd(wants + (d0 >> 6), ~((unsigned long long)m << (d0 & 63)));
+                }
+            }
+        }
     }
     my_vote = block_sum_u64(my_vote, red);
     if (threadIdx.x == 0) vote_add(vote, my_vote);
@@ -576,6 +688,12 @@ int grz_engine_threshold(const grz_graph* g, uint64_t vote)
     return vote > thr ? 1 : 0;
 }
 
+// BFS visit grid: full occupancy (8 blocks of 256 per SM), fewer for small graphs
+static unsigned visit_grid(const grz_graph* g)
+{
+    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(blocks_for((g->V + 3) / 4), (uint64_t)g->num_sms * 8));
+}
+
 // Shared-memory opt-in and resident blocks per SM of the CC pull kernel, per device and block size.
 template <int BT>
 static int cc_pull_config(grz_graph* g, size_t smem, int* resident)
@@ -638,10 +756,13 @@ static int edge_phase(grz_graph* g, int pull, uint64_t first, uint64_t count)
         if (count == 0) return GRZ_OK;
         grz_prof_begin(g, bfs ? GRZ_PROF_BFS_PULL : GRZ_PROF_CC_PULL);
         if (bfs) {
-            k_bfs_pull<<<blocks_for(count), T, 0, st>>>(g->pull.nbr, g->pull.shared, first, count, V, f.has, f.wants, f.cand64,
-                                                       f.touched, f.counters + 1, g->pull.hub_vid, g->pull.nhub); GRZ_COUNT_LAUNCH(g);
-            k_bfs_visit<true><<<g->num_sms * 4, T, 0, st>>>(f.touched, f.counters + 1, f.cand64, f.cand32, f.label, f.level,
-                                                            f.iter, f.level_dev, f.wants, f.has_next, vc, f.vote); GRZ_COUNT_LAUNCH(g);
+            const unsigned pgrid = (unsigned)std::min<uint64_t>(blocks_for(count), (uint64_t)g->num_sms * 8);
+            k_bfs_pull<<<pgrid, T, 0, st>>>(g->pull.nbr, g->pull.shared, first, count, V, f.has, f.wants, f.cand64,
+                                                       f.touched, f.counters + 1, g->pull.hub_vid, g->pull.nhub, f.has_next); GRZ_COUNT_LAUNCH(g);
+            grz_prof_end(g);
+            grz_prof_begin(g, GRZ_PROF_BFS_VISIT);
+            k_bfs_visit<true><<<visit_grid(g), T, 0, st>>>(f.touched, f.counters + 1, f.cand64, f.cand32, f.label, f.level,
+                                                            f.iter, f.level_dev, f.wants, f.has_next, vc, f.vote, V); GRZ_COUNT_LAUNCH(g);
         } else {
             int rc = launch_cc_pull(g, first, count, vc);
             if (rc) return rc;
@@ -649,18 +770,22 @@ static int edge_phase(grz_graph* g, int pull, uint64_t first, uint64_t count)
         grz_prof_end(g);
     } else {
         if (!g->push.nbr) return grz_set_error(g, GRZ_ERR_STATE, "push list not loaded");
-        grz_prof_begin(g, bfs ? GRZ_PROF_BFS_PUSH : GRZ_PROF_CC_PUSH);
+        grz_prof_begin(g, GRZ_PROF_PUSH_COMPACT);
         const unsigned nbw = blocks_for(W);
         k_fr_count<<<nbw, T, 0, st>>>(f.has, f.nonempty_push, W, g->push.rowptr, f.fr_part, f.fr_part + nbw); GRZ_COUNT_LAUNCH(g);
         k_fr_scan<<<1, T, 0, st>>>(f.fr_part, f.fr_part + nbw, nbw, f.counters); GRZ_COUNT_LAUNCH(g);
         k_fr_write<<<nbw, T, 0, st>>>(f.has, f.nonempty_push, W, g->push.rowptr, f.fr_part, f.fr_part + nbw, f.counters,
                                       f.frontier, f.voff, f.vdelta, f.tile_first); GRZ_COUNT_LAUNCH(g);
+        grz_prof_end(g);
+        grz_prof_begin(g, bfs ? GRZ_PROF_BFS_PUSH : GRZ_PROF_CC_PUSH);
         const unsigned grid = (unsigned)g->num_sms * 8;
         if (bfs) {
             k_push_expand<true><<<grid, T, 0, st>>>(f.frontier, f.voff, f.vdelta, f.tile_first, f.counters, g->push.nbr, V, f.label,
                                                     f.has_next, f.wants, f.cand32, f.touched, f.counters + 1, vc, f.vote); GRZ_COUNT_LAUNCH(g);
-            k_bfs_visit<false><<<g->num_sms * 4, T, 0, st>>>(f.touched, f.counters + 1, f.cand64, f.cand32, f.label, f.level,
-                                                             f.iter, f.level_dev, f.wants, f.has_next, vc, f.vote); GRZ_COUNT_LAUNCH(g);
+            grz_prof_end(g);
+            grz_prof_begin(g, GRZ_PROF_BFS_VISIT);
+            k_bfs_visit<false><<<visit_grid(g), T, 0, st>>>(f.touched, f.counters + 1, f.cand64, f.cand32, f.label, f.level,
+                                                             f.iter, f.level_dev, f.wants, f.has_next, vc, f.vote, V); GRZ_COUNT_LAUNCH(g);
         } else {
             k_push_expand<false><<<grid, T, 0, st>>>(f.frontier, f.voff, f.vdelta, f.tile_first, f.counters, g->push.nbr, V, f.label,
                                                      f.has_next, f.wants, f.cand32, f.touched, f.counters + 1, vc, f.vote); GRZ_COUNT_LAUNCH(g);

@@ -370,6 +370,7 @@ enum grz_prof_kind {
     GRZ_PROF_PR_GATHER = 1, GRZ_PROF_PR_APPLY, GRZ_PROF_PR_PUSH, GRZ_PROF_PR_VERTEX,
     GRZ_PROF_CC_PULL, GRZ_PROF_CC_PUSH, GRZ_PROF_BFS_PULL, GRZ_PROF_BFS_PUSH,
     GRZ_PROF_FRONTIER, GRZ_PROF_VERTEX, GRZ_PROF_ITERATION, GRZ_PROF_MLP, GRZ_PROF_BATCH,
+    GRZ_PROF_BFS_VISIT, GRZ_PROF_PUSH_COMPACT,
     GRZ_PROF_KINDS
 };
 

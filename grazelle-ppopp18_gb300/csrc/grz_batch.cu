@@ -1,0 +1,683 @@
+// grz_batch.cu -- many personalized-PageRank and multi-source BFS instances over many graphs
+// of uneven size, each run as one CUDA graph launch.
+//
+// The reference has no batching and no personalized PageRank.  PPR here is the reference's
+// PageRank vertex phase (source/phase_vertex_pr.asm:75-134) with the teleport term and the
+// dangling mass sent to the seed instead of spread over all vertices:
+//   accum[v]   = sum over v's in-edges (u, v) of prop[u]        (edge-pull, phase_edge_pull_pr.asm)
+//   S          = sum over v of accum[v]
+//   rank'[v]   = d * accum[v] + [v == seed] * (d * (1 - S) + (1 - d))
+//   prop'[v]   = rank'[v] / deg'(v)                              (deg' as the reference: V if 0)
+// starting from rank = one-hot(seed).  Ranks sum to 1 in every iteration.
+//
+// GB300 design:
+//   * The graphs become one block-diagonal union graph: each graph's vertex IDs are offset by
+//     the vertices of the graphs before it, and the union is loaded as one grz_graph.  Kernels
+//     never need to know where one graph ends; only the per-graph sums S do.
+//   * Up to GRZ_BATCH_K (8) instances per graph share one pass over the edges.  Props are stored
+//     [vertex][instance], so the 8 lanes that serve one vector's instances read one 64-byte row
+//     per source: the random gather costs one line for 8 instances instead of 8 lines.
+//   * PPR gather: a block is 32 vectors x 8 instances.  Lane (vector, instance) sums its four
+//     sources exactly in 4.124 fixed point; then warp w reduces instance w over the block's 32
+//     vectors with a segmented scan.  Destinations complete inside the block are stored, the
+//     (at most two) cut by the block edge are added with exact u128 atomics.  Sums are exact,
+//     so results do not depend on the launch shape.
+//   * PPR apply: thread per (vertex, instance); it reads S of its graph and instance (summed
+//     exactly by the previous apply as sum deg(u) * prop(u)), writes the new props and the next
+//     S, and clears the accumulators.
+//   * Multi-source BFS: bit-parallel, 8 roots per graph.  visited / frontier are one byte per
+//     vertex (bit i = instance i).  Pull: a vector's new bits are the OR of its sources'
+//     frontier bytes, reduced per destination within the warp, minus the visited bits; the
+//     vertex pass sets level = iteration for each new bit.  Levels are exact (level-synchronous).
+//   * The PPR iteration loop (fixed count) and the BFS loop (WHILE until no new bit, decided on
+//     the device) are each captured once as a CUDA graph and replayed.
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <vector>
+
+#include "grz_internal.cuh"
+#include "../../include/grazelle_gb300.h"
+
+namespace {
+
+constexpr int K = GRZ_BATCH_K;  // instances per graph (8)
+constexpr int GT = 256;         // threads per block: 32 vectors (or vertices) x 8 instances
+constexpr int TV = GT / K;      // vectors per gather tile
+constexpr uint32_t NONE = 0xffffffffu;
+constexpr int MAX_GRAPHS = 1024;
+
+__device__ __forceinline__ u128 shfl_up_u128(u128 v, int off)
+{
+    u128 r;
+    r.lo = __shfl_up_sync(0xffffffffu, v.lo, off);
+    r.hi = __shfl_up_sync(0xffffffffu, v.hi, off);
+    return r;
+}
+
+// graph of union vertex v (voff: G+1 ascending offsets in shared memory)
+__device__ __forceinline__ uint32_t graph_of(const uint32_t* voff, uint32_t G, uint32_t v)
+{
+    uint32_t lo = 0, hi = G - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (voff[mid] <= v) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// initial PPR state: prop = one-hot(seed) / deg'; S = deg(seed) * prop(seed) per (graph, instance)
+__global__ void k_ppr_init(const uint32_t* __restrict__ seeds, uint32_t G, const double* __restrict__ inv_deg,
+                           const uint32_t* __restrict__ degree, double* __restrict__ prop, u128* __restrict__ S)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= G * K) return;
+    const uint32_t s = seeds[t];
+    const uint32_t i = t % K;
+    u128 v = u128_zero();
+    if (s != NONE) {
+        const double p = inv_deg[s];
+        prop[(uint64_t)s * K + i] = p;
+        v = u128_mul32(fx_from_double(p), degree[s]);
+    }
+    S[t] = v;
+}
+
+// edge-pull of all instances (see the file comment); persistent over tiles of TV vectors.
+// Block 0 first clears S_next for the apply that follows.
+__global__ void __launch_bounds__(GT) k_ppr_gather(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv,
+                                                   uint64_t nvec, uint32_t V, const double* __restrict__ prop,
+                                                   u128* __restrict__ rowacc, u128* __restrict__ S_next, uint32_t nS)
+{
+    __shared__ u128 s_val[TV][K];
+    __shared__ uint32_t s_key[TV + 2];
+    if (blockIdx.x == 0)
+        for (uint32_t k = threadIdx.x; k < nS; k += GT) S_next[k] = u128_zero();
+    const int lv = threadIdx.x / K, inst = threadIdx.x % K;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t ntiles = (nvec + TV - 1) / TV;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint64_t v0 = tile * TV;
+        const uint64_t v = v0 + lv;
+        u128 val = u128_zero();
+        if (v < nvec) {
+            const uint4 s = __ldcs(nbr + v);
+            const uint32_t ids[4] = { s.x, s.y, s.z, s.w };
+#pragma unroll
+            for (int l = 0; l < 4; ++l)
+                if (ids[l] < V) val = u128_add(val, fx_from_double(__ldg(prop + (uint64_t)ids[l] * K + inst)));
+            if (inst == 0) s_key[lv + 1] = __ldcs(dstv + v);
+        } else if (inst == 0) {
+            s_key[lv + 1] = NONE;
+        }
+        if (threadIdx.x == 0) s_key[0] = v0 > 0 ? __ldg(dstv + v0 - 1) : NONE - 1;
+        if (threadIdx.x == 1) s_key[TV + 1] = v0 + TV < nvec ? __ldg(dstv + v0 + TV) : NONE - 1;
+        s_val[lv][inst] = val;
+        __syncthreads();
+        // warp w = instance w, lane j = vector j of the tile
+        {
+            const uint32_t key = s_key[lane + 1];
+            u128 x = s_val[lane][warp];
+            const bool head = key != s_key[lane];      // previous vector (or the one before the tile) differs
+            const bool tail = key != s_key[lane + 2];  // next vector (or the one after the tile) differs
+            const unsigned real_heads = __ballot_sync(0xffffffffu, head);
+            const unsigned seg_heads = real_heads | 1u;
+            const int segstart = 31 - __clz(seg_heads & (0xffffffffu >> (31 - lane)));
+            const int maxlen = __reduce_max_sync(0xffffffffu, (unsigned)(lane - segstart + 1));
+            for (int off = 1; off < maxlen; off <<= 1) {
+                const u128 o = shfl_up_u128(x, off);
+                if (lane - off >= segstart) x = u128_add(x, o);
+            }
+            const bool last = tail || lane == 31;
+            if (key != NONE && last) {
+                const bool whole = tail && ((real_heads >> segstart) & 1u);
+                u128* dst = rowacc + (uint64_t)key * K + warp;
+                if (whole) *dst = x;                               // every vector of key is in this tile
+                else if (x.lo | x.hi) u128_atomic_add(dst, x);     // cut by the tile edge
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// vertex phase of all instances; thread per (vertex, instance)
+__global__ void __launch_bounds__(GT) k_ppr_apply(u128* __restrict__ rowacc, const double* __restrict__ inv_deg,
+                                                  const uint32_t* __restrict__ degree, uint32_t V,
+                                                  const uint32_t* __restrict__ voff_g, uint32_t G,
+                                                  const uint32_t* __restrict__ seeds, double damping,
+                                                  const u128* __restrict__ S_cur, u128* __restrict__ S_next,
+                                                  double* __restrict__ prop_out, double* __restrict__ rank_out)
+{
+    __shared__ uint32_t voff[MAX_GRAPHS + 1];
+    __shared__ u128 s_part[2][K];
+    for (uint32_t k = threadIdx.x; k <= G; k += GT) voff[k] = voff_g[k];
+    if (threadIdx.x < 2 * K) s_part[threadIdx.x / K][threadIdx.x % K] = u128_zero();
+    __syncthreads();
+    const int inst = threadIdx.x % K;
+    for (uint64_t base = (uint64_t)blockIdx.x * TV; base < V; base += (uint64_t)gridDim.x * TV) {
+        const uint32_t v = (uint32_t)(base + threadIdx.x / K);
+        const uint32_t g0 = graph_of(voff, G, (uint32_t)base);
+        if (v < V) {
+            const uint64_t idx = (uint64_t)v * K + inst;
+            const u128 a = rowacc[idx];
+            rowacc[idx] = u128_zero();
+            const uint32_t g = graph_of(voff, G, v);
+            const uint32_t seed = seeds[g * K + inst];
+            double rank = 0.0;
+            if (seed != NONE) {
+                const double S = fx_to_double(S_cur[g * K + inst]);
+                const double c = v == seed ? __dadd_rn(__dmul_rn(damping, 1.0 - S), 1.0 - damping) : 0.0;
+                rank = __fma_rn(fx_to_double(a), damping, c);
+            }
+            const double p = __dmul_rn(rank, inv_deg[v]);
+            prop_out[idx] = p;
+            if (rank_out) rank_out[idx] = rank;
+            const u128 contrib = u128_mul32(fx_from_double(p), degree[v]);
+            if (contrib.lo | contrib.hi) {
+                // a block's 32 vertices span at most two graphs (each graph has at least 32 vertices)
+                u128* sp = &s_part[g == g0 ? 0 : 1][inst];
+                const unsigned long long old = atomicAdd(&sp->lo, contrib.lo);
+                const unsigned long long carry = (old + contrib.lo < old) ? 1ull : 0ull;
+                if (contrib.hi | carry) atomicAdd(&sp->hi, contrib.hi + carry);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < 2 * K) {
+            const int slot = threadIdx.x / K, i = threadIdx.x % K;
+            const u128 x = s_part[slot][i];
+            if (x.lo | x.hi) {
+                const uint32_t gg = slot == 0 ? g0 : g0 + 1;
+                u128_atomic_add(S_next + gg * K + i, x);
+                s_part[slot][i] = u128_zero();
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ----------------------------------------------------------------------------------------------
+// multi-source BFS
+
+__global__ void k_msbfs_init(const uint32_t* __restrict__ roots, uint32_t n, uint8_t* __restrict__ visited,
+                             uint8_t* __restrict__ frontier, int32_t* __restrict__ level)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const uint32_t r = roots[t];
+    if (r == NONE) return;
+    const uint32_t bit = 1u << (t % K);
+    // several instances may share a root: byte-wise OR through the containing word
+    atomicOr(reinterpret_cast<unsigned*>(visited) + (r >> 2), bit << (8 * (r & 3)));
+    atomicOr(reinterpret_cast<unsigned*>(frontier) + (r >> 2), bit << (8 * (r & 3)));
+    level[(uint64_t)r * K + t % K] = 0;
+}
+
+// pull: new bits of each destination = OR of its sources' frontier bytes, minus its visited bits
+__global__ void __launch_bounds__(256) k_msbfs_pull(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv, uint64_t nvec,
+                                                    uint32_t V, const uint8_t* __restrict__ frontier,
+                                                    const uint8_t* __restrict__ visited, unsigned* __restrict__ next_words)
+{
+    const int lane = threadIdx.x & 31;
+    const uint64_t ntiles = (nvec + 255) / 256;
+    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const uint64_t v = t * 256 + threadIdx.x;
+        uint32_t key = NONE, m = 0;
+        if (v < nvec) {
+            key = __ldcs(dstv + v);
+            if (visited[key] != 0xffu) {
+                const uint4 s = __ldcs(nbr + v);
+                const uint32_t ids[4] = { s.x, s.y, s.z, s.w };
+#pragma unroll
+                for (int l = 0; l < 4; ++l)
+                    if (ids[l] < V) m |= frontier[ids[l]];
+            }
+        }
+        const uint32_t prevkey = __shfl_up_sync(0xffffffffu, key, 1);
+        const uint32_t nextkey = __shfl_down_sync(0xffffffffu, key, 1);
+        const bool head = lane == 0 || key != prevkey;
+        const bool tail = lane == 31 || key != nextkey;
+        const unsigned heads = __ballot_sync(0xffffffffu, head);
+        const int segstart = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+        const int maxlen = __reduce_max_sync(0xffffffffu, (unsigned)(lane - segstart + 1));
+        for (int off = 1; off < maxlen; off <<= 1) {
+            const uint32_t o = __shfl_up_sync(0xffffffffu, m, off);
+            if (lane - off >= segstart) m |= o;
+        }
+        if (tail && key != NONE) {
+            const uint32_t nb = m & ~(uint32_t)visited[key] & 0xffu;
+            if (nb) atomicOr(next_words + (key >> 2), nb << (8 * (key & 3)));
+        }
+    }
+}
+
+// vertex pass: four vertices (one word) per thread; counts the new bits
+__global__ void __launch_bounds__(256) k_msbfs_vertex(unsigned* __restrict__ next_words, unsigned* __restrict__ visited_words,
+                                                      unsigned* __restrict__ frontier_words, int32_t* __restrict__ level,
+                                                      uint32_t V, const uint32_t* __restrict__ iter,
+                                                      unsigned long long* __restrict__ changed)
+{
+    const uint32_t W = (V + 3) / 4;
+    const uint32_t k = *iter;
+    unsigned long long cnt = 0;
+    for (uint32_t w = blockIdx.x * 256 + threadIdx.x; w < W; w += gridDim.x * 256) {
+        const unsigned nx = next_words[w];
+        const unsigned vis = visited_words[w];
+        const unsigned nb = nx & ~vis;
+        frontier_words[w] = nb;
+        if (nx) next_words[w] = 0;
+        if (nb) {
+            visited_words[w] = vis | nb;
+            cnt += __popc(nb);
+            for (int b = 0; b < 4; ++b) {
+                unsigned bits = (nb >> (8 * b)) & 0xffu;
+                const uint32_t v = w * 4 + b;
+                while (bits) {
+                    const int i = __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    level[(uint64_t)v * K + i] = (int32_t)k;
+                }
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(changed, cnt);
+}
+
+// end of a BFS iteration: stop when no bit changed or the bound is reached; next iteration number
+__global__ void k_msbfs_decide(unsigned long long* __restrict__ ctl, uint32_t* __restrict__ iter, uint32_t max_iter,
+                               cudaGraphConditionalHandle loop)
+{
+    // ctl[0] changed in this iteration, ctl[1] iterations with a change, ctl[2] bound hit
+    // (1: iterations, 2: time), ctl[3] %globaltimer of the first decision
+    unsigned long long now;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+    if (ctl[3] == 0) ctl[3] = now;
+    const unsigned long long c = ctl[0];
+    ctl[0] = 0;
+    unsigned run = c != 0;
+    if (run) ctl[1] += 1;
+    if (run && *iter >= max_iter) { run = 0; ctl[2] = 1; }
+    if (run && now - ctl[3] > 120ull * 1000000000ull) { run = 0; ctl[2] = 2; }
+    if (run) *iter += 1;
+    cudaGraphSetConditional(loop, run);
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------------------------------------
+
+struct grz_batch {
+    int device;
+    cudaStream_t stream;
+    int own_stream;
+    grz_graph* u;                        // the union graph
+    std::vector<uint32_t> voff;          // G+1 vertex offsets
+    std::vector<uint64_t> Vg, Eg;
+    std::vector<std::vector<uint64_t>> pairs;  // pending pull pairs per graph (until build)
+    uint32_t* d_voff;
+    uint32_t* d_seeds;                   // [G][K] union vertex IDs or NONE
+    // PPR
+    double* prop[2];
+    double* rank;
+    u128* rowacc;
+    u128* S[2];
+    cudaGraphExec_t ppr_exec;
+    uint32_t ppr_iters;
+    double ppr_damping;
+    int ppr_final;                        // which prop buffer the last replay wrote
+    // BFS
+    uint8_t* visited;
+    uint8_t* frontier;
+    unsigned* next_words;
+    int32_t* level;
+    unsigned long long* ctl;             // changed, iterations, bound hit
+    uint32_t* iter;
+    cudaGraphExec_t bfs_exec;
+    void* mail;                          // pinned host read-back
+    char err[256];
+};
+
+static int bset(grz_batch* b, int code, const char* msg)
+{
+    snprintf(b->err, sizeof(b->err), "%s", msg);
+    return code;
+}
+
+static int bck(grz_batch* b, cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess) return GRZ_OK;
+    cudaGetLastError();
+    snprintf(b->err, sizeof(b->err), "%s: %s", what, cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? GRZ_ERR_NOMEM : GRZ_ERR_CUDA;
+}
+#define BCK(b, x) do { int rc_ = bck((b), (x), #x); if (rc_) return rc_; } while (0)
+
+static unsigned persistent_grid(const grz_batch* b, uint64_t work_blocks, int per_sm)
+{
+    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(work_blocks, (uint64_t)b->u->num_sms * per_sm));
+}
+
+extern "C" int grz_batch_create(grz_batch** out, int device, void* stream)
+{
+    if (!out) return GRZ_ERR_ARG;
+    *out = nullptr;
+    grz_batch* b = new (std::nothrow) grz_batch();
+    if (!b) return GRZ_ERR_NOMEM;
+    b->device = device;
+    int rc = grz_graph_create(&b->u, device, stream);
+    if (rc) { delete b; return rc; }
+    b->stream = b->u->stream;
+    b->voff.push_back(0);
+    *out = b;
+    return GRZ_OK;
+}
+
+static void free_state(grz_batch* b)
+{
+    void* p[] = { b->d_voff, b->d_seeds, b->prop[0], b->prop[1], b->rank, b->rowacc, b->S[0], b->S[1],
+                  b->visited, b->frontier, b->next_words, b->level, b->ctl, b->iter };
+    for (void* x : p) cudaFree(x);
+    b->d_voff = b->d_seeds = nullptr;
+    b->prop[0] = b->prop[1] = b->rank = nullptr;
+    b->rowacc = b->S[0] = b->S[1] = nullptr;
+    b->visited = b->frontier = nullptr;
+    b->next_words = nullptr;
+    b->level = nullptr;
+    b->ctl = nullptr;
+    b->iter = nullptr;
+    if (b->ppr_exec) cudaGraphExecDestroy(b->ppr_exec);
+    if (b->bfs_exec) cudaGraphExecDestroy(b->bfs_exec);
+    b->ppr_exec = b->bfs_exec = nullptr;
+}
+
+extern "C" void grz_batch_destroy(grz_batch* b)
+{
+    if (!b) return;
+    cudaSetDevice(b->device);
+    free_state(b);
+    if (b->mail) cudaFreeHost(b->mail);
+    grz_graph_destroy(b->u);
+    delete b;
+}
+
+extern "C" const char* grz_batch_last_error(const grz_batch* b) { return b ? b->err : ""; }
+
+// Adds one graph: V vertices, E edges as interleaved (src, dst) pairs sorted by (dst, src) (the
+// -pull order, source/graphdata.c:957).  Copied; the union is built by grz_batch_build.
+extern "C" int grz_batch_add_graph(grz_batch* b, uint64_t V, uint64_t E, const uint64_t* pull_pairs)
+{
+    if (!b || V == 0 || (E > 0 && !pull_pairs)) return GRZ_ERR_ARG;
+    if (b->voff.size() > MAX_GRAPHS) return bset(b, GRZ_ERR_RANGE, "too many graphs");
+    if (V < TV) return bset(b, GRZ_ERR_RANGE, "a batched graph needs at least 32 vertices");
+    const uint64_t base = b->voff.back();
+    if (base + V >= GRZ_HUB_BASE) return bset(b, GRZ_ERR_RANGE, "the union exceeds 2^31 vertices");
+    std::vector<uint64_t> p(2 * E);
+    for (uint64_t e = 0; e < E; ++e) {
+        const uint64_t s = pull_pairs[2 * e], d = pull_pairs[2 * e + 1];
+        if (s >= V || d >= V) return bset(b, GRZ_ERR_RANGE, "vertex ID out of range");
+        if (e > 0) {
+            const uint64_t ps = pull_pairs[2 * e - 2], pd = pull_pairs[2 * e - 1];
+            if (d < pd || (d == pd && s < ps)) return bset(b, GRZ_ERR_UNSORTED, "pairs are not in (dst, src) order");
+        }
+        p[2 * e] = s + base;
+        p[2 * e + 1] = d + base;
+    }
+    b->pairs.push_back(std::move(p));
+    b->Vg.push_back(V);
+    b->Eg.push_back(E);
+    b->voff.push_back((uint32_t)(base + V));
+    return GRZ_OK;
+}
+
+extern "C" int grz_batch_build(grz_batch* b)
+{
+    if (!b || b->pairs.empty()) return GRZ_ERR_ARG;
+    BCK(b, cudaSetDevice(b->device));
+    free_state(b);
+    uint64_t E = 0;
+    for (uint64_t e : b->Eg) E += e;
+    std::vector<uint64_t> all;
+    all.reserve(2 * E);
+    for (auto& p : b->pairs) all.insert(all.end(), p.begin(), p.end());
+    const uint64_t V = b->voff.back();
+    int rc = grz_graph_load_pairs(b->u, V, E, E ? all.data() : nullptr, nullptr);
+    if (rc) return bset(b, rc, grz_graph_last_error(b->u));
+    const uint32_t G = (uint32_t)b->Vg.size();
+    BCK(b, cudaMalloc((void**)&b->d_voff, sizeof(uint32_t) * (G + 1)));
+    BCK(b, cudaMemcpy(b->d_voff, b->voff.data(), sizeof(uint32_t) * (G + 1), cudaMemcpyHostToDevice));
+    BCK(b, cudaMalloc((void**)&b->d_seeds, sizeof(uint32_t) * G * K));
+    if (!b->mail) BCK(b, cudaMallocHost(&b->mail, 64));
+    return GRZ_OK;
+}
+
+extern "C" int grz_batch_info(const grz_batch* b, uint64_t* graphs, uint64_t* vertices, uint64_t* edges, uint64_t* vectors)
+{
+    if (!b) return GRZ_ERR_ARG;
+    if (graphs) *graphs = b->Vg.size();
+    if (vertices) *vertices = b->voff.back();
+    if (edges) *edges = b->u->E;
+    if (vectors) *vectors = b->u->pull.nvec;
+    return GRZ_OK;
+}
+
+static int upload_seeds(grz_batch* b, const uint32_t* local, uint32_t k)
+{
+    const uint32_t G = (uint32_t)b->Vg.size();
+    std::vector<uint32_t> s((size_t)G * K, NONE);
+    for (uint32_t g = 0; g < G; ++g)
+        for (uint32_t i = 0; i < k; ++i) {
+            const uint32_t x = local[(size_t)g * k + i];
+            if (x == NONE) continue;
+            if (x >= b->Vg[g]) return bset(b, GRZ_ERR_ARG, "seed or root outside its graph");
+            s[(size_t)g * K + i] = b->voff[g] + x;
+        }
+    BCK(b, cudaMemcpyAsync(b->d_seeds, s.data(), sizeof(uint32_t) * s.size(), cudaMemcpyHostToDevice, b->stream));
+    BCK(b, cudaStreamSynchronize(b->stream));
+    return GRZ_OK;
+}
+
+// the fixed-length PPR iteration loop as one CUDA graph (gather + apply per iteration)
+static int build_ppr_graph(grz_batch* b, uint32_t iterations, double damping)
+{
+    if (b->ppr_exec) { cudaGraphExecDestroy(b->ppr_exec); b->ppr_exec = nullptr; }
+    grz_graph* u = b->u;
+    const uint32_t V = (uint32_t)u->V, G = (uint32_t)b->Vg.size();
+    cudaStream_t cs = nullptr;
+    BCK(b, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t graph = nullptr;
+    int rc = bck(b, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "begin capture");
+    const unsigned ggrid = persistent_grid(b, (u->pull.nvec + TV - 1) / TV, 8);
+    const unsigned agrid = persistent_grid(b, (V + TV - 1) / TV, 8);
+    int cur = 0;
+    for (uint32_t it = 0; it < iterations && !rc; ++it) {
+        k_ppr_gather<<<ggrid, GT, 0, cs>>>(u->pull.nbr, u->pull.shared, u->pull.nvec, V, b->prop[cur], b->rowacc, b->S[cur ^ 1], G * K);
+        k_ppr_apply<<<agrid, GT, 0, cs>>>(b->rowacc, u->inv_deg, u->degree, V, b->d_voff, G, b->d_seeds, damping, b->S[cur],
+                                         b->S[cur ^ 1], b->prop[cur ^ 1], it + 1 == iterations ? b->rank : nullptr);
+        cur ^= 1;
+        rc = bck(b, cudaGetLastError(), "ppr launch");
+    }
+    const cudaError_t e = cudaStreamEndCapture(cs, &graph);
+    if (!rc) rc = bck(b, e, "end capture");
+    if (!rc) rc = bck(b, cudaGraphInstantiate(&b->ppr_exec, graph, 0), "instantiate");
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(cs);
+    if (rc) { b->ppr_exec = nullptr; return rc; }
+    b->ppr_iters = iterations;
+    b->ppr_damping = damping;
+    b->ppr_final = cur;
+    return GRZ_OK;
+}
+
+// k seeds per graph (local vertex IDs, NONE = unused instance), `iterations` PPR iterations;
+// ranks out as [union vertex][k] (graph g's vertex v at row voff[g] + v)
+extern "C" int grz_batch_ppr(grz_batch* b, const uint32_t* seeds, uint32_t k, uint32_t iterations, double damping,
+                             double* ranks_out, grz_run_stats_t* stats)
+{
+    if (!b || !seeds || k == 0 || k > (uint32_t)K || iterations == 0 || !(damping >= 0.0 && damping <= 1.0)) return GRZ_ERR_ARG;
+    if (!b->d_seeds) return bset(b, GRZ_ERR_STATE, "grz_batch_build not called");
+    BCK(b, cudaSetDevice(b->device));
+    grz_graph* u = b->u;
+    const uint64_t V = u->V;
+    const uint32_t G = (uint32_t)b->Vg.size();
+    if (!b->prop[0]) {
+        BCK(b, cudaMalloc((void**)&b->prop[0], sizeof(double) * V * K));
+        BCK(b, cudaMalloc((void**)&b->prop[1], sizeof(double) * V * K));
+        BCK(b, cudaMalloc((void**)&b->rank, sizeof(double) * V * K));
+        BCK(b, cudaMalloc((void**)&b->rowacc, sizeof(u128) * (V + 1) * K));
+        BCK(b, cudaMalloc((void**)&b->S[0], sizeof(u128) * G * K));
+        BCK(b, cudaMalloc((void**)&b->S[1], sizeof(u128) * G * K));
+        BCK(b, cudaMemsetAsync(b->rowacc, 0, sizeof(u128) * (V + 1) * K, b->stream));
+    }
+    int rc = upload_seeds(b, seeds, k);
+    if (rc) return rc;
+    if (!b->ppr_exec || b->ppr_iters != iterations || b->ppr_damping != damping) {
+        rc = build_ppr_graph(b, iterations, damping);
+        if (rc) return rc;
+    }
+    cudaEvent_t e0, e1;
+    BCK(b, cudaEventCreate(&e0));
+    BCK(b, cudaEventCreate(&e1));
+    cudaStream_t st = b->stream;
+    rc = bck(b, cudaEventRecord(e0, st), "event");
+    if (!rc) rc = bck(b, cudaMemsetAsync(b->prop[0], 0, sizeof(double) * V * K, st), "memset");
+    if (!rc) {
+        k_ppr_init<<<(G * K + 255) / 256, 256, 0, st>>>(b->d_seeds, G, u->inv_deg, u->degree, b->prop[0], b->S[0]);
+        rc = bck(b, cudaGetLastError(), "ppr init");
+    }
+    if (!rc) rc = bck(b, cudaGraphLaunch(b->ppr_exec, st), "graph launch");
+    if (!rc) rc = bck(b, cudaEventRecord(e1, st), "event");
+    if (!rc && ranks_out) {
+        if (k == (uint32_t)K) {
+            rc = bck(b, cudaMemcpyAsync(ranks_out, b->rank, sizeof(double) * V * K, cudaMemcpyDeviceToHost, st), "D2H");
+        } else {
+            rc = bck(b, cudaMemcpy2DAsync(ranks_out, sizeof(double) * k, b->rank, sizeof(double) * K, sizeof(double) * k, V,
+                                          cudaMemcpyDeviceToHost, st), "D2H");
+        }
+    }
+    if (!rc) rc = bck(b, cudaStreamSynchronize(st), "run");
+    if (!rc && stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->iterations = iterations;
+        stats->pull_iterations = iterations;
+        cudaEventElapsedTime(&stats->ms, e0, e1);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    u->nlaunch += 1 + 2ull * iterations;
+    return rc;
+}
+
+// the BFS loop as one CUDA graph: WHILE (a bit changed) { pull; vertex pass; decide }
+static int build_bfs_graph(grz_batch* b)
+{
+    if (b->bfs_exec) { cudaGraphExecDestroy(b->bfs_exec); b->bfs_exec = nullptr; }
+    grz_graph* u = b->u;
+    const uint32_t V = (uint32_t)u->V;
+    cudaGraph_t top = nullptr;
+    BCK(b, cudaGraphCreate(&top, 0));
+    cudaGraphConditionalHandle loop = 0;
+    int rc = bck(b, cudaGraphConditionalHandleCreate(&loop, top, 1, cudaGraphCondAssignDefault), "handle");
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = loop;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    if (!rc) rc = bck(b, cudaGraphAddNode(&node, top, nullptr, nullptr, 0, &p), "while node");
+    cudaStream_t cs = nullptr;
+    if (!rc) rc = bck(b, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "stream");
+    if (!rc) rc = bck(b, cudaStreamBeginCaptureToGraph(cs, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                      cudaStreamCaptureModeThreadLocal), "capture");
+    if (!rc) {
+        const unsigned pgrid = persistent_grid(b, (u->pull.nvec + 255) / 256, 8);
+        const unsigned vgrid = persistent_grid(b, ((V + 3) / 4 + 255) / 256, 8);
+        k_msbfs_pull<<<pgrid, 256, 0, cs>>>(u->pull.nbr, u->pull.shared, u->pull.nvec, V, b->frontier, b->visited, b->next_words);
+        k_msbfs_vertex<<<vgrid, 256, 0, cs>>>(b->next_words, reinterpret_cast<unsigned*>(b->visited),
+                                              reinterpret_cast<unsigned*>(b->frontier), b->level, V, b->iter, b->ctl);
+        k_msbfs_decide<<<1, 1, 0, cs>>>(b->ctl, b->iter, V + 1, loop);
+        rc = bck(b, cudaGetLastError(), "bfs launch");
+        cudaGraph_t g2 = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(cs, &g2);
+        if (!rc) rc = bck(b, e, "end capture");
+    }
+    if (cs) cudaStreamDestroy(cs);
+    if (!rc) rc = bck(b, cudaGraphInstantiate(&b->bfs_exec, top, 0), "instantiate");
+    cudaGraphDestroy(top);
+    if (rc) b->bfs_exec = nullptr;
+    return rc;
+}
+
+// k roots per graph (local IDs, NONE = unused instance); levels out as [union vertex][k]
+// (-1 = unreached)
+extern "C" int grz_batch_msbfs(grz_batch* b, const uint32_t* roots, uint32_t k, int32_t* levels_out, grz_run_stats_t* stats)
+{
+    if (!b || !roots || k == 0 || k > (uint32_t)K) return GRZ_ERR_ARG;
+    if (!b->d_seeds) return bset(b, GRZ_ERR_STATE, "grz_batch_build not called");
+    BCK(b, cudaSetDevice(b->device));
+    grz_graph* u = b->u;
+    const uint64_t V = u->V;
+    const uint32_t G = (uint32_t)b->Vg.size();
+    const uint64_t Vw = (V + 3) / 4 * 4;
+    if (!b->visited) {
+        BCK(b, cudaMalloc((void**)&b->visited, Vw));
+        BCK(b, cudaMalloc((void**)&b->frontier, Vw));
+        BCK(b, cudaMalloc((void**)&b->next_words, Vw));
+        BCK(b, cudaMalloc((void**)&b->level, sizeof(int32_t) * V * K));
+        BCK(b, cudaMalloc((void**)&b->ctl, sizeof(unsigned long long) * 4));
+        BCK(b, cudaMalloc((void**)&b->iter, sizeof(uint32_t)));
+    }
+    int rc = upload_seeds(b, roots, k);
+    if (rc) return rc;
+    if (!b->bfs_exec) {
+        rc = build_bfs_graph(b);
+        if (rc) return rc;
+    }
+    cudaStream_t st = b->stream;
+    cudaEvent_t e0, e1;
+    BCK(b, cudaEventCreate(&e0));
+    BCK(b, cudaEventCreate(&e1));
+    const uint32_t one = 1;
+    rc = bck(b, cudaEventRecord(e0, st), "event");
+    if (!rc) rc = bck(b, cudaMemsetAsync(b->visited, 0, Vw, st), "memset");
+    if (!rc) rc = bck(b, cudaMemsetAsync(b->frontier, 0, Vw, st), "memset");
+    if (!rc) rc = bck(b, cudaMemsetAsync(b->next_words, 0, Vw, st), "memset");
+    if (!rc) rc = bck(b, cudaMemsetAsync(b->level, 0xff, sizeof(int32_t) * V * K, st), "memset");
+    if (!rc) rc = bck(b, cudaMemsetAsync(b->ctl, 0, sizeof(unsigned long long) * 4, st), "memset");
+    if (!rc) {
+        memcpy(b->mail, &one, sizeof(one));
+        rc = bck(b, cudaMemcpyAsync(b->iter, b->mail, sizeof(uint32_t), cudaMemcpyHostToDevice, st), "H2D");
+    }
+    if (!rc) {
+        k_msbfs_init<<<(G * K + 255) / 256, 256, 0, st>>>(b->d_seeds, G * K, b->visited, b->frontier, b->level);
+        rc = bck(b, cudaGetLastError(), "bfs init");
+    }
+    if (!rc) rc = bck(b, cudaGraphLaunch(b->bfs_exec, st), "graph launch");
+    if (!rc) rc = bck(b, cudaEventRecord(e1, st), "event");
+    if (!rc) rc = bck(b, cudaMemcpyAsync(b->mail, b->ctl, sizeof(unsigned long long) * 3, cudaMemcpyDeviceToHost, st), "D2H");
+    if (!rc && levels_out) {
+        if (k == (uint32_t)K)
+            rc = bck(b, cudaMemcpyAsync(levels_out, b->level, sizeof(int32_t) * V * K, cudaMemcpyDeviceToHost, st), "D2H");
+        else
+            rc = bck(b, cudaMemcpy2DAsync(levels_out, sizeof(int32_t) * k, b->level, sizeof(int32_t) * K, sizeof(int32_t) * k, V,
+                                          cudaMemcpyDeviceToHost, st), "D2H");
+    }
+    if (!rc) rc = bck(b, cudaStreamSynchronize(st), "run");
+    unsigned long long c[3];
+    memcpy(c, b->mail, sizeof(c));
+    if (!rc && c[2] == 1) rc = bset(b, GRZ_ERR_STATE, "BFS did not converge within V + 1 iterations");
+    if (!rc && c[2] == 2) rc = bset(b, GRZ_ERR_STATE, "BFS stopped by its time bound");
+    if (!rc && stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->iterations = (uint32_t)c[1] + 1;  // the last iteration found nothing new
+        stats->pull_iterations = stats->iterations;
+        cudaEventElapsedTime(&stats->ms, e0, e1);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    u->nlaunch += 1 + 3ull * (c[1] + 1);
+    return rc;
+}
+
+extern "C" unsigned long long grz_batch_launch_count(const grz_batch* b) { return b ? b->u->nlaunch : 0ull; }

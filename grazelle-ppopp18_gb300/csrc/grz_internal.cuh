@@ -192,6 +192,8 @@ struct grz_list {
 #define GRZ_HUB_BASE 0x80000000u
 #define GRZ_HUB_MAX 49152u
 
+#define GRZ_BATCH_K 8  // instances per graph of a batch (grz_batch.cu)
+
 // the vertex a pull-list neighbour field names (GRZ_INVALID_ID stays invalid)
 __device__ __forceinline__ uint32_t grz_hub_decode(uint32_t x, const uint32_t* __restrict__ hub_vid, uint32_t nhub)
 {

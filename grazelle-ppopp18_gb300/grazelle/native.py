@@ -27,6 +27,7 @@ class GrzError(RuntimeError):
 
 
 FORCE_PULL, FORCE_PUSH, WITHOUT_COUNT, WITHOUT_OUTDEG = 1, 2, 4, 8
+BATCH_K = 8
 TUNE_HUBS, TUNE_CC_CACHE, TUNE_CC_THREADS, TUNE_CC_GRID, TUNE_HUBS_LOADED = 0, 1, 2, 3, 100
 FLAG_HOST_LOOP = 16  # grz_cc_run / grz_bfs_run: host round trip per iteration instead of one CUDA graph
 MLP_FEATURES, MLP_HIDDEN, MLP_PARAMS = 12, 32, 1505
@@ -75,6 +76,15 @@ SIGNATURES = {
     "grz_read_levels": (_I, [_VP, _VP, _U64]),
     "grz_result_digest": (_I, [_VP, _VP]),
     "grz_tune_set": (_I, [_VP, _I, C.c_int64]),
+    "grz_batch_create": (_I, [C.POINTER(_VP), _I, _VP]),
+    "grz_batch_destroy": (None, [_VP]),
+    "grz_batch_last_error": (C.c_char_p, [_VP]),
+    "grz_batch_add_graph": (_I, [_VP, _U64, _U64, _VP]),
+    "grz_batch_build": (_I, [_VP]),
+    "grz_batch_info": (_I, [_VP, _VP, _VP, _VP, _VP]),
+    "grz_batch_ppr": (_I, [_VP, _VP, _U32, _U32, _D, _VP, _VP]),
+    "grz_batch_msbfs": (_I, [_VP, _VP, _U32, _VP, _VP]),
+    "grz_batch_launch_count": (C.c_ulonglong, [_VP]),
     "grz_tune_get": (_I, [_VP, _I, _VP]),
     "grz_frontier_begin": (_I, [_VP, _I, _U32, _I]),
     "grz_frontier_next": (_I, [_VP, _I, C.POINTER(C.c_int), C.POINTER(C.c_uint64)]),

@@ -136,6 +136,30 @@ int grz_read_levels(grz_graph* g, int64_t* host_levels, uint64_t capacity);
 int grz_tune_set(grz_graph* g, int param, int64_t value);
 int grz_tune_get(const grz_graph* g, int param, int64_t* value);
 
+/* -------- batches: many PPR and BFS instances over many graphs (no counterpart in the reference) --------
+ * Graphs of any size are added with their -pull pairs and merged into one block-diagonal union
+ * on the device.  Each run processes up to GRZ_BATCH_K instances of every graph in one CUDA graph
+ * launch.  Outputs are [union vertex][k]: graph g's local vertex v is row voff[g] + v, where voff
+ * is the running sum of the vertex counts of the graphs added before g.
+ * Personalized PageRank: the reference's PageRank vertex phase (source/phase_vertex_pr.asm:75-134)
+ * with teleport and dangling mass sent to the seed: rank' = d*accum + [v == seed]*(d*(1-S) + 1-d),
+ * starting from rank = one-hot(seed); edge sums exact (fixed point), rounded once to double.
+ * Multi-source BFS: levels (-1 unreached), bit-parallel over the instances of a graph. */
+#define GRZ_BATCH_K 8
+typedef struct grz_batch grz_batch;
+int grz_batch_create(grz_batch** out, int device, void* stream);
+void grz_batch_destroy(grz_batch* b);
+const char* grz_batch_last_error(const grz_batch* b);
+/* pull_pairs: interleaved (src, dst) sorted by (dst, src); graphs need at least 32 vertices */
+int grz_batch_add_graph(grz_batch* b, uint64_t num_vertices, uint64_t num_edges, const uint64_t* pull_pairs);
+int grz_batch_build(grz_batch* b);
+int grz_batch_info(const grz_batch* b, uint64_t* graphs, uint64_t* vertices, uint64_t* edges, uint64_t* vectors);
+/* seeds / roots: [graphs][k] local vertex IDs, 0xffffffff = no instance; k <= GRZ_BATCH_K */
+int grz_batch_ppr(grz_batch* b, const uint32_t* seeds, uint32_t k, uint32_t iterations, double damping,
+                  double* ranks_out, grz_run_stats_t* stats);
+int grz_batch_msbfs(grz_batch* b, const uint32_t* roots, uint32_t k, int32_t* levels_out, grz_run_stats_t* stats);
+unsigned long long grz_batch_launch_count(const grz_batch* b);
+
 /* Digest of the last CC/BFS result without reading it back (no counterpart in the reference):
  * out[0] = reached vertices (BFS) or components (CC: vertices whose label is their own ID),
  * out[1] = sum of the reached vertices' out-degrees (BFS; the TEPS numerator),

@@ -349,6 +349,8 @@ def extra_apps(a, G_cc, g_cc, torch, stream, hbm, hbm_kind):
     out["cc_switch"] = cc
     if a.bfs_scale:
         out["bfs_switch"] = bfs_switch_study(a, torch, stream, net, dev)
+    if not a.no_batch:
+        out["batch"] = batch_study(a, torch, stream, dev)
     # PageRank
     g, pull, push = make_graph("pr", 20, a.seed)
     V, E = g.num_vertices, g.num_edges
@@ -426,6 +428,80 @@ def bfs_switch_study(a, torch, stream, net, dev):
     return res
 
 
+def batch_graphs(seed: int):
+    """32 seeded graphs of uneven size: R-MAT scales 14-22 and Erdos-Renyi with average degree
+    4-64."""
+    from grazelle import graphgen as gg
+    out = []
+    for i in range(32):
+        if i % 2 == 0:
+            s = 14 + (i // 2) % 9
+            out.append(("rmat%d" % s, gg.rmat(s, 16, seed=seed + 1000 + i)))
+        else:
+            ln, d = 14 + (i // 2) % 7, 4 << ((i // 2) % 5)
+            out.append(("er%d_d%d" % (ln, d), gg.erdos_renyi(1 << ln, d, seed=seed + 1000 + i)))
+    return out
+
+
+def batch_study(a, torch, stream, dev):
+    """256 personalized-PageRank instances (8 seeds per graph, 20 iterations, d = 0.85, FP64
+    ranks) and 256 BFS instances (8 roots per graph) over the 32 graphs, each run one CUDA graph
+    launch of the batch; every instance of two graphs checked against the CPU oracles."""
+    from grazelle.batch import Batch
+    from oracle import oracle as O
+    from oracle import ppr as P
+    t0 = time.time()
+    gs = batch_graphs(a.seed)
+    E_tot = sum(g.num_edges for _, g in gs)
+    log("batch graphs: %d, E=%d (%.1fs)" % (len(gs), E_tot, time.time() - t0))
+    seeds = [pick_roots(g, 8, seed=a.seed + 7 * i) for i, (_, g) in enumerate(gs)]
+    res = {"workload": "32 graphs (R-MAT 14-22, ER degree 4-64), 256 PPR x 20 iterations + 256 BFS",
+           "graphs": len(gs), "edges": E_tot}
+    with Batch(dev, stream=stream.cuda_stream) as B:
+        t1 = time.time()
+        for _, g in gs:
+            B.add_graph(g.num_vertices, g.pull_order().pairs())
+        B.build()
+        res["build_s"] = round(time.time() - t1, 2)
+        B.ppr(seeds, 20, 0.85, ranks=False)
+        ms = []
+        for _ in range(max(1, a.steps)):
+            _, st = B.ppr(seeds, 20, 0.85, ranks=False)
+            ms.append(st.ms)
+        ranks, _ = B.ppr(seeds, 20, 0.85)
+        ppr_ms = float(np.median(ms))
+        n_inst = sum(len(s) for s in seeds)
+        # edge-instance updates: every instance traverses its graph's edges once per iteration
+        upd = sum(g.num_edges * len(s) for (_, g), s in zip(gs, seeds)) * 20
+        res["ppr"] = {"instances": n_inst, "ms": round(ppr_ms, 3), "gteps": round(upd / (ppr_ms * 1e-3) / 1e9, 2),
+                      "ms_per_instance": round(ppr_ms / n_inst, 4)}
+        B.msbfs(seeds, levels=False)
+        ms = []
+        for _ in range(max(1, a.steps)):
+            _, st = B.msbfs(seeds, levels=False)
+            ms.append(st.ms)
+        levels, st = B.msbfs(seeds)
+        bfs_ms = float(np.median(ms))
+        reached = 0
+        for (_, g), lv in zip(gs, levels):
+            deg = g.out_degrees()
+            for i in range(lv.shape[1]):
+                reached += int(deg[lv[:, i] >= 0].sum())
+        res["msbfs"] = {"instances": n_inst, "ms": round(bfs_ms, 3), "iterations": st.iterations,
+                        "gteps": round(reached / (bfs_ms * 1e-3) / 1e9, 2)}
+        worst, exact = 0.0, True
+        for gi in (0, 1):
+            g = gs[gi][1]
+            pull, push = g.pull_order().pairs(), g.push_order().pairs()
+            for i, s in enumerate(seeds[gi]):
+                ref = P.ppr(g.num_vertices, pull, s, 20, 0.85)
+                worst = max(worst, float(np.abs(ranks[gi][:, i] - ref).sum() / np.abs(ref).sum()))
+                exact &= bool(np.array_equal(levels[gi][:, i].astype(np.int64), O.bfs_levels(push, g.num_vertices, s)))
+        res["parity_sample"] = {"ppr_max_rel_l1": worst, "bfs_levels_exact": exact, "graphs_checked": [gs[0][0], gs[1][0]]}
+        res["gpu_launches_per_run"] = {"ppr": 1 + 2 * 20, "msbfs": 1 + 3 * st.iterations}
+    return res
+
+
 # ---------------------------------------------------------------------------------------------- CPU
 
 def cpu_baseline(wl, g, pull, push, scale, sample=True, threads=0, steps=1):
@@ -499,6 +575,7 @@ def main():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-apps", action="store_true")
     ap.add_argument("--bfs-scale", type=int, default=26, help="R-MAT scale of the BFS switch study (0: skip)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched PPR / multi-source BFS study")
     ap.add_argument("--no-cpu", action="store_true")
     a = ap.parse_args()
     if a.warmup < 3:

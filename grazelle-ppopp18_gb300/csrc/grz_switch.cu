@@ -131,6 +131,8 @@ __global__ void __launch_bounds__(T) k_features_decide(FeatIn in, const float* _
     __shared__ float f[NF];
     __shared__ float h[NH];
     __shared__ float sp[NP];
+    if (use_mlp)
+        for (int k = threadIdx.x; k < NP; k += T) sp[k] = __ldg(params + k);  // staged while counting
     unsigned pf = 0, pw = 0;
     for (uint64_t w = (uint64_t)blockIdx.x * T + threadIdx.x; w < in.words; w += (uint64_t)gridDim.x * T) {
         pf += __popcll(in.frontier[w]);
@@ -164,8 +166,6 @@ __global__ void __launch_bounds__(T) k_features_decide(FeatIn in, const float* _
     __syncwarp();
     int pull;
     if (use_mlp) {
-        for (int i = lane; i < NP; i += 32) sp[i] = params[i];  // coalesced, then the forward from shared memory
-        __syncwarp();
         pull = mlp_logit_warp(sp, f, h, lane) > 0.f ? 1 : 0;
     } else {
         pull = (double)vote > threshold ? 1 : 0;
@@ -205,6 +205,10 @@ __global__ void __launch_bounds__(T) k_run_decide(RunIn in, grz_runctl* __restri
     __shared__ float sp[NP];
     if (!in.initial && !*(volatile uint32_t*)&ctl->running) return;
     const FeatIn& fi = in.feat;
+    // every block stages the MLP parameters (6 KB) while it counts; only the last block uses them
+    const float* params = ctl->params;
+    if (params && ctl->force < 0)
+        for (int i = threadIdx.x; i < NP; i += T) sp[i] = __ldg(params + i);
     unsigned pf = 0, pw = 0;
     for (uint64_t w = (uint64_t)blockIdx.x * T + threadIdx.x; w < fi.words; w += (uint64_t)gridDim.x * T) {
         pf += __popcll(fi.frontier[w]);
@@ -260,12 +264,9 @@ __global__ void __launch_bounds__(T) k_run_decide(RunIn in, grz_runctl* __restri
     if (lane < NF) f[lane] = feature(lane, fe, (float)F, (float)U, (float)vote);
     __syncwarp();
     int pull;
-    const float* params = ctl->params;
     if (ctl->force >= 0) {
         pull = ctl->force;
     } else if (params) {
-        for (int i = lane; i < NP; i += 32) sp[i] = params[i];  // coalesced, then the forward from shared memory
-        __syncwarp();
         pull = mlp_logit_warp(sp, f, h, lane) > 0.f ? 1 : 0;
     } else {
         pull = (double)vote > ctl->threshold ? 1 : 0;

@@ -153,8 +153,8 @@ class Switch:
         return z
 
 
-def training_graphs(scales=(18, 19, 20, 21, 22), er_degrees=(8, 16, 32), er_log2n=(18, 20), seed: int = 100):
-    """Seeded R-MAT and Erdős–Rényi training graphs (BASELINE config 3: R-MAT 18-23, ER degree 8-32)."""
+def training_graphs(scales=(18, 19, 20, 21, 22, 23), er_degrees=(8, 16, 32), er_log2n=(18, 20), seed: int = 100):
+    """Seeded R-MAT (scales 18-23) and Erdős–Rényi (average degree 8-32) training graphs."""
     out = []
     for i, s in enumerate(scales):
         out.append(("rmat%d" % s, gg.rmat(s, seed=seed + i)))

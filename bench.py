@@ -59,6 +59,20 @@ def dist_env():
     return rank, world, local
 
 
+def combine_ranks(units: float, ms: float, dist=None, device: str = "cuda"):
+    """Whole-job (units, ms) over the replicas: units summed over ranks, time the slowest rank's
+    (max over ranks).  Without a process group the local values pass through."""
+    if dist is None:
+        return units, ms
+    import torch
+    t = torch.tensor([float(units), float(ms)], dtype=torch.float64, device=device)
+    u = t[:1].clone()
+    m = t[1:].clone()
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    dist.all_reduce(m, op=dist.ReduceOp.MAX)
+    return float(u.item()), float(m.item())
+
+
 def measured_hbm():
     p = REPO / "MEASURED_PEAKS.json"
     try:
@@ -202,18 +216,16 @@ def run_native(a):
     G = Graph(local, stream=stream.cuda_stream)
     G.load_pointers(V, E, pin_pull.data_ptr(), pin_push.data_ptr())
     hbm, hbm_kind = measured_hbm()
+    # kernel shapes for this graph, chosen by timing (outside every timed region)
+    from grazelle import autotune
+    tuned = autotune.tune_cc(G, device=local) if wl in ("cc", "bfs") else autotune.tune_pr(G, device=local)
+    tuned.pop("trials", None)
 
     def barrier():
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
 
-    def max_over_ranks(x):
-        if not dist:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
 
     # one step of the workload, graph resident; returns (teps units, iterations)
     roots = pick_roots(g, 8) if wl == "bfs" else []
@@ -245,8 +257,8 @@ def run_native(a):
                 units += u
                 iters += it
     launches = G.launch_count() - l0
-    ms = max_over_ranks(tm.ms)
-    value = world * units / (ms * 1e-3) / 1e9
+    units_all, ms = combine_ranks(units, tm.ms, dist)
+    value = units_all / (ms * 1e-3) / 1e9
 
     # Per-kernel CUDA-event durations for the roofline: the same K steps once more with kernel
     # profiling on.  The event pairs need host-launched kernels, so CC/BFS run their host loop
@@ -288,8 +300,8 @@ def run_native(a):
             u, _ = step(i)
             e2e_units += u
             G.lib.grz_read_props(G.h, d2h.ctypes.data, V)
-    e2e_ms = max_over_ranks(te.ms)
-    e2e = {"value": round(world * e2e_units / (e2e_ms * 1e-3) / 1e9, 3), "unit": "GTEPS",
+    e2e_units_all, e2e_ms = combine_ranks(e2e_units, te.ms, dist)
+    e2e = {"value": round(e2e_units_all / (e2e_ms * 1e-3) / 1e9, 3), "unit": "GTEPS",
            "h2d_bytes_per_step": int(pull.nbytes + push.nbytes), "d2h_bytes_per_step": int(d2h.nbytes),
            "ms_per_step": round(e2e_ms / a.steps, 3)}
 
@@ -312,7 +324,7 @@ def run_native(a):
                    "rmat_abcd": [0.57, 0.19, 0.19, 0.05], "seed": a.seed, "V": V, "E": E,
                    "engine": "threshold heuristic (E/5)" if wl != "pr" else "pull", "iterations_per_step": iters / a.steps,
                    "l2": "inputs larger than L2 (%.1f GB of edge vectors)" % (G.info().pull_vectors * 20 / 1e9),
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "parallelism": "replicas" if world > 1 else "single GPU", "autotuned": tuned},
         "roofline": roof, "kernels": {k: {"n": v["n"], "mean_us": round(v["mean_ms"] * 1e3, 2)} for k, v in ks.items()},
         "e2e": e2e, "gpu_launches": int(launches), "clocks": clk.summary(), "cpu_baseline": cpu, "apps": apps,
     }
@@ -463,6 +475,10 @@ def batch_study(a, torch, stream, dev):
             B.add_graph(g.num_vertices, g.pull_order().pairs())
         B.build()
         res["build_s"] = round(time.time() - t1, 2)
+        from grazelle import autotune
+        tb = autotune.tune_batch(B, seeds)
+        res["autotuned"] = {k: {"best": v["best"], "best_ms": round(v["best_ms"], 3),
+                                "default_ms": round(v["default_ms"], 3) if v["default_ms"] else None} for k, v in tb.items()}
         B.ppr(seeds, 20, 0.85, ranks=False)
         ms = []
         for _ in range(max(1, a.steps)):

@@ -101,6 +101,7 @@ extern "C" int grz_graph_create(grz_graph** out, int device, void* stream)
     g->tune.cc_cache = 16384;
     g->tune.cc_threads = 512;
     g->tune.cc_grid = 0;
+    g->tune.pr_grid = 0;
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e != cudaSuccess) {
@@ -557,6 +558,10 @@ extern "C" int grz_tune_set(grz_graph* g, int param, int64_t value)
         if (value > (1 << 20)) return GRZ_ERR_RANGE;
         g->tune.cc_grid = (uint32_t)value;
         return GRZ_OK;
+    case GRZ_TUNE_PR_GRID:
+        if (value > (1 << 20)) return GRZ_ERR_RANGE;
+        g->tune.pr_grid = (uint32_t)value;
+        return GRZ_OK;
     default:
         return grz_set_error(g, GRZ_ERR_ARG, "unknown tuning parameter %d", param);
     }
@@ -570,6 +575,7 @@ extern "C" int grz_tune_get(const grz_graph* g, int param, int64_t* value)
     case GRZ_TUNE_CC_CACHE: *value = g->tune.cc_cache; return GRZ_OK;
     case GRZ_TUNE_CC_THREADS: *value = g->tune.cc_threads; return GRZ_OK;
     case GRZ_TUNE_CC_GRID: *value = g->tune.cc_grid; return GRZ_OK;
+    case GRZ_TUNE_PR_GRID: *value = g->tune.pr_grid; return GRZ_OK;
     case GRZ_TUNE_HUBS_LOADED: *value = g->pull.nhub; return GRZ_OK;
     default: return GRZ_ERR_ARG;
     }

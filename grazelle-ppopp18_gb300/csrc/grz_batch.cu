@@ -335,6 +335,7 @@ struct grz_batch {
     unsigned long long* ctl;             // changed, iterations, bound hit
     uint32_t* iter;
     cudaGraphExec_t bfs_exec;
+    int ppr_blocks, bfs_blocks;          // resident blocks per SM of the persistent kernels
     void* mail;                          // pinned host read-back
     char err[256];
 };
@@ -370,6 +371,8 @@ extern "C" int grz_batch_create(grz_batch** out, int device, void* stream)
     if (rc) { delete b; return rc; }
     b->stream = b->u->stream;
     b->voff.push_back(0);
+    b->ppr_blocks = 8;
+    b->bfs_blocks = 8;
     *out = b;
     return GRZ_OK;
 }
@@ -488,8 +491,8 @@ static int build_ppr_graph(grz_batch* b, uint32_t iterations, double damping)
     BCK(b, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     cudaGraph_t graph = nullptr;
     int rc = bck(b, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "begin capture");
-    const unsigned ggrid = persistent_grid(b, (u->pull.nvec + TV - 1) / TV, 8);
-    const unsigned agrid = persistent_grid(b, (V + TV - 1) / TV, 8);
+    const unsigned ggrid = persistent_grid(b, (u->pull.nvec + TV - 1) / TV, b->ppr_blocks);
+    const unsigned agrid = persistent_grid(b, (V + TV - 1) / TV, b->ppr_blocks);
     int cur = 0;
     for (uint32_t it = 0; it < iterations && !rc; ++it) {
         k_ppr_gather<<<ggrid, GT, 0, cs>>>(u->pull.nbr, u->pull.shared, u->pull.nvec, V, b->prop[cur], b->rowacc, b->S[cur ^ 1], G * K);
@@ -591,8 +594,8 @@ static int build_bfs_graph(grz_batch* b)
     if (!rc) rc = bck(b, cudaStreamBeginCaptureToGraph(cs, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
                                                       cudaStreamCaptureModeThreadLocal), "capture");
     if (!rc) {
-        const unsigned pgrid = persistent_grid(b, (u->pull.nvec + 255) / 256, 8);
-        const unsigned vgrid = persistent_grid(b, ((V + 3) / 4 + 255) / 256, 8);
+        const unsigned pgrid = persistent_grid(b, (u->pull.nvec + 255) / 256, b->bfs_blocks);
+        const unsigned vgrid = persistent_grid(b, ((V + 3) / 4 + 255) / 256, b->bfs_blocks);
         k_msbfs_pull<<<pgrid, 256, 0, cs>>>(u->pull.nbr, u->pull.shared, u->pull.nvec, V, b->frontier, b->visited, b->next_words);
         k_msbfs_vertex<<<vgrid, 256, 0, cs>>>(b->next_words, reinterpret_cast<unsigned*>(b->visited),
                                               reinterpret_cast<unsigned*>(b->frontier), b->level, V, b->iter, b->ctl);
@@ -678,6 +681,31 @@ extern "C" int grz_batch_msbfs(grz_batch* b, const uint32_t* roots, uint32_t k, 
     cudaEventDestroy(e1);
     u->nlaunch += 1 + 3ull * (c[1] + 1);
     return rc;
+}
+
+extern "C" int grz_batch_tune_set(grz_batch* b, int param, int64_t value)
+{
+    if (!b) return GRZ_ERR_ARG;
+    if (value < 1 || value > 32) return bset(b, GRZ_ERR_RANGE, "blocks per SM must be 1..32");
+    int* slot = param == GRZ_BATCH_TUNE_PPR_BLOCKS ? &b->ppr_blocks : (param == GRZ_BATCH_TUNE_BFS_BLOCKS ? &b->bfs_blocks : nullptr);
+    if (!slot) return bset(b, GRZ_ERR_ARG, "unknown batch tuning parameter");
+    if (*slot != (int)value) {
+        *slot = (int)value;
+        // the captured loops bake the grid in: capture again at the next run
+        cudaSetDevice(b->device);
+        if (param == GRZ_BATCH_TUNE_PPR_BLOCKS && b->ppr_exec) { cudaGraphExecDestroy(b->ppr_exec); b->ppr_exec = nullptr; }
+        if (param == GRZ_BATCH_TUNE_BFS_BLOCKS && b->bfs_exec) { cudaGraphExecDestroy(b->bfs_exec); b->bfs_exec = nullptr; }
+    }
+    return GRZ_OK;
+}
+
+extern "C" int grz_batch_tune_get(const grz_batch* b, int param, int64_t* value)
+{
+    if (!b || !value) return GRZ_ERR_ARG;
+    if (param == GRZ_BATCH_TUNE_PPR_BLOCKS) *value = b->ppr_blocks;
+    else if (param == GRZ_BATCH_TUNE_BFS_BLOCKS) *value = b->bfs_blocks;
+    else return GRZ_ERR_ARG;
+    return GRZ_OK;
 }
 
 extern "C" unsigned long long grz_batch_launch_count(const grz_batch* b) { return b ? b->u->nlaunch : 0ull; }

@@ -226,6 +226,7 @@ struct grz_mlp;
 #define GRZ_TUNE_CC_CACHE 1
 #define GRZ_TUNE_CC_THREADS 2
 #define GRZ_TUNE_CC_GRID 3
+#define GRZ_TUNE_PR_GRID 4
 #define GRZ_TUNE_HUBS_LOADED 100
 
 // kernel shapes chosen per graph (grz_tune_set; the autotuner searches them)
@@ -234,6 +235,7 @@ struct grz_tuning {
     uint32_t cc_cache;     // hub labels the CC pull kernel keeps in shared memory
     uint32_t cc_threads;   // threads per block of the CC pull kernel (256, 512, 1024)
     uint32_t cc_grid;      // blocks of the persistent CC pull kernel (0: SMs x resident blocks)
+    uint32_t pr_grid;      // blocks of the persistent PageRank gather kernel (0: SMs x resident blocks)
 };
 
 // Device control block of a CC/BFS run executed as one CUDA graph (grz_ccbfs.cu): the

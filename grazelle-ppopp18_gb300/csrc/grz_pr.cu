@@ -322,7 +322,8 @@ static int pr_gather_resident(grz_graph* g)
 static int pr_gather(grz_graph* g, uint64_t first, uint64_t count, const PRConst& pc)
 {
     if (count == 0) return GRZ_OK;
-    const uint64_t grid = std::min<uint64_t>(blocks_for(count), (uint64_t)g->num_sms * pr_gather_resident(g));
+    const uint64_t want = g->tune.pr_grid ? g->tune.pr_grid : (uint64_t)g->num_sms * pr_gather_resident(g);
+    const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>(blocks_for(count), want));
     grz_prof_begin(g, GRZ_PROF_PR_GATHER);
     k_pr_gather<<<(unsigned)grid, PR_THREADS, 0, g->stream>>>(g->pull.nbr, g->pull.shared, first, count, g->pull.nvec,
                                                                  g->pr_fx[g->pr_cur], (uint32_t)g->V, g->pr_rowacc, g->pull.hub_vid,

@@ -88,5 +88,20 @@ class Batch:
         self._ck(self.lib.grz_batch_msbfs(self.h, a.ctypes.data, k, out.ctypes.data if levels else None, C.byref(st)))
         return ([out[self.voff[g]:self.voff[g + 1]] for g in range(len(self.sizes))] if levels else None), st
 
+    def tune(self, ppr_blocks: int | None = None, bfs_blocks: int | None = None):
+        """Resident blocks per SM of the persistent batch kernels (results never depend on them)."""
+        for p, v in ((native.BATCH_TUNE_PPR_BLOCKS, ppr_blocks), (native.BATCH_TUNE_BFS_BLOCKS, bfs_blocks)):
+            if v is not None:
+                self._ck(self.lib.grz_batch_tune_set(self.h, p, int(v)))
+        return self
+
+    def tuning(self) -> dict:
+        out = {}
+        for k, p in (("ppr_blocks", native.BATCH_TUNE_PPR_BLOCKS), ("bfs_blocks", native.BATCH_TUNE_BFS_BLOCKS)):
+            v = C.c_int64()
+            self._ck(self.lib.grz_batch_tune_get(self.h, p, C.byref(v)))
+            out[k] = v.value
+        return out
+
     def launch_count(self) -> int:
         return int(self.lib.grz_batch_launch_count(self.h))

@@ -28,7 +28,8 @@ class GrzError(RuntimeError):
 
 FORCE_PULL, FORCE_PUSH, WITHOUT_COUNT, WITHOUT_OUTDEG = 1, 2, 4, 8
 BATCH_K = 8
-TUNE_HUBS, TUNE_CC_CACHE, TUNE_CC_THREADS, TUNE_CC_GRID, TUNE_HUBS_LOADED = 0, 1, 2, 3, 100
+TUNE_HUBS, TUNE_CC_CACHE, TUNE_CC_THREADS, TUNE_CC_GRID, TUNE_PR_GRID, TUNE_HUBS_LOADED = 0, 1, 2, 3, 4, 100
+BATCH_TUNE_PPR_BLOCKS, BATCH_TUNE_BFS_BLOCKS = 0, 1
 FLAG_HOST_LOOP = 16  # grz_cc_run / grz_bfs_run: host round trip per iteration instead of one CUDA graph
 MLP_FEATURES, MLP_HIDDEN, MLP_PARAMS = 12, 32, 1505
 POLICY_THRESHOLD, POLICY_LEARNED = 0, 1
@@ -85,6 +86,8 @@ SIGNATURES = {
     "grz_batch_ppr": (_I, [_VP, _VP, _U32, _U32, _D, _VP, _VP]),
     "grz_batch_msbfs": (_I, [_VP, _VP, _U32, _VP, _VP]),
     "grz_batch_launch_count": (C.c_ulonglong, [_VP]),
+    "grz_batch_tune_set": (_I, [_VP, _I, C.c_int64]),
+    "grz_batch_tune_get": (_I, [_VP, _I, _VP]),
     "grz_tune_get": (_I, [_VP, _I, _VP]),
     "grz_frontier_begin": (_I, [_VP, _I, _U32, _I]),
     "grz_frontier_next": (_I, [_VP, _I, C.POINTER(C.c_int), C.POINTER(C.c_uint64)]),

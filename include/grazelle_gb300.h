@@ -132,6 +132,7 @@ int grz_read_levels(grz_graph* g, int64_t* host_levels, uint64_t capacity);
 #define GRZ_TUNE_CC_CACHE 1     /* hub labels the CC pull kernel keeps in shared memory (<= 49152) */
 #define GRZ_TUNE_CC_THREADS 2   /* threads per block of the CC pull kernel: 256, 512 or 1024 */
 #define GRZ_TUNE_CC_GRID 3      /* blocks of the persistent CC pull kernel (0 = SMs x resident blocks) */
+#define GRZ_TUNE_PR_GRID 4      /* blocks of the persistent PageRank gather kernel (0 = SMs x resident blocks) */
 #define GRZ_TUNE_HUBS_LOADED 100 /* read-only: hubs encoded in the loaded pull list */
 int grz_tune_set(grz_graph* g, int param, int64_t value);
 int grz_tune_get(const grz_graph* g, int param, int64_t* value);
@@ -158,6 +159,12 @@ int grz_batch_info(const grz_batch* b, uint64_t* graphs, uint64_t* vertices, uin
 int grz_batch_ppr(grz_batch* b, const uint32_t* seeds, uint32_t k, uint32_t iterations, double damping,
                   double* ranks_out, grz_run_stats_t* stats);
 int grz_batch_msbfs(grz_batch* b, const uint32_t* roots, uint32_t k, int32_t* levels_out, grz_run_stats_t* stats);
+/* kernel shapes of a batch (results never depend on them): resident blocks per SM of the
+ * persistent PPR gather / apply and multi-source BFS pull kernels, 1..32 (default 8) */
+#define GRZ_BATCH_TUNE_PPR_BLOCKS 0
+#define GRZ_BATCH_TUNE_BFS_BLOCKS 1
+int grz_batch_tune_set(grz_batch* b, int param, int64_t value);
+int grz_batch_tune_get(const grz_batch* b, int param, int64_t* value);
 unsigned long long grz_batch_launch_count(const grz_batch* b);
 
 /* Digest of the last CC/BFS result without reading it back (no counterpart in the reference):

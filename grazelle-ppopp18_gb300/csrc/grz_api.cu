@@ -562,6 +562,10 @@ extern "C" int grz_tune_set(grz_graph* g, int param, int64_t value)
         if (value > (1 << 20)) return GRZ_ERR_RANGE;
         g->tune.pr_grid = (uint32_t)value;
         return GRZ_OK;
+    case GRZ_TUNE_BFS_PULL_SCAN:
+        if (value > 1) return grz_set_error(g, GRZ_ERR_ARG, "BFS pull mode must be 0 or 1");
+        g->tune.bfs_pull_scan = (uint32_t)value;
+        return GRZ_OK;
     default:
         return grz_set_error(g, GRZ_ERR_ARG, "unknown tuning parameter %d", param);
     }
@@ -576,6 +580,7 @@ extern "C" int grz_tune_get(const grz_graph* g, int param, int64_t* value)
     case GRZ_TUNE_CC_THREADS: *value = g->tune.cc_threads; return GRZ_OK;
     case GRZ_TUNE_CC_GRID: *value = g->tune.cc_grid; return GRZ_OK;
     case GRZ_TUNE_PR_GRID: *value = g->tune.pr_grid; return GRZ_OK;
+    case GRZ_TUNE_BFS_PULL_SCAN: *value = g->tune.bfs_pull_scan; return GRZ_OK;
     case GRZ_TUNE_HUBS_LOADED: *value = g->pull.nhub; return GRZ_OK;
     default: return GRZ_ERR_ARG;
     }

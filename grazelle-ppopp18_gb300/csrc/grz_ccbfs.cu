@@ -291,82 +291,151 @@ __device__ __forceinline__ void block_scan2(uint32_t& a, uint32_t& b, uint32_t& 
     tot_b = sb[T / 32];
 }
 
-__global__ void __launch_bounds__(T) k_fr_count(const unsigned long long* __restrict__ has,
-                                                const unsigned long long* __restrict__ nonempty, uint64_t words,
+// The compaction kernels give each thread CU = 32 consecutive vertices (half a bitmap word) and
+// each block CCHUNK consecutive vertices, so a block needs a single block-wide scan and a block
+// with nothing selected exits after reading its words.  A thread with a selected vertex reads its
+// 33 row pointers with 128-bit loads issued together and works from registers.  Selected: the bit
+// is set in both bitmaps (HasInfo and out-vectors for push; WantsInfo and in-vectors for the BFS
+// pull).
+constexpr int CU = 32;
+constexpr uint32_t CCHUNK = T * CU;
+
+// selection bits of vertices [v0, v0 + CU), v0 a multiple of CU
+__device__ __forceinline__ uint32_t selected_bits(const unsigned long long* __restrict__ bm1,
+                                                  const unsigned long long* __restrict__ bm2, uint64_t v0, uint64_t V)
+{
+    if (v0 >= V) return 0u;
+    const uint64_t w = v0 >> 6;
+    uint32_t bits = (uint32_t)((bm1[w] & bm2[w]) >> (v0 & 63));
+    if (v0 + CU > V) bits &= (1u << (V - v0)) - 1u;
+    return bits;
+}
+
+// r[0..CU] = rowptr[v0 .. v0 + CU] (entries past V are not read; their bits are clear)
+__device__ __forceinline__ void load_rowptr(const uint32_t* __restrict__ rowptr, uint64_t v0, uint64_t V, uint32_t* r)
+{
+    if (v0 + CU <= V) {
+        const uint4* p = reinterpret_cast<const uint4*>(rowptr + v0);  // v0 * 4 bytes is a multiple of 128
+#pragma unroll
+        for (int q = 0; q < CU / 4; ++q) {
+            const uint4 x = p[q];
+            r[4 * q] = x.x; r[4 * q + 1] = x.y; r[4 * q + 2] = x.z; r[4 * q + 3] = x.w;
+        }
+        r[CU] = rowptr[v0 + CU];
+    } else {
+#pragma unroll
+        for (int j = 0; j <= CU; ++j) r[j] = (v0 + j <= V) ? rowptr[v0 + j] : 0u;
+    }
+}
+
+__global__ void __launch_bounds__(T) k_fr_count(const unsigned long long* __restrict__ bm1,
+                                                const unsigned long long* __restrict__ bm2, uint64_t V,
                                                 const uint32_t* __restrict__ rowptr, uint32_t* __restrict__ part_n,
                                                 uint32_t* __restrict__ part_vec)
 {
     __shared__ uint32_t sa[T / 32 + 1], sb[T / 32 + 1];
-    const uint64_t w = (uint64_t)blockIdx.x * T + threadIdx.x;
-    unsigned long long bits = (w < words) ? (has[w] & nonempty[w]) : 0ull;
-    uint32_t n = __popcll(bits), vec = 0;
-    while (bits) {
-        const int k = __ffsll((long long)bits) - 1;
-        bits &= bits - 1;
-        vec += vec_count(rowptr, (uint32_t)(w * 64 + (uint64_t)k));
+    const uint64_t v0 = (uint64_t)blockIdx.x * CCHUNK + (uint64_t)threadIdx.x * CU;
+    const uint32_t bits = selected_bits(bm1, bm2, v0, V);
+    if (!__syncthreads_or(bits)) {
+        if (threadIdx.x == 0) { part_n[blockIdx.x] = 0; part_vec[blockIdx.x] = 0; }
+        return;
+    }
+    uint32_t n = __popc(bits), vec = 0;
+    if (bits) {
+        uint32_t r[CU + 1];
+        load_rowptr(rowptr, v0, V, r);
+#pragma unroll
+        for (int j = 0; j < CU; ++j)
+            if ((bits >> j) & 1u) vec += r[j + 1] - r[j];
     }
     uint32_t tn, tv;
     block_scan2(n, vec, tn, tv, sa, sb);
     if (threadIdx.x == 0) { part_n[blockIdx.x] = tn; part_vec[blockIdx.x] = tv; }
 }
 
-// one block: exclusive scan of the per-block totals in place; counters[0] = sources,
-// counters[2] = vectors
-__global__ void __launch_bounds__(T) k_fr_scan(uint32_t* __restrict__ part_n, uint32_t* __restrict__ part_vec, uint32_t nb,
-                                               uint32_t* __restrict__ counters)
+// one block of SCAN_T threads: exclusive scan of the per-block totals in place (each thread a
+// contiguous segment); counters[0] = selected vertices, counters[2] = their vectors
+constexpr int SCAN_T = 1024;
+
+__global__ void __launch_bounds__(SCAN_T) k_fr_scan(uint32_t* __restrict__ part_n, uint32_t* __restrict__ part_vec, uint32_t nb,
+                                                    uint32_t* __restrict__ counters)
 {
-    __shared__ uint32_t sa[T / 32 + 1], sb[T / 32 + 1];
-    uint32_t carry_n = 0, carry_v = 0;
-    for (uint32_t base = 0; base < nb; base += T) {
-        const uint32_t i = base + threadIdx.x;
-        uint32_t n = i < nb ? part_n[i] : 0u, v = i < nb ? part_vec[i] : 0u;
-        uint32_t tn, tv;
-        block_scan2(n, v, tn, tv, sa, sb);
-        if (i < nb) { part_n[i] = carry_n + n; part_vec[i] = carry_v + v; }
-        carry_n += tn;
-        carry_v += tv;
-        __syncthreads();
+    __shared__ uint32_t sa[SCAN_T / 32 + 1], sb[SCAN_T / 32 + 1];
+    const uint32_t per = (nb + SCAN_T - 1) / SCAN_T;
+    const uint32_t lo = min(nb, threadIdx.x * per), hi = min(nb, lo + per);
+    uint32_t sn = 0, sv = 0;
+#pragma unroll 8
+    for (uint32_t i = lo; i < hi; ++i) { sn += part_n[i]; sv += part_vec[i]; }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t xa = sn, xb = sv;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t ya = __shfl_up_sync(0xffffffffu, xa, o);
+        const uint32_t yb = __shfl_up_sync(0xffffffffu, xb, o);
+        if (lane >= o) { xa += ya; xb += yb; }
     }
-    if (threadIdx.x == 0) { counters[0] = carry_n; counters[2] = carry_v; }
+    if (lane == 31) { sa[warp] = xa; sb[warp] = xb; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t ra = 0, rb = 0;
+        for (int k = 0; k < SCAN_T / 32; ++k) {
+            const uint32_t ta = sa[k], tb = sb[k];
+            sa[k] = ra; sb[k] = rb;
+            ra += ta; rb += tb;
+        }
+        counters[0] = ra;
+        counters[2] = rb;
+    }
+    __syncthreads();
+    uint32_t en = sa[warp] + xa - sn, ev = sb[warp] + xb - sv;
+    for (uint32_t i = lo; i < hi; ++i) {
+        const uint32_t tn = part_n[i], tv = part_vec[i];
+        part_n[i] = en;
+        part_vec[i] = ev;
+        en += tn;
+        ev += tv;
+    }
 }
 
-// frontier[i] = source, voff[i] = offset of its first vector, vdelta[i] = its first vector's
-// index in the push list minus voff[i] (mod 2^32); tile_first[t] for the tiles that start in
-// its range.  voff[nf] = total vectors.
-__global__ void __launch_bounds__(T) k_fr_write(const unsigned long long* __restrict__ has,
-                                                const unsigned long long* __restrict__ nonempty, uint64_t words,
+// frontier[i] = i-th selected vertex (ID order), voff[i] = offset of its first vector among the
+// selected vertices' vectors, vdelta[i] = its first vector's index in the list minus voff[i]
+// (mod 2^32); tile_first[t] for the tiles that start in its range.  voff[count] = total vectors.
+__global__ void __launch_bounds__(T) k_fr_write(const unsigned long long* __restrict__ bm1,
+                                                const unsigned long long* __restrict__ bm2, uint64_t V,
                                                 const uint32_t* __restrict__ rowptr, const uint32_t* __restrict__ base_n,
                                                 const uint32_t* __restrict__ base_vec, const uint32_t* __restrict__ counters,
-                                                uint32_t* __restrict__ frontier, uint32_t* __restrict__ voff,
+                                                uint32_t nb, uint32_t* __restrict__ frontier, uint32_t* __restrict__ voff,
                                                 uint32_t* __restrict__ vdelta, uint32_t* __restrict__ tile_first)
 {
     __shared__ uint32_t sa[T / 32 + 1], sb[T / 32 + 1];
-    const uint64_t w = (uint64_t)blockIdx.x * T + threadIdx.x;
-    const unsigned long long bits0 = (w < words) ? (has[w] & nonempty[w]) : 0ull;
-    unsigned long long bits = bits0;
-    uint32_t n = __popcll(bits), vec = 0;
-    while (bits) {
-        const int k = __ffsll((long long)bits) - 1;
-        bits &= bits - 1;
-        vec += vec_count(rowptr, (uint32_t)(w * 64 + (uint64_t)k));
+    if (blockIdx.x == 0 && threadIdx.x == 0) voff[counters[0]] = counters[2];
+    const uint32_t b0 = base_n[blockIdx.x];
+    const uint32_t b1 = blockIdx.x + 1 < nb ? base_n[blockIdx.x + 1] : counters[0];
+    if (b0 == b1) return;  // nothing selected in this block (uniform)
+    const uint64_t v0 = (uint64_t)blockIdx.x * CCHUNK + (uint64_t)threadIdx.x * CU;
+    const uint32_t bits = selected_bits(bm1, bm2, v0, V);
+    uint32_t r[CU + 1];
+    uint32_t n = __popc(bits), vec = 0;
+    if (bits) {
+        load_rowptr(rowptr, v0, V, r);
+#pragma unroll
+        for (int j = 0; j < CU; ++j)
+            if ((bits >> j) & 1u) vec += r[j + 1] - r[j];
     }
     uint32_t tn, tv;
     block_scan2(n, vec, tn, tv, sa, sb);
-    uint32_t pos = base_n[blockIdx.x] + n, vo = base_vec[blockIdx.x] + vec;
-    bits = bits0;
-    while (bits) {
-        const int k = __ffsll((long long)bits) - 1;
-        bits &= bits - 1;
-        const uint32_t u = (uint32_t)(w * 64 + (uint64_t)k);
-        const uint32_t r0 = rowptr[u], cnt = rowptr[u + 1] - r0;
-        frontier[pos] = u;
+    if (!bits) return;
+    uint32_t pos = b0 + n, vo = base_vec[blockIdx.x] + vec;
+#pragma unroll
+    for (int j = 0; j < CU; ++j) {
+        if (!((bits >> j) & 1u)) continue;
+        const uint32_t cnt = r[j + 1] - r[j];
+        frontier[pos] = (uint32_t)(v0 + j);
         voff[pos] = vo;
-        vdelta[pos] = r0 - vo;
+        vdelta[pos] = r[j] - vo;
         for (uint64_t t = ((uint64_t)vo + PUSH_TILE - 1) / PUSH_TILE; t * PUSH_TILE < (uint64_t)vo + cnt; ++t) tile_first[t] = pos;
         ++pos;
         vo += cnt;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) voff[counters[0]] = counters[2];
 }
 
 // Expand the compacted frontier, one tile of PUSH_TILE vectors at a time (grid-stride over
@@ -445,6 +514,86 @@ __global__ void __launch_bounds__(T) k_push_expand(const uint32_t* __restrict__ 
     if (!IsBfs) {
         my_vote = block_sum_u64(my_vote, red);
         if (threadIdx.x == 0) vote_add(vote, my_vote);
+    }
+}
+
+// BFS pull over the compacted wanted destinations (WantsInfo and in-vectors): only their vectors
+// are read, in tiles of PUSH_TILE vectors over the grid.  The vectors of one destination are
+// consecutive in the concatenation, so the per-destination minimum candidate (the reference's
+// parent rule, as in k_bfs_pull) is reduced within the warp before one atomicMin.
+__global__ void __launch_bounds__(T) k_bfs_pull_expand(const uint32_t* __restrict__ dests, const uint32_t* __restrict__ voff,
+                                                       const uint32_t* __restrict__ vdelta, const uint32_t* __restrict__ tile_first,
+                                                       const uint32_t* __restrict__ counters, const uint4* __restrict__ nbr,
+                                                       uint32_t V, const unsigned long long* __restrict__ has,
+                                                       unsigned long long* __restrict__ cand, uint32_t* __restrict__ touched,
+                                                       uint32_t* __restrict__ ntouched, const uint32_t* __restrict__ hub_vid,
+                                                       uint32_t nhub, unsigned long long* __restrict__ has_next)
+{
+    __shared__ uint32_t s_dst[PUSH_TILE + 1];
+    __shared__ uint32_t s_off[PUSH_TILE + 1];
+    __shared__ uint32_t s_delta[PUSH_TILE + 1];
+    const uint32_t nd = counters[0], total = counters[2];
+    const uint32_t ntiles = (total + PUSH_TILE - 1) / PUSH_TILE;
+    const int lane = threadIdx.x & 31;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint32_t first = tile_first[tile];
+        const uint32_t t0 = tile * PUSH_TILE;
+        const uint32_t tend = min(total, t0 + PUSH_TILE);
+        const uint32_t nw = min(PUSH_TILE, nd - first);
+        for (uint32_t i = threadIdx.x; i <= nw; i += T) {
+            s_off[i] = voff[first + i];
+            if (i < nw) {
+                s_dst[i] = dests[first + i];
+                s_delta[i] = vdelta[first + i];
+            }
+        }
+        __syncthreads();
+        for (uint32_t base = t0; base < tend; base += T) {  // warp-uniform trip count
+            const uint32_t gv = base + threadIdx.x;
+            uint32_t key = INF;
+            unsigned long long k = ~0ull;
+            if (gv < tend) {
+                int lo = 0, hi = (int)nw - 1;  // last entry with s_off <= gv
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (s_off[mid] <= gv) lo = mid; else hi = mid - 1;
+                }
+                key = s_dst[lo];
+                const uint32_t vec = gv + s_delta[lo];
+                const uint4 s = __ldcs(nbr + vec);
+                const uint32_t ids[4] = { grz_hub_decode(s.x, hub_vid, nhub), grz_hub_decode(s.y, hub_vid, nhub),
+                                          grz_hub_decode(s.z, hub_vid, nhub), grz_hub_decode(s.w, hub_vid, nhub) };
+                uint32_t best = 0;
+                bool any = false;
+#pragma unroll
+                for (int l = 0; l < 4; ++l) {
+                    const uint32_t id = ids[l];
+                    if (id < V && bit_of(has, id)) {
+                        best = any ? max(best, id) : id;
+                        any = true;
+                    }
+                }
+                if (any) k = ((unsigned long long)vec << 32) | (unsigned long long)(~best);
+            }
+            const uint32_t prevkey = __shfl_up_sync(0xffffffffu, key, 1);
+            const uint32_t nextkey = __shfl_down_sync(0xffffffffu, key, 1);
+            const bool head = lane == 0 || key != prevkey;
+            const bool tail = lane == 31 || key != nextkey;
+            const unsigned heads = __ballot_sync(0xffffffffu, head);
+            const int segstart = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+            const int maxlen = __reduce_max_sync(0xffffffffu, (unsigned)(lane - segstart + 1));
+            for (int off = 1; off < maxlen; off <<= 1) {
+                const unsigned long long o = __shfl_up_sync(0xffffffffu, k, off);
+                if (lane - off >= segstart) k = min(k, o);
+            }
+            bool first_touch = false;
+            if (tail && k != ~0ull && k < cand[key]) {
+                first_touch = atomicMin(cand + key, k) == ~0ull;
+                if (first_touch) atomicOr(has_next + (key >> 6), 1ull << (key & 63));
+            }
+            warp_append(first_touch, key, touched, ntouched);
+        }
+        __syncthreads();
     }
 }
 
@@ -602,8 +751,9 @@ static int ensure_frontier_state(grz_graph* g)
     GRZ_CK(g, cudaMalloc((void**)&f.frontier, sizeof(uint32_t) * (V + 1)));
     GRZ_CK(g, cudaMalloc((void**)&f.voff, sizeof(uint32_t) * (V + 1)));
     GRZ_CK(g, cudaMalloc((void**)&f.vdelta, sizeof(uint32_t) * (V + 1)));
-    GRZ_CK(g, cudaMalloc((void**)&f.tile_first, sizeof(uint32_t) * (g->push.nvec / PUSH_TILE + 2)));
-    GRZ_CK(g, cudaMalloc((void**)&f.fr_part, sizeof(uint32_t) * 2 * blocks_for(W)));
+    GRZ_CK(g, cudaMalloc((void**)&f.tile_first, sizeof(uint32_t) * (std::max(g->push.nvec, g->pull.nvec) / PUSH_TILE + 2)));
+    GRZ_CK(g, cudaMalloc((void**)&f.fr_part, sizeof(uint32_t) * 2 * (V / CCHUNK + 1)));
+    GRZ_CK(g, cudaMalloc((void**)&f.nonempty_pull, sizeof(unsigned long long) * W));
     GRZ_CK(g, cudaMalloc((void**)&f.touched, sizeof(uint32_t) * (V + 1)));
     GRZ_CK(g, cudaMalloc((void**)&f.cand64, sizeof(unsigned long long) * (V + 1)));
     GRZ_CK(g, cudaMalloc((void**)&f.cand32, sizeof(uint32_t) * (V + 1)));
@@ -613,6 +763,11 @@ static int ensure_frontier_state(grz_graph* g)
     GRZ_CK(g, cudaMemsetAsync(f.cand64, 0xff, sizeof(unsigned long long) * (V + 1), g->stream));
     GRZ_CK(g, cudaMemsetAsync(f.cand32, 0xff, sizeof(uint32_t) * (V + 1), g->stream));
     GRZ_CK(g, cudaMemsetAsync(f.nonempty_push, 0, sizeof(unsigned long long) * W, g->stream));
+    GRZ_CK(g, cudaMemsetAsync(f.nonempty_pull, 0, sizeof(unsigned long long) * W, g->stream));
+    if (g->pull.rowptr && V) {
+        k_nonempty<<<blocks_for(W), T, 0, g->stream>>>(g->pull.rowptr, V, f.nonempty_pull, W); GRZ_COUNT_LAUNCH(g);
+        GRZ_CK(g, cudaGetLastError());
+    }
     if (g->push.rowptr && V) {
         k_nonempty<<<blocks_for(W), T, 0, g->stream>>>(g->push.rowptr, V, f.nonempty_push, W); GRZ_COUNT_LAUNCH(g);
         GRZ_CK(g, cudaGetLastError());
@@ -740,6 +895,19 @@ static int launch_cc_pull(grz_graph* g, uint64_t first, uint64_t count, const Vo
     }
 }
 
+// Compacts the vertices selected by bm1 & bm2, with their vector ranges in `rowptr`, into
+// fr.frontier / voff / vdelta / tile_first (counts on the device in counters[0], [2]).
+static void compact(grz_graph* g, const unsigned long long* bm1, const unsigned long long* bm2, const uint32_t* rowptr)
+{
+    grz_frontier_state& f = g->fr;
+    cudaStream_t st = g->stream;
+    const unsigned nb = (unsigned)(g->V / CCHUNK + 1);
+    k_fr_count<<<nb, T, 0, st>>>(bm1, bm2, g->V, rowptr, f.fr_part, f.fr_part + nb); GRZ_COUNT_LAUNCH(g);
+    k_fr_scan<<<1, SCAN_T, 0, st>>>(f.fr_part, f.fr_part + nb, nb, f.counters); GRZ_COUNT_LAUNCH(g);
+    k_fr_write<<<nb, T, 0, st>>>(bm1, bm2, g->V, rowptr, f.fr_part, f.fr_part + nb, f.counters, nb, f.frontier, f.voff,
+                                 f.vdelta, f.tile_first); GRZ_COUNT_LAUNCH(g);
+}
+
 // One edge phase on a vector range of the pull (pull=1) or push list.  Leaves the vote of the
 // phase in fr.vote[0] on the device.  The push engine always expands the whole compacted frontier.
 static int edge_phase(grz_graph* g, int pull, uint64_t first, uint64_t count)
@@ -754,11 +922,25 @@ static int edge_phase(grz_graph* g, int pull, uint64_t first, uint64_t count)
     if (pull) {
         if (!g->pull.nbr) return grz_set_error(g, GRZ_ERR_STATE, "pull list not loaded");
         if (count == 0) return GRZ_OK;
-        grz_prof_begin(g, bfs ? GRZ_PROF_BFS_PULL : GRZ_PROF_CC_PULL);
-        if (bfs) {
+        const bool compacted = bfs && first == 0 && count == g->pull.nvec && !g->tune.bfs_pull_scan;
+        if (compacted) {
+            // the whole list: only the vectors of wanted destinations
+            grz_prof_begin(g, GRZ_PROF_PUSH_COMPACT);
+            compact(g, f.wants, f.nonempty_pull, g->pull.rowptr);
+            grz_prof_end(g);
+            grz_prof_begin(g, GRZ_PROF_BFS_PULL);
+            k_bfs_pull_expand<<<(unsigned)g->num_sms * 8, T, 0, st>>>(f.frontier, f.voff, f.vdelta, f.tile_first, f.counters,
+                                                                     g->pull.nbr, V, f.has, f.cand64, f.touched, f.counters + 1,
+                                                                     g->pull.hub_vid, g->pull.nhub, f.has_next); GRZ_COUNT_LAUNCH(g);
+        } else {
+            grz_prof_begin(g, bfs ? GRZ_PROF_BFS_PULL : GRZ_PROF_CC_PULL);
+        }
+        if (bfs && !compacted) {
             const unsigned pgrid = (unsigned)std::min<uint64_t>(blocks_for(count), (uint64_t)g->num_sms * 8);
             k_bfs_pull<<<pgrid, T, 0, st>>>(g->pull.nbr, g->pull.shared, first, count, V, f.has, f.wants, f.cand64,
                                                        f.touched, f.counters + 1, g->pull.hub_vid, g->pull.nhub, f.has_next); GRZ_COUNT_LAUNCH(g);
+        }
+        if (bfs) {
             grz_prof_end(g);
             grz_prof_begin(g, GRZ_PROF_BFS_VISIT);
             k_bfs_visit<true><<<visit_grid(g), T, 0, st>>>(f.touched, f.counters + 1, f.cand64, f.cand32, f.label, f.level,
@@ -771,11 +953,7 @@ static int edge_phase(grz_graph* g, int pull, uint64_t first, uint64_t count)
     } else {
         if (!g->push.nbr) return grz_set_error(g, GRZ_ERR_STATE, "push list not loaded");
         grz_prof_begin(g, GRZ_PROF_PUSH_COMPACT);
-        const unsigned nbw = blocks_for(W);
-        k_fr_count<<<nbw, T, 0, st>>>(f.has, f.nonempty_push, W, g->push.rowptr, f.fr_part, f.fr_part + nbw); GRZ_COUNT_LAUNCH(g);
-        k_fr_scan<<<1, T, 0, st>>>(f.fr_part, f.fr_part + nbw, nbw, f.counters); GRZ_COUNT_LAUNCH(g);
-        k_fr_write<<<nbw, T, 0, st>>>(f.has, f.nonempty_push, W, g->push.rowptr, f.fr_part, f.fr_part + nbw, f.counters,
-                                      f.frontier, f.voff, f.vdelta, f.tile_first); GRZ_COUNT_LAUNCH(g);
+        compact(g, f.has, f.nonempty_push, g->push.rowptr);
         grz_prof_end(g);
         grz_prof_begin(g, bfs ? GRZ_PROF_BFS_PUSH : GRZ_PROF_CC_PUSH);
         const unsigned grid = (unsigned)g->num_sms * 8;
@@ -960,7 +1138,7 @@ int grz_frontier_props(grz_graph* g)
 void grz_frontier_free(grz_graph* g)
 {
     grz_frontier_state& f = g->fr;
-    void* ptrs[] = { f.label, f.level, f.has, f.has_next, f.wants, f.nonempty_push, f.frontier, f.voff, f.vdelta, f.tile_first,
+    void* ptrs[] = { f.label, f.level, f.has, f.has_next, f.wants, f.nonempty_push, f.nonempty_pull, f.frontier, f.voff, f.vdelta, f.tile_first,
                      f.fr_part, f.touched, f.cand64, f.cand32,
                      f.counters, f.vote, f.sw_out, f.snap };
     for (void* p : ptrs) cudaFree(p);
@@ -1177,7 +1355,7 @@ int grz_frontier_run_graph(grz_graph* g, uint64_t* launches)
         f.has_next = t;
     }
     const bool bfs = f.app == GRZ_APP_BREADTH_FIRST_SEARCH;
-    const uint64_t per_pull = bfs ? 2 : 1, per_push = bfs ? 5 : 4;
+    const uint64_t per_pull = bfs ? (g->tune.bfs_pull_scan ? 2 : 5) : 1, per_push = bfs ? 5 : 4;
     uint64_t k = 1 + n + (uint64_t)c.npull * per_pull + (uint64_t)c.npush * per_push + (n % 2);
     g->nlaunch += k;
     if (launches) *launches = k;

@@ -227,6 +227,7 @@ struct grz_mlp;
 #define GRZ_TUNE_CC_THREADS 2
 #define GRZ_TUNE_CC_GRID 3
 #define GRZ_TUNE_PR_GRID 4
+#define GRZ_TUNE_BFS_PULL_SCAN 5
 #define GRZ_TUNE_HUBS_LOADED 100
 
 // kernel shapes chosen per graph (grz_tune_set; the autotuner searches them)
@@ -236,6 +237,7 @@ struct grz_tuning {
     uint32_t cc_threads;   // threads per block of the CC pull kernel (256, 512, 1024)
     uint32_t cc_grid;      // blocks of the persistent CC pull kernel (0: SMs x resident blocks)
     uint32_t pr_grid;      // blocks of the persistent PageRank gather kernel (0: SMs x resident blocks)
+    uint32_t bfs_pull_scan;  // 1: BFS pull scans every vector; 0: only the wanted destinations' (compacted)
 };
 
 // Device control block of a CC/BFS run executed as one CUDA graph (grz_ccbfs.cu): the
@@ -273,6 +275,7 @@ struct grz_frontier_state {
     unsigned long long* has_next;    // HasInfo*
     unsigned long long* wants;       // WantsInfo
     unsigned long long* nonempty_push;  // vertices with out-vectors
+    unsigned long long* nonempty_pull;  // vertices with in-vectors
     uint32_t* frontier;              // compacted active sources
     uint32_t* voff;                  // push: offset of each source's first vector among the frontier's
     uint32_t* vdelta;                // push: first vector index in the list minus voff (mod 2^32)

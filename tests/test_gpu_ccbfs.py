@@ -254,3 +254,23 @@ def test_hub_encoding_and_kernel_shapes_do_not_change_results(name):
         np.testing.assert_array_equal(par, results[0][0])
         np.testing.assert_array_equal(lv, results[0][1])
         np.testing.assert_array_equal(pr, results[0][2])
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_bfs_pull_compacted_equals_scan(name):
+    """The BFS pull over only the wanted destinations' vectors (compacted, the default) and the
+    scan of every vector give the same parents, levels, iterations and engine counts, and both
+    equal the single-thread reference's."""
+    rec, g = load_golden(name)
+    with gpu_graph(g) as G:
+        for variant, flags in BFS_VARIANTS:
+            out = []
+            for scan in (0, 1):
+                G.tune(bfs_pull_scan=scan)
+                par, lv, st = G.bfs(0, flags, stats=True)
+                out.append((par, lv, (st.iterations, st.pull_iterations, st.push_iterations)))
+            np.testing.assert_array_equal(out[0][0], out[1][0], err_msg=variant)
+            np.testing.assert_array_equal(out[0][1], out[1][1], err_msg=variant)
+            assert out[0][2] == out[1][2]
+            np.testing.assert_array_equal(out[0][0], rec[variant + "_parents"], err_msg=variant)
+        G.tune(bfs_pull_scan=0)

@@ -204,11 +204,11 @@ int grz_build_list(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t 
         nvec = nv32;
     }
     L->nvec = nvec;
-    LCK(cudaMalloc((void**)&L->vs, sizeof(uint64_t) * 4 * nvec));
-    LCK(cudaMalloc((void**)&L->nbr, sizeof(uint4) * nvec));
-    LCK(cudaMalloc((void**)&L->shared, sizeof(uint32_t) * nvec));
-    LCK(cudaMalloc((void**)&L->vindex, sizeof(uint64_t) * vi_count));
-    LCK(cudaMalloc((void**)&L->rowptr, sizeof(uint32_t) * (V + 1)));
+    LCK(cudaMallocAsync((void**)&L->vs, sizeof(uint64_t) * 4 * nvec, st));
+    LCK(cudaMallocAsync((void**)&L->nbr, sizeof(uint4) * nvec, st));
+    LCK(cudaMallocAsync((void**)&L->shared, sizeof(uint32_t) * nvec, st));
+    LCK(cudaMallocAsync((void**)&L->vindex, sizeof(uint64_t) * vi_count, st));
+    LCK(cudaMallocAsync((void**)&L->rowptr, sizeof(uint32_t) * (V + 1), st));
     if (E > 0) {
         LCK(cudaMallocAsync((void**)&vfirst, sizeof(uint32_t) * nvec, st));
         LCK(cudaMallocAsync((void**)&l1, sizeof(uint32_t) * nvec * 3, st));
@@ -263,9 +263,10 @@ int grz_build_outdegrees(grz_graph* g, const uint64_t* d_pull_pairs, uint64_t E)
 {
     const uint64_t V = g->V;
     cudaStream_t st = g->stream;
-    GRZ_CK(g, cudaMalloc((void**)&g->degree, sizeof(uint32_t) * (V + 1)));
-    GRZ_CK(g, cudaMalloc((void**)&g->outdeg, sizeof(double) * (V + 8)));
-    GRZ_CK(g, cudaMalloc((void**)&g->inv_deg, sizeof(double) * (V + 1)));
+    int rc = grz_dev_alloc(g, (void**)&g->degree, sizeof(uint32_t) * (V + 1));
+    if (!rc) rc = grz_dev_alloc(g, (void**)&g->outdeg, sizeof(double) * (V + 8));
+    if (!rc) rc = grz_dev_alloc(g, (void**)&g->inv_deg, sizeof(double) * (V + 1));
+    if (rc) return rc;
     GRZ_CK(g, cudaMemsetAsync(g->degree, 0, sizeof(uint32_t) * (V + 1), st));
     GRZ_CK(g, cudaMemsetAsync(g->outdeg, 0, sizeof(double) * (V + 8), st));
     if (E > 0) {
@@ -393,7 +394,7 @@ int grz_build_hubs(grz_graph* g, grz_list* L, uint32_t max_hubs)
         const uint32_t nhub = std::min<uint32_t>(ncand, max_hubs);
         std::vector<uint32_t> vid(nhub);
         for (uint32_t i = 0; i < nhub; ++i) vid[i] = hc[order[i]];
-        HCK(cudaMalloc((void**)&L->hub_vid, sizeof(uint32_t) * nhub));
+        HCK(cudaMallocAsync((void**)&L->hub_vid, sizeof(uint32_t) * nhub, st));
         HCK(cudaMemcpyAsync(L->hub_vid, vid.data(), sizeof(uint32_t) * nhub, cudaMemcpyHostToDevice, st));
         HCK(cudaMallocAsync((void**)&slot_of, sizeof(uint32_t) * V, st));
         HCK(cudaMemsetAsync(slot_of, 0xff, sizeof(uint32_t) * V, st));

@@ -79,19 +79,30 @@ __global__ void k_tile_reduce(const uint32_t* __restrict__ in, uint64_t n, uint3
     if (threadIdx.x == 0) tile_tot[blockIdx.x] = v;
 }
 
-// scans a tile; each thread owns SCAN_ITEMS consecutive elements
+// scans a tile; each thread owns SCAN_ITEMS consecutive elements.  The tile moves between global
+// and shared memory in striped order (coalesced), and each thread works on its consecutive items
+// in shared memory.
 template <class Op, bool Inclusive>
-__global__ void k_tile_scan(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, uint64_t n,
-                            const uint32_t* __restrict__ tile_off, uint32_t* __restrict__ grand_total)
+__global__ void __launch_bounds__(SCAN_THREADS) k_tile_scan(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
+                                                            uint64_t n, const uint32_t* __restrict__ tile_off,
+                                                            uint32_t* __restrict__ grand_total)
 {
     __shared__ uint32_t sm[32];
-    const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
+    __shared__ uint32_t tile[SCAN_TILE + SCAN_TILE / 32];  // one pad word per 32 against bank conflicts
+    const uint64_t tbase = (uint64_t)blockIdx.x * SCAN_TILE;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        const uint32_t e = (uint32_t)i * SCAN_THREADS + threadIdx.x;
+        const uint64_t k = tbase + e;
+        tile[e + (e >> 5)] = (k < n) ? in[k] : Op::id();
+    }
+    __syncthreads();
     uint32_t v[SCAN_ITEMS];
     uint32_t acc = Op::id();
 #pragma unroll
     for (int i = 0; i < SCAN_ITEMS; ++i) {
-        const uint64_t k = base + i;
-        v[i] = (k < n) ? in[k] : Op::id();
+        const uint32_t e = threadIdx.x * SCAN_ITEMS + i;
+        v[i] = tile[e + (e >> 5)];
         acc = Op::op(acc, v[i]);
     }
     uint32_t tot;
@@ -99,12 +110,19 @@ __global__ void k_tile_scan(const uint32_t* __restrict__ in, uint32_t* __restric
     if (tile_off) run = Op::op(tile_off[blockIdx.x], run);
 #pragma unroll
     for (int i = 0; i < SCAN_ITEMS; ++i) {
-        const uint64_t k = base + i;
+        const uint32_t e = threadIdx.x * SCAN_ITEMS + i;
         const uint32_t nxt = Op::op(run, v[i]);
-        if (k < n) out[k] = Inclusive ? nxt : run;
+        tile[e + (e >> 5)] = Inclusive ? nxt : run;
         run = nxt;
     }
     if (grand_total && threadIdx.x == SCAN_THREADS - 1 && blockIdx.x == gridDim.x - 1) *grand_total = run;
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        const uint32_t e = (uint32_t)i * SCAN_THREADS + threadIdx.x;
+        const uint64_t k = tbase + e;
+        if (k < n) out[k] = tile[e + (e >> 5)];
+    }
 }
 
 template <class Op, bool Inclusive>

@@ -277,8 +277,25 @@ static bool is_device_ptr(const void* p)
     return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
 }
 
+static int load_pairs(grz_graph* g, uint64_t V, uint64_t E, const uint64_t* pull_pairs, const uint64_t* push_pairs,
+                      int flags);
+
 extern "C" int grz_graph_load_pairs(grz_graph* g, uint64_t V, uint64_t E, const uint64_t* pull_pairs,
                                     const uint64_t* push_pairs)
+{
+    return load_pairs(g, V, E, pull_pairs, push_pairs, 0);
+}
+
+extern "C" int grz_graph_load_pairs_ex(grz_graph* g, uint64_t V, uint64_t E, const uint64_t* pull_pairs,
+                                       const uint64_t* push_pairs, int flags)
+{
+    if (flags & ~GRZ_LOAD_DERIVE_PUSH) return GRZ_ERR_ARG;
+    if ((flags & GRZ_LOAD_DERIVE_PUSH) && push_pairs) return grz_set_error(g, GRZ_ERR_ARG, "push pairs given and asked to derive them");
+    return load_pairs(g, V, E, pull_pairs, push_pairs, flags);
+}
+
+static int load_pairs(grz_graph* g, uint64_t V, uint64_t E, const uint64_t* pull_pairs, const uint64_t* push_pairs,
+                      int flags)
 {
     if (!g || (E > 0 && !pull_pairs)) return GRZ_ERR_ARG;
     if (V >= 0xffffffffull) return grz_set_error(g, GRZ_ERR_RANGE, "V = %llu exceeds the 32-bit device ID limit", (unsigned long long)V);
@@ -317,8 +334,16 @@ extern "C" int grz_graph_load_pairs(grz_graph* g, uint64_t V, uint64_t E, const 
         if (e != cudaSuccess) rc = grz_cuda_check(g, e, "H2D push pairs");
         else { dsrc[1] = (const uint64_t*)dbuf[1]; push_on_copy_stream = true; }
     }
+    const bool derive = (flags & GRZ_LOAD_DERIVE_PUSH) && !push_pairs && E > 0;
     for (int which = 0; which < 2 && rc == GRZ_OK; ++which) {
-        if (which == 1 && !push_pairs) break;
+        if (which == 1 && derive) {
+            // the -push order from the -pull pairs already on the device (stable sort by source)
+            rc = grz_dev_alloc(g, &dbuf[1], pbytes);
+            if (rc == GRZ_OK) rc = grz_derive_push_pairs(g, dsrc[0], E, (uint64_t*)dbuf[1]);
+            if (rc != GRZ_OK) break;
+            dsrc[1] = (const uint64_t*)dbuf[1];
+        }
+        if (which == 1 && !push_pairs && !derive) break;
         if (which == 1 && push_on_copy_stream) {
             cudaError_t e = cudaStreamWaitEvent(st, g->copy_ev[1], 0);
             if (e != cudaSuccess) { rc = grz_cuda_check(g, e, "wait for push pairs"); break; }

@@ -435,6 +435,8 @@ void grz_frontier_free(grz_graph* g);
 // layout (grz_layout.cu)
 int grz_build_list(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t E, int shared_is_dst);
 int grz_build_hubs(grz_graph* g, grz_list* L, uint32_t max_hubs);
+int grz_derive_push_pairs(grz_graph* g, const uint64_t* pull_pairs, uint64_t E, uint64_t* push_out);
+#define GRZ_LOAD_DERIVE_PUSH 1
 int grz_build_outdegrees(grz_graph* g, const uint64_t* d_pull_pairs, uint64_t E);
 
 // scans (grz_scan.cu): exclusive sum of uint32 into uint32 (n < 2^32), inclusive max of uint32

@@ -117,6 +117,14 @@ class Graph:
         self.V, self.E = num_vertices, num_edges
         return self
 
+    def load_pull_derive_push(self, num_vertices: int, num_edges: int, pull_ptr: int):
+        """Only the -pull list (raw pointer, pinned host or device); the -push list is built on the
+        device from it (GRZ_LOAD_DERIVE_PUSH)."""
+        self._ck(self.lib.grz_graph_load_pairs_ex(self.h, num_vertices, num_edges, C.c_void_p(pull_ptr), None,
+                                                  native.LOAD_DERIVE_PUSH))
+        self.V, self.E = num_vertices, num_edges
+        return self
+
     def load_device_pairs(self, num_vertices: int, num_edges: int, pull_ptr: int, push_ptr: int | None = None):
         self._ck(self.lib.grz_graph_load_pairs(self.h, num_vertices, num_edges, C.c_void_p(pull_ptr),
                                                C.c_void_p(push_ptr) if push_ptr else None))

@@ -1,6 +1,6 @@
 """Seeded synthetic graphs in Grazelle's binary edge-list format.
 
-Grazelle reads a graph as two files (README.md, "Datasets"): ``<name>-pull`` with
+Grazelle reads a graph as two files (the reference's README.md, "Datasets"): ``<name>-pull`` with
 edges grouped by destination in ascending order, and ``<name>-push`` grouped by
 source.  Each file is a 64-bit header ``{V, E}`` followed by ``E`` pairs of
 64-bit ``(source, destination)`` IDs.  The header is read by

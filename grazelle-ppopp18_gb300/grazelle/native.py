@@ -28,6 +28,7 @@ class GrzError(RuntimeError):
 
 FORCE_PULL, FORCE_PUSH, WITHOUT_COUNT, WITHOUT_OUTDEG = 1, 2, 4, 8
 BATCH_K = 8
+LOAD_DERIVE_PUSH = 1
 TUNE_HUBS, TUNE_CC_CACHE, TUNE_CC_THREADS, TUNE_CC_GRID, TUNE_PR_GRID, TUNE_BFS_PULL_SCAN, TUNE_HUBS_LOADED = 0, 1, 2, 3, 4, 5, 100
 BATCH_TUNE_PPR_BLOCKS, BATCH_TUNE_BFS_BLOCKS = 0, 1
 FLAG_HOST_LOOP = 16  # grz_cc_run / grz_bfs_run: host round trip per iteration instead of one CUDA graph
@@ -77,6 +78,7 @@ SIGNATURES = {
     "grz_read_levels": (_I, [_VP, _VP, _U64]),
     "grz_result_digest": (_I, [_VP, _VP]),
     "grz_tune_set": (_I, [_VP, _I, C.c_int64]),
+    "grz_graph_load_pairs_ex": (_I, [_VP, _U64, _U64, _VP, _VP, _I]),
     "grz_batch_create": (_I, [C.POINTER(_VP), _I, _VP]),
     "grz_batch_destroy": (None, [_VP]),
     "grz_batch_last_error": (C.c_char_p, [_VP]),

@@ -80,7 +80,14 @@ int grz_sync(grz_graph* g);
  * vector-sparse lists, vertex indices and outdegrees on the device. */
 int grz_graph_load_pairs(grz_graph* g, uint64_t num_vertices, uint64_t num_edges,
                          const uint64_t* pull_pairs, const uint64_t* push_pairs);
-/* Reads `<base>-pull` and `<base>-push` (README.md "Datasets"); push is optional. */
+/* The same with options (no counterpart in the reference).  GRZ_LOAD_DERIVE_PUSH, with
+ * push_pairs NULL: build the -push list on the device from the -pull pairs (a stable sort by
+ * source gives exactly the -push order), so only one list crosses the host link. */
+#define GRZ_LOAD_DERIVE_PUSH 1
+int grz_graph_load_pairs_ex(grz_graph* g, uint64_t num_vertices, uint64_t num_edges, const uint64_t* pull_pairs,
+                            const uint64_t* push_pairs, int flags);
+/* Reads `<base>-pull` and `<base>-push`, each a {V, E} header and E (src, dst) uint64 pairs
+ * (source/graphdata.c:957-1049); push is optional. */
 int grz_graph_load_files(grz_graph* g, const char* base);
 
 int grz_graph_get_info(const grz_graph* g, grz_graph_info_t* out);

@@ -5,7 +5,7 @@ Test infrastructure only: the binaries it makes are the golden source the
 C restatement in ``oracle/grz_oracle.c`` is pinned against.  Nothing in the
 product links or runs them.
 
-The reference is x86-64 C plus MASM-syntax AVX2 assembly (README.md, "Requirements").
+The reference is x86-64 C plus MASM-syntax AVX2 assembly (the reference's README.md, "Requirements").
 This script does not run the reference's Makefile.  Instead it:
 
 1. Translates each ``source/*.asm`` and ``include/*.inc`` to GNU ``as`` syntax

@@ -1,0 +1,86 @@
+"""Ingest: the -push list derived on the device from the -pull pairs (GRZ_LOAD_DERIVE_PUSH) must be
+bit-identical to the one built from the -push pairs themselves, including duplicate edges and
+self-loops; loads from pinned host memory, pageable host memory and device memory agree."""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _lists(G):
+    from grazelle import native
+    return (G.list_vectors(native.LIST_PULL), G.list_vectors(native.LIST_PUSH), G.vertex_index(native.LIST_PUSH),
+            G.outdegrees())
+
+
+def _check_derived(V, pull, push):
+    import torch
+    from grazelle.engine import Graph
+    with Graph(0) as A, Graph(0) as B:
+        A.load_pairs(V, pull, push)
+        hp = torch.from_numpy(pull.view(np.int64)).pin_memory()
+        B.load_pull_derive_push(V, pull.shape[0] // 2, hp.data_ptr())
+        for a, b in zip(_lists(A), _lists(B)):
+            np.testing.assert_array_equal(a, b)
+        np.testing.assert_array_equal(A.connected_components(), B.connected_components())
+        pa, la = A.bfs(0)
+        pb, lb = B.bfs(0)
+        np.testing.assert_array_equal(pa, pb)
+        np.testing.assert_array_equal(la, lb)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_derived_push_list_equals_built(name):
+    rec, g = load_golden(name)
+    _check_derived(g.num_vertices, g.pull_order().pairs(), g.push_order().pairs())
+
+
+@pytest.mark.parametrize("scale", [12, 17])
+def test_derived_push_list_multigraph(scale):
+    """Duplicate edges and self-loops kept, several sort passes (V > 2^16 at scale 17)."""
+    from grazelle import graphgen as gg
+    g = gg.rmat(scale, seed=scale)
+    src = np.concatenate([g.src, g.src[:1000], np.arange(50, dtype=g.src.dtype)])
+    dst = np.concatenate([g.dst, g.dst[:1000], np.arange(50, dtype=g.dst.dtype)])
+    V = g.num_vertices
+    o = np.lexsort((src, dst))
+    pull = np.empty(2 * src.shape[0], dtype=np.uint64)
+    pull[0::2], pull[1::2] = src[o], dst[o]
+    o = np.lexsort((dst, src))
+    push = np.empty_like(pull)
+    push[0::2], push[1::2] = src[o], dst[o]
+    _check_derived(V, pull, push)
+
+
+def test_device_and_host_sources_agree():
+    import torch
+    from grazelle import graphgen as gg
+    from grazelle.engine import Graph
+    g = gg.rmat(15, seed=3, symmetric=True)
+    V, E = g.num_vertices, g.num_edges
+    pull, push = g.pull_order().pairs(), g.push_order().pairs()
+    dp = torch.from_numpy(pull.view(np.int64)).cuda()
+    dq = torch.from_numpy(push.view(np.int64)).cuda()
+    with Graph(0) as A, Graph(0) as B, Graph(0) as C:
+        A.load_pairs(V, pull, push)                               # pageable host
+        B.load_device_pairs(V, E, dp.data_ptr(), dq.data_ptr())   # device
+        C.load_pull_derive_push(V, E, dp.data_ptr())              # device, derived push
+        for G in (B, C):
+            for a, b in zip(_lists(A), _lists(G)):
+                np.testing.assert_array_equal(a, b)
+        for _ in range(2):                                        # reloads reuse pooled memory
+            C.load_pull_derive_push(V, E, dp.data_ptr())
+            np.testing.assert_array_equal(A.connected_components(), C.connected_components())
+
+
+def test_derive_rejects_both_lists():
+    from grazelle import graphgen as gg, native
+    from grazelle.engine import Graph
+    g = gg.rmat(8, seed=1)
+    pull, push = g.pull_order().pairs(), g.push_order().pairs()
+    with Graph(0) as G:
+        rc = G.lib.grz_graph_load_pairs_ex(G.h, g.num_vertices, pull.shape[0] // 2, pull.ctypes.data, push.ctypes.data,
+                                           native.LOAD_DERIVE_PUSH)
+        assert rc == -1  # GRZ_ERR_ARG

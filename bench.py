@@ -20,7 +20,7 @@ threshold engine switch.  One step is one full CC run.
 `--impl reference` times only the CPU implementation, on all host threads.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference]
-                       [--workload cc|pr|bfs] [--scale S]
+                       [--workload cc|pr|bfs|batch] [--scale S] [--no-tune]
 Multi-GPU (torchrun): independent replicas, one graph per GPU ("replicas only"): nothing in
 the path exchanges data between GPUs.
 """
@@ -246,9 +246,11 @@ def run_native(a):
     load()
     hbm, hbm_kind = measured_hbm()
     # kernel shapes for this graph, chosen by timing (outside every timed region)
-    from grazelle import autotune
-    tuned = autotune.tune_cc(G, device=local) if wl in ("cc", "bfs") else autotune.tune_pr(G, device=local)
-    tuned.pop("trials", None)
+    tuned = None
+    if not a.no_tune:
+        from grazelle import autotune
+        tuned = autotune.tune_cc(G, device=local) if wl in ("cc", "bfs") else autotune.tune_pr(G, device=local)
+        tuned.pop("trials", None)
 
     def barrier():
         if dist:
@@ -511,10 +513,11 @@ def batch_study(a, torch, stream, dev):
             B.add_graph(g.num_vertices, g.pull_order().pairs())
         B.build()
         res["build_s"] = round(time.time() - t1, 2)
-        from grazelle import autotune
-        tb = autotune.tune_batch(B, seeds)
-        res["autotuned"] = {k: {"best": v["best"], "best_ms": round(v["best_ms"], 3),
-                                "default_ms": round(v["default_ms"], 3) if v["default_ms"] else None} for k, v in tb.items()}
+        if not a.no_tune:
+            from grazelle import autotune
+            tb = autotune.tune_batch(B, seeds)
+            res["autotuned"] = {k: {"best": v["best"], "best_ms": round(v["best_ms"], 3),
+                                    "default_ms": round(v["default_ms"], 3) if v["default_ms"] else None} for k, v in tb.items()}
         B.ppr(seeds, 20, 0.85, ranks=False)
         ms = []
         for _ in range(max(1, a.steps)):
@@ -552,6 +555,25 @@ def batch_study(a, torch, stream, dev):
         res["parity_sample"] = {"ppr_max_rel_l1": worst, "bfs_levels_exact": exact, "graphs_checked": [gs[0][0], gs[1][0]]}
         res["gpu_launches_per_run"] = {"ppr": 1 + 2 * 20, "msbfs": 1 + 3 * st.iterations}
     return res
+
+
+def run_batch(a):
+    """The batched workload on its own: 256 PPR and 256 BFS instances over 32 graphs, one CUDA
+    graph launch per run.  Value: PPR edge-instance updates per second (GTEPS).  Under torchrun
+    every rank runs its own replica of the batch; rank 0 reports its own numbers."""
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    stream = torch.cuda.Stream()
+    res = batch_study(a, torch, stream, local)
+    if rank != 0:
+        return
+    line = {"metric": "GTEPS (batched personalized PageRank, edge-instance updates / time)", "value": res["ppr"]["gteps"],
+            "unit": "GTEPS", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup, "ms_per_step": res["ppr"]["ms"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u128 fixed point + f64",
+            "data": "synthetic (seeded R-MAT and Erdos-Renyi)", "config": {"workload": res["workload"]}, "batch": res}
+    print(json.dumps(line), flush=True)
 
 
 # ---------------------------------------------------------------------------------------------- CPU
@@ -622,13 +644,15 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["native", "reference"], default="native")
-    ap.add_argument("--workload", choices=["cc", "pr", "bfs"], default="cc")
+    ap.add_argument("--workload", choices=["cc", "pr", "bfs", "batch"], default="cc",
+                    help="batch: only the batched PPR / multi-source BFS workload (its own JSON line)")
     ap.add_argument("--scale", type=int, default=0)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-apps", action="store_true")
     ap.add_argument("--bfs-scale", type=int, default=26, help="R-MAT scale of the BFS switch study (0: skip)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched PPR / multi-source BFS study")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default kernel shapes (no autotuning pass)")
     ap.add_argument("--lean", action="store_true", help="host keeps only the -pull pairs (default from scale 26)")
     ap.add_argument("--directed", action="store_true", help="CC/BFS on the directed R-MAT (no symmetrisation), as the scale-27 stress configuration")
     a = ap.parse_args()
@@ -637,6 +661,8 @@ def main():
         a.warmup = 3
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "batch":
+        run_batch(a)
     else:
         run_native(a)
 

@@ -15,16 +15,20 @@
 //     the vertices of the graphs before it, and the union is loaded as one grz_graph.  Kernels
 //     never need to know where one graph ends; only the per-graph sums S do.
 //   * Up to GRZ_BATCH_K (8) instances per graph share one pass over the edges.  Props are stored
-//     [vertex][instance], so the 8 lanes that serve one vector's instances read one 64-byte row
-//     per source: the random gather costs one line for 8 instances instead of 8 lines.
+//     [vertex][instance] in 4.124 fixed point (the apply converts each prop once), so the 8 lanes
+//     that serve one vector's instances read one aligned 128-byte row per source: the random
+//     gather costs one line for 8 instances instead of 8 lines, and no conversion per edge.
 //   * PPR gather: a block is 32 vectors x 8 instances.  Lane (vector, instance) sums its four
-//     sources exactly in 4.124 fixed point; then warp w reduces instance w over the block's 32
-//     vectors with a segmented scan.  Destinations complete inside the block are stored, the
-//     (at most two) cut by the block edge are added with exact u128 atomics.  Sums are exact,
-//     so results do not depend on the launch shape.
+//     sources exactly; then warp w reduces instance w over the block's 32 vectors with a
+//     segmented scan (the staging rows are padded so that the transposed read is free of bank
+//     conflicts).  Destinations complete inside the block are stored, the (at most two) cut by
+//     the block edge are added with exact u128 atomics.  Sums are exact, so results do not
+//     depend on the launch shape.
 //   * PPR apply: thread per (vertex, instance); it reads S of its graph and instance (summed
-//     exactly by the previous apply as sum deg(u) * prop(u)), writes the new props and the next
-//     S, and clears the accumulators.
+//     exactly by the previous apply as sum deg(u) * prop(u)), writes the new props and clears
+//     the accumulators.  The next S is summed in registers per graph, then per block in shared
+//     memory, and reaches global memory with one atomic per block, graph and instance (one
+//     cache line per graph would otherwise take an atomic from every 32 vertices).
 //   * Multi-source BFS: bit-parallel, 8 roots per graph.  visited / frontier are one byte per
 //     vertex (bit i = instance i).  Pull: a vector's new bits are the OR of its sources'
 //     frontier bytes, reduced per destination within the warp, minus the visited bits; the
@@ -70,7 +74,7 @@ __device__ __forceinline__ uint32_t graph_of(const uint32_t* voff, uint32_t G, u
 
 // initial PPR state: prop = one-hot(seed) / deg'; S = deg(seed) * prop(seed) per (graph, instance)
 __global__ void k_ppr_init(const uint32_t* __restrict__ seeds, uint32_t G, const double* __restrict__ inv_deg,
-                           const uint32_t* __restrict__ degree, double* __restrict__ prop, u128* __restrict__ S)
+                           const uint32_t* __restrict__ degree, u128* __restrict__ prop, u128* __restrict__ S)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= G * K) return;
@@ -78,122 +82,182 @@ __global__ void k_ppr_init(const uint32_t* __restrict__ seeds, uint32_t G, const
     const uint32_t i = t % K;
     u128 v = u128_zero();
     if (s != NONE) {
-        const double p = inv_deg[s];
+        const u128 p = fx_from_double(inv_deg[s]);
         prop[(uint64_t)s * K + i] = p;
-        v = u128_mul32(fx_from_double(p), degree[s]);
+        v = u128_mul32(p, degree[s]);
     }
     S[t] = v;
+}
+
+__device__ __forceinline__ u128 ldg_u128(const u128* p)
+{
+    const ulonglong2 q = __ldg(reinterpret_cast<const ulonglong2*>(p));
+    u128 r;
+    r.lo = q.x;
+    r.hi = q.y;
+    return r;
 }
 
 // edge-pull of all instances (see the file comment); persistent over tiles of TV vectors.
 // Block 0 first clears S_next for the apply that follows.
 __global__ void __launch_bounds__(GT) k_ppr_gather(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv,
-                                                   uint64_t nvec, uint32_t V, const double* __restrict__ prop,
+                                                   uint64_t nvec, uint32_t V, const u128* __restrict__ prop,
                                                    u128* __restrict__ rowacc, u128* __restrict__ S_next, uint32_t nS)
 {
-    __shared__ u128 s_val[TV][K];
-    __shared__ uint32_t s_key[TV + 2];
+    // double-buffered staging: the next tile writes the other buffer, so one barrier per tile
+    // separates the writes from the transposed reads (+1 row padding: the [lane][warp] read
+    // hits 8 distinct 16-byte bank groups)
+    __shared__ u128 s_val[2][TV][K + 1];
+    __shared__ uint32_t s_key[2][TV + 2];
     if (blockIdx.x == 0)
         for (uint32_t k = threadIdx.x; k < nS; k += GT) S_next[k] = u128_zero();
     const int lv = threadIdx.x / K, inst = threadIdx.x % K;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t ntiles = (nvec + TV - 1) / TV;
-    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const uint4 none4 = make_uint4(NONE, NONE, NONE, NONE);
+    // the next tile's source vector is loaded while this tile's sources are gathered
+    uint4 nx = none4;
+    if (blockIdx.x < ntiles && (uint64_t)blockIdx.x * TV + lv < nvec) nx = __ldcs(nbr + (uint64_t)blockIdx.x * TV + lv);
+    int buf = 0;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, buf ^= 1) {
         const uint64_t v0 = tile * TV;
         const uint64_t v = v0 + lv;
+        const uint4 sv = nx;
+        const uint64_t vn = v + (uint64_t)gridDim.x * TV;
+        nx = vn < nvec ? __ldcs(nbr + vn) : none4;
         u128 val = u128_zero();
-        if (v < nvec) {
-            const uint4 s = __ldcs(nbr + v);
-            const uint32_t ids[4] = { s.x, s.y, s.z, s.w };
+        const uint32_t ids[4] = { sv.x, sv.y, sv.z, sv.w };
 #pragma unroll
-            for (int l = 0; l < 4; ++l)
-                if (ids[l] < V) val = u128_add(val, fx_from_double(__ldg(prop + (uint64_t)ids[l] * K + inst)));
-            if (inst == 0) s_key[lv + 1] = __ldcs(dstv + v);
-        } else if (inst == 0) {
-            s_key[lv + 1] = NONE;
-        }
-        if (threadIdx.x == 0) s_key[0] = v0 > 0 ? __ldg(dstv + v0 - 1) : NONE - 1;
-        if (threadIdx.x == 1) s_key[TV + 1] = v0 + TV < nvec ? __ldg(dstv + v0 + TV) : NONE - 1;
-        s_val[lv][inst] = val;
+        for (int l = 0; l < 4; ++l)
+            if (ids[l] < V) val = u128_add(val, ldg_u128(prop + (uint64_t)ids[l] * K + inst));
+        uint32_t* key_s = s_key[buf];
+        if (inst == 0) key_s[lv + 1] = v < nvec ? __ldcs(dstv + v) : NONE;
+        if (threadIdx.x == 0) key_s[0] = v0 > 0 ? __ldg(dstv + v0 - 1) : NONE - 1;
+        if (threadIdx.x == 1) key_s[TV + 1] = v0 + TV < nvec ? __ldg(dstv + v0 + TV) : NONE - 1;
+        s_val[buf][lv][inst] = val;
         __syncthreads();
         // warp w = instance w, lane j = vector j of the tile
-        {
-            const uint32_t key = s_key[lane + 1];
-            u128 x = s_val[lane][warp];
-            const bool head = key != s_key[lane];      // previous vector (or the one before the tile) differs
-            const bool tail = key != s_key[lane + 2];  // next vector (or the one after the tile) differs
-            const unsigned real_heads = __ballot_sync(0xffffffffu, head);
-            const unsigned seg_heads = real_heads | 1u;
-            const int segstart = 31 - __clz(seg_heads & (0xffffffffu >> (31 - lane)));
-            const int maxlen = __reduce_max_sync(0xffffffffu, (unsigned)(lane - segstart + 1));
-            for (int off = 1; off < maxlen; off <<= 1) {
-                const u128 o = shfl_up_u128(x, off);
-                if (lane - off >= segstart) x = u128_add(x, o);
-            }
-            const bool last = tail || lane == 31;
-            if (key != NONE && last) {
-                const bool whole = tail && ((real_heads >> segstart) & 1u);
-                u128* dst = rowacc + (uint64_t)key * K + warp;
-                if (whole) *dst = x;                               // every vector of key is in this tile
-                else if (x.lo | x.hi) u128_atomic_add(dst, x);     // cut by the tile edge
-            }
+        const uint32_t key = key_s[lane + 1];
+        u128 x = s_val[buf][lane][warp];
+        const bool head = key != key_s[lane];      // previous vector (or the one before the tile) differs
+        const bool tail = key != key_s[lane + 2];  // next vector (or the one after the tile) differs
+        const unsigned real_heads = __ballot_sync(0xffffffffu, head);
+        const unsigned seg_heads = real_heads | 1u;
+        const int segstart = 31 - __clz(seg_heads & (0xffffffffu >> (31 - lane)));
+        const int maxlen = __reduce_max_sync(0xffffffffu, (unsigned)(lane - segstart + 1));
+        for (int off = 1; off < maxlen; off <<= 1) {
+            const u128 o = shfl_up_u128(x, off);
+            if (lane - off >= segstart) x = u128_add(x, o);
         }
-        __syncthreads();
+        const bool last = tail || lane == 31;
+        if (key != NONE && last) {
+            const bool whole = tail && ((real_heads >> segstart) & 1u);
+            u128* dst = rowacc + (uint64_t)key * K + warp;
+            if (whole) *dst = x;                               // every vector of key is in this tile
+            else if (x.lo | x.hi) u128_atomic_add(dst, x);     // cut by the tile edge
+        }
     }
 }
 
-// vertex phase of all instances; thread per (vertex, instance)
-__global__ void __launch_bounds__(GT) k_ppr_apply(u128* __restrict__ rowacc, const double* __restrict__ inv_deg,
-                                                  const uint32_t* __restrict__ degree, uint32_t V,
-                                                  const uint32_t* __restrict__ voff_g, uint32_t G,
-                                                  const uint32_t* __restrict__ seeds, double damping,
-                                                  const u128* __restrict__ S_cur, u128* __restrict__ S_next,
-                                                  double* __restrict__ prop_out, double* __restrict__ rank_out)
+constexpr int APPLY_SLOTS = 64;  // graphs whose next S a block sums in shared memory (beyond: global atomics)
+constexpr int APPLY_U = 8;       // tiles whose accumulators a thread loads before it stores anything
+
+// bit j of word t: vertex 32t + j has pull vectors in two or more gather tiles, so its
+// accumulator is summed with atomics and the apply must clear it.  Every other accumulator is
+// either stored whole by each gather or never written (no in-edges), and needs no clearing.
+__global__ void k_ppr_cutbits(const uint32_t* __restrict__ rowptr, uint32_t V, uint32_t* __restrict__ cut)
+{
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    bool c = false;
+    if (v < V) {
+        const uint32_t r0 = rowptr[v], r1 = rowptr[v + 1];
+        c = r1 > r0 && r0 / TV != (r1 - 1) / TV;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, c);
+    if ((threadIdx.x & 31) == 0 && v < V) cut[v / 32] = m;
+}
+
+__device__ __forceinline__ void s_flush(u128* s_part, u128* S_next, uint32_t g, int inst, u128 x)
+{
+    if ((x.lo | x.hi) == 0) return;
+    if (g < (uint32_t)APPLY_SLOTS) u128_atomic_add(s_part + g * K + inst, x);
+    else u128_atomic_add(S_next + (uint64_t)g * K + inst, x);
+}
+
+// vertex phase of all instances; thread per (vertex, instance).  The grid strides over tiles of
+// 32 vertices (all blocks on one moving front of the arrays), APPLY_U tiles at a time: their
+// accumulators are loaded first, so that enough bytes are in flight to cover DRAM latency.
+__global__ void __launch_bounds__(GT, 3) k_ppr_apply(u128* __restrict__ rowacc, const uint32_t* __restrict__ cut,
+                                                     const double* __restrict__ inv_deg,
+                                                     const uint32_t* __restrict__ degree, uint32_t V,
+                                                     const uint32_t* __restrict__ voff_g, uint32_t G,
+                                                     const uint32_t* __restrict__ seeds, double damping,
+                                                     const u128* __restrict__ S_cur, u128* __restrict__ S_next,
+                                                     u128* __restrict__ prop_out, double* __restrict__ rank_out)
 {
     __shared__ uint32_t voff[MAX_GRAPHS + 1];
-    __shared__ u128 s_part[2][K];
+    __shared__ u128 s_part[APPLY_SLOTS * K];
+    const uint32_t nslots = (G < (uint32_t)APPLY_SLOTS ? G : (uint32_t)APPLY_SLOTS) * K;
     for (uint32_t k = threadIdx.x; k <= G; k += GT) voff[k] = voff_g[k];
-    if (threadIdx.x < 2 * K) s_part[threadIdx.x / K][threadIdx.x % K] = u128_zero();
+    for (uint32_t k = threadIdx.x; k < nslots; k += GT) s_part[k] = u128_zero();
     __syncthreads();
-    const int inst = threadIdx.x % K;
-    for (uint64_t base = (uint64_t)blockIdx.x * TV; base < V; base += (uint64_t)gridDim.x * TV) {
-        const uint32_t v = (uint32_t)(base + threadIdx.x / K);
-        const uint32_t g0 = graph_of(voff, G, (uint32_t)base);
-        if (v < V) {
-            const uint64_t idx = (uint64_t)v * K + inst;
-            const u128 a = rowacc[idx];
-            rowacc[idx] = u128_zero();
-            const uint32_t g = graph_of(voff, G, v);
-            const uint32_t seed = seeds[g * K + inst];
-            double rank = 0.0;
-            if (seed != NONE) {
+    const uint64_t ntiles = ((uint64_t)V + TV - 1) / TV;
+    const int inst = threadIdx.x % K, lv = threadIdx.x / K;
+    // per-thread state of the graph of its current vertex (vertices ascend); the seed's teleport
+    // term d * (1 - S) + (1 - d) is computed once per graph
+    uint32_t g = 0, gend = 0, seed = NONE;
+    double cseed = 0.0;
+    u128 acc = u128_zero();
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += (uint64_t)APPLY_U * gridDim.x) {
+        u128 a[APPLY_U];
+        uint32_t cw[APPLY_U];
+#pragma unroll
+        for (int j = 0; j < APPLY_U; ++j) {
+            const uint64_t t = tile + (uint64_t)j * gridDim.x;
+            const uint64_t v = t * TV + lv;
+            a[j] = u128_zero();
+            cw[j] = 0;
+            if (v < V) {
+                const ulonglong2 q = *(reinterpret_cast<const ulonglong2*>(rowacc) + v * K + inst);
+                a[j].lo = q.x;
+                a[j].hi = q.y;
+                cw[j] = __ldg(cut + t);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < APPLY_U; ++j) {
+            const uint64_t v64 = (tile + (uint64_t)j * gridDim.x) * TV + lv;
+            if (v64 >= V) break;
+            const uint32_t v = (uint32_t)v64;
+            if (v >= gend) {
+                s_flush(s_part, S_next, g, inst, acc);
+                acc = u128_zero();
+                g = graph_of(voff, G, v);
+                gend = voff[g + 1];
+                seed = seeds[g * K + inst];
                 const double S = fx_to_double(S_cur[g * K + inst]);
-                const double c = v == seed ? __dadd_rn(__dmul_rn(damping, 1.0 - S), 1.0 - damping) : 0.0;
-                rank = __fma_rn(fx_to_double(a), damping, c);
+                cseed = __dadd_rn(__dmul_rn(damping, 1.0 - S), 1.0 - damping);
             }
-            const double p = __dmul_rn(rank, inv_deg[v]);
-            prop_out[idx] = p;
+            const uint64_t idx = (uint64_t)v * K + inst;
+            const bool mass = (a[j].lo | a[j].hi) != 0;
+            if (mass && ((cw[j] >> lv) & 1u)) rowacc[idx] = u128_zero();
+            // rank' = fma(accum, d, [v == seed] * teleport); zero without mass (most vertices early on)
+            double rank = 0.0;
+            u128 p = u128_zero();
+            if (seed != NONE && (mass || v == seed)) {
+                rank = __fma_rn(fx_to_double(a[j]), damping, v == seed ? cseed : 0.0);
+                p = fx_from_double(__dmul_rn(rank, __ldg(inv_deg + v)));
+                if (p.lo | p.hi) acc = u128_add(acc, u128_mul32(p, __ldg(degree + v)));
+            }
+            *(reinterpret_cast<ulonglong2*>(prop_out) + idx) = make_ulonglong2(p.lo, p.hi);
             if (rank_out) rank_out[idx] = rank;
-            const u128 contrib = u128_mul32(fx_from_double(p), degree[v]);
-            if (contrib.lo | contrib.hi) {
-                // a block's 32 vertices span at most two graphs (each graph has at least 32 vertices)
-                u128* sp = &s_part[g == g0 ? 0 : 1][inst];
-                const unsigned long long old = atomicAdd(&sp->lo, contrib.lo);
-                const unsigned long long carry = (old + contrib.lo < old) ? 1ull : 0ull;
-                if (contrib.hi | carry) atomicAdd(&sp->hi, contrib.hi + carry);
-            }
         }
-        __syncthreads();
-        if (threadIdx.x < 2 * K) {
-            const int slot = threadIdx.x / K, i = threadIdx.x % K;
-            const u128 x = s_part[slot][i];
-            if (x.lo | x.hi) {
-                const uint32_t gg = slot == 0 ? g0 : g0 + 1;
-                u128_atomic_add(S_next + gg * K + i, x);
-                s_part[slot][i] = u128_zero();
-            }
-        }
-        __syncthreads();
+    }
+    s_flush(s_part, S_next, g, inst, acc);
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < nslots; k += GT) {
+        const u128 x = s_part[k];
+        if (x.lo | x.hi) u128_atomic_add(S_next + k, x);
     }
 }
 
@@ -319,9 +383,10 @@ struct grz_batch {
     uint32_t* d_voff;
     uint32_t* d_seeds;                   // [G][K] union vertex IDs or NONE
     // PPR
-    double* prop[2];
+    u128* prop[2];                       // [vertex][instance] 4.124 fixed point
     double* rank;
     u128* rowacc;
+    uint32_t* cut;                       // [V/32] accumulators the apply clears (k_ppr_cutbits)
     u128* S[2];
     cudaGraphExec_t ppr_exec;
     uint32_t ppr_iters;
@@ -379,12 +444,14 @@ extern "C" int grz_batch_create(grz_batch** out, int device, void* stream)
 
 static void free_state(grz_batch* b)
 {
-    void* p[] = { b->d_voff, b->d_seeds, b->prop[0], b->prop[1], b->rank, b->rowacc, b->S[0], b->S[1],
+    void* p[] = { b->d_voff, b->d_seeds, b->prop[0], b->prop[1], b->rank, b->rowacc, b->cut, b->S[0], b->S[1],
                   b->visited, b->frontier, b->next_words, b->level, b->ctl, b->iter };
     for (void* x : p) cudaFree(x);
     b->d_voff = b->d_seeds = nullptr;
-    b->prop[0] = b->prop[1] = b->rank = nullptr;
+    b->prop[0] = b->prop[1] = nullptr;
+    b->rank = nullptr;
     b->rowacc = b->S[0] = b->S[1] = nullptr;
+    b->cut = nullptr;
     b->visited = b->frontier = nullptr;
     b->next_words = nullptr;
     b->level = nullptr;
@@ -492,11 +559,12 @@ static int build_ppr_graph(grz_batch* b, uint32_t iterations, double damping)
     cudaGraph_t graph = nullptr;
     int rc = bck(b, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "begin capture");
     const unsigned ggrid = persistent_grid(b, (u->pull.nvec + TV - 1) / TV, b->ppr_blocks);
-    const unsigned agrid = persistent_grid(b, (V + TV - 1) / TV, b->ppr_blocks);
+    // 3 blocks per SM fit the apply's registers (8 tiles of accumulators per thread in flight)
+    const unsigned agrid = persistent_grid(b, (V + TV - 1) / TV, std::min(b->ppr_blocks, 3));
     int cur = 0;
     for (uint32_t it = 0; it < iterations && !rc; ++it) {
         k_ppr_gather<<<ggrid, GT, 0, cs>>>(u->pull.nbr, u->pull.shared, u->pull.nvec, V, b->prop[cur], b->rowacc, b->S[cur ^ 1], G * K);
-        k_ppr_apply<<<agrid, GT, 0, cs>>>(b->rowacc, u->inv_deg, u->degree, V, b->d_voff, G, b->d_seeds, damping, b->S[cur],
+        k_ppr_apply<<<agrid, GT, 0, cs>>>(b->rowacc, b->cut, u->inv_deg, u->degree, V, b->d_voff, G, b->d_seeds, damping, b->S[cur],
                                          b->S[cur ^ 1], b->prop[cur ^ 1], it + 1 == iterations ? b->rank : nullptr);
         cur ^= 1;
         rc = bck(b, cudaGetLastError(), "ppr launch");
@@ -525,13 +593,16 @@ extern "C" int grz_batch_ppr(grz_batch* b, const uint32_t* seeds, uint32_t k, ui
     const uint64_t V = u->V;
     const uint32_t G = (uint32_t)b->Vg.size();
     if (!b->prop[0]) {
-        BCK(b, cudaMalloc((void**)&b->prop[0], sizeof(double) * V * K));
-        BCK(b, cudaMalloc((void**)&b->prop[1], sizeof(double) * V * K));
+        BCK(b, cudaMalloc((void**)&b->prop[0], sizeof(u128) * V * K));
+        BCK(b, cudaMalloc((void**)&b->prop[1], sizeof(u128) * V * K));
         BCK(b, cudaMalloc((void**)&b->rank, sizeof(double) * V * K));
         BCK(b, cudaMalloc((void**)&b->rowacc, sizeof(u128) * (V + 1) * K));
         BCK(b, cudaMalloc((void**)&b->S[0], sizeof(u128) * G * K));
         BCK(b, cudaMalloc((void**)&b->S[1], sizeof(u128) * G * K));
         BCK(b, cudaMemsetAsync(b->rowacc, 0, sizeof(u128) * (V + 1) * K, b->stream));
+        BCK(b, cudaMalloc((void**)&b->cut, sizeof(uint32_t) * ((V + 31) / 32)));
+        k_ppr_cutbits<<<(unsigned)((V + 255) / 256), 256, 0, b->stream>>>(u->pull.rowptr, (uint32_t)V, b->cut);
+        BCK(b, cudaGetLastError());
     }
     int rc = upload_seeds(b, seeds, k);
     if (rc) return rc;
@@ -544,7 +615,7 @@ extern "C" int grz_batch_ppr(grz_batch* b, const uint32_t* seeds, uint32_t k, ui
     BCK(b, cudaEventCreate(&e1));
     cudaStream_t st = b->stream;
     rc = bck(b, cudaEventRecord(e0, st), "event");
-    if (!rc) rc = bck(b, cudaMemsetAsync(b->prop[0], 0, sizeof(double) * V * K, st), "memset");
+    if (!rc) rc = bck(b, cudaMemsetAsync(b->prop[0], 0, sizeof(u128) * V * K, st), "memset");
     if (!rc) {
         k_ppr_init<<<(G * K + 255) / 256, 256, 0, st>>>(b->d_seeds, G, u->inv_deg, u->degree, b->prop[0], b->S[0]);
         rc = bck(b, cudaGetLastError(), "ppr init");

@@ -100,10 +100,12 @@ static void free_graph_data(grz_graph* g)
     // reads at random (pool memory measured 12% slower for random gathers)
     void* pooled[] = { g->outdeg, g->degree, g->inv_deg, g->prop, g->accum, g->glob, g->scratch };
     for (void* p : pooled) grz_dev_free(g, p);
-    void* plain[] = { g->pr_fx[0], g->pr_fx[1], g->pr_sum, g->pr_K, g->pr_rowacc };
+    void* plain[] = { g->pr_fx[0], g->pr_fx[1], g->pr_sum, g->pr_K, g->pr_rowacc, g->pr_cut };
     for (void* p : plain) cudaFree(p);
     g->outdeg = nullptr; g->degree = nullptr; g->inv_deg = nullptr;
     g->pr_fx[0] = g->pr_fx[1] = nullptr; g->pr_sum = nullptr; g->pr_K = nullptr; g->pr_rowacc = nullptr;
+    g->pr_cut = nullptr;
+    g->pr_rowacc_stale = 0;
     g->prop = nullptr; g->accum = nullptr; g->glob = nullptr; g->scratch = nullptr;
     g->scratch_bytes = 0;
     g->max_degree_known = 0;

@@ -327,7 +327,10 @@ struct grz_graph {
     u128* pr_sum;         // u128[2][V/256]: per-block partials of S_k (ping-pong)
     double* pr_K;         // per-iteration constant G*d + (1-d)/V, written by the gather kernel
     int pr_sum_cur;
-    u128* pr_rowacc;      // u128[V+1] exact per-destination accumulators (all zero between iterations)
+    u128* pr_rowacc;      // u128[V+1] exact per-destination accumulators
+    uint32_t* pr_cut;     // uint32[V/32]: destinations whose pull vectors straddle a gather tile
+    int pr_rowacc_stale;  // fused iterations cleared only the straddling accumulators
+    uint32_t pr_nparts[2];  // partials in each half of pr_sum
     double pr_damping;
     uint32_t pr_iters_done;
     double* prop;         // double[V+8]: reference-format vertex props (PR props, CC labels, BFS parents)

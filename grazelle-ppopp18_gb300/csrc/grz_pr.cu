@@ -63,9 +63,11 @@ __device__ __forceinline__ u128 u128_shfl_up(u128 v, int off)
 // addition makes the order immaterial anyway.  A warp-segmented inclusive scan over the
 // destination keys then sums the vectors of each destination within the warp.  A destination
 // whose vectors all lie in this warp is stored with one plain store.  One that continues into a
-// neighbouring warp is added with exact u128 atomics.  rowacc[] is all zero on entry (the apply
-// kernel clears it after reading), and a destination with no in-edges is never touched, so it
-// stays 0.  The loads of nbr/dst are streamed once (evict-first); the prop gathers go through L1.
+// neighbouring warp is combined across the block and stored once; only a destination whose
+// vectors straddle the block's tile edge is added with exact u128 atomics, so only those
+// accumulators must be zero on entry (the fused apply clears exactly those, marked in pr_cut).
+// A destination with no in-edges is never touched and stays 0.  The loads of nbr/dst are
+// streamed once (evict-first); the prop gathers go through L1.
 __device__ __forceinline__ u128 block_reduce_u128(u128 s, u128* red);
 
 __global__ void __launch_bounds__(PR_THREADS) k_pr_gather(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv,
@@ -180,31 +182,71 @@ __device__ __forceinline__ u128 block_reduce_u128(u128 s, u128* red)
 // Vertex phase fused with reading the accumulators (phase_vertex_pr.asm:75-134):
 //   prop[v] = (acc[v]*d + G*d + (1-d)/V) / deg'[v],  G = (1 - S)/V
 // computed as fma + multiply by the precomputed 1/deg'.  It writes the new props in fixed point
-// (plus double when asked), clears rowacc, and accumulates S' = sum deg[v]*prop[v] exactly.
-// S' is the next iteration's sum of accumulators.
-__global__ void __launch_bounds__(PR_THREADS) k_pr_apply(u128* __restrict__ rowacc, const double* __restrict__ inv_deg,
-                                                         const uint32_t* __restrict__ degree, uint64_t V,
-                                                         const double* __restrict__ Kp, u128* __restrict__ part_out, double damping,
-                                                         u128* __restrict__ prop_fx, double* __restrict__ prop_out)
+// (plus double when asked) and accumulates S' = sum deg[v]*prop[v] exactly; S' is the next
+// iteration's sum of accumulators.  Of the accumulators it clears only those the next gather
+// adds to atomically (bit set in `cut`); the others are overwritten by the next gather's stores.
+// The grid strides over the vertices, PR_APPLY_U vertices per thread at a time whose
+// accumulators are loaded before anything is stored, so that enough bytes are in flight to
+// cover DRAM latency; one partial of S' per block.
+constexpr int PR_APPLY_U = 8;
+constexpr int PR_APPLY_RESIDENT = 3;  // blocks per SM that the launch bounds fit
+
+__global__ void __launch_bounds__(PR_THREADS, PR_APPLY_RESIDENT) k_pr_apply(u128* __restrict__ rowacc, const uint32_t* __restrict__ cut,
+                                                                            const double* __restrict__ inv_deg,
+                                                                            const uint32_t* __restrict__ degree, uint64_t V,
+                                                                            const double* __restrict__ Kp, u128* __restrict__ part_out,
+                                                                            double damping, u128* __restrict__ prop_fx,
+                                                                            double* __restrict__ prop_out)
 {
     __shared__ u128 red[PR_THREADS / 32];
     const double sK = *Kp;
-    const uint64_t v = (uint64_t)blockIdx.x * PR_THREADS + threadIdx.x;
+    const uint64_t stride = (uint64_t)gridDim.x * PR_THREADS;
     u128 s = u128_zero();
-    if (v < V) {
-        const ulonglong2 a = __ldcs(reinterpret_cast<const ulonglong2*>(rowacc) + v);
-        __stcs(reinterpret_cast<ulonglong2*>(rowacc) + v, make_ulonglong2(0ull, 0ull));
-        u128 acc;
-        acc.lo = a.x;
-        acc.hi = a.y;
-        const double p = __dmul_rn(__fma_rn(fx_to_double(acc), damping, sK), __ldcs(inv_deg + v));
-        const u128 pf = fx_from_double(p);
-        __stcg(reinterpret_cast<ulonglong2*>(prop_fx) + v, make_ulonglong2(pf.lo, pf.hi));
-        if (prop_out) prop_out[v] = p;
-        s = u128_mul32(pf, __ldcs(degree + v));
+    for (uint64_t base = (uint64_t)blockIdx.x * PR_THREADS + threadIdx.x; base < V; base += stride * PR_APPLY_U) {
+        ulonglong2 a[PR_APPLY_U];
+        uint32_t cw[PR_APPLY_U];
+#pragma unroll
+        for (int j = 0; j < PR_APPLY_U; ++j) {
+            const uint64_t v = base + (uint64_t)j * stride;
+            a[j] = make_ulonglong2(0ull, 0ull);
+            cw[j] = 0;
+            if (v < V) {
+                a[j] = __ldcs(reinterpret_cast<const ulonglong2*>(rowacc) + v);
+                cw[j] = __ldg(cut + (v >> 5));
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < PR_APPLY_U; ++j) {
+            const uint64_t v = base + (uint64_t)j * stride;
+            if (v >= V) break;
+            if ((a[j].x | a[j].y) && ((cw[j] >> (v & 31)) & 1u))
+                *(reinterpret_cast<ulonglong2*>(rowacc) + v) = make_ulonglong2(0ull, 0ull);
+            u128 acc;
+            acc.lo = a[j].x;
+            acc.hi = a[j].y;
+            const double p = __dmul_rn(__fma_rn(fx_to_double(acc), damping, sK), __ldg(inv_deg + v));
+            const u128 pf = fx_from_double(p);
+            __stcg(reinterpret_cast<ulonglong2*>(prop_fx) + v, make_ulonglong2(pf.lo, pf.hi));
+            if (prop_out) prop_out[v] = p;
+            s = u128_add(s, u128_mul32(pf, __ldg(degree + v)));
+        }
     }
     s = block_reduce_u128(s, red);
     if (threadIdx.x == 0) part_out[blockIdx.x] = s;  // summed by the next gather kernel's block 0
+}
+
+// bit j of word t: vertex 32t + j has pull vectors in two or more gather tiles of PR_THREADS
+// vectors (its accumulator is summed with atomics)
+__global__ void k_pr_cutbits(const uint32_t* __restrict__ rowptr, uint64_t V, uint32_t* __restrict__ cut)
+{
+    const uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool c = false;
+    if (v < V) {
+        const uint32_t r0 = rowptr[v], r1 = rowptr[v + 1];
+        c = r1 > r0 && r0 / PR_THREADS != (r1 - 1) / PR_THREADS;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, c);
+    if ((threadIdx.x & 31) == 0 && v < V) cut[v >> 5] = m;
 }
 
 // Edge-pull phase alone (the phases.h boundary): accumulators as doubles plus their exact sum
@@ -268,6 +310,17 @@ unsigned blocks_for(uint64_t n) { return (unsigned)((n + PR_THREADS - 1) / PR_TH
 
 }  // namespace
 
+// The phase-API gathers and the push phase add into every accumulator: after fused iterations,
+// which leave the accumulators of non-straddling destinations holding their last sums, clear all.
+int grz_pr_rowacc_clean(grz_graph* g)
+{
+    if (g->pr_rowacc && g->pr_rowacc_stale) {
+        GRZ_CK(g, cudaMemsetAsync(g->pr_rowacc, 0, sizeof(u128) * (g->V + 1), g->stream));
+        g->pr_rowacc_stale = 0;
+    }
+    return GRZ_OK;
+}
+
 int grz_pr_prepare(grz_graph* g)
 {
     const uint64_t V = g->V;
@@ -278,6 +331,12 @@ int grz_pr_prepare(grz_graph* g)
         GRZ_CK(g, cudaMalloc((void**)&g->pr_K, sizeof(double) * 2));
         GRZ_CK(g, cudaMalloc((void**)&g->pr_rowacc, sizeof(u128) * (V + 1)));
         GRZ_CK(g, cudaMemsetAsync(g->pr_rowacc, 0, sizeof(u128) * (V + 1), g->stream));
+        g->pr_rowacc_stale = 0;
+        GRZ_CK(g, cudaMalloc((void**)&g->pr_cut, sizeof(uint32_t) * ((V + 31) / 32 + 1)));
+        if (V) {
+            k_pr_cutbits<<<blocks_for(V), PR_THREADS, 0, g->stream>>>(g->pull.rowptr, V, g->pr_cut); GRZ_COUNT_LAUNCH(g);
+            GRZ_CK(g, cudaGetLastError());
+        }
         // entry V of both prop arrays is a permanent zero that invalid lanes gather
         GRZ_CK(g, cudaMemsetAsync(g->pr_fx[0], 0, sizeof(u128) * (V + 1), g->stream));
         GRZ_CK(g, cudaMemsetAsync(g->pr_fx[1], 0, sizeof(u128) * (V + 1), g->stream));
@@ -296,6 +355,7 @@ int grz_pr_init_state(grz_graph* g, double damping)
     g->pr_iters_done = 0;
     GRZ_CK(g, cudaMemsetAsync(g->pr_sum, 0, sizeof(u128) * 2 * (blocks_for(g->V) + 1), g->stream));
     GRZ_CK(g, cudaMemsetAsync(g->accum, 0, sizeof(double) * (g->V + 8), g->stream));
+    g->pr_nparts[0] = g->pr_nparts[1] = blocks_for(g->V);
     if (g->V) {
         k_pr_init<<<blocks_for(g->V), PR_THREADS, 0, g->stream>>>(g->outdeg, g->degree, g->V, g->prop, g->accum, g->pr_fx[0], g->pr_sum); GRZ_COUNT_LAUNCH(g);
         GRZ_CK(g, cudaGetLastError());
@@ -338,10 +398,10 @@ int grz_pr_fused_iteration(grz_graph* g, int write_double_props)
     if (g->V == 0) return GRZ_OK;
     const int k = g->pr_sum_cur;
     const double dV = (double)g->V;
-    const uint32_t nparts = blocks_for(g->V);
+    const uint32_t stride = blocks_for(g->V) + 1;  // each half of pr_sum holds up to blocks_for(V) partials
     PRConst pc;
-    pc.part_in = g->pr_sum + (size_t)k * nparts;
-    pc.nparts = nparts;
+    pc.part_in = g->pr_sum + (size_t)k * stride;
+    pc.nparts = g->pr_nparts[k];
     pc.K_out = g->pr_K;
     pc.damping = g->pr_damping;
     pc.c = (1.0 - g->pr_damping) / dV;
@@ -349,11 +409,16 @@ int grz_pr_fused_iteration(grz_graph* g, int write_double_props)
     int rc = pr_gather(g, 0, g->pull.nvec, pc);
     if (rc) return rc;
     grz_prof_begin(g, GRZ_PROF_PR_APPLY);
-    k_pr_apply<<<blocks_for(g->V), PR_THREADS, 0, g->stream>>>(g->pr_rowacc, g->inv_deg, g->degree, g->V, g->pr_K,
-                                                               g->pr_sum + (size_t)(k ^ 1) * nparts, g->pr_damping, g->pr_fx[g->pr_cur ^ 1],
-                                                               write_double_props ? g->prop : nullptr); GRZ_COUNT_LAUNCH(g);
+    const uint64_t agrid = std::max<uint64_t>(1, std::min<uint64_t>((g->V + (uint64_t)PR_THREADS * PR_APPLY_U - 1) /
+                                                                        ((uint64_t)PR_THREADS * PR_APPLY_U),
+                                                                    (uint64_t)g->num_sms * PR_APPLY_RESIDENT));
+    k_pr_apply<<<(unsigned)agrid, PR_THREADS, 0, g->stream>>>(g->pr_rowacc, g->pr_cut, g->inv_deg, g->degree, g->V, g->pr_K,
+                                                              g->pr_sum + (size_t)(k ^ 1) * stride, g->pr_damping, g->pr_fx[g->pr_cur ^ 1],
+                                                              write_double_props ? g->prop : nullptr); GRZ_COUNT_LAUNCH(g);
     grz_prof_end(g);
     GRZ_CK(g, cudaGetLastError());
+    g->pr_nparts[k ^ 1] = (uint32_t)agrid;
+    g->pr_rowacc_stale = 1;
     g->pr_cur ^= 1;
     g->pr_sum_cur = k ^ 1;
     g->pr_iters_done++;
@@ -366,9 +431,11 @@ int grz_pr_fused_iteration(grz_graph* g, int write_double_props)
 int grz_pr_edge_pull(grz_graph* g, uint64_t first, uint64_t count)
 {
     if (g->V == 0) return GRZ_OK;
+    int rc = grz_pr_rowacc_clean(g);
+    if (rc) return rc;
     PRConst pc;
     memset(&pc, 0, sizeof(pc));
-    int rc = pr_gather(g, first, count, pc);
+    rc = pr_gather(g, first, count, pc);
     if (rc) return rc;
     if (first + count < g->pull.nvec) return GRZ_OK;
     k_pr_accum_out<<<blocks_for(g->V), PR_THREADS, 0, g->stream>>>(g->pr_rowacc, g->V, g->accum, g->glob); GRZ_COUNT_LAUNCH(g);
@@ -455,7 +522,9 @@ int grz_pr_push_phase(grz_graph* g, uint64_t first_vec, uint64_t count)
 {
     if (!g->push.nbr) return grz_set_error(g, GRZ_ERR_STATE, "push list not loaded");
     if (count == 0) return GRZ_OK;
-    // the pull accumulators double as the push accumulators (zero between uses)
+    // the pull accumulators double as the push accumulators (all zero between uses)
+    int rc = grz_pr_rowacc_clean(g);
+    if (rc) return rc;
     k_pr_push<<<blocks_for(count), PR_THREADS, 0, g->stream>>>(g->push.nbr, g->push.shared, first_vec, count,
                                                                g->pr_fx[g->pr_cur], g->pr_rowacc, g->glob); GRZ_COUNT_LAUNCH(g);
     GRZ_CK(g, cudaGetLastError());

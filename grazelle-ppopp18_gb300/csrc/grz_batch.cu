@@ -18,12 +18,12 @@
 //     [vertex][instance] in 4.124 fixed point (the apply converts each prop once), so the 8 lanes
 //     that serve one vector's instances read one aligned 128-byte row per source: the random
 //     gather costs one line for 8 instances instead of 8 lines, and no conversion per edge.
-//   * PPR gather: a block is 32 vectors x 8 instances.  Lane (vector, instance) sums its four
-//     sources exactly; then warp w reduces instance w over the block's 32 vectors with a
-//     segmented scan (the staging rows are padded so that the transposed read is free of bank
-//     conflicts).  Destinations complete inside the block are stored, the (at most two) cut by
-//     the block edge are added with exact u128 atomics.  Sums are exact, so results do not
-//     depend on the launch shape.
+//   * PPR gather: a warp owns a tile of 32 vectors and walks it 4 vectors x 8 instances at a
+//     time.  Lane (vector, instance) sums its four sources exactly; a shuffle scan over the 4
+//     vectors and a carried running sum complete each destination inside the warp, with no
+//     shared memory and no barrier.  Destinations complete inside the tile are stored, the (at
+//     most two) cut by the tile edge are added with exact u128 atomics.  Sums are exact, so
+//     results do not depend on the launch shape.
 //   * PPR apply: thread per (vertex, instance); it reads S of its graph and instance (summed
 //     exactly by the previous apply as sum deg(u) * prop(u)), writes the new props and clears
 //     the accumulators.  The next S is summed in registers per graph, then per block in shared
@@ -98,63 +98,80 @@ __device__ __forceinline__ u128 ldg_u128(const u128* p)
     return r;
 }
 
-// edge-pull of all instances (see the file comment); persistent over tiles of TV vectors.
-// Block 0 first clears S_next for the apply that follows.
+// edge-pull of all instances (see the file comment).  Warp-level tiles of TV = 32 vectors,
+// persistent over the grid's warps.  A warp walks its tile in 8 steps of 4 vectors x 8 instances
+// (lane = 8 * slot + instance): it sums each lane's four sources exactly, scans the step's 4
+// vectors per instance (keys ascend, so equal keys form one run), and carries the open
+// destination's running sum into the next step.  A destination whose vectors all lie in the
+// tile is stored once by the lane of its last vector; one cut by the tile edge is added with
+// exact u128 atomics.  Block 0 first clears S_next for the apply that follows.
+constexpr int GSTEPS = TV / 4;  // steps of 4 vectors per tile
+constexpr int GCHUNK = 4;       // steps whose loads are issued together
+
+__device__ __forceinline__ u128 shfl_u128(u128 v, int src)
+{
+    u128 r;
+    r.lo = __shfl_sync(0xffffffffu, v.lo, src);
+    r.hi = __shfl_sync(0xffffffffu, v.hi, src);
+    return r;
+}
+
 __global__ void __launch_bounds__(GT) k_ppr_gather(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv,
                                                    uint64_t nvec, uint32_t V, const u128* __restrict__ prop,
                                                    u128* __restrict__ rowacc, u128* __restrict__ S_next, uint32_t nS)
 {
-    // double-buffered staging: the next tile writes the other buffer, so one barrier per tile
-    // separates the writes from the transposed reads (+1 row padding: the [lane][warp] read
-    // hits 8 distinct 16-byte bank groups)
-    __shared__ u128 s_val[2][TV][K + 1];
-    __shared__ uint32_t s_key[2][TV + 2];
     if (blockIdx.x == 0)
         for (uint32_t k = threadIdx.x; k < nS; k += GT) S_next[k] = u128_zero();
-    const int lv = threadIdx.x / K, inst = threadIdx.x % K;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const int q = lane / K, inst = lane % K;
     const uint64_t ntiles = (nvec + TV - 1) / TV;
-    const uint4 none4 = make_uint4(NONE, NONE, NONE, NONE);
-    // the next tile's source vector is loaded while this tile's sources are gathered
-    uint4 nx = none4;
-    if (blockIdx.x < ntiles && (uint64_t)blockIdx.x * TV + lv < nvec) nx = __ldcs(nbr + (uint64_t)blockIdx.x * TV + lv);
-    int buf = 0;
-    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, buf ^= 1) {
+    const uint64_t nwarps = (uint64_t)gridDim.x * (GT / 32);
+    for (uint64_t tile = (uint64_t)blockIdx.x * (GT / 32) + (threadIdx.x >> 5); tile < ntiles; tile += nwarps) {
         const uint64_t v0 = tile * TV;
-        const uint64_t v = v0 + lv;
-        const uint4 sv = nx;
-        const uint64_t vn = v + (uint64_t)gridDim.x * TV;
-        nx = vn < nvec ? __ldcs(nbr + vn) : none4;
-        u128 val = u128_zero();
-        const uint32_t ids[4] = { sv.x, sv.y, sv.z, sv.w };
+        // the tile's 32 keys, one per lane (NONE past the list), and the keys either side of it
+        const uint32_t kall = v0 + lane < nvec ? __ldcs(dstv + v0 + lane) : NONE;
+        const uint32_t kbefore = v0 > 0 ? __ldg(dstv + v0 - 1) : NONE - 1;
+        const uint32_t kafter = v0 + TV < nvec ? __ldg(dstv + v0 + TV) : NONE - 1;
+        u128 carry = u128_zero();
+        uint32_t ckey = NONE - 1;  // destination of the open run carried from the previous step
 #pragma unroll
-        for (int l = 0; l < 4; ++l)
-            if (ids[l] < V) val = u128_add(val, ldg_u128(prop + (uint64_t)ids[l] * K + inst));
-        uint32_t* key_s = s_key[buf];
-        if (inst == 0) key_s[lv + 1] = v < nvec ? __ldcs(dstv + v) : NONE;
-        if (threadIdx.x == 0) key_s[0] = v0 > 0 ? __ldg(dstv + v0 - 1) : NONE - 1;
-        if (threadIdx.x == 1) key_s[TV + 1] = v0 + TV < nvec ? __ldg(dstv + v0 + TV) : NONE - 1;
-        s_val[buf][lv][inst] = val;
-        __syncthreads();
-        // warp w = instance w, lane j = vector j of the tile
-        const uint32_t key = key_s[lane + 1];
-        u128 x = s_val[buf][lane][warp];
-        const bool head = key != key_s[lane];      // previous vector (or the one before the tile) differs
-        const bool tail = key != key_s[lane + 2];  // next vector (or the one after the tile) differs
-        const unsigned real_heads = __ballot_sync(0xffffffffu, head);
-        const unsigned seg_heads = real_heads | 1u;
-        const int segstart = 31 - __clz(seg_heads & (0xffffffffu >> (31 - lane)));
-        const int maxlen = __reduce_max_sync(0xffffffffu, (unsigned)(lane - segstart + 1));
-        for (int off = 1; off < maxlen; off <<= 1) {
-            const u128 o = shfl_up_u128(x, off);
-            if (lane - off >= segstart) x = u128_add(x, o);
-        }
-        const bool last = tail || lane == 31;
-        if (key != NONE && last) {
-            const bool whole = tail && ((real_heads >> segstart) & 1u);
-            u128* dst = rowacc + (uint64_t)key * K + warp;
-            if (whole) *dst = x;                               // every vector of key is in this tile
-            else if (x.lo | x.hi) u128_atomic_add(dst, x);     // cut by the tile edge
+        for (int h = 0; h < GSTEPS; h += GCHUNK) {
+            u128 val[GCHUNK];
+#pragma unroll
+            for (int j = 0; j < GCHUNK; ++j) {
+                const uint64_t v = v0 + (uint64_t)(h + j) * 4 + q;
+                val[j] = u128_zero();
+                if (v < nvec) {
+                    const uint4 sv = __ldg(nbr + v);
+                    const uint32_t ids[4] = { sv.x, sv.y, sv.z, sv.w };
+#pragma unroll
+                    for (int l = 0; l < 4; ++l)
+                        if (ids[l] < V) val[j] = u128_add(val[j], ldg_u128(prop + (uint64_t)ids[l] * K + inst));
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < GCHUNK; ++j) {
+                const int pos = (h + j) * 4 + q;  // vector of this lane within the tile
+                u128 x = val[j];
+                const uint32_t k = __shfl_sync(0xffffffffu, kall, pos);
+#pragma unroll
+                for (int off = 1; off < 4; off <<= 1) {
+                    const u128 o = shfl_up_u128(x, off * K);
+                    const uint32_t ko = __shfl_sync(0xffffffffu, kall, pos >= off ? pos - off : 0);
+                    if (q >= off && ko == k) x = u128_add(x, o);
+                }
+                if (k == ckey) x = u128_add(x, carry);
+                const uint32_t kn_in = __shfl_sync(0xffffffffu, kall, (pos + 1) & (TV - 1));  // every lane shuffles
+                const uint32_t kn = pos + 1 < TV ? kn_in : kafter;
+                const bool tail = kn != k;
+                if (k != NONE && (tail || pos == TV - 1)) {
+                    u128* dst = rowacc + (uint64_t)k * K + inst;
+                    if (tail && k != kbefore) *dst = x;                // every vector of k is in this tile
+                    else if (x.lo | x.hi) u128_atomic_add(dst, x);     // cut by the tile edge
+                }
+                carry = shfl_u128(x, 3 * K + inst);
+                ckey = __shfl_sync(0xffffffffu, k, 3 * K + inst);
+            }
         }
     }
 }
@@ -558,7 +575,14 @@ static int build_ppr_graph(grz_batch* b, uint32_t iterations, double damping)
     BCK(b, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     cudaGraph_t graph = nullptr;
     int rc = bck(b, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "begin capture");
-    const unsigned ggrid = persistent_grid(b, (u->pull.nvec + TV - 1) / TV, b->ppr_blocks);
+    // the gather's unit is a warp tile of TV vectors; blocks beyond residency would only queue
+    int gres = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gres, k_ppr_gather, GT, 0) != cudaSuccess || gres < 1) {
+        cudaGetLastError();
+        gres = 1;
+    }
+    const uint64_t gtiles = (u->pull.nvec + TV - 1) / TV;
+    const unsigned ggrid = persistent_grid(b, (gtiles + GT / 32 - 1) / (GT / 32), std::min(b->ppr_blocks, gres));
     // 3 blocks per SM fit the apply's registers (8 tiles of accumulators per thread in flight)
     const unsigned agrid = persistent_grid(b, (V + TV - 1) / TV, std::min(b->ppr_blocks, 3));
     int cur = 0;

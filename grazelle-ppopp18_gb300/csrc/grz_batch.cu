@@ -106,7 +106,10 @@ __device__ __forceinline__ u128 ldg_u128(const u128* p)
 // tile is stored once by the lane of its last vector; one cut by the tile edge is added with
 // exact u128 atomics.  Block 0 first clears S_next for the apply that follows.
 constexpr int GSTEPS = TV / 4;  // steps of 4 vectors per tile
-constexpr int GCHUNK = 4;       // steps whose loads are issued together
+constexpr int GCHUNK = 2;       // steps whose loads are issued together
+// 6 blocks per SM: occupancy beats deeper per-warp load batches (GB300 sweep over steps per
+// chunk 1-8 and 4-8 blocks per SM: 99.8 ms per 256-instance run here, 102-163 ms elsewhere)
+constexpr int GATHER_RESIDENT = 6;
 
 __device__ __forceinline__ u128 shfl_u128(u128 v, int src)
 {
@@ -116,7 +119,7 @@ __device__ __forceinline__ u128 shfl_u128(u128 v, int src)
     return r;
 }
 
-__global__ void __launch_bounds__(GT) k_ppr_gather(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv,
+__global__ void __launch_bounds__(GT, GATHER_RESIDENT) k_ppr_gather(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv,
                                                    uint64_t nvec, uint32_t V, const u128* __restrict__ prop,
                                                    u128* __restrict__ rowacc, u128* __restrict__ S_next, uint32_t nS)
 {

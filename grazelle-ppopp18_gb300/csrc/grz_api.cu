@@ -350,9 +350,19 @@ static int load_pairs(grz_graph* g, uint64_t V, uint64_t E, const uint64_t* pull
             cudaError_t e = cudaStreamWaitEvent(st, g->copy_ev[1], 0);
             if (e != cudaSuccess) { rc = grz_cuda_check(g, e, "wait for push pairs"); break; }
         }
-        rc = grz_build_list(g, which == 0 ? &g->pull : &g->push, dsrc[which], E, which == 0 ? 1 : 0);
-        if (rc == GRZ_OK && which == 0) rc = grz_build_outdegrees(g, dsrc[0], E);
-        if (rc == GRZ_OK && which == 0) rc = grz_build_hubs(g, &g->pull, g->tune.hub_max);
+        // Outdegrees credit the sources of the -pull pairs (graphdata.c:792-821).  A -push list
+        // derived from those pairs holds the same edges, so its run lengths are the outdegrees
+        // and no counting pass is needed.
+        uint32_t* run_len = nullptr;
+        if (which == 1 && derive) {
+            rc = grz_alloc_outdegrees(g);
+            if (rc != GRZ_OK) break;
+            run_len = g->degree;
+        }
+        rc = grz_build_list(g, which == 0 ? &g->pull : &g->push, dsrc[which], E, which == 0 ? 1 : 0, run_len);
+        const bool degrees_now = (which == 0 && !derive) || (which == 1 && derive);
+        if (rc == GRZ_OK && degrees_now) rc = grz_build_outdegrees(g, which == 0 ? dsrc[0] : nullptr, E);
+        if (rc == GRZ_OK && degrees_now) rc = grz_build_hubs(g, &g->pull, g->tune.hub_max);
         if (rc == GRZ_OK) rc = grz_cuda_check(g, cudaStreamSynchronize(st), "layout build");
     }
     if (push_on_copy_stream && rc != GRZ_OK) cudaStreamSynchronize(g->copy_stream);
@@ -410,10 +420,19 @@ extern "C" int grz_graph_load_files(grz_graph* g, const char* base)
     return rc;
 }
 
-extern "C" int grz_graph_get_info(const grz_graph* g, grz_graph_info_t* out)
+extern "C" int grz_graph_get_info(const grz_graph* gc, grz_graph_info_t* out)
 {
-    if (!g || !out) return GRZ_ERR_ARG;
+    if (!gc || !out) return GRZ_ERR_ARG;
     memset(out, 0, sizeof(*out));
+    // the reference-format lists whose device pointers the info hands out are a cache built on
+    // first request; the graph is otherwise unchanged
+    grz_graph* g = const_cast<grz_graph*>(gc);
+    if (g->V || g->E) {
+        GRZ_CK(g, cudaSetDevice(g->device));
+        int rc = grz_list_reference(g, &g->pull);
+        if (rc == GRZ_OK) rc = grz_list_reference(g, &g->push);
+        if (rc != GRZ_OK) return rc;
+    }
     out->num_vertices = g->V;
     out->num_edges = g->E;
     out->pull_vectors = g->pull.nvec;
@@ -427,7 +446,7 @@ extern "C" int grz_graph_get_info(const grz_graph* g, grz_graph_info_t* out)
     uint64_t b = 0;
     const grz_list* Ls[2] = { &g->pull, &g->push };
     for (const grz_list* L : Ls)
-        if (L->vs) b += L->nvec * (32 + 16 + 4) + (g->V + 64) * 8 + (g->V + 1) * 4;
+        if (L->nbr) b += L->nvec * ((L->vs ? 32 : 0) + 16 + 4) + (g->V + 64) * 8 + (g->V + 1) * 4;
     b += (g->V + 8) * 8 * 3 + g->V * 12;
     if (g->pr_fx[0]) b += g->V * (16 * 3 + 4);
     out->device_bytes = b;
@@ -439,8 +458,11 @@ static const grz_list* list_of(const grz_graph* g, int list) { return list == GR
 extern "C" int grz_graph_copy_list(grz_graph* g, int list, uint64_t* host, uint64_t cap)
 {
     if (!g || !host) return GRZ_ERR_ARG;
-    const grz_list* L = list_of(g, list);
-    if (!L->vs) return grz_set_error(g, GRZ_ERR_STATE, "list not built");
+    grz_list* L = list == GRZ_LIST_PUSH ? &g->push : &g->pull;
+    if (!L->nbr) return grz_set_error(g, GRZ_ERR_STATE, "list not built");
+    GRZ_CK(g, cudaSetDevice(g->device));
+    int rc = grz_list_reference(g, L);
+    if (rc) return rc;
     if (cap < L->nvec) return grz_set_error(g, GRZ_ERR_ARG, "capacity %llu < %llu vectors", (unsigned long long)cap, (unsigned long long)L->nvec);
     GRZ_CK(g, cudaMemcpyAsync(host, L->vs, sizeof(uint64_t) * 4 * L->nvec, cudaMemcpyDeviceToHost, g->stream));
     GRZ_CK(g, cudaStreamSynchronize(g->stream));

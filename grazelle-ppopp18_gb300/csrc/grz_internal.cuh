@@ -2,7 +2,8 @@
 //
 // Data layout in HBM for one graph (V vertices, E edges, N vector-sparse vectors per list):
 //
-//   Reference layout (bit-identical to Grazelle's host packer, source/graphdata.c:143-173):
+//   Reference layout (bit-identical to Grazelle's host packer, source/graphdata.c:143-173; the
+//   vectors are derived from the execution layout when first asked for):
 //     list[l].vs        uint64[4N]   4-lane 256-bit vectors: valid bit 63, spread shared ID in
 //                                    bits 62:48, 48-bit neighbour ID in bits 47:0
 //     list[l].vindex    uint64[V+64] first vector of each shared vertex (graphdata.c:219-267)
@@ -174,7 +175,7 @@ __device__ __forceinline__ u128 u128_shfl_down(u128 v, int off)
 
 struct grz_list {
     uint64_t nvec;          // number of 4-lane vectors
-    uint64_t* vs;           // reference-format vectors, 4 words each
+    uint64_t* vs;           // reference-format vectors, 4 words each (built on first request)
     uint64_t* vindex;       // uint64[V+64]
     uint64_t vindex_start;  // first shared vertex with vectors
     uint64_t vindex_end;    // last shared vertex with vectors
@@ -436,10 +437,14 @@ int grz_switch_decide(grz_graph* g, const unsigned long long* frontier, uint64_t
 void grz_frontier_free(grz_graph* g);
 
 // layout (grz_layout.cu)
-int grz_build_list(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t E, int shared_is_dst);
+// run_len (optional, uint32[V]): edges of each shared vertex
+int grz_build_list(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t E, int shared_is_dst,
+                   uint32_t* run_len = nullptr);
+int grz_list_reference(grz_graph* g, grz_list* L);  // reference-format vectors, built on first request
 int grz_build_hubs(grz_graph* g, grz_list* L, uint32_t max_hubs);
 int grz_derive_push_pairs(grz_graph* g, const uint64_t* pull_pairs, uint64_t E, uint64_t* push_out);
 #define GRZ_LOAD_DERIVE_PUSH 1
+int grz_alloc_outdegrees(grz_graph* g);
 int grz_build_outdegrees(grz_graph* g, const uint64_t* d_pull_pairs, uint64_t E);
 
 // scans (grz_scan.cu): exclusive sum of uint32 into uint32 (n < 2^32), inclusive max of uint32

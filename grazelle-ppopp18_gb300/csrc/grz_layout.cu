@@ -9,9 +9,12 @@
 //   * the execution layout: uint4 neighbour IDs, per-vector shared vertex, CSR row pointers.
 // Outdegrees follow graphdata.c:792-821 (credit per source of the -pull list).
 //
-// Edge e starts a new vector when it starts a run of its shared vertex or when its position in
-// the run is a multiple of 4 (the stash flushes on a change of shared vertex or when full), so
-// vector numbers come from a scan over those flags, and a lane is (position in run) mod 4.
+// The execution form is built in three passes: the edge range [start, end) of each shared
+// vertex (one pass over the pairs: run heads and tails), the vector offsets (ceil(run / 4) per
+// vertex, one scan over V), and the vectors themselves (the edge whose position in its run is a
+// multiple of 4 writes one vector, since the reference's stash flushes on a change of shared
+// vertex or when full).  The reference-format vectors, whose invalid lanes inherit the stale
+// stash values, are derived from the execution form on first request (grz_list_reference).
 #include <algorithm>
 #include <vector>
 
@@ -34,65 +37,113 @@ __device__ __forceinline__ uint64_t piece_of(uint64_t s, int lane)
     }
 }
 
-// flags[0]: unsorted, flags[1]: id out of range
-__global__ void k_edge_heads(const uint64_t* __restrict__ pairs, uint64_t E, uint64_t V, int shared_is_dst,
-                             uint32_t* __restrict__ head_pos, unsigned* __restrict__ flags)
+// edge range of each shared vertex: start[s] = its first edge, end[s] = one past its last (both
+// 0 without edges).  flags[0]: not grouped in ascending order, flags[1]: an ID >= V.
+__global__ void k_group_bounds(const uint64_t* __restrict__ pairs, uint64_t E, uint64_t V, int shared_is_dst,
+                               uint32_t* __restrict__ start, uint32_t* __restrict__ end, unsigned* __restrict__ flags)
 {
     const uint64_t e = (uint64_t)blockIdx.x * BT + threadIdx.x;
     if (e >= E) return;
-    const uint64_t s = pairs[2 * e + (shared_is_dst ? 1 : 0)];
-    const uint64_t nb = pairs[2 * e + (shared_is_dst ? 0 : 1)];
-    bool head = (e == 0);
+    const int sh = shared_is_dst ? 1 : 0;
+    const uint64_t s = pairs[2 * e + sh];
+    const uint64_t nb = pairs[2 * e + (1 - sh)];
+    if (s >= V || nb >= V) atomicOr(&flags[1], 1u);
+    bool head = true, tail = true;
     if (e > 0) {
-        const uint64_t sp = pairs[2 * (e - 1) + (shared_is_dst ? 1 : 0)];
-        head = (sp != s);
+        const uint64_t sp = pairs[2 * (e - 1) + sh];
+        head = sp != s;
         if (sp > s) atomicOr(&flags[0], 1u);
     }
-    if (s >= V || nb >= V) atomicOr(&flags[1], 1u);
-    head_pos[e] = head ? (uint32_t)e : 0u;
+    if (e + 1 < E) tail = pairs[2 * (e + 1) + sh] != s;
+    if (s < V) {
+        if (head) start[s] = (uint32_t)e;
+        if (tail) end[s] = (uint32_t)(e + 1);
+    }
 }
 
-__global__ void k_vector_starts(const uint32_t* __restrict__ run_start, uint64_t E, uint32_t* __restrict__ vstart)
+// vectors of each shared vertex (entry V is 0 for the exclusive scan's total); edges of each
+// shared vertex into `edges` when asked
+__global__ void k_group_vectors(const uint32_t* __restrict__ start, const uint32_t* __restrict__ end, uint64_t V,
+                                uint32_t* __restrict__ cnt, uint32_t* __restrict__ edges)
+{
+    const uint64_t v = (uint64_t)blockIdx.x * BT + threadIdx.x;
+    if (v < V) {
+        const uint32_t d = end[v] - start[v];
+        cnt[v] = (d + 3u) / 4u;
+        if (edges) edges[v] = d;
+    } else if (v == V) {
+        cnt[v] = 0;
+    }
+}
+
+// the edge at a multiple-of-4 position of its run writes that vector: up to four neighbours,
+// the rest of the lanes invalid, and the shared vertex
+__global__ void k_vector_write(const uint64_t* __restrict__ pairs, uint64_t E, int shared_is_dst,
+                               const uint32_t* __restrict__ start, const uint32_t* __restrict__ end,
+                               const uint32_t* __restrict__ rowptr, uint4* __restrict__ nbr, uint32_t* __restrict__ shared)
 {
     const uint64_t e = (uint64_t)blockIdx.x * BT + threadIdx.x;
     if (e >= E) return;
-    const uint32_t pos = (uint32_t)e - run_start[e];
-    vstart[e] = (pos & 3u) == 0 ? 1u : 0u;  // a run start has pos 0
+    const int sh = shared_is_dst ? 1 : 0;
+    const uint32_t s = (uint32_t)pairs[2 * e + sh];
+    const uint32_t pos = (uint32_t)e - __ldg(start + s);
+    if (pos & 3u) return;
+    const uint32_t n = min(4u, __ldg(end + s) - (uint32_t)e);
+    uint32_t ids[4] = { GRZ_INVALID_ID, GRZ_INVALID_ID, GRZ_INVALID_ID, GRZ_INVALID_ID };
+#pragma unroll
+    for (uint32_t k = 0; k < 4; ++k)
+        if (k < n) ids[k] = (uint32_t)pairs[2 * (e + k) + (1 - sh)];
+    const uint32_t vec = __ldg(rowptr + s) + pos / 4u;
+    nbr[vec] = make_uint4(ids[0], ids[1], ids[2], ids[3]);
+    shared[vec] = s;
 }
 
-// vfirst[v] = first edge of vector v; written by the edge that starts it
-__global__ void k_vector_first(const uint32_t* __restrict__ vstart, const uint32_t* __restrict__ vnum_excl, uint64_t E,
-                               uint32_t* __restrict__ vfirst)
+// the reference vertex index (graphdata.c:219-267): first vector of each vertex with edges,
+// 0x7fff... for one without edges up to the last shared vertex, 0xffff... beyond it
+__global__ void k_vindex(const uint32_t* __restrict__ start, const uint32_t* __restrict__ end,
+                         const uint32_t* __restrict__ rowptr, uint64_t V, uint64_t count, uint64_t last_shared,
+                         uint64_t* __restrict__ vindex)
 {
-    const uint64_t e = (uint64_t)blockIdx.x * BT + threadIdx.x;
-    if (e >= E) return;
-    if (vstart[e]) vfirst[vnum_excl[e]] = (uint32_t)e;
+    const uint64_t i = (uint64_t)blockIdx.x * BT + threadIdx.x;
+    if (i >= count) return;
+    if (i < V && end[i] > start[i]) vindex[i] = rowptr[i];
+    else vindex[i] = (i > last_shared) ? 0xffffffffffffffffull : 0x7fffffffffffffffull;
 }
 
-// per vector: lane count, shared vertex, valid neighbours; keys for the stale-lane scans
-__global__ void k_vector_fill(const uint64_t* __restrict__ pairs, int shared_is_dst, const uint32_t* __restrict__ vfirst,
-                              uint64_t nvec, uint64_t E, uint32_t* __restrict__ shared_out, uint4* __restrict__ nbr_out,
-                              uint32_t* __restrict__ last1, uint32_t* __restrict__ last2, uint32_t* __restrict__ last3)
+// the empty list: one vector with no valid lane and shared vertex 0 (graphdata.c:700), which the
+// index and row pointers attribute to vertex 0
+__global__ void k_empty_list(uint64_t* vs, uint4* nbr, uint32_t* shared)
+{
+    for (int l = 0; l < 4; ++l) vs[l] = 0;
+    nbr[0] = make_uint4(GRZ_INVALID_ID, GRZ_INVALID_ID, GRZ_INVALID_ID, GRZ_INVALID_ID);
+    shared[0] = 0;
+}
+
+__global__ void k_empty_index(uint64_t* __restrict__ vindex, uint64_t count, uint32_t* __restrict__ rowptr, uint64_t V)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * BT + threadIdx.x;
+    if (i < count) vindex[i] = i == 0 ? 0ull : 0xffffffffffffffffull;
+    if (i <= V) rowptr[i] = i == 0 ? 0u : 1u;
+}
+
+// key = v+1 when lane l of vector v holds a neighbour, else 0 (inclusive max scan -> last filler)
+__global__ void k_lane_keys(const uint4* __restrict__ nbr, uint64_t nvec, uint32_t* __restrict__ last1,
+                            uint32_t* __restrict__ last2, uint32_t* __restrict__ last3)
 {
     const uint64_t v = (uint64_t)blockIdx.x * BT + threadIdx.x;
     if (v >= nvec) return;
-    const uint64_t f = vfirst[v];
-    const uint64_t nx = (v + 1 < nvec) ? vfirst[v + 1] : E;
-    const uint32_t cnt = (uint32_t)(nx - f);
-    uint32_t ids[4] = { GRZ_INVALID_ID, GRZ_INVALID_ID, GRZ_INVALID_ID, GRZ_INVALID_ID };
-    for (uint32_t k = 0; k < cnt && k < 4; ++k) ids[k] = (uint32_t)pairs[2 * (f + k) + (shared_is_dst ? 0 : 1)];
-    shared_out[v] = (uint32_t)pairs[2 * f + (shared_is_dst ? 1 : 0)];
-    nbr_out[v] = make_uint4(ids[0], ids[1], ids[2], ids[3]);
-    // key = v+1 when lane l is filled by this vector, else 0 (inclusive max scan -> last filler)
-    last1[v] = cnt > 1 ? (uint32_t)(v + 1) : 0u;
-    last2[v] = cnt > 2 ? (uint32_t)(v + 1) : 0u;
-    last3[v] = cnt > 3 ? (uint32_t)(v + 1) : 0u;
+    const uint4 n = nbr[v];
+    last1[v] = n.y != GRZ_INVALID_ID ? (uint32_t)(v + 1) : 0u;
+    last2[v] = n.z != GRZ_INVALID_ID ? (uint32_t)(v + 1) : 0u;
+    last3[v] = n.w != GRZ_INVALID_ID ? (uint32_t)(v + 1) : 0u;
 }
 
-// reference 256-bit vectors; invalid lanes take the stale stash value (0 before any fill)
+// reference 256-bit vectors; invalid lanes take the stale stash value (0 before any fill).
+// Hub-encoded neighbours are decoded back to their vertex IDs.
 __global__ void k_vector_encode(const uint32_t* __restrict__ shared, const uint4* __restrict__ nbr,
                                 const uint32_t* __restrict__ last1, const uint32_t* __restrict__ last2,
-                                const uint32_t* __restrict__ last3, uint64_t nvec, uint64_t* __restrict__ vs)
+                                const uint32_t* __restrict__ last3, uint64_t nvec, const uint32_t* __restrict__ hub_vid,
+                                uint32_t nhub, uint64_t* __restrict__ vs)
 {
     const uint64_t v = (uint64_t)blockIdx.x * BT + threadIdx.x;
     if (v >= nvec) return;
@@ -103,56 +154,28 @@ __global__ void k_vector_encode(const uint32_t* __restrict__ shared, const uint4
     for (int l = 0; l < 4; ++l) {
         uint64_t word = piece_of(s, l) << 48;
         if (own[l] != GRZ_INVALID_ID) {
-            word |= (1ull << 63) | (uint64_t)own[l];
+            word |= (1ull << 63) | (uint64_t)grz_hub_decode(own[l], hub_vid, nhub);
         } else if (l > 0) {
-            const uint32_t src = last[l][v];  // 1 + vector that last filled lane l (<= v, not v itself)
+            const uint32_t src = last[l][v];  // 1 + vector that last filled lane l (< v)
             if (src) {
                 const uint4 m = nbr[src - 1];
                 const uint32_t mm[4] = { m.x, m.y, m.z, m.w };
-                word |= (uint64_t)mm[l];
+                word |= (uint64_t)grz_hub_decode(mm[l], hub_vid, nhub);
             }
         }
         vs[4 * v + l] = word;
     }
 }
 
-// the empty list: one vector with no valid lane and shared vertex 0 (graphdata.c:700)
-__global__ void k_empty_list(uint64_t* vs, uint4* nbr, uint32_t* shared)
-{
-    for (int l = 0; l < 4; ++l) vs[l] = 0;
-    nbr[0] = make_uint4(GRZ_INVALID_ID, GRZ_INVALID_ID, GRZ_INVALID_ID, GRZ_INVALID_ID);
-    shared[0] = 0;
-}
-
-__global__ void k_vindex_fill(uint64_t* __restrict__ vindex, uint64_t count, uint64_t first_shared, uint64_t last_shared)
-{
-    const uint64_t i = (uint64_t)blockIdx.x * BT + threadIdx.x;
-    if (i >= count) return;
-    vindex[i] = (i > last_shared) ? 0xffffffffffffffffull : 0x7fffffffffffffffull;
-}
-
-__global__ void k_vindex_heads(const uint32_t* __restrict__ shared, uint64_t nvec, uint64_t* __restrict__ vindex)
-{
-    const uint64_t v = (uint64_t)blockIdx.x * BT + threadIdx.x;
-    if (v >= nvec) return;
-    if (v == 0 || shared[v - 1] != shared[v]) vindex[shared[v]] = v;
-}
-
-// vectors per vertex, written at the last vector of each run
-__global__ void k_row_counts(const uint32_t* __restrict__ shared, uint64_t nvec, const uint64_t* __restrict__ vindex,
-                             uint32_t* __restrict__ cnt)
-{
-    const uint64_t v = (uint64_t)blockIdx.x * BT + threadIdx.x;
-    if (v >= nvec) return;
-    const uint32_t s = shared[v];
-    if (v + 1 == nvec || shared[v + 1] != s) cnt[s] = (uint32_t)(v + 1 - vindex[s]);
-}
-
+// outdegree credit per source of the -pull list (graphdata.c:792-821); lanes of a warp that
+// name the same source add once
 __global__ void k_degree(const uint64_t* __restrict__ pairs, uint64_t E, uint32_t* __restrict__ degree)
 {
     const uint64_t e = (uint64_t)blockIdx.x * BT + threadIdx.x;
-    if (e >= E) return;
-    atomicAdd(&degree[pairs[2 * e]], 1u);
+    const bool live = e < E;
+    const uint32_t s = live ? (uint32_t)pairs[2 * e] : GRZ_INVALID_ID;
+    const unsigned peers = __match_any_sync(0xffffffffu, s);
+    if (live && (int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&degree[s], (uint32_t)__popc(peers));
 }
 
 __global__ void k_degree_to_double(const uint32_t* __restrict__ degree, uint64_t V, double* __restrict__ outdeg,
@@ -167,109 +190,127 @@ __global__ void k_degree_to_double(const uint32_t* __restrict__ degree, uint64_t
 
 }  // namespace
 
-int grz_build_list(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t E, int shared_is_dst)
+int grz_build_list(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t E, int shared_is_dst, uint32_t* run_len)
 {
     const uint64_t V = g->V;
     cudaStream_t st = g->stream;
     if (E >= 0xffffffffull) return grz_set_error(g, GRZ_ERR_RANGE, "edge count %llu too large (limit 2^32-2)", (unsigned long long)E);
-    uint64_t nvec = 1;
-    unsigned flags_h[2] = { 0, 0 };
-    uint32_t *head = nullptr, *vstart = nullptr, *vexcl = nullptr, *vfirst = nullptr, *l1 = nullptr, *l2 = nullptr, *l3 = nullptr;
+    const uint64_t vi_count = V + 64;
+    uint32_t *start = nullptr, *end = nullptr, *cnt = nullptr, *tot = nullptr;
     unsigned* flags = nullptr;
     int rc = GRZ_OK;
-    const uint64_t vi_count = V + 64;
-
 #define LCK(call) do { cudaError_t e__ = (call); if (e__ != cudaSuccess) { rc = grz_cuda_check(g, e__, #call); goto done; } } while (0)
-    if (E > 0) {
+    LCK(cudaMallocAsync((void**)&L->vindex, sizeof(uint64_t) * vi_count, st));
+    LCK(cudaMallocAsync((void**)&L->rowptr, sizeof(uint32_t) * (V + 1), st));
+    if (E == 0) {
+        L->nvec = 1;
+        LCK(cudaMallocAsync((void**)&L->vs, sizeof(uint64_t) * 4, st));
+        LCK(cudaMallocAsync((void**)&L->nbr, sizeof(uint4), st));
+        LCK(cudaMallocAsync((void**)&L->shared, sizeof(uint32_t), st));
+        k_empty_list<<<1, 1, 0, st>>>(L->vs, L->nbr, L->shared); GRZ_COUNT_LAUNCH(g);
+        k_empty_index<<<grid_blocks_for(std::max<uint64_t>(vi_count, V + 1)), BT, 0, st>>>(L->vindex, vi_count, L->rowptr, V); GRZ_COUNT_LAUNCH(g);
+        LCK(cudaGetLastError());
+        L->vindex_start = L->vindex_end = 0;
+    } else {
+        unsigned flags_h[2] = { 0, 0 };
+        uint64_t ends_h[2] = { 0, 0 };
+        uint32_t nv32 = 0;
+        const int sh = shared_is_dst ? 1 : 0;
         LCK(cudaMallocAsync((void**)&flags, 2 * sizeof(unsigned), st));
+        LCK(cudaMallocAsync((void**)&start, sizeof(uint32_t) * (V + 1), st));
+        LCK(cudaMallocAsync((void**)&end, sizeof(uint32_t) * (V + 1), st));
+        LCK(cudaMallocAsync((void**)&cnt, sizeof(uint32_t) * (V + 1), st));
+        LCK(cudaMallocAsync((void**)&tot, sizeof(uint32_t), st));
         LCK(cudaMemsetAsync(flags, 0, 2 * sizeof(unsigned), st));
-        LCK(cudaMallocAsync((void**)&head, sizeof(uint32_t) * E, st));
-        LCK(cudaMallocAsync((void**)&vstart, sizeof(uint32_t) * E, st));
-        LCK(cudaMallocAsync((void**)&vexcl, sizeof(uint32_t) * (E + 1), st));
-        k_edge_heads<<<grid_blocks_for(E), BT, 0, st>>>(d_pairs, E, V, shared_is_dst, head, flags); GRZ_COUNT_LAUNCH(g);
+        LCK(cudaMemsetAsync(start, 0, sizeof(uint32_t) * (V + 1), st));
+        LCK(cudaMemsetAsync(end, 0, sizeof(uint32_t) * (V + 1), st));
+        k_group_bounds<<<grid_blocks_for(E), BT, 0, st>>>(d_pairs, E, V, shared_is_dst, start, end, flags); GRZ_COUNT_LAUNCH(g);
         LCK(cudaGetLastError());
         LCK(cudaMemcpyAsync(flags_h, flags, sizeof(flags_h), cudaMemcpyDeviceToHost, st));
+        LCK(cudaMemcpyAsync(&ends_h[0], d_pairs + sh, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+        LCK(cudaMemcpyAsync(&ends_h[1], d_pairs + 2 * (E - 1) + sh, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
         LCK(cudaStreamSynchronize(st));
         if (flags_h[0]) { rc = grz_set_error(g, GRZ_ERR_UNSORTED, "%s list is not grouped by %s in ascending order", shared_is_dst ? "pull" : "push", shared_is_dst ? "destination" : "source"); goto done; }
         if (flags_h[1]) { rc = grz_set_error(g, GRZ_ERR_RANGE, "%s list holds a vertex ID >= V (%llu)", shared_is_dst ? "pull" : "push", (unsigned long long)V); goto done; }
-        rc = grz_inclusive_max_u32(g, head, head, E);  // head[] now holds each edge's run start
-        if (rc) goto done;
-        k_vector_starts<<<grid_blocks_for(E), BT, 0, st>>>(head, E, vstart); GRZ_COUNT_LAUNCH(g);
+        k_group_vectors<<<grid_blocks_for(V + 1), BT, 0, st>>>(start, end, V, cnt, run_len); GRZ_COUNT_LAUNCH(g);
         LCK(cudaGetLastError());
-        rc = grz_exclusive_sum_u32(g, vstart, vexcl, E, vexcl + E);
+        rc = grz_exclusive_sum_u32(g, cnt, L->rowptr, V + 1, tot);
         if (rc) goto done;
-        uint32_t nv32 = 0;
-        LCK(cudaMemcpyAsync(&nv32, vexcl + E, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        LCK(cudaMemcpyAsync(&nv32, tot, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         LCK(cudaStreamSynchronize(st));
-        nvec = nv32;
-    }
-    L->nvec = nvec;
-    LCK(cudaMallocAsync((void**)&L->vs, sizeof(uint64_t) * 4 * nvec, st));
-    LCK(cudaMallocAsync((void**)&L->nbr, sizeof(uint4) * nvec, st));
-    LCK(cudaMallocAsync((void**)&L->shared, sizeof(uint32_t) * nvec, st));
-    LCK(cudaMallocAsync((void**)&L->vindex, sizeof(uint64_t) * vi_count, st));
-    LCK(cudaMallocAsync((void**)&L->rowptr, sizeof(uint32_t) * (V + 1), st));
-    if (E > 0) {
-        LCK(cudaMallocAsync((void**)&vfirst, sizeof(uint32_t) * nvec, st));
-        LCK(cudaMallocAsync((void**)&l1, sizeof(uint32_t) * nvec * 3, st));
-        l2 = l1 + nvec;
-        l3 = l2 + nvec;
-        k_vector_first<<<grid_blocks_for(E), BT, 0, st>>>(vstart, vexcl, E, vfirst); GRZ_COUNT_LAUNCH(g);
+        L->nvec = nv32;
+        LCK(cudaMallocAsync((void**)&L->nbr, sizeof(uint4) * L->nvec, st));
+        LCK(cudaMallocAsync((void**)&L->shared, sizeof(uint32_t) * L->nvec, st));
+        k_vector_write<<<grid_blocks_for(E), BT, 0, st>>>(d_pairs, E, shared_is_dst, start, end, L->rowptr, L->nbr, L->shared); GRZ_COUNT_LAUNCH(g);
         LCK(cudaGetLastError());
-        k_vector_fill<<<grid_blocks_for(nvec), BT, 0, st>>>(d_pairs, shared_is_dst, vfirst, nvec, E, L->shared, L->nbr, l1, l2, l3); GRZ_COUNT_LAUNCH(g);
+        k_vindex<<<grid_blocks_for(vi_count), BT, 0, st>>>(start, end, L->rowptr, V, vi_count, ends_h[1], L->vindex); GRZ_COUNT_LAUNCH(g);
         LCK(cudaGetLastError());
-        if ((rc = grz_inclusive_max_u32(g, l1, l1, nvec))) goto done;
-        if ((rc = grz_inclusive_max_u32(g, l2, l2, nvec))) goto done;
-        if ((rc = grz_inclusive_max_u32(g, l3, l3, nvec))) goto done;
-        k_vector_encode<<<grid_blocks_for(nvec), BT, 0, st>>>(L->shared, L->nbr, l1, l2, l3, nvec, L->vs); GRZ_COUNT_LAUNCH(g);
-        LCK(cudaGetLastError());
-    } else {
-        k_empty_list<<<1, 1, 0, st>>>(L->vs, L->nbr, L->shared); GRZ_COUNT_LAUNCH(g);
-        LCK(cudaGetLastError());
-    }
-    {
-        uint32_t fs = 0, ls = 0;
-        LCK(cudaMemcpyAsync(&fs, L->shared, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-        LCK(cudaMemcpyAsync(&ls, L->shared + (nvec - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-        LCK(cudaStreamSynchronize(st));
-        L->vindex_start = fs;
-        L->vindex_end = ls;
-        k_vindex_fill<<<grid_blocks_for(vi_count), BT, 0, st>>>(L->vindex, vi_count, fs, ls); GRZ_COUNT_LAUNCH(g);
-        LCK(cudaGetLastError());
-        k_vindex_heads<<<grid_blocks_for(nvec), BT, 0, st>>>(L->shared, nvec, L->vindex); GRZ_COUNT_LAUNCH(g);
-        LCK(cudaGetLastError());
-        uint32_t* cnt = nullptr;
-        LCK(cudaMallocAsync((void**)&cnt, sizeof(uint32_t) * (V + 1), st));
-        LCK(cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * (V + 1), st));
-        k_row_counts<<<grid_blocks_for(nvec), BT, 0, st>>>(L->shared, nvec, L->vindex, cnt); GRZ_COUNT_LAUNCH(g);
-        LCK(cudaGetLastError());
-        rc = grz_exclusive_sum_u32(g, cnt, L->rowptr, V + 1, nullptr);
-        cudaFreeAsync(cnt, st);
-        if (rc) goto done;
+        L->vindex_start = ends_h[0];
+        L->vindex_end = ends_h[1];
+        L->vs = nullptr;  // reference-format vectors: on first request
     }
 done:
-    if (flags) cudaFreeAsync(flags, st);
-    if (head) cudaFreeAsync(head, st);
-    if (vstart) cudaFreeAsync(vstart, st);
-    if (vexcl) cudaFreeAsync(vexcl, st);
-    if (vfirst) cudaFreeAsync(vfirst, st);
-    if (l1) cudaFreeAsync(l1, st);
+    for (void* p : { (void*)flags, (void*)start, (void*)end, (void*)cnt, (void*)tot })
+        if (p) cudaFreeAsync(p, st);
 #undef LCK
     if (rc == GRZ_OK) rc = grz_cuda_check(g, cudaStreamSynchronize(st), "build list");
     return rc;
 }
 
-int grz_build_outdegrees(grz_graph* g, const uint64_t* d_pull_pairs, uint64_t E)
+// The reference-format vectors of a built list (graphdata.c:143-173 with the stash of
+// graphdata.c:618-788), derived from the execution form: a lane the vector leaves empty holds
+// the neighbour of the last earlier vector that filled that lane (the never-cleared stash).
+int grz_list_reference(grz_graph* g, grz_list* L)
+{
+    if (L->vs || !L->nbr) return GRZ_OK;
+    cudaStream_t st = g->stream;
+    const uint64_t nvec = L->nvec;
+    uint32_t* l1 = nullptr;
+    int rc = GRZ_OK;
+#define LCK(call) do { cudaError_t e__ = (call); if (e__ != cudaSuccess) { rc = grz_cuda_check(g, e__, #call); goto done; } } while (0)
+    LCK(cudaMallocAsync((void**)&L->vs, sizeof(uint64_t) * 4 * nvec, st));
+    LCK(cudaMallocAsync((void**)&l1, sizeof(uint32_t) * nvec * 3, st));
+    k_lane_keys<<<grid_blocks_for(nvec), BT, 0, st>>>(L->nbr, nvec, l1, l1 + nvec, l1 + 2 * nvec); GRZ_COUNT_LAUNCH(g);
+    LCK(cudaGetLastError());
+    for (int k = 0; k < 3 && rc == GRZ_OK; ++k) rc = grz_inclusive_max_u32(g, l1 + k * nvec, l1 + k * nvec, nvec);
+    if (rc) goto done;
+    k_vector_encode<<<grid_blocks_for(nvec), BT, 0, st>>>(L->shared, L->nbr, l1, l1 + nvec, l1 + 2 * nvec, nvec, L->hub_vid,
+                                                          L->nhub, L->vs); GRZ_COUNT_LAUNCH(g);
+    LCK(cudaGetLastError());
+done:
+    if (l1) cudaFreeAsync(l1, st);
+#undef LCK
+    if (rc == GRZ_OK) rc = grz_cuda_check(g, cudaStreamSynchronize(st), "reference vectors");
+    if (rc != GRZ_OK && L->vs) {
+        cudaFree(L->vs);
+        L->vs = nullptr;
+    }
+    return rc;
+}
+
+// the outdegree arrays, degree zeroed
+int grz_alloc_outdegrees(grz_graph* g)
 {
     const uint64_t V = g->V;
-    cudaStream_t st = g->stream;
+    if (g->degree) return GRZ_OK;
     int rc = grz_dev_alloc(g, (void**)&g->degree, sizeof(uint32_t) * (V + 1));
     if (!rc) rc = grz_dev_alloc(g, (void**)&g->outdeg, sizeof(double) * (V + 8));
     if (!rc) rc = grz_dev_alloc(g, (void**)&g->inv_deg, sizeof(double) * (V + 1));
     if (rc) return rc;
-    GRZ_CK(g, cudaMemsetAsync(g->degree, 0, sizeof(uint32_t) * (V + 1), st));
+    GRZ_CK(g, cudaMemsetAsync(g->degree, 0, sizeof(uint32_t) * (V + 1), g->stream));
+    return GRZ_OK;
+}
+
+// Outdegrees: counted from the -pull pairs, or (d_pull_pairs null) already in g->degree, where
+// grz_build_list put the run lengths of a -push list derived from those pairs.
+int grz_build_outdegrees(grz_graph* g, const uint64_t* d_pull_pairs, uint64_t E)
+{
+    const uint64_t V = g->V;
+    cudaStream_t st = g->stream;
+    int rc = grz_alloc_outdegrees(g);
+    if (rc) return rc;
     GRZ_CK(g, cudaMemsetAsync(g->outdeg, 0, sizeof(double) * (V + 8), st));
-    if (E > 0) {
+    if (E > 0 && d_pull_pairs) {
         k_degree<<<grid_blocks_for(E), BT, 0, st>>>(d_pull_pairs, E, g->degree); GRZ_COUNT_LAUNCH(g);
         GRZ_CK(g, cudaGetLastError());
     }

@@ -48,8 +48,10 @@ static int resolve(const void* edge_list, uint64_t count, int want_push, uint64_
 {
     grz_graph* g = g_bound;
     if (!g) return GRZ_ERR_STATE;
-    const grz_list* L = want_push ? &g->push : &g->pull;
-    if (!L->vs) return grz_set_error(g, GRZ_ERR_STATE, "%s list not loaded", want_push ? "push" : "pull");
+    grz_list* L = want_push ? &g->push : &g->pull;
+    if (!L->nbr) return grz_set_error(g, GRZ_ERR_STATE, "%s list not loaded", want_push ? "push" : "pull");
+    const int rc = grz_list_reference(g, L);  // the caller's pointer came from these vectors
+    if (rc) return rc;
     const uintptr_t base = (uintptr_t)L->vs, p = (uintptr_t)edge_list;
     if (p < base || ((p - base) & 31) != 0) return grz_set_error(g, GRZ_ERR_ARG, "edge_list is not a vector of the bound graph's list");
     const uint64_t off = (p - base) / 32;

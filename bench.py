@@ -9,8 +9,10 @@ threshold engine switch.  One step is one full CC run.
   value     GTEPS = E x iterations / device time, graph resident in HBM (the reference's
             "Effective Processing Rate", source/main.c:129)
   e2e       the same metric through the C ABI from pinned HOST edge lists.  Each step does
-            the H2D copy of both lists, builds the vector-sparse layout on the device, runs CC
-            and reads the labels back (D2H).
+            the H2D copy of the -pull pairs (grz_graph_load_pairs_ex with
+            GRZ_LOAD_DERIVE_PUSH: the library derives the -push list on the device; --ingest
+            both copies both lists instead), builds the vector-sparse layout on the device,
+            runs CC and reads the labels back (D2H).
   roofline  the dominant kernel's algorithmic bytes per launch over its mean CUDA-event
             duration, against the measured HBM copy peak
   apps      PageRank (R-MAT scale 20, 16 pull iterations) and BFS on the same graph
@@ -230,15 +232,18 @@ def run_native(a):
         V, E = g.num_vertices, g.num_edges
     log("graph: %s scale %d V=%d E=%d (%.1fs)%s" % (wl, scale, V, E, time.time() - t0, " lean" if lean else ""))
     pin_pull = torch.from_numpy(pull.view(np.int64)).pin_memory()
-    pin_push = torch.from_numpy(push.view(np.int64)).pin_memory() if push is not None else None
-    pull_bytes, push_bytes = int(pull.nbytes), int(push.nbytes) if push is not None else 0
+    # the e2e leg hands the library the -pull pairs only (it derives the -push list on the device)
+    # unless --ingest both, which copies both lists as the reference reads both files
+    derive = lean or a.ingest == "pull"
+    pin_push = torch.from_numpy(push.view(np.int64)).pin_memory() if (push is not None and not derive) else None
+    pull_bytes, push_bytes = int(pull.nbytes), (int(push.nbytes) if pin_push is not None else 0)
     if lean:
         deg_lean = np.bincount(pull[0::2].astype(np.int64), minlength=V) if wl == "bfs" else None
         del pull
     G = Graph(local, stream=stream.cuda_stream)
 
     def load():
-        if lean:
+        if derive:
             G.load_pull_derive_push(V, E, pin_pull.data_ptr())
         else:
             G.load_pointers(V, E, pin_pull.data_ptr(), pin_push.data_ptr())
@@ -337,7 +342,7 @@ def run_native(a):
     e2e_units_all, e2e_ms = combine_ranks(e2e_units, te.ms, dist)
     e2e = {"value": round(e2e_units_all / (e2e_ms * 1e-3) / 1e9, 3), "unit": "GTEPS",
            "h2d_bytes_per_step": pull_bytes + push_bytes, "d2h_bytes_per_step": int(d2h.nbytes),
-           "ingest": ("the -pull pairs; the -push list derived on the device" if lean else "both lists"),
+           "ingest": ("the -pull pairs; the -push list derived on the device" if derive else "both lists"),
            "ms_per_step": round(e2e_ms / a.steps, 3)}
 
     apps = {}
@@ -654,6 +659,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the default kernel shapes (no autotuning pass)")
     ap.add_argument("--lean", action="store_true", help="host keeps only the -pull pairs (default from scale 26)")
+    ap.add_argument("--ingest", choices=["pull", "both"], default="pull",
+                    help="e2e input: the -pull pairs (the library derives the -push list) or both lists")
     ap.add_argument("--directed", action="store_true", help="CC/BFS on the directed R-MAT (no symmetrisation), as the scale-27 stress configuration")
     a = ap.parse_args()
     if a.warmup < 3:

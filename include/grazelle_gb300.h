@@ -90,6 +90,9 @@ int grz_graph_load_pairs_ex(grz_graph* g, uint64_t num_vertices, uint64_t num_ed
  * (source/graphdata.c:957-1049); push is optional. */
 int grz_graph_load_files(grz_graph* g, const char* base);
 
+/* The info's pull_list_device / push_list_device point at the reference-format 256-bit
+ * vectors.  The engine runs on its own execution layout, so those vectors are derived from it
+ * on the first request (this call, grz_graph_copy_list, or a phases.h binding) and then kept. */
 int grz_graph_get_info(const grz_graph* g, grz_graph_info_t* out);
 /* copies the reference-format 256-bit vectors (4 uint64 each) to host memory */
 int grz_graph_copy_list(grz_graph* g, int list, uint64_t* host_vectors, uint64_t capacity_vectors);

@@ -100,8 +100,10 @@ static void free_graph_data(grz_graph* g)
     // reads at random (pool memory measured 12% slower for random gathers)
     void* pooled[] = { g->outdeg, g->degree, g->inv_deg, g->prop, g->accum, g->glob, g->scratch };
     for (void* p : pooled) grz_dev_free(g, p);
-    void* plain[] = { g->pr_fx[0], g->pr_fx[1], g->pr_sum, g->pr_K, g->pr_rowacc, g->pr_cut };
+    void* plain[] = { g->pr_fx[0], g->pr_fx[1], g->pr_sum, g->pr_K, g->pr_rowacc, g->pr_cut, g->pr_d[0], g->pr_d[1] };
     for (void* p : plain) cudaFree(p);
+    g->pr_d[0] = g->pr_d[1] = nullptr;
+    g->pr_dmode = g->pr_fx_stale = g->pr_d_stale = 0;
     g->outdeg = nullptr; g->degree = nullptr; g->inv_deg = nullptr;
     g->pr_fx[0] = g->pr_fx[1] = nullptr; g->pr_sum = nullptr; g->pr_K = nullptr; g->pr_rowacc = nullptr;
     g->pr_cut = nullptr;
@@ -138,8 +140,10 @@ extern "C" int grz_graph_create(grz_graph** out, int device, void* stream)
     g->tune.cc_threads = 512;
     g->tune.cc_grid = 0;
     g->tune.pr_grid = 0;
+    g->tune.pr_props = 0;
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g->l2_bytes, cudaDevAttrL2CacheSize, device);
     if (e == cudaSuccess && pool_setup(device) != GRZ_OK) e = cudaErrorUnknown;
     if (e != cudaSuccess) {
         free(g);
@@ -449,6 +453,7 @@ extern "C" int grz_graph_get_info(const grz_graph* gc, grz_graph_info_t* out)
         if (L->nbr) b += L->nvec * ((L->vs ? 32 : 0) + 16 + 4) + (g->V + 64) * 8 + (g->V + 1) * 4;
     b += (g->V + 8) * 8 * 3 + g->V * 12;
     if (g->pr_fx[0]) b += g->V * (16 * 3 + 4);
+    if (g->pr_d[0]) b += g->V * 16;
     out->device_bytes = b;
     return GRZ_OK;
 }
@@ -675,6 +680,10 @@ extern "C" int grz_tune_set(grz_graph* g, int param, int64_t value)
         if (value > 1) return grz_set_error(g, GRZ_ERR_ARG, "BFS pull mode must be 0 or 1");
         g->tune.bfs_pull_scan = (uint32_t)value;
         return GRZ_OK;
+    case GRZ_TUNE_PR_PROPS:
+        if (value > 2) return grz_set_error(g, GRZ_ERR_ARG, "PageRank gathered props must be 0 (by size), 1 (fixed point) or 2 (doubles)");
+        g->tune.pr_props = (uint32_t)value;  // from the next grz_pr_init
+        return GRZ_OK;
     default:
         return grz_set_error(g, GRZ_ERR_ARG, "unknown tuning parameter %d", param);
     }
@@ -690,6 +699,7 @@ extern "C" int grz_tune_get(const grz_graph* g, int param, int64_t* value)
     case GRZ_TUNE_CC_GRID: *value = g->tune.cc_grid; return GRZ_OK;
     case GRZ_TUNE_PR_GRID: *value = g->tune.pr_grid; return GRZ_OK;
     case GRZ_TUNE_BFS_PULL_SCAN: *value = g->tune.bfs_pull_scan; return GRZ_OK;
+    case GRZ_TUNE_PR_PROPS: *value = g->tune.pr_props; return GRZ_OK;
     case GRZ_TUNE_HUBS_LOADED: *value = g->pull.nhub; return GRZ_OK;
     default: return GRZ_ERR_ARG;
     }

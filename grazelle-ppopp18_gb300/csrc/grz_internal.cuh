@@ -229,6 +229,7 @@ struct grz_mlp;
 #define GRZ_TUNE_CC_GRID 3
 #define GRZ_TUNE_PR_GRID 4
 #define GRZ_TUNE_BFS_PULL_SCAN 5
+#define GRZ_TUNE_PR_PROPS 6
 #define GRZ_TUNE_HUBS_LOADED 100
 
 // kernel shapes chosen per graph (grz_tune_set; the autotuner searches them)
@@ -239,6 +240,7 @@ struct grz_tuning {
     uint32_t cc_grid;      // blocks of the persistent CC pull kernel (0: SMs x resident blocks)
     uint32_t pr_grid;      // blocks of the persistent PageRank gather kernel (0: SMs x resident blocks)
     uint32_t bfs_pull_scan;  // 1: BFS pull scans every vector; 0: only the wanted destinations' (compacted)
+    uint32_t pr_props;     // props the PageRank gather reads: 0 by size, 1 fixed point, 2 doubles
 };
 
 // Device control block of a CC/BFS run executed as one CUDA graph (grz_ccbfs.cu): the
@@ -332,6 +334,10 @@ struct grz_graph {
     uint32_t* pr_cut;     // uint32[V/32]: destinations whose pull vectors straddle a gather tile
     int pr_rowacc_stale;  // fused iterations cleared only the straddling accumulators
     uint32_t pr_nparts[2];  // partials in each half of pr_sum
+    double* pr_d[2];      // double[V+1]: the props as doubles, gathered instead of pr_fx in pr_dmode
+    int pr_dmode;         // fused iterations gather pr_d
+    int pr_fx_stale;      // pr_fx[pr_cur] is behind pr_d[pr_cur]
+    int pr_d_stale;       // pr_d[pr_cur] is behind pr_fx[pr_cur]
     double pr_damping;
     uint32_t pr_iters_done;
     double* prop;         // double[V+8]: reference-format vertex props (PR props, CC labels, BFS parents)
@@ -343,6 +349,7 @@ struct grz_graph {
     u128* glob;           // u128[GRZ_SUM_SLOTS] device
     int app;              // 0 PR, 1 CC, 2 BFS
     int num_sms;
+    int l2_bytes;
     uint32_t max_degree;
     int max_degree_known;
     grz_frontier_state fr;

@@ -42,6 +42,11 @@ __device__ __forceinline__ u128 ld_fx(const u128* p, uint32_t i)
     return r;
 }
 
+// a gathered prop as fixed point: stored so (16 bytes), or as the double it exactly converts
+// from (8 bytes: half the gathered working set, the same sums)
+__device__ __forceinline__ u128 ld_prop(const u128* p, uint32_t i) { return ld_fx(p, i); }
+__device__ __forceinline__ u128 ld_prop(const double* p, uint32_t i) { return fx_from_double(__ldg(p + i)); }
+
 // per-iteration constants handed from the gather kernel to the apply kernel
 struct PRConst {
     const u128* part_in;  // per-block partial sums whose total is S_k (exact)
@@ -67,12 +72,14 @@ __device__ __forceinline__ u128 u128_shfl_up(u128 v, int off)
 // vectors straddle the block's tile edge is added with exact u128 atomics, so only those
 // accumulators must be zero on entry (the fused apply clears exactly those, marked in pr_cut).
 // A destination with no in-edges is never touched and stays 0.  The loads of nbr/dst are
-// streamed once (evict-first); the prop gathers go through L1.
+// streamed once (evict-first); the prop gathers go through L1.  P is the gathered props' type:
+// u128 fixed point, or double (converted exactly to fixed point after the load).
 __device__ __forceinline__ u128 block_reduce_u128(u128 s, u128* red);
 
+template <typename P>
 __global__ void __launch_bounds__(PR_THREADS) k_pr_gather(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv,
                                                           uint64_t first, uint64_t nvec, uint64_t list_nvec,
-                                                          const u128* __restrict__ prop_fx, uint32_t V, u128* __restrict__ rowacc,
+                                                          const P* __restrict__ prop_fx, uint32_t V, u128* __restrict__ rowacc,
                                                           const uint32_t* __restrict__ hub_vid, uint32_t nhub, const PRConst pc)
 {
     constexpr int NW = PR_THREADS / 32;
@@ -100,10 +107,10 @@ __global__ void __launch_bounds__(PR_THREADS) k_pr_gather(const uint4* __restric
         if (live) {
             const uint4 s = __ldcs(nbr + v);
             key = __ldcs(dstv + v);
-            const u128 g0 = ld_fx(prop_fx, min(grz_hub_decode(s.x, hub_vid, nhub), V));
-            const u128 g1 = ld_fx(prop_fx, min(grz_hub_decode(s.y, hub_vid, nhub), V));
-            const u128 g2 = ld_fx(prop_fx, min(grz_hub_decode(s.z, hub_vid, nhub), V));
-            const u128 g3 = ld_fx(prop_fx, min(grz_hub_decode(s.w, hub_vid, nhub), V));
+            const u128 g0 = ld_prop(prop_fx, min(grz_hub_decode(s.x, hub_vid, nhub), V));
+            const u128 g1 = ld_prop(prop_fx, min(grz_hub_decode(s.y, hub_vid, nhub), V));
+            const u128 g2 = ld_prop(prop_fx, min(grz_hub_decode(s.z, hub_vid, nhub), V));
+            const u128 g3 = ld_prop(prop_fx, min(grz_hub_decode(s.w, hub_vid, nhub), V));
             val = u128_add(u128_add(g2, g3), u128_add(g0, g1));
         }
         uint32_t prevkey = __shfl_up_sync(0xffffffffu, key, 1);
@@ -181,8 +188,9 @@ __device__ __forceinline__ u128 block_reduce_u128(u128 s, u128* red)
 
 // Vertex phase fused with reading the accumulators (phase_vertex_pr.asm:75-134):
 //   prop[v] = (acc[v]*d + G*d + (1-d)/V) / deg'[v],  G = (1 - S)/V
-// computed as fma + multiply by the precomputed 1/deg'.  It writes the new props in fixed point
-// (plus double when asked) and accumulates S' = sum deg[v]*prop[v] exactly; S' is the next
+// computed as fma + multiply by the precomputed 1/deg'.  It writes the new props in fixed point,
+// or as doubles when the next gather reads doubles (plus the reference-format doubles when
+// asked), and accumulates S' = sum deg[v]*prop[v] exactly; S' is the next
 // iteration's sum of accumulators.  Of the accumulators it clears only those the next gather
 // adds to atomically (bit set in `cut`); the others are overwritten by the next gather's stores.
 // The grid strides over the vertices, PR_APPLY_U vertices per thread at a time whose
@@ -196,7 +204,7 @@ __global__ void __launch_bounds__(PR_THREADS, PR_APPLY_RESIDENT) k_pr_apply(u128
                                                                             const uint32_t* __restrict__ degree, uint64_t V,
                                                                             const double* __restrict__ Kp, u128* __restrict__ part_out,
                                                                             double damping, u128* __restrict__ prop_fx,
-                                                                            double* __restrict__ prop_out)
+                                                                            double* __restrict__ prop_d, double* __restrict__ prop_out)
 {
     __shared__ u128 red[PR_THREADS / 32];
     const double sK = *Kp;
@@ -226,7 +234,8 @@ __global__ void __launch_bounds__(PR_THREADS, PR_APPLY_RESIDENT) k_pr_apply(u128
             acc.hi = a[j].y;
             const double p = __dmul_rn(__fma_rn(fx_to_double(acc), damping, sK), __ldg(inv_deg + v));
             const u128 pf = fx_from_double(p);
-            __stcg(reinterpret_cast<ulonglong2*>(prop_fx) + v, make_ulonglong2(pf.lo, pf.hi));
+            if (prop_d) __stcg(prop_d + v, p);  // the next gather reads doubles
+            else __stcg(reinterpret_cast<ulonglong2*>(prop_fx) + v, make_ulonglong2(pf.lo, pf.hi));
             if (prop_out) prop_out[v] = p;
             s = u128_add(s, u128_mul32(pf, __ldg(degree + v)));
         }
@@ -282,7 +291,7 @@ __global__ void k_pr_vertex(const double* __restrict__ accum, const double* __re
 // execution_initialize_vertex_prop_pr (source/execution_pr.c:85-88): (1/V) / deg'
 __global__ void k_pr_init(const double* __restrict__ outdeg, const uint32_t* __restrict__ degree, uint64_t V,
                           double* __restrict__ prop, double* __restrict__ accum, u128* __restrict__ prop_fx,
-                          u128* __restrict__ part0)
+                          double* __restrict__ prop_d, u128* __restrict__ part0)
 {
     __shared__ u128 red[PR_THREADS / 32];
     const uint64_t v = (uint64_t)blockIdx.x * PR_THREADS + threadIdx.x;
@@ -294,6 +303,7 @@ __global__ void k_pr_init(const double* __restrict__ outdeg, const uint32_t* __r
         accum[v] = 0.0;
         const u128 pf = fx_from_double(p);
         prop_fx[v] = pf;
+        if (prop_d) prop_d[v] = p;
         s = u128_mul32(pf, degree[v]);
     }
     s = block_reduce_u128(s, red);
@@ -306,9 +316,41 @@ __global__ void k_fx_to_double(const u128* __restrict__ fx, uint64_t V, double* 
     if (v < V) out[v] = fx_to_double(fx[v]);
 }
 
+// double props -> the fixed-point props they convert to (and, when asked, back to the double
+// the fixed-point value rounds to, which is what the fixed-point path reports)
+__global__ void k_double_to_fx(const double* __restrict__ d, uint64_t V, u128* __restrict__ fx, double* __restrict__ out)
+{
+    const uint64_t v = (uint64_t)blockIdx.x * PR_THREADS + threadIdx.x;
+    if (v >= V) return;
+    const u128 f = fx_from_double(d[v]);
+    if (fx) fx[v] = f;
+    if (out) out[v] = fx_to_double(f);
+}
+
 unsigned blocks_for(uint64_t n) { return (unsigned)((n + PR_THREADS - 1) / PR_THREADS); }
 
 }  // namespace
+
+// The current props live in pr_fx[pr_cur] (fixed point) or, after fused iterations that gather
+// doubles, in pr_d[pr_cur]; each form is brought up to date from the other before a path that
+// reads it.
+static int pr_sync_fx(grz_graph* g)
+{
+    if (!g->pr_fx_stale) return GRZ_OK;
+    k_double_to_fx<<<blocks_for(g->V), PR_THREADS, 0, g->stream>>>(g->pr_d[g->pr_cur], g->V, g->pr_fx[g->pr_cur], nullptr); GRZ_COUNT_LAUNCH(g);
+    GRZ_CK(g, cudaGetLastError());
+    g->pr_fx_stale = 0;
+    return GRZ_OK;
+}
+
+static int pr_sync_d(grz_graph* g)
+{
+    if (!g->pr_d_stale) return GRZ_OK;
+    k_fx_to_double<<<blocks_for(g->V), PR_THREADS, 0, g->stream>>>(g->pr_fx[g->pr_cur], g->V, g->pr_d[g->pr_cur]); GRZ_COUNT_LAUNCH(g);
+    GRZ_CK(g, cudaGetLastError());
+    g->pr_d_stale = 0;
+    return GRZ_OK;
+}
 
 // The phase-API gathers and the push phase add into every accumulator: after fused iterations,
 // which leave the accumulators of non-straddling destinations holding their last sums, clear all.
@@ -341,6 +383,16 @@ int grz_pr_prepare(grz_graph* g)
         GRZ_CK(g, cudaMemsetAsync(g->pr_fx[0], 0, sizeof(u128) * (V + 1), g->stream));
         GRZ_CK(g, cudaMemsetAsync(g->pr_fx[1], 0, sizeof(u128) * (V + 1), g->stream));
     }
+    // doubles gathered instead of 16-byte fixed point: chosen, or when the fixed-point props
+    // would not fit half of L2 (the gathered form then halves the DRAM working set)
+    const int pick = g->tune.pr_props;
+    g->pr_dmode = pick == 2 || (pick == 0 && (uint64_t)sizeof(u128) * V > (uint64_t)g->l2_bytes / 2);
+    if (g->pr_dmode && !g->pr_d[0]) {
+        GRZ_CK(g, cudaMalloc((void**)&g->pr_d[0], sizeof(double) * (V + 1)));
+        GRZ_CK(g, cudaMalloc((void**)&g->pr_d[1], sizeof(double) * (V + 1)));
+        GRZ_CK(g, cudaMemsetAsync(g->pr_d[0], 0, sizeof(double) * (V + 1), g->stream));
+        GRZ_CK(g, cudaMemsetAsync(g->pr_d[1], 0, sizeof(double) * (V + 1), g->stream));
+    }
     return GRZ_OK;
 }
 
@@ -351,26 +403,29 @@ int grz_pr_init_state(grz_graph* g, double damping)
     if (rc) return rc;
     g->pr_damping = damping;
     g->pr_cur = 0;
+    g->pr_fx_stale = g->pr_d_stale = 0;
     g->pr_sum_cur = 0;
     g->pr_iters_done = 0;
     GRZ_CK(g, cudaMemsetAsync(g->pr_sum, 0, sizeof(u128) * 2 * (blocks_for(g->V) + 1), g->stream));
     GRZ_CK(g, cudaMemsetAsync(g->accum, 0, sizeof(double) * (g->V + 8), g->stream));
     g->pr_nparts[0] = g->pr_nparts[1] = blocks_for(g->V);
     if (g->V) {
-        k_pr_init<<<blocks_for(g->V), PR_THREADS, 0, g->stream>>>(g->outdeg, g->degree, g->V, g->prop, g->accum, g->pr_fx[0], g->pr_sum); GRZ_COUNT_LAUNCH(g);
+        k_pr_init<<<blocks_for(g->V), PR_THREADS, 0, g->stream>>>(g->outdeg, g->degree, g->V, g->prop, g->accum, g->pr_fx[0],
+                                                                 g->pr_dmode ? g->pr_d[0] : nullptr, g->pr_sum); GRZ_COUNT_LAUNCH(g);
         GRZ_CK(g, cudaGetLastError());
     }
     return GRZ_OK;
 }
 
 // resident blocks per SM of the gather kernel (its grid is persistent: SMs x resident)
+template <typename P>
 static int pr_gather_resident(grz_graph* g)
 {
     static int resident[64] = {};
     if (g->device < 0 || g->device >= 64) return 1;
     if (!resident[g->device]) {
         int r = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_pr_gather, PR_THREADS, 0) != cudaSuccess || r < 1) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_pr_gather<P>, PR_THREADS, 0) != cudaSuccess || r < 1) {
             cudaGetLastError();
             r = 1;
         }
@@ -379,15 +434,16 @@ static int pr_gather_resident(grz_graph* g)
     return resident[g->device];
 }
 
-static int pr_gather(grz_graph* g, uint64_t first, uint64_t count, const PRConst& pc)
+template <typename P>
+static int pr_gather(grz_graph* g, uint64_t first, uint64_t count, const PRConst& pc, const P* props)
 {
     if (count == 0) return GRZ_OK;
-    const uint64_t want = g->tune.pr_grid ? g->tune.pr_grid : (uint64_t)g->num_sms * pr_gather_resident(g);
+    const uint64_t want = g->tune.pr_grid ? g->tune.pr_grid : (uint64_t)g->num_sms * pr_gather_resident<P>(g);
     const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>(blocks_for(count), want));
     grz_prof_begin(g, GRZ_PROF_PR_GATHER);
-    k_pr_gather<<<(unsigned)grid, PR_THREADS, 0, g->stream>>>(g->pull.nbr, g->pull.shared, first, count, g->pull.nvec,
-                                                                 g->pr_fx[g->pr_cur], (uint32_t)g->V, g->pr_rowacc, g->pull.hub_vid,
-                                                                 g->pull.nhub, pc); GRZ_COUNT_LAUNCH(g);
+    k_pr_gather<P><<<(unsigned)grid, PR_THREADS, 0, g->stream>>>(g->pull.nbr, g->pull.shared, first, count, g->pull.nvec,
+                                                                    props, (uint32_t)g->V, g->pr_rowacc, g->pull.hub_vid,
+                                                                    g->pull.nhub, pc); GRZ_COUNT_LAUNCH(g);
     grz_prof_end(g);
     return grz_cuda_check(g, cudaGetLastError(), "k_pr_gather");
 }
@@ -406,7 +462,14 @@ int grz_pr_fused_iteration(grz_graph* g, int write_double_props)
     pc.damping = g->pr_damping;
     pc.c = (1.0 - g->pr_damping) / dV;
     pc.nverts = dV;
-    int rc = pr_gather(g, 0, g->pull.nvec, pc);
+    int rc = GRZ_OK;
+    if (g->pr_dmode) {
+        rc = pr_sync_d(g);
+        if (rc == GRZ_OK) rc = pr_gather(g, 0, g->pull.nvec, pc, (const double*)g->pr_d[g->pr_cur]);
+    } else {
+        rc = pr_sync_fx(g);
+        if (rc == GRZ_OK) rc = pr_gather(g, 0, g->pull.nvec, pc, (const u128*)g->pr_fx[g->pr_cur]);
+    }
     if (rc) return rc;
     grz_prof_begin(g, GRZ_PROF_PR_APPLY);
     const uint64_t agrid = std::max<uint64_t>(1, std::min<uint64_t>((g->V + (uint64_t)PR_THREADS * PR_APPLY_U - 1) /
@@ -414,10 +477,12 @@ int grz_pr_fused_iteration(grz_graph* g, int write_double_props)
                                                                     (uint64_t)g->num_sms * PR_APPLY_RESIDENT));
     k_pr_apply<<<(unsigned)agrid, PR_THREADS, 0, g->stream>>>(g->pr_rowacc, g->pr_cut, g->inv_deg, g->degree, g->V, g->pr_K,
                                                               g->pr_sum + (size_t)(k ^ 1) * stride, g->pr_damping, g->pr_fx[g->pr_cur ^ 1],
+                                                              g->pr_dmode ? g->pr_d[g->pr_cur ^ 1] : nullptr,
                                                               write_double_props ? g->prop : nullptr); GRZ_COUNT_LAUNCH(g);
     grz_prof_end(g);
     GRZ_CK(g, cudaGetLastError());
     g->pr_nparts[k ^ 1] = (uint32_t)agrid;
+    g->pr_fx_stale = g->pr_dmode;  // the new props are only in pr_d
     g->pr_rowacc_stale = 1;
     g->pr_cur ^= 1;
     g->pr_sum_cur = k ^ 1;
@@ -432,10 +497,11 @@ int grz_pr_edge_pull(grz_graph* g, uint64_t first, uint64_t count)
 {
     if (g->V == 0) return GRZ_OK;
     int rc = grz_pr_rowacc_clean(g);
+    if (rc == GRZ_OK) rc = pr_sync_fx(g);
     if (rc) return rc;
     PRConst pc;
     memset(&pc, 0, sizeof(pc));
-    rc = pr_gather(g, first, count, pc);
+    rc = pr_gather(g, first, count, pc, (const u128*)g->pr_fx[g->pr_cur]);
     if (rc) return rc;
     if (first + count < g->pull.nvec) return GRZ_OK;
     k_pr_accum_out<<<blocks_for(g->V), PR_THREADS, 0, g->stream>>>(g->pr_rowacc, g->V, g->accum, g->glob); GRZ_COUNT_LAUNCH(g);
@@ -452,6 +518,9 @@ int grz_pr_vertex(grz_graph* g, uint64_t first, uint64_t count, double S)
     const double G = (1.0 - S) / dV;
     const double c = (1.0 - g->pr_damping) / dV;
     const double K = fma(G, g->pr_damping, c);
+    int rc = pr_sync_fx(g);
+    if (rc) return rc;
+    g->pr_d_stale = g->pr_d[0] != nullptr;  // the props change in the fixed-point form only
     // the props being gathered are rewritten in place: the boundary path keeps one live copy
     k_pr_vertex<<<blocks_for(count), PR_THREADS, 0, g->stream>>>(g->accum, g->inv_deg, g->prop, g->pr_fx[g->pr_cur],
                                                                  first, count, g->pr_damping, K); GRZ_COUNT_LAUNCH(g);
@@ -463,7 +532,12 @@ int grz_pr_vertex(grz_graph* g, uint64_t first, uint64_t count, double S)
 int grz_pr_props_to_double(grz_graph* g)
 {
     if (g->V == 0) return GRZ_OK;
-    k_fx_to_double<<<blocks_for(g->V), PR_THREADS, 0, g->stream>>>(g->pr_fx[g->pr_cur], g->V, g->prop); GRZ_COUNT_LAUNCH(g);
+    if (g->pr_fx_stale) {
+        // the double props convert exactly to the fixed-point ones; report what those round to
+        k_double_to_fx<<<blocks_for(g->V), PR_THREADS, 0, g->stream>>>(g->pr_d[g->pr_cur], g->V, nullptr, g->prop); GRZ_COUNT_LAUNCH(g);
+    } else {
+        k_fx_to_double<<<blocks_for(g->V), PR_THREADS, 0, g->stream>>>(g->pr_fx[g->pr_cur], g->V, g->prop); GRZ_COUNT_LAUNCH(g);
+    }
     GRZ_CK(g, cudaGetLastError());
     return GRZ_OK;
 }
@@ -524,6 +598,7 @@ int grz_pr_push_phase(grz_graph* g, uint64_t first_vec, uint64_t count)
     if (count == 0) return GRZ_OK;
     // the pull accumulators double as the push accumulators (all zero between uses)
     int rc = grz_pr_rowacc_clean(g);
+    if (rc == GRZ_OK) rc = pr_sync_fx(g);
     if (rc) return rc;
     k_pr_push<<<blocks_for(count), PR_THREADS, 0, g->stream>>>(g->push.nbr, g->push.shared, first_vec, count,
                                                                g->pr_fx[g->pr_cur], g->pr_rowacc, g->glob); GRZ_COUNT_LAUNCH(g);

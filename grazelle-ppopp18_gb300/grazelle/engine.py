@@ -72,7 +72,8 @@ class Graph:
         """Set kernel shapes: hubs=, cc_cache=, cc_threads=, cc_grid=, pr_grid=, bfs_pull_scan= (results
         never depend on them; hubs takes effect at the next load)."""
         keys = {"hubs": native.TUNE_HUBS, "cc_cache": native.TUNE_CC_CACHE, "cc_threads": native.TUNE_CC_THREADS,
-                "cc_grid": native.TUNE_CC_GRID, "pr_grid": native.TUNE_PR_GRID, "bfs_pull_scan": native.TUNE_BFS_PULL_SCAN}
+                "cc_grid": native.TUNE_CC_GRID, "pr_grid": native.TUNE_PR_GRID, "bfs_pull_scan": native.TUNE_BFS_PULL_SCAN,
+                "pr_props": native.TUNE_PR_PROPS}
         for k, v in kw.items():
             self._ck(self.lib.grz_tune_set(self.h, keys[k], int(v)))
         return self
@@ -81,7 +82,7 @@ class Graph:
         out = {}
         for k, p in (("hubs", native.TUNE_HUBS), ("cc_cache", native.TUNE_CC_CACHE), ("cc_threads", native.TUNE_CC_THREADS),
                      ("cc_grid", native.TUNE_CC_GRID), ("pr_grid", native.TUNE_PR_GRID),
-                     ("bfs_pull_scan", native.TUNE_BFS_PULL_SCAN),
+                     ("bfs_pull_scan", native.TUNE_BFS_PULL_SCAN), ("pr_props", native.TUNE_PR_PROPS),
                      ("hubs_loaded", native.TUNE_HUBS_LOADED)):
             v = C.c_int64()
             self._ck(self.lib.grz_tune_get(self.h, p, C.byref(v)))

@@ -165,3 +165,50 @@ def test_empty_graph():
         p = G.pagerank(4)
     # every vertex is dangling: prop = rank / V with rank = 1/V in every iteration
     np.testing.assert_allclose(p, np.full(100, 1.0 / 100 / 100), rtol=1e-12)
+
+
+@pytest.mark.parametrize("scale, seed", [(12, 31), (17, 32)])
+def test_gathered_prop_form_does_not_change_results(scale, seed):
+    """The gather can read 8-byte doubles instead of 16-byte fixed-point props (GRZ_TUNE_PR_PROPS):
+    the apply's fixed-point prop is the exact conversion of the same double, so every sum and
+    every reported prop is bit-identical."""
+    from grazelle import graphgen as gg
+    g = gg.rmat(scale, seed=seed)
+    with gpu_graph(g) as G:
+        G.tune(pr_props=1)
+        fixed = G.pagerank(16)
+        G.tune(pr_props=2)
+        dbl = G.pagerank(16)
+        G.tune(pr_props=0)
+        auto = G.pagerank(16)
+    np.testing.assert_array_equal(dbl.view(np.uint64), fixed.view(np.uint64))
+    np.testing.assert_array_equal(auto.view(np.uint64), fixed.view(np.uint64))
+
+
+def test_phase_api_continues_fused_double_gather_iterations():
+    """Fused iterations that gather doubles, then phase-API iterations on the fixed-point form:
+    the same props as fused iterations throughout."""
+    import ctypes as C
+    from grazelle import graphgen as gg, native
+    g = gg.rmat(14, seed=33)
+    with gpu_graph(g) as G:
+        G.tune(pr_props=1)
+        ref = G.pagerank(8)
+        G.tune(pr_props=2)
+        G.pr_init(0.875).pr_iterate(4)
+        lib = G.lib
+        native.check(lib.grz_phases_bind(G.h, native.APP_PAGERANK))
+        info = G.info()
+        rb = np.zeros(8, dtype=np.uint64)
+        mb = np.zeros(32 * 4, dtype=np.uint64)
+        mb[0::4] = np.uint64(0xFFFFFFFFFFFFFFFF)
+        acc_host = np.zeros(g.num_vertices + 8)
+        for _ in range(4):
+            lib.phase_op_reset_global_accum()
+            lib.perform_edge_pull_phase_pr(C.c_void_p(info.pull_list_device), info.pull_vectors)
+            lib.edge_pull_op_merge_with_merge_buffer(C.c_void_p(mb.ctypes.data), 32, C.c_void_p(acc_host.ctypes.data))
+            lib.phase_op_write_global_accum_to_buf(C.c_void_p(rb.ctypes.data))
+            lib.perform_vertex_phase_pr(0, g.num_vertices, C.c_void_p(rb.ctypes.data))
+        assert lib.grz_phases_last_status() == 0
+        mixed = G.props()
+    np.testing.assert_array_equal(mixed.view(np.uint64), ref.view(np.uint64))

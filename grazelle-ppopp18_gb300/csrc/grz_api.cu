@@ -1,10 +1,16 @@
 // grz_api.cu -- graph context, ingest, queries and the exported C ABI (include/grazelle_gb300.h).
+#include <errno.h>
+#include <fcntl.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include <mutex>
+#include <thread>
+#include <vector>
 
 #include "grz_internal.cuh"
 #include "../../include/grazelle_gb300.h"
@@ -385,43 +391,143 @@ static int load_pairs(grz_graph* g, uint64_t V, uint64_t E, const uint64_t* pull
     return rc;
 }
 
-extern "C" int grz_graph_load_files(grz_graph* g, const char* base)
+// ---------------------------------------------------------------------------------------------
+// File ingest (source/graphdata.c:957-1049): each list file is a {V, E} header and E (src, dst)
+// uint64 pairs.  The pairs are streamed into a device buffer: reader threads fill one pinned
+// staging buffer with pread while the previous one is copied to the device, so the disk (or page
+// cache) and the host link work at the same time.  Sort order and ID range are checked on the
+// device by the layout builder.
+
+namespace {
+
+constexpr size_t STAGE_BYTES = 64u << 20;  // per staging buffer
+constexpr int STAGE_READERS = 4;           // pread threads per chunk
+
+struct ListFile {
+    int fd = -1;
+    uint64_t V = 0, E = 0;
+};
+
+int open_list(grz_graph* g, const char* path, ListFile* lf, bool optional, bool* missing)
+{
+    if (missing) *missing = false;
+    lf->fd = open(path, O_RDONLY);
+    if (lf->fd < 0) {
+        if (optional && errno == ENOENT) {
+            if (missing) *missing = true;
+            return GRZ_OK;
+        }
+        return grz_set_error(g, GRZ_ERR_IO, "unable to read file \"%s\"", path);
+    }
+    uint64_t hdr[2];
+    if (pread(lf->fd, hdr, sizeof(hdr), 0) != (ssize_t)sizeof(hdr))
+        return grz_set_error(g, GRZ_ERR_IO, "\"%s\": missing {V, E} header", path);
+    if (hdr[1] > (1ull << 40))
+        return grz_set_error(g, GRZ_ERR_IO, "\"%s\": implausible edge count %llu", path, (unsigned long long)hdr[1]);
+    struct stat st;
+    if (fstat(lf->fd, &st) == 0 && (uint64_t)st.st_size < sizeof(hdr) + 16 * hdr[1])
+        return grz_set_error(g, GRZ_ERR_IO, "\"%s\": truncated (header says %llu edges)", path, (unsigned long long)hdr[1]);
+    lf->V = hdr[0];
+    lf->E = hdr[1];
+    return GRZ_OK;
+}
+
+// reads [off, off + n) of fd into buf completely; false on an error or a short file
+bool pread_all(int fd, char* buf, size_t n, uint64_t off)
+{
+    while (n > 0) {
+        const ssize_t r = pread(fd, buf, n, (off_t)off);
+        if (r < 0 && errno == EINTR) continue;
+        if (r <= 0) return false;
+        buf += r;
+        off += (uint64_t)r;
+        n -= (size_t)r;
+    }
+    return true;
+}
+
+int stream_to_device(grz_graph* g, const ListFile& lf, const char* path, char* dst)
+{
+    const uint64_t bytes = 16 * lf.E;
+    if (bytes == 0) return GRZ_OK;
+    char* stage[2] = { nullptr, nullptr };
+    cudaEvent_t ev[2] = { nullptr, nullptr };
+    int rc = GRZ_OK;
+    for (int i = 0; i < 2 && rc == GRZ_OK; ++i) {
+        cudaError_t e = cudaMallocHost((void**)&stage[i], STAGE_BYTES);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming);
+        if (e != cudaSuccess) rc = grz_cuda_check(g, e, "staging buffers");
+    }
+    for (uint64_t off = 0, k = 0; off < bytes && rc == GRZ_OK; off += STAGE_BYTES, ++k) {
+        const int b = (int)(k & 1);
+        const size_t n = (size_t)std::min<uint64_t>(STAGE_BYTES, bytes - off);
+        cudaError_t e = cudaEventSynchronize(ev[b]);  // the copy out of this buffer two chunks ago
+        if (e != cudaSuccess) { rc = grz_cuda_check(g, e, "staging copy"); break; }
+        bool ok[STAGE_READERS];
+        std::vector<std::thread> th;
+        const size_t part = (n + STAGE_READERS - 1) / STAGE_READERS;
+        for (int t = 0; t < STAGE_READERS; ++t) {
+            const size_t lo = std::min(n, t * part), hi = std::min(n, lo + part);
+            ok[t] = true;
+            if (hi > lo)
+                th.emplace_back([&, t, lo, hi] { ok[t] = pread_all(lf.fd, stage[b] + lo, hi - lo, 16 + off + lo); });
+        }
+        for (auto& x : th) x.join();
+        for (int t = 0; t < STAGE_READERS; ++t)
+            if (!ok[t]) rc = grz_set_error(g, GRZ_ERR_IO, "\"%s\": read failed at byte %llu", path, (unsigned long long)(16 + off));
+        if (rc) break;
+        e = cudaMemcpyAsync(dst + off, stage[b], n, cudaMemcpyHostToDevice, g->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[b], g->stream);
+        if (e != cudaSuccess) rc = grz_cuda_check(g, e, "H2D pairs");
+    }
+    cudaStreamSynchronize(g->stream);
+    for (int i = 0; i < 2; ++i) {
+        if (stage[i]) cudaFreeHost(stage[i]);
+        if (ev[i]) cudaEventDestroy(ev[i]);
+    }
+    return rc;
+}
+
+}  // namespace
+
+extern "C" int grz_graph_load_files_ex(grz_graph* g, const char* base, int flags)
 {
     if (!g || !base) return GRZ_ERR_ARG;
+    if (flags & ~GRZ_LOAD_DERIVE_PUSH) return GRZ_ERR_ARG;
+    GRZ_CK(g, cudaSetDevice(g->device));
     char path[2][4096];
     snprintf(path[0], sizeof(path[0]), "%s-pull", base);
     snprintf(path[1], sizeof(path[1]), "%s-push", base);
-    uint64_t hdr[2][2] = { { 0, 0 }, { 0, 0 } };
-    uint64_t* pairs[2] = { nullptr, nullptr };
-    int rc = GRZ_OK;
-    for (int i = 0; i < 2 && rc == GRZ_OK; ++i) {
-        FILE* f = fopen(path[i], "rb");
-        if (!f) {
-            if (i == 1) break;  // the push list is optional
-            return grz_set_error(g, GRZ_ERR_IO, "unable to read file \"%s\"", path[i]);
+    const bool derive = (flags & GRZ_LOAD_DERIVE_PUSH) != 0;
+    ListFile lf[2];
+    bool push_missing = derive;
+    int rc = open_list(g, path[0], &lf[0], false, nullptr);
+    if (rc == GRZ_OK && !derive) rc = open_list(g, path[1], &lf[1], true, &push_missing);  // the push list is optional
+    if (rc == GRZ_OK && !push_missing && (lf[1].V != lf[0].V || lf[1].E != lf[0].E))
+        rc = grz_set_error(g, GRZ_ERR_IO, "\"%s\": header {V, E} differs from the -pull file", path[1]);
+    void* dbuf[2] = { nullptr, nullptr };
+    if (rc == GRZ_OK) {
+        free_graph_data(g);  // the old graph's memory back to the pool before the new pairs take it
+        const uint64_t E = lf[0].E;
+        for (int i = 0; i < 2 && rc == GRZ_OK; ++i) {
+            if (i == 1 && push_missing) break;
+            if (E > 0) rc = grz_dev_alloc(g, &dbuf[i], 16 * E);
+            if (rc == GRZ_OK) rc = stream_to_device(g, lf[i], path[i], (char*)dbuf[i]);
         }
-        if (fread(hdr[i], sizeof(uint64_t), 2, f) != 2) {
-            rc = grz_set_error(g, GRZ_ERR_IO, "\"%s\": missing {V, E} header", path[i]);
-        } else if (i == 1 && (hdr[1][0] != hdr[0][0] || hdr[1][1] != hdr[0][1])) {
-            rc = grz_set_error(g, GRZ_ERR_IO, "\"%s\": header {V, E} differs from the -pull file", path[i]);
-        } else {
-            const uint64_t E = hdr[i][1];
-            if (E > (1ull << 40)) {
-                rc = grz_set_error(g, GRZ_ERR_IO, "\"%s\": implausible edge count %llu", path[i], (unsigned long long)E);
-            } else {
-                cudaError_t e = cudaMallocHost((void**)&pairs[i], sizeof(uint64_t) * 2 * (E ? E : 1));
-                if (e != cudaSuccess) {
-                    rc = grz_cuda_check(g, e, "pinned host buffer");
-                } else if (fread(pairs[i], sizeof(uint64_t), 2 * E, f) != 2 * E) {
-                    rc = grz_set_error(g, GRZ_ERR_IO, "\"%s\": truncated (header says %llu edges)", path[i], (unsigned long long)E);
-                }
-            }
-        }
-        fclose(f);
+        if (rc == GRZ_OK)
+            rc = load_pairs(g, lf[0].V, E, (const uint64_t*)dbuf[0], (const uint64_t*)dbuf[1],
+                            derive && E > 0 ? GRZ_LOAD_DERIVE_PUSH : 0);
     }
-    if (rc == GRZ_OK) rc = grz_graph_load_pairs(g, hdr[0][0], hdr[0][1], pairs[0], pairs[1]);
-    for (int i = 0; i < 2; ++i) if (pairs[i]) cudaFreeHost(pairs[i]);
+    for (int i = 0; i < 2; ++i) {
+        if (lf[i].fd >= 0) close(lf[i].fd);
+        grz_dev_free(g, dbuf[i]);
+    }
     return rc;
+}
+
+extern "C" int grz_graph_load_files(grz_graph* g, const char* base)
+{
+    return grz_graph_load_files_ex(g, base, 0);
 }
 
 extern "C" int grz_graph_get_info(const grz_graph* gc, grz_graph_info_t* out)

@@ -132,8 +132,9 @@ class Graph:
         self.V, self.E = num_vertices, num_edges
         return self
 
-    def load_files(self, base: str):
-        self._ck(self.lib.grz_graph_load_files(self.h, base.encode()))
+    def load_files(self, base: str, derive_push: bool = False):
+        """`<base>-pull` (and `<base>-push`, or with derive_push the -push list built on the device)."""
+        self._ck(self.lib.grz_graph_load_files_ex(self.h, base.encode(), native.LOAD_DERIVE_PUSH if derive_push else 0))
         info = self.info()
         self.V, self.E = info.num_vertices, info.num_edges
         return self

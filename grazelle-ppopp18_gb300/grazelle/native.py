@@ -65,6 +65,7 @@ SIGNATURES = {
     "grz_sync": (_I, [_VP]),
     "grz_graph_load_pairs": (_I, [_VP, _U64, _U64, _VP, _VP]),
     "grz_graph_load_files": (_I, [_VP, C.c_char_p]),
+    "grz_graph_load_files_ex": (_I, [_VP, C.c_char_p, _I]),
     "grz_graph_get_info": (_I, [_VP, C.POINTER(GraphInfo)]),
     "grz_graph_copy_list": (_I, [_VP, _I, _VP, _U64]),
     "grz_graph_copy_vertex_index": (_I, [_VP, _I, _VP, _U64]),

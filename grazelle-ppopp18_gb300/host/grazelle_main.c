@@ -13,7 +13,8 @@
  * Differences from the reference host code:
  *   - one host thread drives the GPU, so -n and -u are accepted and reported but do not
  *     spawn threads;
- *   - graph_data_read_from_file becomes grz_graph_load_files (the layout is built on the GPU);
+ *   - graph_data_read_from_file becomes grz_graph_load_files (the pairs stream to the GPU, which
+ *     builds the layout); CC and BFS without a -push file derive that list on the device;
  *   - the CC/BFS HasInfo / HasInfo* pointer swap (execution_cc.c:245-250) happens inside
  *     perform_vertex_phase_*, because the bitmaps live on the device;
  *   - the run is timed with CLOCK_MONOTONIC (the reference uses CLOCK_REALTIME_COARSE,
@@ -132,14 +133,15 @@ static void parse(int argc, char** argv, opts_t* o)
 
 /* -------- the host check of source/graphdata.c:957-967 before touching the GPU -------- */
 
-static void check_file_or_die(const char* base, const char* suffix, int required)
+/* 1 when the file exists; exits like the reference when a required file is missing or malformed */
+static int check_file_or_die(const char* base, const char* suffix, int required)
 {
     char p[1100];
     snprintf(p, sizeof(p), "%s%s", base, suffix);
     FILE* f = fopen(p, "rb");
     uint64_t hdr[2];
     if (!f) {
-        if (!required) return;
+        if (!required) return 0;
         fprintf(stderr, "Error: unable to read file \"%s\"\n", p);
         exit(255);
     }
@@ -151,6 +153,7 @@ static void check_file_or_die(const char* base, const char* suffix, int required
         fprintf(stderr, "Error: unable to read file \"%s\"\n", p);
         exit(255);
     }
+    return 1;
 }
 
 static double now_ms(void)
@@ -248,12 +251,17 @@ int main(int argc, char** argv)
     opts_t o;
     parse(argc, argv, &o);
     check_file_or_die(o.input, "-pull", 1);
-    check_file_or_die(o.input, "-push", 0);
+    const int have_push = check_file_or_die(o.input, "-push", 0);
 
     grz_graph* g = NULL;
     gpu_or_die(grz_graph_create(&g, o.device, NULL), NULL, "GPU");
     const double t_load = now_ms();
+#if APP == GRZ_APP_PAGERANK
     gpu_or_die(grz_graph_load_files(g, o.input), g, "load");
+#else
+    /* CC and BFS need the -push list: without the file, it is derived on the device */
+    gpu_or_die(grz_graph_load_files_ex(g, o.input, have_push ? 0 : GRZ_LOAD_DERIVE_PUSH), g, "load");
+#endif
     grz_graph_info_t info;
     grz_graph_get_info(g, &info);
     printf("In-edges:  created %llu vectors, efficiency = %.1lf%%\n", (unsigned long long)info.pull_vectors,

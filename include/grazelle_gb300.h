@@ -87,8 +87,12 @@ int grz_graph_load_pairs(grz_graph* g, uint64_t num_vertices, uint64_t num_edges
 int grz_graph_load_pairs_ex(grz_graph* g, uint64_t num_vertices, uint64_t num_edges, const uint64_t* pull_pairs,
                             const uint64_t* push_pairs, int flags);
 /* Reads `<base>-pull` and `<base>-push`, each a {V, E} header and E (src, dst) uint64 pairs
- * (source/graphdata.c:957-1049); push is optional. */
+ * (source/graphdata.c:957-1049); push is optional.  The pairs are streamed to the device
+ * through two pinned 64 MB staging buffers (parallel reads overlapping the copies). */
 int grz_graph_load_files(grz_graph* g, const char* base);
+/* The same with GRZ_LOAD_DERIVE_PUSH: only `<base>-pull` is read and the -push list is derived
+ * on the device. */
+int grz_graph_load_files_ex(grz_graph* g, const char* base, int flags);
 
 /* The info's pull_list_device / push_list_device point at the reference-format 256-bit
  * vectors.  The engine runs on its own execution layout, so those vectors are derived from it

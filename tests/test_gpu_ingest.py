@@ -84,3 +84,42 @@ def test_derive_rejects_both_lists():
         rc = G.lib.grz_graph_load_pairs_ex(G.h, g.num_vertices, pull.shape[0] // 2, pull.ctypes.data, push.ctypes.data,
                                            native.LOAD_DERIVE_PUSH)
         assert rc == -1  # GRZ_ERR_ARG
+
+
+def test_streamed_file_load(tmp_path):
+    """`<base>-pull` / `<base>-push` streamed through the pinned staging buffers (several 64 MB
+    chunks here) give the lists of an in-memory load; with derive_push only the -pull file is
+    read."""
+    import os
+    from grazelle import graphgen as gg
+    from grazelle.engine import Graph
+    g = gg.rmat(19, seed=41)  # ~8M edges: 128 MB per file
+    base = str(tmp_path / "g")
+    gg.write_grazelle(g, base)
+    with Graph(0) as A, Graph(0) as B, Graph(0) as C:
+        A.load_pairs(g.num_vertices, g.pull_order().pairs(), g.push_order().pairs())
+        B.load_files(base)
+        os.rename(base + "-push", base + "-push.hidden")
+        C.load_files(base, derive_push=True)
+        la, lb, lc = _lists(A), _lists(B), _lists(C)
+        for a, b, c in zip(la, lb, lc):
+            np.testing.assert_array_equal(a, b)
+            np.testing.assert_array_equal(a, c)
+        np.testing.assert_array_equal(B.connected_components(), A.connected_components())
+
+
+def test_file_load_errors(tmp_path):
+    from grazelle import native
+    from grazelle.engine import Graph
+    base = str(tmp_path / "bad")
+    np.array([10, 5, 1, 2], dtype=np.uint64).tofile(base + "-pull")  # header promises 5 edges
+    with Graph(0) as G:
+        with pytest.raises(native.GrzError):
+            G.load_files(base)
+        np.array([10, 1, 3, 2], dtype=np.uint64).tofile(base + "-pull")
+        np.array([11, 1, 3, 2], dtype=np.uint64).tofile(base + "-push")  # V differs
+        with pytest.raises(native.GrzError):
+            G.load_files(base)
+        np.array([10, 2, 3, 2, 1, 1], dtype=np.uint64).tofile(base + "-pull")  # not grouped by dst
+        with pytest.raises(native.GrzError):
+            G.load_files(base, derive_push=True)

@@ -63,3 +63,24 @@ def test_driver_output_matches_reference(app, tmp_path):
         it = rec["bfs_iters"]
         assert "Total Iterations          = %d" % it[0] in r.stdout
         assert "Pull-Based Iterations     = %d" % it[1] in r.stdout
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("app", ["cc", "bfs"])
+def test_driver_derives_a_missing_push_file(app, tmp_path):
+    """Without `<base>-push`, the CC and BFS drivers derive that list on the device and print the
+    same output file and iteration counts as with both files."""
+    import os
+    from grazelle import graphgen as gg
+    rec, g = load_golden("rmat10_s12")
+    both, pull_only = str(tmp_path / "both"), str(tmp_path / "pull")
+    gg.write_grazelle(g, both)
+    gg.write_grazelle(g, pull_only)
+    os.remove(pull_only + "-push")
+    outs = []
+    for base in (both, pull_only):
+        out = tmp_path / (os.path.basename(base) + ".txt")
+        r = run([exe(app), "-i", base, "-o", str(out)])
+        assert r.returncode == 0, r.stdout + r.stderr
+        outs.append((out.read_text(), [l for l in r.stdout.splitlines() if "Iterations" in l]))
+    assert outs[0] == outs[1]

@@ -263,6 +263,7 @@ extern "C" void grz_graph_destroy(grz_graph* g)
     }
     free_graph_data(g);
     cudaStreamSynchronize(g->stream);
+    if (g->stats_dev) cudaFree(g->stats_dev);
     if (g->copy_stream) {
         cudaStreamDestroy(g->copy_stream);
         cudaEventDestroy(g->copy_ev[0]);
@@ -672,7 +673,8 @@ static int frontier_run(grz_graph* g, int app, uint32_t root, int flags, grz_run
     if (!g) return GRZ_ERR_ARG;
     GRZ_CK(g, cudaSetDevice(g->device));
     g->app = app;
-    const bool graph = !(flags & GRZ_FLAG_HOST_LOOP) && !g->prof && g->pull.nvec && g->push.nvec;
+    // the counting of kernel profiling and iteration stats happens on the host loop
+    const bool graph = !(flags & GRZ_FLAG_HOST_LOOP) && !g->prof && !g->stats_on && g->pull.nvec && g->push.nvec;
     if (graph) grz_frontier_run_prepare(g);
     int rc = grz_frontier_init(g, app, flags, root);
     if (rc) return rc;

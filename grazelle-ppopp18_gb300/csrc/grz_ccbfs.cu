@@ -928,11 +928,13 @@ static int edge_phase(grz_graph* g, int pull, uint64_t first, uint64_t count)
             grz_prof_begin(g, GRZ_PROF_PUSH_COMPACT);
             compact(g, f.wants, f.nonempty_pull, g->pull.rowptr);
             grz_prof_end(g);
+            GRZ_TRY(grz_stats_count_selected(g, &g->pull, f.frontier, f.counters));
             grz_prof_begin(g, GRZ_PROF_BFS_PULL);
             k_bfs_pull_expand<<<(unsigned)g->num_sms * 8, T, 0, st>>>(f.frontier, f.voff, f.vdelta, f.tile_first, f.counters,
                                                                      g->pull.nbr, V, f.has, f.cand64, f.touched, f.counters + 1,
                                                                      g->pull.hub_vid, g->pull.nhub, f.has_next); GRZ_COUNT_LAUNCH(g);
         } else {
+            GRZ_TRY(grz_stats_count_range(g, &g->pull, first, count));
             grz_prof_begin(g, bfs ? GRZ_PROF_BFS_PULL : GRZ_PROF_CC_PULL);
         }
         if (bfs && !compacted) {
@@ -955,6 +957,7 @@ static int edge_phase(grz_graph* g, int pull, uint64_t first, uint64_t count)
         grz_prof_begin(g, GRZ_PROF_PUSH_COMPACT);
         compact(g, f.has, f.nonempty_push, g->push.rowptr);
         grz_prof_end(g);
+        GRZ_TRY(grz_stats_count_selected(g, &g->push, f.frontier, f.counters));
         grz_prof_begin(g, bfs ? GRZ_PROF_BFS_PUSH : GRZ_PROF_CC_PUSH);
         const unsigned grid = (unsigned)g->num_sms * 8;
         if (bfs) {

@@ -350,6 +350,10 @@ struct grz_graph {
     int app;              // 0 PR, 1 CC, 2 BFS
     int num_sms;
     int l2_bytes;
+    // iteration stats (grz_stats.cu): vectors and valid lanes the edge phases processed
+    int stats_on;
+    unsigned long long* stats_dev;  // [vectors counted on the device, valid lanes]
+    uint64_t stats_host[1];         // vectors of whole ranges, counted on the host
     uint32_t max_degree;
     int max_degree_known;
     grz_frontier_state fr;
@@ -416,6 +420,7 @@ int grz_set_error(grz_graph* g, int code, const char* fmt, ...);
 int grz_cuda_check(grz_graph* g, cudaError_t e, const char* what);
 int grz_scratch(grz_graph* g, size_t bytes, void** out);
 
+#define GRZ_TRY(expr) do { const int rc_try_ = (expr); if (rc_try_) return rc_try_; } while (0)
 #define GRZ_CK(g, call)                                         \
     do {                                                        \
         cudaError_t e__ = (call);                               \
@@ -448,6 +453,8 @@ void grz_frontier_free(grz_graph* g);
 int grz_build_list(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t E, int shared_is_dst,
                    uint32_t* run_len = nullptr);
 int grz_list_reference(grz_graph* g, grz_list* L);  // reference-format vectors, built on first request
+int grz_stats_count_range(grz_graph* g, const grz_list* L, uint64_t first, uint64_t count);
+int grz_stats_count_selected(grz_graph* g, const grz_list* L, const uint32_t* sel, const uint32_t* counters);
 int grz_build_hubs(grz_graph* g, grz_list* L, uint32_t max_hubs);
 int grz_derive_push_pairs(grz_graph* g, const uint64_t* pull_pairs, uint64_t E, uint64_t* push_out);
 #define GRZ_LOAD_DERIVE_PUSH 1

@@ -86,20 +86,25 @@ def build(verbose: bool = False, jobs: int | None = None, ptxas_verbose: bool = 
     return LIB
 
 
+def build_driver(app: str, experiments=()) -> Path:
+    """The C host driver of one application, with the reference's EXPERIMENTS as
+    -DEXPERIMENT_<name> (Makefile:59-176), e.g. build_driver("cc", ["ITERATION_STATS"])."""
+    srcs = sorted(HOST.glob("*.c"))
+    hdrs = list(HOST.glob("*.h")) + list(INCLUDE.glob("*.h"))
+    exps = sorted(experiments)
+    exe = BUILD / ("grazelle-gb300-" + app + "".join("-" + e.lower() for e in exps))
+    if _newer(exe, srcs + hdrs + [LIB]):
+        _run(["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-D" + APPS[app]] + ["-DEXPERIMENT_" + e for e in exps]
+             + ["-I", str(INCLUDE), "-I", str(HOST), "-o", str(exe)]
+             + [str(s) for s in srcs] + ["-L", str(BUILD), "-lgrazelle_gb300", "-Wl,-rpath," + str(BUILD), "-lm"])
+    return exe
+
+
 def build_drivers() -> list[Path]:
     """C host driver, one binary per application (compile-time selection as in the reference)."""
-    srcs = sorted(HOST.glob("*.c"))
-    if not srcs:
+    if not sorted(HOST.glob("*.c")):
         return []
-    hdrs = list(HOST.glob("*.h")) + list(INCLUDE.glob("*.h"))
-    out = []
-    for app, macro in APPS.items():
-        exe = BUILD / ("grazelle-gb300-" + app)
-        out.append(exe)
-        if _newer(exe, srcs + hdrs + [LIB]):
-            _run(["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-D" + macro, "-I", str(INCLUDE), "-I", str(HOST), "-o", str(exe)]
-                 + [str(s) for s in srcs] + ["-L", str(BUILD), "-lgrazelle_gb300", "-Wl,-rpath," + str(BUILD), "-lm"])
-    return out
+    return [build_driver(app) for app in APPS]
 
 
 if __name__ == "__main__":

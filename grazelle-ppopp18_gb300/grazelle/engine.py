@@ -161,6 +161,22 @@ class Graph:
         self._ck(self.lib.grz_graph_copy_outdegrees(self.h, _ptr(out), out.shape[0]))
         return out
 
+    def vector_model(self, list_id: int, lanes: int) -> int:
+        """Vectors the list would need with `lanes`-wide vectors (the reference's MODEL_LONG_VECTORS)."""
+        n = C.c_uint64()
+        self._ck(self.lib.grz_graph_vector_model(self.h, list_id, lanes, C.byref(n)))
+        return n.value
+
+    def stats_enable(self, on: bool = True):
+        """Per-phase counts of processed vectors and their edges (the reference's ITERATION_STATS)."""
+        self._ck(self.lib.grz_stats_enable(self.h, 1 if on else 0))
+        return self
+
+    def stats_take(self) -> tuple[int, int]:
+        v, e = C.c_uint64(), C.c_uint64()
+        self._ck(self.lib.grz_stats_take(self.h, C.byref(v), C.byref(e)))
+        return v.value, e.value
+
     # ------------------------------------------------------------------ PageRank
     def pr_init(self, damping: float = 0.875):
         self._ck(self.lib.grz_pr_init(self.h, damping))

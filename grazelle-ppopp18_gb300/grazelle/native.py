@@ -66,6 +66,9 @@ SIGNATURES = {
     "grz_graph_load_pairs": (_I, [_VP, _U64, _U64, _VP, _VP]),
     "grz_graph_load_files": (_I, [_VP, C.c_char_p]),
     "grz_graph_load_files_ex": (_I, [_VP, C.c_char_p, _I]),
+    "grz_stats_enable": (_I, [_VP, _I]),
+    "grz_stats_take": (_I, [_VP, C.POINTER(_U64), C.POINTER(_U64)]),
+    "grz_graph_vector_model": (_I, [_VP, _I, C.c_uint32, C.POINTER(_U64)]),
     "grz_graph_get_info": (_I, [_VP, C.POINTER(GraphInfo)]),
     "grz_graph_copy_list": (_I, [_VP, _I, _VP, _U64]),
     "grz_graph_copy_vertex_index": (_I, [_VP, _I, _VP, _U64]),

@@ -174,6 +174,27 @@ static void gpu_or_die(int rc, grz_graph* g, const char* what)
 
 static uint64_t total_iterations, iterations_pull, iterations_push;
 
+#ifdef EXPERIMENT_ITERATION_STATS
+/* vectors and edges the edge phase processed in each iteration (execution_cc.c:209-231) */
+static uint64_t* stat_vectors;
+static uint64_t* stat_edges;
+static uint64_t stat_cap;
+
+static void stats_record(grz_graph* g, uint64_t iteration)
+{
+    uint64_t v = 0, e = 0;
+    gpu_or_die(grz_stats_take(g, &v, &e), g, "iteration stats");
+    if (iteration >= stat_cap) {
+        stat_cap = stat_cap ? 2 * stat_cap : 64;
+        stat_vectors = (uint64_t*)realloc(stat_vectors, sizeof(uint64_t) * stat_cap);
+        stat_edges = (uint64_t*)realloc(stat_edges, sizeof(uint64_t) * stat_cap);
+        if (!stat_vectors || !stat_edges) { fprintf(stderr, "Error: out of memory\n"); exit(255); }
+    }
+    stat_vectors[iteration] = v;
+    stat_edges[iteration] = e;
+}
+#endif
+
 static void execution_impl(grz_graph* g, const grz_graph_info_t* info, const opts_t* o)
 {
     uint64_t reduce_buffer[8] = { 0, 0, 0, 0, 0, 0, 0, 0 };  /* sz_reduce_buffer for one thread, execution_*.c:37-45 */
@@ -219,6 +240,9 @@ static void execution_impl(grz_graph* g, const grz_graph_info_t* info, const opt
     uint64_t converge_vote = 0;
     gpu_or_die(grz_frontier_current_vote(g, &converge_vote, NULL), g, "initial vote");
     (void)o;
+#ifdef EXPERIMENT_ITERATION_STATS
+    gpu_or_die(grz_stats_enable(g, 1), g, "iteration stats");
+#endif
     for (;;) {
         total_iterations += 1;
 #if defined(EXPERIMENT_EDGE_FORCE_PULL)
@@ -240,6 +264,9 @@ static void execution_impl(grz_graph* g, const grz_graph_info_t* info, const opt
         }
         phase_op_write_global_accum_to_buf(reduce_buffer);
         converge_vote = phase_op_combine_global_var_from_buf(reduce_buffer);
+#ifdef EXPERIMENT_ITERATION_STATS
+        stats_record(g, total_iterations - 1);
+#endif
         if (0 == converge_vote) break;
         perform_vertex_phase(0, info->num_vertices, NULL);
     }
@@ -257,6 +284,7 @@ int main(int argc, char** argv)
     gpu_or_die(grz_graph_create(&g, o.device, NULL), NULL, "GPU");
     const double t_load = now_ms();
 #if APP == GRZ_APP_PAGERANK
+    (void)have_push;
     gpu_or_die(grz_graph_load_files(g, o.input), g, "load");
 #else
     /* CC and BFS need the -push list: without the file, it is derived on the device */
@@ -269,7 +297,28 @@ int main(int argc, char** argv)
     if (info.push_vectors)
         printf("Out-edges: created %llu vectors, efficiency = %.1lf%%\n", (unsigned long long)info.push_vectors,
                (double)info.num_edges / (double)info.push_vectors / 4.0 * 100.0);
+#ifdef EXPERIMENT_MODEL_LONG_VECTORS
+    /* graphdata.c:919-923, 946-950: the same lists with 8- and 16-lane vectors */
+    {
+        const int lists[2] = { GRZ_LIST_PULL, GRZ_LIST_PUSH };
+        const char* names[2] = { "In-edges: ", "Out-edges:" };
+        for (int l = 0; l < 2; ++l) {
+            if (l == 1 && !info.push_vectors) break;
+            for (uint32_t lanes = 8; lanes <= 16; lanes *= 2) {
+                uint64_t n = 0;
+                gpu_or_die(grz_graph_vector_model(g, lists[l], lanes, &n), g, "vector model");
+                printf("%s VL%u: created %llu vectors, efficiency = %.1lf%%\n", names[l], lanes, (unsigned long long)n,
+                       (double)info.num_edges / (double)n / (double)lanes * 100.0);
+            }
+        }
+    }
+#endif
     printf("Loading graph took %.2lfms.\n", now_ms() - t_load);
+#ifdef EXPERIMENT_MODEL_LONG_VECTORS
+    printf("Not executing application, since this was a modelling experiment.\n");
+    grz_graph_destroy(g);
+    return 0;
+#endif
 #if APP == GRZ_APP_PAGERANK
     gpu_or_die(grz_pr_init(g, 0.875), g, "PageRank init");
 #endif
@@ -302,6 +351,15 @@ int main(int argc, char** argv)
     printf("%-25s = %llu\n", "Pull-Based Iterations", (unsigned long long)iterations_pull);
     printf("%-25s = %llu\n", "Push-Based Iterations", (unsigned long long)iterations_push);
     printf("----------------------------------------------\n");
+#if defined(EXPERIMENT_ITERATION_STATS) && APP != GRZ_APP_PAGERANK
+    /* main.c:147-157 */
+    fprintf(stderr, "%s,%s,%s\n", "Iteration", "# Vectors", "Packing Efficiency");
+    for (uint64_t i = 0; i < total_iterations; ++i) {
+        const uint64_t nv = stat_vectors[i];
+        const double eff = nv == 0 ? 0.0 : (double)stat_edges[i] / (4.0 * (double)nv);
+        fprintf(stderr, "%llu,%llu,%lf\n", (unsigned long long)(1 + i), (unsigned long long)nv, eff);
+    }
+#endif
 
     if (o.output) {
         /* graph_data_write_ranks_to_file, source/graphdata.c:1119-1138 */

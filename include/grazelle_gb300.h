@@ -104,6 +104,15 @@ int grz_graph_copy_list(grz_graph* g, int list, uint64_t* host_vectors, uint64_t
 int grz_graph_copy_vertex_index(grz_graph* g, int list, uint64_t* host_index, uint64_t capacity);
 int grz_graph_copy_outdegrees(grz_graph* g, double* host_outdeg, uint64_t capacity);
 
+/* The reference's measurement experiments.  ITERATION_STATS (source/execution_cc.c:209-231):
+ * while enabled, the CC/BFS edge phases count the vectors they process and those vectors'
+ * valid lanes; grz_stats_take returns the counts since the last take and resets them (packing
+ * efficiency = edges / (4 vectors)).  MODEL_LONG_VECTORS (source/graphdata.c:628-675): the
+ * vectors a list would need with `lanes`-wide vectors. */
+int grz_stats_enable(grz_graph* g, int on);
+int grz_stats_take(grz_graph* g, uint64_t* vectors, uint64_t* edges);
+int grz_graph_vector_model(grz_graph* g, int list, uint32_t lanes, uint64_t* vectors);
+
 /* PageRank (FP64 props; exact fixed-point accumulation).  damping 0.875 reproduces the
  * reference's hard-coded constant (source/constants.asm:75-79). */
 int grz_pr_init(grz_graph* g, double damping);

@@ -123,3 +123,50 @@ def test_file_load_errors(tmp_path):
         np.array([10, 2, 3, 2, 1, 1], dtype=np.uint64).tofile(base + "-pull")  # not grouped by dst
         with pytest.raises(native.GrzError):
             G.load_files(base, derive_push=True)
+
+
+def test_vector_model_and_iteration_stats():
+    """MODEL_LONG_VECTORS: vectors at 4, 8 and 16 lanes are sums of ceil(run / lanes) over the
+    shared vertices.  ITERATION_STATS: a pull iteration processes every pull vector and all E
+    edges; a push iteration the frontier's out-vectors (the first CC push: all of them)."""
+    from grazelle import graphgen as gg
+    from grazelle import native
+    g = gg.rmat(14, seed=51)
+    pull, push = g.pull_order().pairs(), g.push_order().pairs()
+    V, E = g.num_vertices, g.num_edges
+    indeg = np.bincount(pull[1::2].astype(np.int64), minlength=V)
+    outdeg = np.bincount(push[0::2].astype(np.int64), minlength=V)
+    with _graph(V, pull, push) as G:
+        info = G.info()
+        assert G.vector_model(native.LIST_PULL, 4) == info.pull_vectors
+        assert G.vector_model(native.LIST_PUSH, 4) == info.push_vectors
+        for lanes in (8, 16):
+            assert G.vector_model(native.LIST_PULL, lanes) == int(np.sum((indeg + lanes - 1) // lanes))
+            assert G.vector_model(native.LIST_PUSH, lanes) == int(np.sum((outdeg + lanes - 1) // lanes))
+        G.stats_enable(True)
+        for app in (native.APP_CONNECTED_COMPONENTS, native.APP_BREADTH_FIRST_SEARCH):
+            G.frontier_begin(app, 0, native.FORCE_PUSH if app == native.APP_CONNECTED_COMPONENTS else 0)
+            first = True
+            for _ in range(200):
+                running, used, _ = G.frontier_next()
+                v, e = G.stats_take()
+                if used == 1:  # pull
+                    if app == native.APP_CONNECTED_COMPONENTS:
+                        assert (v, e) == (info.pull_vectors, E)
+                    else:
+                        assert v <= info.pull_vectors and v <= e <= 4 * v
+                else:
+                    if first and app == native.APP_CONNECTED_COMPONENTS:
+                        assert (v, e) == (info.push_vectors, E)  # every vertex starts in the frontier
+                    assert v <= info.push_vectors and v <= e <= 4 * v
+                first = False
+                if not running:
+                    break
+        G.stats_enable(False)
+
+
+def _graph(V, pull, push):
+    from grazelle.engine import Graph
+    G = Graph(0)
+    G.load_pairs(V, pull, push)
+    return G

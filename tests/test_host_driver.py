@@ -84,3 +84,32 @@ def test_driver_derives_a_missing_push_file(app, tmp_path):
         assert r.returncode == 0, r.stdout + r.stderr
         outs.append((out.read_text(), [l for l in r.stdout.splitlines() if "Iterations" in l]))
     assert outs[0] == outs[1]
+
+
+@pytest.mark.gpu
+def test_driver_experiments_iteration_stats_and_long_vectors(tmp_path):
+    """EXPERIMENT_ITERATION_STATS prints the reference's per-iteration CSV to stderr (one row per
+    iteration); EXPERIMENT_MODEL_LONG_VECTORS prints the 8- and 16-lane vector counts and stops."""
+    from grazelle import build
+    from grazelle import graphgen as gg
+    rec, g = load_golden("rmat10_s12")
+    base = str(tmp_path / "g")
+    gg.write_grazelle(g, base)
+    build.build()
+    r = run([str(build.build_driver("cc", ["ITERATION_STATS"])), "-i", base])
+    assert r.returncode == 0, r.stdout + r.stderr
+    rows = [l for l in r.stderr.splitlines() if l and l[0].isdigit()]
+    assert r.stderr.splitlines()[0] == "Iteration,# Vectors,Packing Efficiency"
+    total = int([l for l in r.stdout.splitlines() if l.startswith("Total Iterations")][0].split("=")[1])
+    assert len(rows) == total
+    for i, row in enumerate(rows):
+        it, nv, eff = row.split(",")
+        assert int(it) == i + 1 and int(nv) >= 0 and 0.0 <= float(eff) <= 1.0
+    r = run([str(build.build_driver("bfs", ["MODEL_LONG_VECTORS"])), "-i", base])
+    assert r.returncode == 0, r.stdout + r.stderr
+    pull = g.pull_order().pairs()
+    indeg = np.bincount(pull[1::2].astype(np.int64), minlength=g.num_vertices)
+    for lanes in (8, 16):
+        n = int(np.sum((indeg + lanes - 1) // lanes))
+        assert "In-edges:  VL%d: created %d vectors" % (lanes, n) in r.stdout
+    assert "Not executing application" in r.stdout and "EXECUTION STATISTICS" not in r.stdout

@@ -290,8 +290,20 @@ static bool is_device_ptr(const void* p)
     return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
 }
 
+// the device's address of page-locked host memory, or null for any other pointer
+static const void* pinned_device_view(const void* p)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 static int load_pairs(grz_graph* g, uint64_t V, uint64_t E, const uint64_t* pull_pairs, const uint64_t* push_pairs,
                       int flags);
+static int finish_load(grz_graph* g, int rc);
 
 extern "C" int grz_graph_load_pairs(grz_graph* g, uint64_t V, uint64_t E, const uint64_t* pull_pairs,
                                     const uint64_t* push_pairs)
@@ -319,6 +331,24 @@ static int load_pairs(grz_graph* g, uint64_t V, uint64_t E, const uint64_t* pull
     cudaStream_t st = g->stream;
     const size_t pbytes = sizeof(uint64_t) * 2 * E;
     int rc = GRZ_OK;
+    if ((flags & GRZ_LOAD_DERIVE_PUSH) && !push_pairs && E > 0) {
+        // Pull-only ingest: one fused pass reads the pairs where they are (pinned host memory over
+        // the link, or device memory) and both lists and the outdegrees follow on the device.
+        // Pageable host memory is first copied into a device buffer.
+        const void* view = is_device_ptr(pull_pairs) ? (const void*)pull_pairs : pinned_device_view(pull_pairs);
+        void* dbuf = nullptr;
+        if (!view) {
+            rc = grz_dev_alloc(g, &dbuf, pbytes);
+            if (rc == GRZ_OK) rc = grz_cuda_check(g, cudaMemcpyAsync(dbuf, pull_pairs, pbytes, cudaMemcpyHostToDevice, st), "H2D pull pairs");
+            view = dbuf;
+        }
+        const bool on_device = dbuf != nullptr || is_device_ptr(pull_pairs);
+        if (rc == GRZ_OK) rc = grz_ingest_pull_derive(g, (const uint64_t*)view, E, on_device ? 1 : 0);
+        if (rc == GRZ_OK) rc = grz_build_hubs(g, &g->pull, g->tune.hub_max);
+        if (rc == GRZ_OK) rc = grz_cuda_check(g, cudaStreamSynchronize(st), "layout build");
+        grz_dev_free(g, dbuf);
+        return finish_load(g, rc);
+    }
     // Host lists are copied into device buffers.  The -push copy runs on a second stream after the
     // -pull copy, so it overlaps the -pull list's build instead of following it.
     const uint64_t* dsrc[2] = { pull_pairs, push_pairs };
@@ -347,37 +377,28 @@ static int load_pairs(grz_graph* g, uint64_t V, uint64_t E, const uint64_t* pull
         if (e != cudaSuccess) rc = grz_cuda_check(g, e, "H2D push pairs");
         else { dsrc[1] = (const uint64_t*)dbuf[1]; push_on_copy_stream = true; }
     }
-    const bool derive = (flags & GRZ_LOAD_DERIVE_PUSH) && !push_pairs && E > 0;
     for (int which = 0; which < 2 && rc == GRZ_OK; ++which) {
-        if (which == 1 && derive) {
-            // the -push order from the -pull pairs already on the device (stable sort by source)
-            rc = grz_dev_alloc(g, &dbuf[1], pbytes);
-            if (rc == GRZ_OK) rc = grz_derive_push_pairs(g, dsrc[0], E, (uint64_t*)dbuf[1]);
-            if (rc != GRZ_OK) break;
-            dsrc[1] = (const uint64_t*)dbuf[1];
-        }
-        if (which == 1 && !push_pairs && !derive) break;
+        if (which == 1 && !push_pairs) break;
         if (which == 1 && push_on_copy_stream) {
             cudaError_t e = cudaStreamWaitEvent(st, g->copy_ev[1], 0);
             if (e != cudaSuccess) { rc = grz_cuda_check(g, e, "wait for push pairs"); break; }
         }
-        // Outdegrees credit the sources of the -pull pairs (graphdata.c:792-821).  A -push list
-        // derived from those pairs holds the same edges, so its run lengths are the outdegrees
-        // and no counting pass is needed.
-        uint32_t* run_len = nullptr;
-        if (which == 1 && derive) {
-            rc = grz_alloc_outdegrees(g);
-            if (rc != GRZ_OK) break;
-            run_len = g->degree;
-        }
-        rc = grz_build_list(g, which == 0 ? &g->pull : &g->push, dsrc[which], E, which == 0 ? 1 : 0, run_len);
-        const bool degrees_now = (which == 0 && !derive) || (which == 1 && derive);
-        if (rc == GRZ_OK && degrees_now) rc = grz_build_outdegrees(g, which == 0 ? dsrc[0] : nullptr, E);
-        if (rc == GRZ_OK && degrees_now) rc = grz_build_hubs(g, &g->pull, g->tune.hub_max);
+        // outdegrees credit the sources of the -pull pairs (graphdata.c:792-821)
+        rc = grz_build_list(g, which == 0 ? &g->pull : &g->push, dsrc[which], E, which == 0 ? 1 : 0);
+        if (rc == GRZ_OK && which == 0) rc = grz_build_outdegrees(g, dsrc[0], E);
+        if (rc == GRZ_OK && which == 0) rc = grz_build_hubs(g, &g->pull, g->tune.hub_max);
         if (rc == GRZ_OK) rc = grz_cuda_check(g, cudaStreamSynchronize(st), "layout build");
     }
     if (push_on_copy_stream && rc != GRZ_OK) cudaStreamSynchronize(g->copy_stream);
     for (void* p : dbuf) grz_dev_free(g, p);
+    return finish_load(g, rc);
+}
+
+// per-vertex state of a loaded graph (or, on a failed load, nothing)
+static int finish_load(grz_graph* g, int rc)
+{
+    const uint64_t V = g->V;
+    cudaStream_t st = g->stream;
     if (rc == GRZ_OK) {
         if ((rc = grz_dev_alloc(g, (void**)&g->prop, sizeof(double) * (V + 8))) == GRZ_OK &&
             (rc = grz_dev_alloc(g, (void**)&g->accum, sizeof(double) * (V + 8))) == GRZ_OK &&

@@ -190,13 +190,52 @@ __global__ void k_degree_to_double(const uint32_t* __restrict__ degree, uint64_t
 
 }  // namespace
 
+// The rest of a list build once the run bounds [start, end) of every shared vertex are known
+// (k_group_bounds, or the fused ingest of grz_sort.cu): vector offsets, vectors, vertex index.
+// last_shared: the shared vertex of the last edge; first_shared: of the first.
+int grz_build_list_from_bounds(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t E, int shared_is_dst,
+                               const uint32_t* start, const uint32_t* end, uint64_t first_shared, uint64_t last_shared,
+                               uint32_t* run_len)
+{
+    const uint64_t V = g->V;
+    cudaStream_t st = g->stream;
+    const uint64_t vi_count = V + 64;
+    uint32_t *cnt = nullptr, *tot = nullptr;
+    uint32_t nv32 = 0;
+    int rc = GRZ_OK;
+#define LCK(call) do { cudaError_t e__ = (call); if (e__ != cudaSuccess) { rc = grz_cuda_check(g, e__, #call); goto done; } } while (0)
+    LCK(cudaMallocAsync((void**)&cnt, sizeof(uint32_t) * (V + 1), st));
+    LCK(cudaMallocAsync((void**)&tot, sizeof(uint32_t), st));
+    k_group_vectors<<<grid_blocks_for(V + 1), BT, 0, st>>>(start, end, V, cnt, run_len); GRZ_COUNT_LAUNCH(g);
+    LCK(cudaGetLastError());
+    rc = grz_exclusive_sum_u32(g, cnt, L->rowptr, V + 1, tot);
+    if (rc) goto done;
+    LCK(cudaMemcpyAsync(&nv32, tot, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    LCK(cudaStreamSynchronize(st));
+    L->nvec = nv32;
+    LCK(cudaMallocAsync((void**)&L->nbr, sizeof(uint4) * L->nvec, st));
+    LCK(cudaMallocAsync((void**)&L->shared, sizeof(uint32_t) * L->nvec, st));
+    k_vector_write<<<grid_blocks_for(E), BT, 0, st>>>(d_pairs, E, shared_is_dst, start, end, L->rowptr, L->nbr, L->shared); GRZ_COUNT_LAUNCH(g);
+    LCK(cudaGetLastError());
+    k_vindex<<<grid_blocks_for(vi_count), BT, 0, st>>>(start, end, L->rowptr, V, vi_count, last_shared, L->vindex); GRZ_COUNT_LAUNCH(g);
+    LCK(cudaGetLastError());
+    L->vindex_start = first_shared;
+    L->vindex_end = last_shared;
+    L->vs = nullptr;  // reference-format vectors: on first request
+done:
+    if (cnt) cudaFreeAsync(cnt, st);
+    if (tot) cudaFreeAsync(tot, st);
+#undef LCK
+    return rc;
+}
+
 int grz_build_list(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t E, int shared_is_dst, uint32_t* run_len)
 {
     const uint64_t V = g->V;
     cudaStream_t st = g->stream;
     if (E >= 0xffffffffull) return grz_set_error(g, GRZ_ERR_RANGE, "edge count %llu too large (limit 2^32-2)", (unsigned long long)E);
     const uint64_t vi_count = V + 64;
-    uint32_t *start = nullptr, *end = nullptr, *cnt = nullptr, *tot = nullptr;
+    uint32_t *start = nullptr, *end = nullptr;
     unsigned* flags = nullptr;
     int rc = GRZ_OK;
 #define LCK(call) do { cudaError_t e__ = (call); if (e__ != cudaSuccess) { rc = grz_cuda_check(g, e__, #call); goto done; } } while (0)
@@ -214,13 +253,10 @@ int grz_build_list(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t 
     } else {
         unsigned flags_h[2] = { 0, 0 };
         uint64_t ends_h[2] = { 0, 0 };
-        uint32_t nv32 = 0;
         const int sh = shared_is_dst ? 1 : 0;
         LCK(cudaMallocAsync((void**)&flags, 2 * sizeof(unsigned), st));
         LCK(cudaMallocAsync((void**)&start, sizeof(uint32_t) * (V + 1), st));
         LCK(cudaMallocAsync((void**)&end, sizeof(uint32_t) * (V + 1), st));
-        LCK(cudaMallocAsync((void**)&cnt, sizeof(uint32_t) * (V + 1), st));
-        LCK(cudaMallocAsync((void**)&tot, sizeof(uint32_t), st));
         LCK(cudaMemsetAsync(flags, 0, 2 * sizeof(unsigned), st));
         LCK(cudaMemsetAsync(start, 0, sizeof(uint32_t) * (V + 1), st));
         LCK(cudaMemsetAsync(end, 0, sizeof(uint32_t) * (V + 1), st));
@@ -232,25 +268,10 @@ int grz_build_list(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t 
         LCK(cudaStreamSynchronize(st));
         if (flags_h[0]) { rc = grz_set_error(g, GRZ_ERR_UNSORTED, "%s list is not grouped by %s in ascending order", shared_is_dst ? "pull" : "push", shared_is_dst ? "destination" : "source"); goto done; }
         if (flags_h[1]) { rc = grz_set_error(g, GRZ_ERR_RANGE, "%s list holds a vertex ID >= V (%llu)", shared_is_dst ? "pull" : "push", (unsigned long long)V); goto done; }
-        k_group_vectors<<<grid_blocks_for(V + 1), BT, 0, st>>>(start, end, V, cnt, run_len); GRZ_COUNT_LAUNCH(g);
-        LCK(cudaGetLastError());
-        rc = grz_exclusive_sum_u32(g, cnt, L->rowptr, V + 1, tot);
-        if (rc) goto done;
-        LCK(cudaMemcpyAsync(&nv32, tot, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-        LCK(cudaStreamSynchronize(st));
-        L->nvec = nv32;
-        LCK(cudaMallocAsync((void**)&L->nbr, sizeof(uint4) * L->nvec, st));
-        LCK(cudaMallocAsync((void**)&L->shared, sizeof(uint32_t) * L->nvec, st));
-        k_vector_write<<<grid_blocks_for(E), BT, 0, st>>>(d_pairs, E, shared_is_dst, start, end, L->rowptr, L->nbr, L->shared); GRZ_COUNT_LAUNCH(g);
-        LCK(cudaGetLastError());
-        k_vindex<<<grid_blocks_for(vi_count), BT, 0, st>>>(start, end, L->rowptr, V, vi_count, ends_h[1], L->vindex); GRZ_COUNT_LAUNCH(g);
-        LCK(cudaGetLastError());
-        L->vindex_start = ends_h[0];
-        L->vindex_end = ends_h[1];
-        L->vs = nullptr;  // reference-format vectors: on first request
+        rc = grz_build_list_from_bounds(g, L, d_pairs, E, shared_is_dst, start, end, ends_h[0], ends_h[1], run_len);
     }
 done:
-    for (void* p : { (void*)flags, (void*)start, (void*)end, (void*)cnt, (void*)tot })
+    for (void* p : { (void*)flags, (void*)start, (void*)end })
         if (p) cudaFreeAsync(p, st);
 #undef LCK
     if (rc == GRZ_OK) rc = grz_cuda_check(g, cudaStreamSynchronize(st), "build list");

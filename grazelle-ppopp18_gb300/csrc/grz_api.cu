@@ -342,8 +342,7 @@ static int load_pairs(grz_graph* g, uint64_t V, uint64_t E, const uint64_t* pull
             if (rc == GRZ_OK) rc = grz_cuda_check(g, cudaMemcpyAsync(dbuf, pull_pairs, pbytes, cudaMemcpyHostToDevice, st), "H2D pull pairs");
             view = dbuf;
         }
-        const bool on_device = dbuf != nullptr || is_device_ptr(pull_pairs);
-        if (rc == GRZ_OK) rc = grz_ingest_pull_derive(g, (const uint64_t*)view, E, on_device ? 1 : 0);
+        if (rc == GRZ_OK) rc = grz_ingest_pull_derive(g, (const uint64_t*)view, E);
         if (rc == GRZ_OK) rc = grz_build_hubs(g, &g->pull, g->tune.hub_max);
         if (rc == GRZ_OK) rc = grz_cuda_check(g, cudaStreamSynchronize(st), "layout build");
         grz_dev_free(g, dbuf);

@@ -457,10 +457,10 @@ int grz_stats_count_range(grz_graph* g, const grz_list* L, uint64_t first, uint6
 int grz_stats_count_selected(grz_graph* g, const grz_list* L, const uint32_t* sel, const uint32_t* counters);
 int grz_build_hubs(grz_graph* g, grz_list* L, uint32_t max_hubs);
 // both lists and the outdegrees from E > 0 -pull pairs in pinned host or device memory (grz_sort.cu)
-int grz_ingest_pull_derive(grz_graph* g, const uint64_t* pull, uint64_t E, int on_device);
+int grz_ingest_pull_derive(grz_graph* g, const uint64_t* pull, uint64_t E);
 int grz_build_list_from_bounds(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t E, int shared_is_dst,
                                const uint32_t* start, const uint32_t* end, uint64_t first_shared, uint64_t last_shared,
-                               uint32_t* run_len);
+                               uint32_t* run_len, const unsigned long long* keys);
 #define GRZ_LOAD_DERIVE_PUSH 1
 int grz_alloc_outdegrees(grz_graph* g);
 int grz_build_outdegrees(grz_graph* g, const uint64_t* d_pull_pairs, uint64_t E);

@@ -7,11 +7,12 @@
 // source, and a stable sort keeps that.  Duplicate edges are kept, as the reference keeps them.
 //
 // 1. One fused pass reads the -pull pairs where they are (pinned host memory over the host link,
-//    or device memory) and, while the link is the bottleneck, also writes the device copy of the
-//    pairs, the sort keys (src << 32 | dst), the run bounds of every destination (the -pull
-//    list's first build step), the per-tile histogram of the first radix digit, and the
+//    or device memory) and, while the link is the bottleneck, also writes the sort keys
+//    (src << 32 | dst, the pairs in half the bytes), the run bounds of every destination (the
+//    -pull list's first build step), the per-tile histogram of the first radix digit, and the
 //    outdegrees (graphdata.c:792-821 credits the sources of the -pull list).
-// 2. The -pull list is finished from the run bounds (grz_build_list_from_bounds).
+// 2. The -pull list is finished from the run bounds and the keys (grz_build_list_from_bounds),
+//    before the sort permutes them.
 // 3. The -push list's offsets come from the outdegrees: its runs are the sources' out-edges.
 // 4. LSD radix sort over the source's 8-bit digits (as many passes as V needs): per pass,
 //    per-tile digit histograms, one exclusive scan in (digit, tile) order, and a stable scatter
@@ -34,9 +35,8 @@ static_assert(ST == RBINS, "the histogram and digit passes give each thread one 
 
 // Step 1 over one tile of STILE pairs.  The tile's destinations go through shared memory so that
 // each pair crosses the link once; only the two neighbours outside the tile are read again.
-template <bool Copy>
 __global__ void __launch_bounds__(ST) k_ingest(const ulonglong2* __restrict__ in, uint64_t E, uint64_t V,
-                                              ulonglong2* __restrict__ pairs_out, unsigned long long* __restrict__ keys,
+                                              unsigned long long* __restrict__ keys,
                                               uint32_t* __restrict__ start, uint32_t* __restrict__ end,
                                               uint32_t* __restrict__ deg, uint32_t ntiles, uint32_t* __restrict__ hist,
                                               unsigned* __restrict__ flags)
@@ -63,7 +63,6 @@ __global__ void __launch_bounds__(ST) k_ingest(const ulonglong2* __restrict__ in
         const uint64_t s = p[c].x, d = p[c].y;
         const uint64_t dp = i > 0 ? s_dst[i - 1] : (e > 0 ? in[e - 1].y : d);
         const uint64_t dn = i + 1 < STILE ? s_dst[i + 1] : (e + 1 < E ? in[e + 1].y : d);
-        if (Copy) pairs_out[e] = p[c];
         keys[e] = (s << 32) | (d & 0xffffffffull);
         if (s >= V || d >= V) bad_range = true;
         if (e > 0 && dp > d) bad_order = true;
@@ -248,9 +247,9 @@ inline unsigned blocks_of(uint64_t n) { return (unsigned)((n + ST - 1) / ST); }
 }  // namespace
 
 // Both lists and the outdegrees from E > 0 -pull pairs at `pull` (pinned host memory or device
-// memory; on_device: no device copy of the pairs is made).  Temporaries come from the graph's
-// pool; g->pull, g->push and the outdegree arrays must be empty.
-int grz_ingest_pull_derive(grz_graph* g, const uint64_t* pull, uint64_t E, int on_device)
+// memory).  Temporaries come from the graph's pool; g->pull, g->push and the outdegree arrays
+// must be empty.
+int grz_ingest_pull_derive(grz_graph* g, const uint64_t* pull, uint64_t E)
 {
     const uint64_t V = g->V;
     cudaStream_t st = g->stream;
@@ -262,7 +261,6 @@ int grz_ingest_pull_derive(grz_graph* g, const uint64_t* pull, uint64_t E, int o
     const uint64_t vi_count = V + 64;
     grz_list* P = &g->pull;
     grz_list* Q = &g->push;
-    ulonglong2* dpairs = nullptr;
     unsigned long long *ka = nullptr, *kb = nullptr;
     uint32_t *hist = nullptr, *start = nullptr, *end = nullptr, *pstart = nullptr, *cnt = nullptr, *tot = nullptr;
     unsigned* flags = nullptr;
@@ -273,7 +271,6 @@ int grz_ingest_pull_derive(grz_graph* g, const uint64_t* pull, uint64_t E, int o
     int rc = GRZ_OK;
 #define ICK(call) do { cudaError_t e__ = (call); if (e__ != cudaSuccess) { rc = grz_cuda_check(g, e__, #call); goto done; } } while (0)
 #define IRC(expr) do { rc = (expr); if (rc) goto done; } while (0)
-    if (!on_device) IRC(grz_dev_alloc(g, (void**)&dpairs, sizeof(ulonglong2) * E));
     IRC(grz_dev_alloc(g, (void**)&ka, sizeof(unsigned long long) * E));
     if (passes > 1) IRC(grz_dev_alloc(g, (void**)&kb, sizeof(unsigned long long) * E));
     IRC(grz_dev_alloc(g, (void**)&hist, sizeof(uint32_t) * RBINS * (uint64_t)ntiles));
@@ -285,26 +282,23 @@ int grz_ingest_pull_derive(grz_graph* g, const uint64_t* pull, uint64_t E, int o
     ICK(cudaMemsetAsync(end, 0, sizeof(uint32_t) * (V + 1), st));
     ICK(cudaMemsetAsync(flags, 0, sizeof(unsigned) * 2, st));
     // 1. the fused pass over the pairs
-    if (on_device)
-        k_ingest<false><<<ntiles, ST, 0, st>>>(reinterpret_cast<const ulonglong2*>(pull), E, V, nullptr, ka, start, end,
-                                               g->degree, ntiles, hist, flags);
-    else
-        k_ingest<true><<<ntiles, ST, 0, st>>>(reinterpret_cast<const ulonglong2*>(pull), E, V, dpairs, ka, start, end,
-                                              g->degree, ntiles, hist, flags);
-    GRZ_COUNT_LAUNCH(g);
+    k_ingest<<<ntiles, ST, 0, st>>>(reinterpret_cast<const ulonglong2*>(pull), E, V, ka, start, end, g->degree, ntiles,
+                                    hist, flags); GRZ_COUNT_LAUNCH(g);
     ICK(cudaGetLastError());
     {
-        const uint64_t* dp = on_device ? pull : reinterpret_cast<const uint64_t*>(dpairs);
+        unsigned long long kends[2] = { 0, 0 };
         ICK(cudaMemcpyAsync(flags_h, flags, sizeof(flags_h), cudaMemcpyDeviceToHost, st));
-        ICK(cudaMemcpyAsync(&ends_h[0], dp + 1, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
-        ICK(cudaMemcpyAsync(&ends_h[1], dp + 2 * (E - 1) + 1, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+        ICK(cudaMemcpyAsync(&kends[0], ka, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        ICK(cudaMemcpyAsync(&kends[1], ka + (E - 1), sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
         ICK(cudaStreamSynchronize(st));
+        ends_h[0] = kends[0] & 0xffffffffull;  // first and last destination
+        ends_h[1] = kends[1] & 0xffffffffull;
         if (flags_h[0]) { rc = grz_set_error(g, GRZ_ERR_UNSORTED, "pull list is not grouped by destination in ascending order"); goto done; }
         if (flags_h[1]) { rc = grz_set_error(g, GRZ_ERR_RANGE, "pull list holds a vertex ID >= V (%llu)", (unsigned long long)V); goto done; }
         // 2. the -pull list from its run bounds
         ICK(cudaMallocAsync((void**)&P->vindex, sizeof(uint64_t) * vi_count, st));
         ICK(cudaMallocAsync((void**)&P->rowptr, sizeof(uint32_t) * (V + 1), st));
-        IRC(grz_build_list_from_bounds(g, P, dp, E, 1, start, end, ends_h[0], ends_h[1], nullptr));
+        IRC(grz_build_list_from_bounds(g, P, nullptr, E, 1, start, end, ends_h[0], ends_h[1], nullptr, ka));
     }
     // 3. the -push list's offsets from the outdegrees
     IRC(grz_dev_alloc(g, (void**)&pstart, sizeof(uint32_t) * (V + 1)));
@@ -360,7 +354,6 @@ int grz_ingest_pull_derive(grz_graph* g, const uint64_t* pull, uint64_t E, int o
 done:
 #undef ICK
 #undef IRC
-    grz_dev_free(g, dpairs);
     grz_dev_free(g, ka);
     grz_dev_free(g, kb);
     for (void* q : { (void*)hist, (void*)start, (void*)end, (void*)pstart, (void*)cnt, (void*)tot, (void*)flags })

@@ -694,7 +694,8 @@ static int frontier_run(grz_graph* g, int app, uint32_t root, int flags, grz_run
     GRZ_CK(g, cudaSetDevice(g->device));
     g->app = app;
     // the counting of kernel profiling and iteration stats happens on the host loop
-    const bool graph = !(flags & GRZ_FLAG_HOST_LOOP) && !g->prof && !g->stats_on && g->pull.nvec && g->push.nvec;
+    const bool profiling = g->prof && g->prof->on;
+    const bool graph = !(flags & GRZ_FLAG_HOST_LOOP) && !profiling && !g->stats_on && g->pull.nvec && g->push.nvec;
     if (graph) grz_frontier_run_prepare(g);
     int rc = grz_frontier_init(g, app, flags, root);
     if (rc) return rc;

@@ -274,3 +274,24 @@ def test_bfs_pull_compacted_equals_scan(name):
             assert out[0][2] == out[1][2]
             np.testing.assert_array_equal(out[0][0], rec[variant + "_parents"], err_msg=variant)
         G.tune(bfs_pull_scan=0)
+
+
+def test_profiler_off_restores_the_graph_run():
+    """Kernel profiling needs the host loop; once profiling is switched off again, whole runs go
+    back to the single CUDA-graph launch (same launch accounting as a graph never profiled)."""
+    from grazelle import graphgen as gg
+    from grazelle.engine import Graph
+    g = gg.rmat(14, seed=61, symmetric=True)
+    counts = []
+    for toggle in (False, True):
+        with Graph(0) as G:
+            G.load_pairs(g.num_vertices, g.pull_order().pairs(), g.push_order().pairs())
+            G.cc_run()
+            if toggle:
+                G.profile(True)
+                G.cc_run()
+                G.profile(False)
+            l0 = G.launch_count()
+            G.cc_run()
+            counts.append(G.launch_count() - l0)
+    assert counts[0] == counts[1]

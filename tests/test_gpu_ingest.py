@@ -170,3 +170,37 @@ def _graph(V, pull, push):
     G = Graph(0)
     G.load_pairs(V, pull, push)
     return G
+
+
+@pytest.mark.parametrize("V, edges", [
+    (1, [(0, 0)]),                                   # one vertex, one self-loop
+    (2, [(1, 0)]),                                   # one edge
+    (3, [(2, 0), (2, 0), (0, 1), (1, 1), (2, 1)]),   # duplicates and a self-loop
+    (200, "random"),                                 # one radix pass (V <= 256)
+    (257, "random"),                                 # two passes
+    (5000, "sparse"),                                # mostly isolated vertices
+])
+def test_pull_only_ingest_small_and_ragged(V, edges):
+    import torch
+    from grazelle.engine import Graph
+    rng = np.random.default_rng(V)
+    if edges == "random":
+        e = rng.integers(0, V, size=(4 * V, 2))
+    elif edges == "sparse":
+        e = rng.integers(0, V, size=(40, 2))
+    else:
+        e = np.array(edges)
+    src, dst = e[:, 0].astype(np.uint64), e[:, 1].astype(np.uint64)
+    o = np.lexsort((src, dst))
+    pull = np.empty(2 * len(o), dtype=np.uint64)
+    pull[0::2], pull[1::2] = src[o], dst[o]
+    o = np.lexsort((dst, src))
+    push = np.empty(2 * len(o), dtype=np.uint64)
+    push[0::2], push[1::2] = src[o], dst[o]
+    with Graph(0) as A, Graph(0) as B:
+        A.load_pairs(V, pull, push)
+        hp = torch.from_numpy(pull.view(np.int64)).pin_memory()
+        B.load_pull_derive_push(V, len(o), hp.data_ptr())
+        for a, b in zip(_lists(A), _lists(B)):
+            np.testing.assert_array_equal(a, b)
+        np.testing.assert_array_equal(A.connected_components(), B.connected_components())

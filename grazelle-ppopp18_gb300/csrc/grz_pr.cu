@@ -383,10 +383,14 @@ int grz_pr_prepare(grz_graph* g)
         GRZ_CK(g, cudaMemsetAsync(g->pr_fx[0], 0, sizeof(u128) * (V + 1), g->stream));
         GRZ_CK(g, cudaMemsetAsync(g->pr_fx[1], 0, sizeof(u128) * (V + 1), g->stream));
     }
-    // doubles gathered instead of 16-byte fixed point: chosen, or when the fixed-point props
-    // would not fit half of L2 (the gathered form then halves the DRAM working set)
+    // Doubles gathered instead of 16-byte fixed point: chosen, or when the fixed-point props
+    // exceed 6x L2.  Below that the gathers are bound by the L1/L2 path and the per-edge
+    // conversion costs more than the smaller working set saves; above it the DRAM sectors of the
+    // random gathers dominate and halving the props wins.  GB300 sweep (16 iterations,
+    // fixed vs doubles): R-MAT 24 25.7 vs 31.8 ms, 25 64.6 vs 67.4 ms, 26 179.1 vs 156.4 ms,
+    // 27 413 vs 371 ms.
     const int pick = g->tune.pr_props;
-    g->pr_dmode = pick == 2 || (pick == 0 && (uint64_t)sizeof(u128) * V > (uint64_t)g->l2_bytes / 2);
+    g->pr_dmode = pick == 2 || (pick == 0 && (uint64_t)sizeof(u128) * V > 6ull * (uint64_t)g->l2_bytes);
     if (g->pr_dmode && !g->pr_d[0]) {
         GRZ_CK(g, cudaMalloc((void**)&g->pr_d[0], sizeof(double) * (V + 1)));
         GRZ_CK(g, cudaMalloc((void**)&g->pr_d[1], sizeof(double) * (V + 1)));

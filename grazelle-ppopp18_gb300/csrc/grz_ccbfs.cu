@@ -518,82 +518,110 @@ __global__ void __launch_bounds__(T) k_push_expand(const uint32_t* __restrict__ 
 }
 
 // BFS pull over the compacted wanted destinations (WantsInfo and in-vectors): only their vectors
-// are read, in tiles of PUSH_TILE vectors over the grid.  The vectors of one destination are
-// consecutive in the concatenation, so the per-destination minimum candidate (the reference's
-// parent rule, as in k_bfs_pull) is reduced within the warp before one atomicMin.
+// are read, in tiles of PUSH_TILE vectors.  The vectors of one destination are consecutive in the
+// concatenation, so the per-destination minimum candidate (the reference's parent rule, as in
+// k_bfs_pull) is reduced within the warp before one atomicMin.
+// Early exit: the candidate is (first vector with a frontier source, ~largest such source), so
+// once a destination has a candidate, its later vectors cannot win.  Blocks take runs of
+// PULL_CHUNK consecutive tiles from a queue (balanced, and a long destination's tiles are
+// processed roughly in order), and a vector past its destination's first LONG_RUN vectors is
+// skipped (no neighbour or frontier reads) when the candidate already names an earlier vector.
+// In R-MAT the sources of a destination ascend and the hubs have small IDs, so a long
+// destination next to a frontier hub stops after its first vectors.
+constexpr uint32_t PULL_CHUNK = 2;  // GB300 sweep of 2-16 (queue of runs): 2 keeps small pulls cheapest
+constexpr uint32_t LONG_RUN = 32;
+
 __global__ void __launch_bounds__(T) k_bfs_pull_expand(const uint32_t* __restrict__ dests, const uint32_t* __restrict__ voff,
                                                        const uint32_t* __restrict__ vdelta, const uint32_t* __restrict__ tile_first,
                                                        const uint32_t* __restrict__ counters, const uint4* __restrict__ nbr,
                                                        uint32_t V, const unsigned long long* __restrict__ has,
                                                        unsigned long long* __restrict__ cand, uint32_t* __restrict__ touched,
                                                        uint32_t* __restrict__ ntouched, const uint32_t* __restrict__ hub_vid,
-                                                       uint32_t nhub, unsigned long long* __restrict__ has_next)
+                                                       uint32_t nhub, unsigned long long* __restrict__ has_next,
+                                                       uint32_t* __restrict__ queue)
 {
     __shared__ uint32_t s_dst[PUSH_TILE + 1];
     __shared__ uint32_t s_off[PUSH_TILE + 1];
     __shared__ uint32_t s_delta[PUSH_TILE + 1];
+    __shared__ uint32_t s_chunk;
     const uint32_t nd = counters[0], total = counters[2];
     const uint32_t ntiles = (total + PUSH_TILE - 1) / PUSH_TILE;
     const int lane = threadIdx.x & 31;
-    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const uint32_t first = tile_first[tile];
-        const uint32_t t0 = tile * PUSH_TILE;
-        const uint32_t tend = min(total, t0 + PUSH_TILE);
-        const uint32_t nw = min(PUSH_TILE, nd - first);
-        for (uint32_t i = threadIdx.x; i <= nw; i += T) {
-            s_off[i] = voff[first + i];
-            if (i < nw) {
-                s_dst[i] = dests[first + i];
-                s_delta[i] = vdelta[first + i];
-            }
-        }
+    for (;;) {
+        if (threadIdx.x == 0) s_chunk = atomicAdd(queue, 1u);
         __syncthreads();
-        for (uint32_t base = t0; base < tend; base += T) {  // warp-uniform trip count
-            const uint32_t gv = base + threadIdx.x;
-            uint32_t key = INF;
-            unsigned long long k = ~0ull;
-            if (gv < tend) {
-                int lo = 0, hi = (int)nw - 1;  // last entry with s_off <= gv
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (s_off[mid] <= gv) lo = mid; else hi = mid - 1;
+        const uint32_t chunk = s_chunk;
+        __syncthreads();  // every thread has read s_chunk before it is replaced
+        if ((uint64_t)chunk * PULL_CHUNK >= ntiles) break;
+        const uint32_t chunk_end = min(ntiles, (chunk + 1) * PULL_CHUNK);
+        for (uint32_t tile = chunk * PULL_CHUNK; tile < chunk_end; ++tile) {
+            const uint32_t first = tile_first[tile];
+            const uint32_t t0 = tile * PUSH_TILE;
+            const uint32_t tend = min(total, t0 + PUSH_TILE);
+            const uint32_t nw = min(PUSH_TILE, nd - first);
+            for (uint32_t i = threadIdx.x; i <= nw; i += T) {
+                s_off[i] = voff[first + i];
+                if (i < nw) {
+                    s_dst[i] = dests[first + i];
+                    s_delta[i] = vdelta[first + i];
                 }
-                key = s_dst[lo];
-                const uint32_t vec = gv + s_delta[lo];
-                const uint4 s = __ldcs(nbr + vec);
-                const uint32_t ids[4] = { grz_hub_decode(s.x, hub_vid, nhub), grz_hub_decode(s.y, hub_vid, nhub),
-                                          grz_hub_decode(s.z, hub_vid, nhub), grz_hub_decode(s.w, hub_vid, nhub) };
-                uint32_t best = 0;
-                bool any = false;
-#pragma unroll
-                for (int l = 0; l < 4; ++l) {
-                    const uint32_t id = ids[l];
-                    if (id < V && bit_of(has, id)) {
-                        best = any ? max(best, id) : id;
-                        any = true;
+            }
+            __syncthreads();
+            for (uint32_t base = t0; base < tend; base += T) {  // warp-uniform trip count
+                const uint32_t gv = base + threadIdx.x;
+                uint32_t key = INF;
+                unsigned long long k = ~0ull;
+                if (gv < tend) {
+                    int lo = 0, hi = (int)nw - 1;  // last entry with s_off <= gv
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (s_off[mid] <= gv) lo = mid; else hi = mid - 1;
+                    }
+                    key = s_dst[lo];
+                    const uint32_t vec = gv + s_delta[lo];
+                    bool skip = false;
+                    if (gv >= s_off[lo] + LONG_RUN) {
+                        const unsigned long long c = __ldcg(cand + key);  // atomics of other blocks land in L2
+                        skip = c != ~0ull && (uint32_t)(c >> 32) < vec;
+                    }
+                    if (!skip) {
+                        const uint4 s = __ldcs(nbr + vec);
+                        const uint32_t ids[4] = { grz_hub_decode(s.x, hub_vid, nhub), grz_hub_decode(s.y, hub_vid, nhub),
+                                                  grz_hub_decode(s.z, hub_vid, nhub), grz_hub_decode(s.w, hub_vid, nhub) };
+                        uint32_t best = 0;
+                        bool any = false;
+    #pragma unroll
+                        for (int l = 0; l < 4; ++l) {
+                            const uint32_t id = ids[l];
+                            if (id < V && bit_of(has, id)) {
+                                best = any ? max(best, id) : id;
+                                any = true;
+                            }
+                        }
+                        if (any) k = ((unsigned long long)vec << 32) | (unsigned long long)(~best);
                     }
                 }
-                if (any) k = ((unsigned long long)vec << 32) | (unsigned long long)(~best);
+                if (!__any_sync(0xffffffffu, k != ~0ull)) continue;  // no frontier source in the warp's vectors
+                const uint32_t prevkey = __shfl_up_sync(0xffffffffu, key, 1);
+                const uint32_t nextkey = __shfl_down_sync(0xffffffffu, key, 1);
+                const bool head = lane == 0 || key != prevkey;
+                const bool tail = lane == 31 || key != nextkey;
+                const unsigned heads = __ballot_sync(0xffffffffu, head);
+                const int segstart = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+                const int maxlen = __reduce_max_sync(0xffffffffu, (unsigned)(lane - segstart + 1));
+                for (int off = 1; off < maxlen; off <<= 1) {
+                    const unsigned long long o = __shfl_up_sync(0xffffffffu, k, off);
+                    if (lane - off >= segstart) k = min(k, o);
+                }
+                bool first_touch = false;
+                if (tail && k != ~0ull && k < cand[key]) {
+                    first_touch = atomicMin(cand + key, k) == ~0ull;
+                    if (first_touch) atomicOr(has_next + (key >> 6), 1ull << (key & 63));
+                }
+                warp_append(first_touch, key, touched, ntouched);
             }
-            const uint32_t prevkey = __shfl_up_sync(0xffffffffu, key, 1);
-            const uint32_t nextkey = __shfl_down_sync(0xffffffffu, key, 1);
-            const bool head = lane == 0 || key != prevkey;
-            const bool tail = lane == 31 || key != nextkey;
-            const unsigned heads = __ballot_sync(0xffffffffu, head);
-            const int segstart = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
-            const int maxlen = __reduce_max_sync(0xffffffffu, (unsigned)(lane - segstart + 1));
-            for (int off = 1; off < maxlen; off <<= 1) {
-                const unsigned long long o = __shfl_up_sync(0xffffffffu, k, off);
-                if (lane - off >= segstart) k = min(k, o);
-            }
-            bool first_touch = false;
-            if (tail && k != ~0ull && k < cand[key]) {
-                first_touch = atomicMin(cand + key, k) == ~0ull;
-                if (first_touch) atomicOr(has_next + (key >> 6), 1ull << (key & 63));
-            }
-            warp_append(first_touch, key, touched, ntouched);
+            __syncthreads();
         }
-        __syncthreads();
     }
 }
 
@@ -932,7 +960,7 @@ static int edge_phase(grz_graph* g, int pull, uint64_t first, uint64_t count)
             grz_prof_begin(g, GRZ_PROF_BFS_PULL);
             k_bfs_pull_expand<<<(unsigned)g->num_sms * 8, T, 0, st>>>(f.frontier, f.voff, f.vdelta, f.tile_first, f.counters,
                                                                      g->pull.nbr, V, f.has, f.cand64, f.touched, f.counters + 1,
-                                                                     g->pull.hub_vid, g->pull.nhub, f.has_next); GRZ_COUNT_LAUNCH(g);
+                                                                     g->pull.hub_vid, g->pull.nhub, f.has_next, f.counters + 5); GRZ_COUNT_LAUNCH(g);
         } else {
             GRZ_TRY(grz_stats_count_range(g, &g->pull, first, count));
             grz_prof_begin(g, bfs ? GRZ_PROF_BFS_PULL : GRZ_PROF_CC_PULL);

@@ -303,6 +303,16 @@ static const void* pinned_device_view(const void* p)
 
 static int load_pairs(grz_graph* g, uint64_t V, uint64_t E, const uint64_t* pull_pairs, const uint64_t* push_pairs,
                       int flags);
+
+// the graph's second stream for host-to-device copies, and its two events, made on first use
+cudaError_t grz_copy_stream(grz_graph* g)
+{
+    if (g->copy_stream) return cudaSuccess;
+    cudaError_t e = cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->copy_ev[0], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->copy_ev[1], cudaEventDisableTiming);
+    return e;
+}
 static int finish_load(grz_graph* g, int rc);
 
 extern "C" int grz_graph_load_pairs(grz_graph* g, uint64_t V, uint64_t E, const uint64_t* pull_pairs,
@@ -332,9 +342,9 @@ static int load_pairs(grz_graph* g, uint64_t V, uint64_t E, const uint64_t* pull
     const size_t pbytes = sizeof(uint64_t) * 2 * E;
     int rc = GRZ_OK;
     if ((flags & GRZ_LOAD_DERIVE_PUSH) && !push_pairs && E > 0) {
-        // Pull-only ingest: one fused pass reads the pairs where they are (pinned host memory over
-        // the link, or device memory) and both lists and the outdegrees follow on the device.
-        // Pageable host memory is first copied into a device buffer.
+        // Pull-only ingest: pinned host pairs cross the link chunk by chunk while the chunks already
+        // in are processed; device pairs are read where they are.  Pageable host memory is first
+        // copied into a device buffer.
         const void* view = is_device_ptr(pull_pairs) ? (const void*)pull_pairs : pinned_device_view(pull_pairs);
         void* dbuf = nullptr;
         if (!view) {
@@ -342,7 +352,7 @@ static int load_pairs(grz_graph* g, uint64_t V, uint64_t E, const uint64_t* pull
             if (rc == GRZ_OK) rc = grz_cuda_check(g, cudaMemcpyAsync(dbuf, pull_pairs, pbytes, cudaMemcpyHostToDevice, st), "H2D pull pairs");
             view = dbuf;
         }
-        if (rc == GRZ_OK) rc = grz_ingest_pull_derive(g, (const uint64_t*)view, E);
+        if (rc == GRZ_OK) rc = grz_ingest_pull_derive(g, (const uint64_t*)view, E, dbuf || is_device_ptr(pull_pairs) ? nullptr : pull_pairs);
         if (rc == GRZ_OK) rc = grz_build_hubs(g, &g->pull, g->tune.hub_max);
         if (rc == GRZ_OK) rc = grz_cuda_check(g, cudaStreamSynchronize(st), "layout build");
         grz_dev_free(g, dbuf);
@@ -363,12 +373,7 @@ static int load_pairs(grz_graph* g, uint64_t V, uint64_t E, const uint64_t* pull
     }
     bool push_on_copy_stream = false;
     if (rc == GRZ_OK && E > 0 && dbuf[1]) {
-        cudaError_t e = cudaSuccess;
-        if (!g->copy_stream) {
-            e = cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking);
-            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->copy_ev[0], cudaEventDisableTiming);
-            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->copy_ev[1], cudaEventDisableTiming);
-        }
+        cudaError_t e = grz_copy_stream(g);
         if (e == cudaSuccess) e = cudaEventRecord(g->copy_ev[0], st);  // after the -pull copy (and the allocations)
         if (e == cudaSuccess) e = cudaStreamWaitEvent(g->copy_stream, g->copy_ev[0], 0);
         if (e == cudaSuccess) e = cudaMemcpyAsync(dbuf[1], push_pairs, pbytes, cudaMemcpyHostToDevice, g->copy_stream);
@@ -813,6 +818,10 @@ extern "C" int grz_tune_set(grz_graph* g, int param, int64_t value)
         if (value > 2) return grz_set_error(g, GRZ_ERR_ARG, "PageRank gathered props must be 0 (by size), 1 (fixed point) or 2 (doubles)");
         g->tune.pr_props = (uint32_t)value;  // from the next grz_pr_init
         return GRZ_OK;
+    case GRZ_TUNE_INGEST_CHUNKS:
+        if (value > GRZ_INGEST_MAX_CHUNKS) return grz_set_error(g, GRZ_ERR_RANGE, "at most %d ingest chunks", GRZ_INGEST_MAX_CHUNKS);
+        g->tune.ingest_chunks = (uint32_t)value;
+        return GRZ_OK;
     default:
         return grz_set_error(g, GRZ_ERR_ARG, "unknown tuning parameter %d", param);
     }
@@ -829,6 +838,7 @@ extern "C" int grz_tune_get(const grz_graph* g, int param, int64_t* value)
     case GRZ_TUNE_PR_GRID: *value = g->tune.pr_grid; return GRZ_OK;
     case GRZ_TUNE_BFS_PULL_SCAN: *value = g->tune.bfs_pull_scan; return GRZ_OK;
     case GRZ_TUNE_PR_PROPS: *value = g->tune.pr_props; return GRZ_OK;
+    case GRZ_TUNE_INGEST_CHUNKS: *value = g->tune.ingest_chunks; return GRZ_OK;
     case GRZ_TUNE_HUBS_LOADED: *value = g->pull.nhub; return GRZ_OK;
     default: return GRZ_ERR_ARG;
     }

@@ -192,6 +192,7 @@ struct grz_list {
 // through L1.  Invalid lanes stay GRZ_INVALID_ID; other sources are plain IDs (< V < 2^31).
 #define GRZ_HUB_BASE 0x80000000u
 #define GRZ_HUB_MAX 49152u
+#define GRZ_INGEST_MAX_CHUNKS 64
 
 #define GRZ_BATCH_K 8  // instances per graph of a batch (grz_batch.cu)
 
@@ -230,6 +231,7 @@ struct grz_mlp;
 #define GRZ_TUNE_PR_GRID 4
 #define GRZ_TUNE_BFS_PULL_SCAN 5
 #define GRZ_TUNE_PR_PROPS 6
+#define GRZ_TUNE_INGEST_CHUNKS 7
 #define GRZ_TUNE_HUBS_LOADED 100
 
 // kernel shapes chosen per graph (grz_tune_set; the autotuner searches them)
@@ -241,6 +243,7 @@ struct grz_tuning {
     uint32_t pr_grid;      // blocks of the persistent PageRank gather kernel (0: SMs x resident blocks)
     uint32_t bfs_pull_scan;  // 1: BFS pull scans every vector; 0: only the wanted destinations' (compacted)
     uint32_t pr_props;     // props the PageRank gather reads: 0 by size, 1 fixed point, 2 doubles
+    uint32_t ingest_chunks;  // chunks of the pull-only ingest (0: by edge count)
 };
 
 // Device control block of a CC/BFS run executed as one CUDA graph (grz_ccbfs.cu): the
@@ -457,14 +460,19 @@ int grz_stats_count_range(grz_graph* g, const grz_list* L, uint64_t first, uint6
 int grz_stats_count_selected(grz_graph* g, const grz_list* L, const uint32_t* sel, const uint32_t* counters);
 int grz_build_hubs(grz_graph* g, grz_list* L, uint32_t max_hubs);
 // both lists and the outdegrees from E > 0 -pull pairs in pinned host or device memory (grz_sort.cu)
-int grz_ingest_pull_derive(grz_graph* g, const uint64_t* pull, uint64_t E);
+// (pull: device-readable pairs; host: the same pairs' pinned host address, to copy them chunk by
+// chunk, or null when pull is device memory)
+int grz_ingest_pull_derive(grz_graph* g, const uint64_t* pull, uint64_t E, const uint64_t* host);
+cudaError_t grz_copy_stream(grz_graph* g);
 int grz_build_list_from_bounds(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t E, int shared_is_dst,
                                const uint32_t* start, const uint32_t* end, uint64_t first_shared, uint64_t last_shared,
-                               uint32_t* run_len, const unsigned long long* keys);
+                               uint32_t* run_len, cudaStream_t st, uint64_t written_cap);
 #define GRZ_LOAD_DERIVE_PUSH 1
 int grz_alloc_outdegrees(grz_graph* g);
 int grz_build_outdegrees(grz_graph* g, const uint64_t* d_pull_pairs, uint64_t E);
 
 // scans (grz_scan.cu): exclusive sum of uint32 into uint32 (n < 2^32), inclusive max of uint32
 int grz_exclusive_sum_u32(grz_graph* g, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total_out_dev);
+int grz_exclusive_sum_u32_on(grz_graph* g, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total_out_dev,
+                             cudaStream_t st);  // ordered on st
 int grz_inclusive_max_u32(grz_graph* g, const uint32_t* in, uint32_t* out, uint64_t n);

@@ -98,27 +98,6 @@ __global__ void k_vector_write(const uint64_t* __restrict__ pairs, uint64_t E, i
     shared[vec] = s;
 }
 
-// k_vector_write for the -pull list from packed keys (src << 32 | dst) in -pull order instead of
-// pairs: half the bytes read
-__global__ void k_vector_write_keys(const unsigned long long* __restrict__ keys, uint64_t E,
-                                    const uint32_t* __restrict__ start, const uint32_t* __restrict__ end,
-                                    const uint32_t* __restrict__ rowptr, uint4* __restrict__ nbr, uint32_t* __restrict__ shared)
-{
-    const uint64_t e = (uint64_t)blockIdx.x * BT + threadIdx.x;
-    if (e >= E) return;
-    const uint32_t d = (uint32_t)(keys[e] & 0xffffffffull);
-    const uint32_t pos = (uint32_t)e - __ldg(start + d);
-    if (pos & 3u) return;
-    const uint32_t n = min(4u, __ldg(end + d) - (uint32_t)e);
-    uint32_t ids[4] = { GRZ_INVALID_ID, GRZ_INVALID_ID, GRZ_INVALID_ID, GRZ_INVALID_ID };
-#pragma unroll
-    for (uint32_t k = 0; k < 4; ++k)
-        if (k < n) ids[k] = (uint32_t)(keys[e + k] >> 32);
-    const uint32_t vec = __ldg(rowptr + d) + pos / 4u;
-    nbr[vec] = make_uint4(ids[0], ids[1], ids[2], ids[3]);
-    shared[vec] = d;
-}
-
 // the reference vertex index (graphdata.c:219-267): first vector of each vertex with edges,
 // 0x7fff... for one without edges up to the last shared vertex, 0xffff... beyond it
 __global__ void k_vindex(const uint32_t* __restrict__ start, const uint32_t* __restrict__ end,
@@ -214,13 +193,14 @@ __global__ void k_degree_to_double(const uint32_t* __restrict__ degree, uint64_t
 // The rest of a list build once the run bounds [start, end) of every shared vertex are known
 // (k_group_bounds, or the fused ingest of grz_sort.cu): vector offsets, vectors, vertex index.
 // last_shared: the shared vertex of the last edge; first_shared: of the first.
-// The edges come as pairs, or (d_pairs null, -pull list only) as packed keys src << 32 | dst.
+// The edges come as pairs (written_cap 0), or L->nbr and L->shared (written_cap vectors) already
+// hold the vectors and only the offsets and the index are built.  Everything, the temporaries
+// included, is ordered on `st`.
 int grz_build_list_from_bounds(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t E, int shared_is_dst,
                                const uint32_t* start, const uint32_t* end, uint64_t first_shared, uint64_t last_shared,
-                               uint32_t* run_len, const unsigned long long* keys)
+                               uint32_t* run_len, cudaStream_t st, uint64_t written_cap)
 {
     const uint64_t V = g->V;
-    cudaStream_t st = g->stream;
     const uint64_t vi_count = V + 64;
     uint32_t *cnt = nullptr, *tot = nullptr;
     uint32_t nv32 = 0;
@@ -230,19 +210,22 @@ int grz_build_list_from_bounds(grz_graph* g, grz_list* L, const uint64_t* d_pair
     LCK(cudaMallocAsync((void**)&tot, sizeof(uint32_t), st));
     k_group_vectors<<<grid_blocks_for(V + 1), BT, 0, st>>>(start, end, V, cnt, run_len); GRZ_COUNT_LAUNCH(g);
     LCK(cudaGetLastError());
-    rc = grz_exclusive_sum_u32(g, cnt, L->rowptr, V + 1, tot);
+    rc = grz_exclusive_sum_u32_on(g, cnt, L->rowptr, V + 1, tot, st);
     if (rc) goto done;
     LCK(cudaMemcpyAsync(&nv32, tot, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     LCK(cudaStreamSynchronize(st));
     L->nvec = nv32;
-    LCK(cudaMallocAsync((void**)&L->nbr, sizeof(uint4) * L->nvec, st));
-    LCK(cudaMallocAsync((void**)&L->shared, sizeof(uint32_t) * L->nvec, st));
-    if (d_pairs)
+    if (written_cap) {
+        // the caller allocated the vectors (written_cap of them) and wrote them already
+        if (L->nvec > written_cap) { rc = grz_set_error(g, GRZ_ERR_STATE, "list needs %llu vectors, %llu were written",
+                                                         (unsigned long long)L->nvec, (unsigned long long)written_cap); goto done; }
+    } else {
+        LCK(cudaMallocAsync((void**)&L->nbr, sizeof(uint4) * L->nvec, st));
+        LCK(cudaMallocAsync((void**)&L->shared, sizeof(uint32_t) * L->nvec, st));
         k_vector_write<<<grid_blocks_for(E), BT, 0, st>>>(d_pairs, E, shared_is_dst, start, end, L->rowptr, L->nbr, L->shared);
-    else
-        k_vector_write_keys<<<grid_blocks_for(E), BT, 0, st>>>(keys, E, start, end, L->rowptr, L->nbr, L->shared);
-    GRZ_COUNT_LAUNCH(g);
-    LCK(cudaGetLastError());
+        GRZ_COUNT_LAUNCH(g);
+        LCK(cudaGetLastError());
+    }
     k_vindex<<<grid_blocks_for(vi_count), BT, 0, st>>>(start, end, L->rowptr, V, vi_count, last_shared, L->vindex); GRZ_COUNT_LAUNCH(g);
     LCK(cudaGetLastError());
     L->vindex_start = first_shared;
@@ -294,7 +277,7 @@ int grz_build_list(grz_graph* g, grz_list* L, const uint64_t* d_pairs, uint64_t 
         LCK(cudaStreamSynchronize(st));
         if (flags_h[0]) { rc = grz_set_error(g, GRZ_ERR_UNSORTED, "%s list is not grouped by %s in ascending order", shared_is_dst ? "pull" : "push", shared_is_dst ? "destination" : "source"); goto done; }
         if (flags_h[1]) { rc = grz_set_error(g, GRZ_ERR_RANGE, "%s list holds a vertex ID >= V (%llu)", shared_is_dst ? "pull" : "push", (unsigned long long)V); goto done; }
-        rc = grz_build_list_from_bounds(g, L, d_pairs, E, shared_is_dst, start, end, ends_h[0], ends_h[1], run_len, nullptr);
+        rc = grz_build_list_from_bounds(g, L, d_pairs, E, shared_is_dst, start, end, ends_h[0], ends_h[1], run_len, g->stream, 0);
     }
 done:
     for (void* p : { (void*)flags, (void*)start, (void*)end })

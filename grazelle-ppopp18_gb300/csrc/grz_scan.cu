@@ -126,28 +126,28 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_tile_scan(const uint32_t* __re
 }
 
 template <class Op, bool Inclusive>
-int scan_impl(grz_graph* g, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total_dev)
+int scan_impl(grz_graph* g, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total_dev, cudaStream_t st)
 {
     if (n == 0) {
-        if (total_dev) GRZ_CK(g, cudaMemsetAsync(total_dev, 0, sizeof(uint32_t), g->stream));
+        if (total_dev) GRZ_CK(g, cudaMemsetAsync(total_dev, 0, sizeof(uint32_t), st));
         return GRZ_OK;
     }
     const uint64_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
     if (tiles == 1) {
-        k_tile_scan<Op, Inclusive><<<1, SCAN_THREADS, 0, g->stream>>>(in, out, n, nullptr, total_dev);
+        k_tile_scan<Op, Inclusive><<<1, SCAN_THREADS, 0, st>>>(in, out, n, nullptr, total_dev);
         return grz_cuda_check(g, cudaGetLastError(), "k_tile_scan");
     }
     uint32_t* tot = nullptr;
-    GRZ_CK(g, cudaMallocAsync((void**)&tot, sizeof(uint32_t) * (2 * tiles + 1), g->stream));
+    GRZ_CK(g, cudaMallocAsync((void**)&tot, sizeof(uint32_t) * (2 * tiles + 1), st));
     uint32_t* off = tot + tiles;
-    k_tile_reduce<Op><<<(unsigned)tiles, SCAN_THREADS, 0, g->stream>>>(in, n, tot);
+    k_tile_reduce<Op><<<(unsigned)tiles, SCAN_THREADS, 0, st>>>(in, n, tot);
     int rc = grz_cuda_check(g, cudaGetLastError(), "k_tile_reduce");
-    if (rc == GRZ_OK) rc = scan_impl<Op, false>(g, tot, off, tiles, nullptr);
+    if (rc == GRZ_OK) rc = scan_impl<Op, false>(g, tot, off, tiles, nullptr, st);
     if (rc == GRZ_OK) {
-        k_tile_scan<Op, Inclusive><<<(unsigned)tiles, SCAN_THREADS, 0, g->stream>>>(in, out, n, off, total_dev);
+        k_tile_scan<Op, Inclusive><<<(unsigned)tiles, SCAN_THREADS, 0, st>>>(in, out, n, off, total_dev);
         rc = grz_cuda_check(g, cudaGetLastError(), "k_tile_scan");
     }
-    cudaFreeAsync(tot, g->stream);
+    cudaFreeAsync(tot, st);
     return rc;
 }
 
@@ -155,10 +155,16 @@ int scan_impl(grz_graph* g, const uint32_t* in, uint32_t* out, uint64_t n, uint3
 
 int grz_exclusive_sum_u32(grz_graph* g, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total_out_dev)
 {
-    return scan_impl<OpSum, false>(g, in, out, n, total_out_dev);
+    return scan_impl<OpSum, false>(g, in, out, n, total_out_dev, g->stream);
+}
+
+int grz_exclusive_sum_u32_on(grz_graph* g, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total_out_dev,
+                             cudaStream_t st)
+{
+    return scan_impl<OpSum, false>(g, in, out, n, total_out_dev, st);
 }
 
 int grz_inclusive_max_u32(grz_graph* g, const uint32_t* in, uint32_t* out, uint64_t n)
 {
-    return scan_impl<OpMax, true>(g, in, out, n, nullptr);
+    return scan_impl<OpMax, true>(g, in, out, n, nullptr, g->stream);
 }

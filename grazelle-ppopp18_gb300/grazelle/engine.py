@@ -69,11 +69,12 @@ class Graph:
         return [(self.lib.grz_profile_kind_name(kinds[i]).decode(), ms[i]) for i in range(n)]
 
     def tune(self, **kw):
-        """Set kernel shapes: hubs=, cc_cache=, cc_threads=, cc_grid=, pr_grid=, bfs_pull_scan= (results
-        never depend on them; hubs takes effect at the next load)."""
+        """Set kernel shapes: hubs=, cc_cache=, cc_threads=, cc_grid=, pr_grid=, bfs_pull_scan=, pr_props=,
+        ingest_chunks= (results never depend on them; hubs and ingest_chunks take effect at the next
+        load)."""
         keys = {"hubs": native.TUNE_HUBS, "cc_cache": native.TUNE_CC_CACHE, "cc_threads": native.TUNE_CC_THREADS,
                 "cc_grid": native.TUNE_CC_GRID, "pr_grid": native.TUNE_PR_GRID, "bfs_pull_scan": native.TUNE_BFS_PULL_SCAN,
-                "pr_props": native.TUNE_PR_PROPS}
+                "pr_props": native.TUNE_PR_PROPS, "ingest_chunks": native.TUNE_INGEST_CHUNKS}
         for k, v in kw.items():
             self._ck(self.lib.grz_tune_set(self.h, keys[k], int(v)))
         return self
@@ -83,6 +84,7 @@ class Graph:
         for k, p in (("hubs", native.TUNE_HUBS), ("cc_cache", native.TUNE_CC_CACHE), ("cc_threads", native.TUNE_CC_THREADS),
                      ("cc_grid", native.TUNE_CC_GRID), ("pr_grid", native.TUNE_PR_GRID),
                      ("bfs_pull_scan", native.TUNE_BFS_PULL_SCAN), ("pr_props", native.TUNE_PR_PROPS),
+                     ("ingest_chunks", native.TUNE_INGEST_CHUNKS),
                      ("hubs_loaded", native.TUNE_HUBS_LOADED)):
             v = C.c_int64()
             self._ck(self.lib.grz_tune_get(self.h, p, C.byref(v)))

@@ -15,12 +15,18 @@ def _lists(G):
             G.outdegrees())
 
 
-def _check_derived(V, pull, push):
+def _check_derived(V, pull, push, chunks=0):
     import torch
     from grazelle.engine import Graph
     with Graph(0) as A, Graph(0) as B:
         A.load_pairs(V, pull, push)
-        hp = torch.from_numpy(pull.view(np.int64)).pin_memory()
+        B.tune(ingest_chunks=chunks)
+        if chunks:   # chunks read in place from device memory
+            dp = torch.from_numpy(pull.view(np.int64)).cuda()
+            B.load_pull_derive_push(V, pull.shape[0] // 2, dp.data_ptr())
+            for a, b in zip(_lists(A), _lists(B)):
+                np.testing.assert_array_equal(a, b)
+        hp = torch.from_numpy(pull.view(np.int64)).pin_memory()   # chunks copied through staging slots
         B.load_pull_derive_push(V, pull.shape[0] // 2, hp.data_ptr())
         for a, b in zip(_lists(A), _lists(B)):
             np.testing.assert_array_equal(a, b)
@@ -52,6 +58,61 @@ def test_derived_push_list_multigraph(scale):
     push = np.empty_like(pull)
     push[0::2], push[1::2] = src[o], dst[o]
     _check_derived(V, pull, push)
+
+
+def _pairs(src, dst):
+    o = np.lexsort((src, dst))
+    pull = np.empty(2 * len(o), dtype=np.uint64)
+    pull[0::2], pull[1::2] = src[o], dst[o]
+    o = np.lexsort((dst, src))
+    push = np.empty(2 * len(o), dtype=np.uint64)
+    push[0::2], push[1::2] = src[o], dst[o]
+    return pull, push
+
+
+@pytest.mark.parametrize("chunks", [2, 3, 7, 64])
+def test_pull_only_ingest_in_chunks(chunks):
+    """The ingest cuts the pairs into chunks that are sorted while later chunks cross the link;
+    an edge's rank in its source's run adds up over chunks.  Hubs whose edges fall in every chunk,
+    destinations whose runs cross chunk edges, duplicates and a last chunk shorter than the rest
+    must give the lists of one sort."""
+    from grazelle import graphgen as gg
+    g = gg.rmat(14, seed=chunks)
+    V = g.num_vertices
+    rng = np.random.default_rng(chunks)
+    hub_dst = rng.integers(0, V, size=3000).astype(np.uint64)          # source 7: edges everywhere
+    long_src = rng.integers(0, V, size=5000).astype(np.uint64)         # destination 9: a run over chunks
+    src = np.concatenate([g.src, np.full(3000, 7, dtype=np.uint64), long_src, g.src[:777]])
+    dst = np.concatenate([g.dst, hub_dst, np.full(5000, 9, dtype=np.uint64), g.dst[:777]])
+    pull, push = _pairs(src, dst)
+    _check_derived(V, pull, push, chunks=chunks)
+
+
+def test_chunked_ingest_input_errors_leave_the_graph_usable():
+    """Unsorted pairs and out-of-range IDs are reported after the chunks were already being
+    sorted; the graph loads the next valid list."""
+    import torch
+    from grazelle import graphgen as gg, native
+    from grazelle.engine import Graph
+    g = gg.rmat(13, seed=5)
+    V = g.num_vertices
+    pull, push = _pairs(g.src, g.dst)
+    unsorted = pull.copy()
+    unsorted[1::2][[10, len(unsorted) // 2 - 10]] = unsorted[1::2][[len(unsorted) // 2 - 10, 10]]
+    out_of_range = pull.copy()
+    out_of_range[2 * 1000] = V + 5
+    with Graph(0) as A, Graph(0) as B:
+        A.load_pairs(V, pull, push)
+        B.tune(ingest_chunks=5)
+        for bad, code in ((unsorted, -4), (out_of_range, -5)):
+            hb = torch.from_numpy(bad.view(np.int64)).pin_memory()
+            with pytest.raises(native.GrzError) as ei:
+                B.load_pull_derive_push(V, len(bad) // 2, hb.data_ptr())
+            assert ei.value.code == code
+        hp = torch.from_numpy(pull.view(np.int64)).pin_memory()
+        B.load_pull_derive_push(V, len(pull) // 2, hp.data_ptr())
+        for a, b in zip(_lists(A), _lists(B)):
+            np.testing.assert_array_equal(a, b)
 
 
 def test_device_and_host_sources_agree():

@@ -97,22 +97,31 @@ static void free_list(grz_graph* g, grz_list* L)
     memset(L, 0, sizeof(*L));
 }
 
-static void free_graph_data(grz_graph* g)
+// next_V: the V of the graph about to be loaded; the CC/BFS buffers stay when it is the same
+static void free_graph_data(grz_graph* g, uint64_t next_V = ~0ull)
 {
-    grz_frontier_free(g);
+    if (g->fr.label && g->fr.alloc_V == next_V)
+        grz_frontier_park(g);
+    else
+        grz_frontier_free(g);
     free_list(g, &g->pull);
     free_list(g, &g->push);
     // pool: streamed per-vertex arrays; cudaMalloc: the PageRank props and sums, which the gather
     // reads at random (pool memory measured 12% slower for random gathers)
     void* pooled[] = { g->outdeg, g->degree, g->inv_deg, g->prop, g->accum, g->glob, g->scratch };
     for (void* p : pooled) grz_dev_free(g, p);
-    void* plain[] = { g->pr_fx[0], g->pr_fx[1], g->pr_sum, g->pr_K, g->pr_rowacc, g->pr_cut, g->pr_d[0], g->pr_d[1] };
-    for (void* p : plain) cudaFree(p);
-    g->pr_d[0] = g->pr_d[1] = nullptr;
+    if (g->pr_fx[0] && g->V == next_V) {
+        // the PageRank arrays are sized by V alone: kept, and refilled at the next grz_pr_init
+        g->pr_lists_changed = 1;
+    } else {
+        void* plain[] = { g->pr_fx[0], g->pr_fx[1], g->pr_sum, g->pr_K, g->pr_rowacc, g->pr_cut, g->pr_d[0], g->pr_d[1] };
+        for (void* p : plain) cudaFree(p);
+        g->pr_d[0] = g->pr_d[1] = nullptr;
+        g->pr_fx[0] = g->pr_fx[1] = nullptr; g->pr_sum = nullptr; g->pr_K = nullptr; g->pr_rowacc = nullptr;
+        g->pr_cut = nullptr;
+    }
     g->pr_dmode = g->pr_fx_stale = g->pr_d_stale = 0;
     g->outdeg = nullptr; g->degree = nullptr; g->inv_deg = nullptr;
-    g->pr_fx[0] = g->pr_fx[1] = nullptr; g->pr_sum = nullptr; g->pr_K = nullptr; g->pr_rowacc = nullptr;
-    g->pr_cut = nullptr;
     g->pr_rowacc_stale = 0;
     g->prop = nullptr; g->accum = nullptr; g->glob = nullptr; g->scratch = nullptr;
     g->scratch_bytes = 0;
@@ -335,7 +344,7 @@ static int load_pairs(grz_graph* g, uint64_t V, uint64_t E, const uint64_t* pull
     if (!g || (E > 0 && !pull_pairs)) return GRZ_ERR_ARG;
     if (V >= 0xffffffffull) return grz_set_error(g, GRZ_ERR_RANGE, "V = %llu exceeds the 32-bit device ID limit", (unsigned long long)V);
     GRZ_CK(g, cudaSetDevice(g->device));
-    free_graph_data(g);
+    free_graph_data(g, V);
     g->V = V;
     g->E = E;
     cudaStream_t st = g->stream;
@@ -533,7 +542,7 @@ extern "C" int grz_graph_load_files_ex(grz_graph* g, const char* base, int flags
         rc = grz_set_error(g, GRZ_ERR_IO, "\"%s\": header {V, E} differs from the -pull file", path[1]);
     void* dbuf[2] = { nullptr, nullptr };
     if (rc == GRZ_OK) {
-        free_graph_data(g);  // the old graph's memory back to the pool before the new pairs take it
+        free_graph_data(g, lf[0].V);  // the old graph's memory back to the pool before the new pairs take it
         const uint64_t E = lf[0].E;
         for (int i = 0; i < 2 && rc == GRZ_OK; ++i) {
             if (i == 1 && push_missing) break;

@@ -764,12 +764,28 @@ __global__ void k_u32_to_double(const uint32_t* __restrict__ x, uint64_t V, doub
 // host side
 
 static uint64_t words_of(uint64_t V) { return (V >> 6) + 2; }
+static int frontier_list_state(grz_graph* g);
 
 static int ensure_frontier_state(grz_graph* g)
 {
-    if (g->fr.label) return GRZ_OK;
-    const uint64_t V = g->V, W = words_of(V);
     grz_frontier_state& f = g->fr;
+    if (f.label && !f.lists_changed) return GRZ_OK;
+    const uint64_t V = g->V, W = words_of(V);
+    const uint64_t tiles = std::max(g->push.nvec, g->pull.nvec) / PUSH_TILE + 2;
+    if (f.label) {
+        // kept from the graph loaded before, which had the same V
+        if (f.alloc_V != V) return grz_set_error(g, GRZ_ERR_STATE, "frontier buffers sized for another graph");
+        if (tiles > f.tile_cap) {
+            GRZ_CK(g, cudaFree(f.tile_first));
+            f.tile_first = nullptr;
+            GRZ_CK(g, cudaMalloc((void**)&f.tile_first, sizeof(uint32_t) * tiles));
+            f.tile_cap = tiles;
+        }
+        f.lists_changed = 0;
+        return frontier_list_state(g);
+    }
+    f.alloc_V = V;
+    f.tile_cap = tiles;
     GRZ_CK(g, cudaMalloc((void**)&f.label, sizeof(uint32_t) * (V + 1)));
     GRZ_CK(g, cudaMalloc((void**)&f.level, sizeof(uint32_t) * (V + 1)));
     GRZ_CK(g, cudaMalloc((void**)&f.has, sizeof(unsigned long long) * W));
@@ -779,7 +795,7 @@ static int ensure_frontier_state(grz_graph* g)
     GRZ_CK(g, cudaMalloc((void**)&f.frontier, sizeof(uint32_t) * (V + 1)));
     GRZ_CK(g, cudaMalloc((void**)&f.voff, sizeof(uint32_t) * (V + 1)));
     GRZ_CK(g, cudaMalloc((void**)&f.vdelta, sizeof(uint32_t) * (V + 1)));
-    GRZ_CK(g, cudaMalloc((void**)&f.tile_first, sizeof(uint32_t) * (std::max(g->push.nvec, g->pull.nvec) / PUSH_TILE + 2)));
+    GRZ_CK(g, cudaMalloc((void**)&f.tile_first, sizeof(uint32_t) * tiles));
     GRZ_CK(g, cudaMalloc((void**)&f.fr_part, sizeof(uint32_t) * 2 * (V / CCHUNK + 1)));
     GRZ_CK(g, cudaMalloc((void**)&f.nonempty_pull, sizeof(unsigned long long) * W));
     GRZ_CK(g, cudaMalloc((void**)&f.touched, sizeof(uint32_t) * (V + 1)));
@@ -787,6 +803,14 @@ static int ensure_frontier_state(grz_graph* g)
     GRZ_CK(g, cudaMalloc((void**)&f.cand32, sizeof(uint32_t) * (V + 1)));
     GRZ_CK(g, cudaMalloc((void**)&f.counters, sizeof(uint32_t) * 8));
     GRZ_CK(g, cudaMalloc((void**)&f.vote, sizeof(unsigned long long) * GRZ_VOTE_SLOTS * GRZ_VOTE_STRIDE));
+    return frontier_list_state(g);
+}
+
+// the state that depends on the loaded lists, and the scratch values the kernels expect
+static int frontier_list_state(grz_graph* g)
+{
+    const uint64_t V = g->V, W = words_of(V);
+    grz_frontier_state& f = g->fr;
     GRZ_CK(g, cudaMemsetAsync(f.vote, 0, sizeof(unsigned long long) * GRZ_VOTE_SLOTS * GRZ_VOTE_STRIDE, g->stream));
     GRZ_CK(g, cudaMemsetAsync(f.cand64, 0xff, sizeof(unsigned long long) * (V + 1), g->stream));
     GRZ_CK(g, cudaMemsetAsync(f.cand32, 0xff, sizeof(uint32_t) * (V + 1), g->stream));
@@ -1164,6 +1188,16 @@ int grz_frontier_props(grz_graph* g)
     k_u32_to_double<<<blocks_for(g->V), T, 0, g->stream>>>(f.label, g->V, g->prop, f.app == GRZ_APP_BREADTH_FIRST_SEARCH); GRZ_COUNT_LAUNCH(g);
     GRZ_CK(g, cudaGetLastError());
     return GRZ_OK;
+}
+
+void grz_frontier_park(grz_graph* g)
+{
+    grz_frontier_state& f = g->fr;
+    // the captured run names the old lists
+    if (f.run_exec) cudaGraphExecDestroy(f.run_exec);
+    f.run_exec = nullptr;
+    f.run_bm[0] = f.run_bm[1] = nullptr;
+    f.lists_changed = 1;
 }
 
 void grz_frontier_free(grz_graph* g)

@@ -314,6 +314,11 @@ struct grz_frontier_state {
     void* snap;
     uint64_t snap_bytes;
     uint64_t snap_scalars[8];
+    // the buffers outlive a reload of a graph with the same V (cudaMalloc and cudaFree synchronise
+    // the device); what depends on the lists is rebuilt at the next initialisation
+    uint64_t alloc_V;                // V the per-vertex buffers are sized for
+    uint64_t tile_cap;               // entries of tile_first
+    int lists_changed;
 };
 
 struct grz_graph {
@@ -336,6 +341,7 @@ struct grz_graph {
     u128* pr_rowacc;      // u128[V+1] exact per-destination accumulators
     uint32_t* pr_cut;     // uint32[V/32]: destinations whose pull vectors straddle a gather tile
     int pr_rowacc_stale;  // fused iterations cleared only the straddling accumulators
+    int pr_lists_changed; // the PageRank arrays were kept across a reload with the same V
     uint32_t pr_nparts[2];  // partials in each half of pr_sum
     double* pr_d[2];      // double[V+1]: the props as doubles, gathered instead of pr_fx in pr_dmode
     int pr_dmode;         // fused iterations gather pr_d
@@ -450,6 +456,7 @@ int grz_switch_launch_run_decide(grz_graph* g, const unsigned long long* next_fr
 int grz_switch_decide(grz_graph* g, const unsigned long long* frontier, uint64_t vote_override, uint32_t iter,
                       uint64_t* vote, int* next_pull, float* features);
 void grz_frontier_free(grz_graph* g);
+void grz_frontier_park(grz_graph* g);  // before a reload with the same V: keep the buffers
 
 // layout (grz_layout.cu)
 // run_len (optional, uint32[V]): edges of each shared vertex

@@ -372,9 +372,13 @@ int grz_pr_prepare(grz_graph* g)
         GRZ_CK(g, cudaMalloc((void**)&g->pr_sum, sizeof(u128) * 2 * (blocks_for(V) + 1)));
         GRZ_CK(g, cudaMalloc((void**)&g->pr_K, sizeof(double) * 2));
         GRZ_CK(g, cudaMalloc((void**)&g->pr_rowacc, sizeof(u128) * (V + 1)));
+        GRZ_CK(g, cudaMalloc((void**)&g->pr_cut, sizeof(uint32_t) * ((V + 31) / 32 + 1)));
+        g->pr_lists_changed = 1;
+    }
+    if (g->pr_lists_changed) {
+        // (also after a reload with the same V, which kept the arrays)
         GRZ_CK(g, cudaMemsetAsync(g->pr_rowacc, 0, sizeof(u128) * (V + 1), g->stream));
         g->pr_rowacc_stale = 0;
-        GRZ_CK(g, cudaMalloc((void**)&g->pr_cut, sizeof(uint32_t) * ((V + 31) / 32 + 1)));
         if (V) {
             k_pr_cutbits<<<blocks_for(V), PR_THREADS, 0, g->stream>>>(g->pull.rowptr, V, g->pr_cut); GRZ_COUNT_LAUNCH(g);
             GRZ_CK(g, cudaGetLastError());
@@ -382,6 +386,9 @@ int grz_pr_prepare(grz_graph* g)
         // entry V of both prop arrays is a permanent zero that invalid lanes gather
         GRZ_CK(g, cudaMemsetAsync(g->pr_fx[0], 0, sizeof(u128) * (V + 1), g->stream));
         GRZ_CK(g, cudaMemsetAsync(g->pr_fx[1], 0, sizeof(u128) * (V + 1), g->stream));
+        for (double* d : g->pr_d)
+            if (d) GRZ_CK(g, cudaMemsetAsync(d, 0, sizeof(double) * (V + 1), g->stream));
+        g->pr_lists_changed = 0;
     }
     // Doubles gathered instead of 16-byte fixed point: chosen, or when the fixed-point props
     // exceed 6x L2.  Below that the gathers are bound by the L1/L2 path and the per-edge

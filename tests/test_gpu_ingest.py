@@ -265,3 +265,33 @@ def test_pull_only_ingest_small_and_ragged(V, edges):
         for a, b in zip(_lists(A), _lists(B)):
             np.testing.assert_array_equal(a, b)
         np.testing.assert_array_equal(A.connected_components(), B.connected_components())
+
+
+def test_reload_with_same_vertex_count_keeps_buffers_and_results():
+    """A reload with the same V keeps the CC/BFS and PageRank buffers (no cudaFree/cudaMalloc);
+    what depends on the lists (non-empty bitmaps, push tiles, straddle bits, the captured run) is
+    rebuilt.  Every reload must give a fresh graph's results, also after a larger list and after
+    a reload with another V."""
+    import torch
+    from grazelle import graphgen as gg
+    from grazelle.engine import Graph
+    graphs = [gg.rmat(13, 8, seed=1, symmetric=True), gg.rmat(13, 16, seed=2, symmetric=True),
+              gg.rmat(13, 4, seed=3), gg.rmat(12, 16, seed=4, symmetric=True), gg.rmat(13, 16, seed=5)]
+    with Graph(0) as R:
+        for i, g in enumerate(graphs):
+            V = g.num_vertices
+            pull, push = g.pull_order().pairs(), g.push_order().pairs()
+            if i % 2:
+                R.load_pairs(V, pull, push)
+            else:
+                hp = torch.from_numpy(pull.view(np.int64)).pin_memory()
+                R.load_pull_derive_push(V, g.num_edges, hp.data_ptr())
+            with Graph(0) as F:
+                F.load_pairs(V, pull, push)
+                np.testing.assert_array_equal(R.connected_components(), F.connected_components())
+                for root in (0, 5):
+                    pr_, lr = R.bfs(root)
+                    pf, lf = F.bfs(root)
+                    np.testing.assert_array_equal(pr_, pf)
+                    np.testing.assert_array_equal(lr, lf)
+                np.testing.assert_array_equal(R.pagerank(8), F.pagerank(8))

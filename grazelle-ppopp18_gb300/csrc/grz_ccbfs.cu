@@ -735,17 +735,15 @@ __global__ void k_bitmap_init(unsigned long long* __restrict__ bm, uint64_t word
     bm[w] = x;
 }
 
-// bitmap of vertices that own at least one vector in a list
+// bitmap of vertices that own at least one vector in a list: a thread per vertex, a warp per
+// 32-bit half of a bitmap word (the words are little-endian), all `words` words written
 __global__ void k_nonempty(const uint32_t* __restrict__ rowptr, uint64_t V, unsigned long long* __restrict__ bm, uint64_t words)
 {
-    const uint64_t w = (uint64_t)blockIdx.x * T + threadIdx.x;
-    if (w >= words) return;
-    unsigned long long x = 0;
-    for (int k = 0; k < 64; ++k) {
-        const uint64_t v = w * 64 + (uint64_t)k;
-        if (v < V && rowptr[v + 1] > rowptr[v]) x |= 1ull << k;
-    }
-    bm[w] = x;
+    const uint64_t v = (uint64_t)blockIdx.x * T + threadIdx.x;
+    const bool in = v < 64 * words;  // uniform per warp: 64 words is a multiple of 32
+    const bool bit = in && v < V && rowptr[v + 1] > rowptr[v];
+    const unsigned m = __ballot_sync(0xffffffffu, bit);
+    if (in && (threadIdx.x & 31) == 0) reinterpret_cast<uint32_t*>(bm)[v >> 5] = m;
 }
 
 // reference-format output: CC labels as double; BFS parents as double with -1 for unvisited
@@ -817,11 +815,11 @@ static int frontier_list_state(grz_graph* g)
     GRZ_CK(g, cudaMemsetAsync(f.nonempty_push, 0, sizeof(unsigned long long) * W, g->stream));
     GRZ_CK(g, cudaMemsetAsync(f.nonempty_pull, 0, sizeof(unsigned long long) * W, g->stream));
     if (g->pull.rowptr && V) {
-        k_nonempty<<<blocks_for(W), T, 0, g->stream>>>(g->pull.rowptr, V, f.nonempty_pull, W); GRZ_COUNT_LAUNCH(g);
+        k_nonempty<<<blocks_for(64 * W), T, 0, g->stream>>>(g->pull.rowptr, V, f.nonempty_pull, W); GRZ_COUNT_LAUNCH(g);
         GRZ_CK(g, cudaGetLastError());
     }
     if (g->push.rowptr && V) {
-        k_nonempty<<<blocks_for(W), T, 0, g->stream>>>(g->push.rowptr, V, f.nonempty_push, W); GRZ_COUNT_LAUNCH(g);
+        k_nonempty<<<blocks_for(64 * W), T, 0, g->stream>>>(g->push.rowptr, V, f.nonempty_push, W); GRZ_COUNT_LAUNCH(g);
         GRZ_CK(g, cudaGetLastError());
     }
     return GRZ_OK;

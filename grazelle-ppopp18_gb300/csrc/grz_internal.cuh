@@ -476,7 +476,7 @@ int grz_build_list_from_bounds(grz_graph* g, grz_list* L, const uint64_t* d_pair
                                uint32_t* run_len, cudaStream_t st, uint64_t written_cap);
 #define GRZ_LOAD_DERIVE_PUSH 1
 int grz_alloc_outdegrees(grz_graph* g);
-int grz_build_outdegrees(grz_graph* g, const uint64_t* d_pull_pairs, uint64_t E);
+int grz_build_outdegrees(grz_graph* g, const uint64_t* d_pull_pairs, uint64_t E, cudaStream_t st = nullptr);
 
 // scans (grz_scan.cu): exclusive sum of uint32 into uint32 (n < 2^32), inclusive max of uint32
 int grz_exclusive_sum_u32(grz_graph* g, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total_out_dev);

@@ -333,13 +333,13 @@ int grz_alloc_outdegrees(grz_graph* g)
 
 // Outdegrees: counted from the -pull pairs, or (d_pull_pairs null) already in g->degree, where
 // grz_build_list put the run lengths of a -push list derived from those pairs.
-int grz_build_outdegrees(grz_graph* g, const uint64_t* d_pull_pairs, uint64_t E)
+int grz_build_outdegrees(grz_graph* g, const uint64_t* d_pull_pairs, uint64_t E, cudaStream_t st)
 {
     const uint64_t V = g->V;
-    cudaStream_t st = g->stream;
+    if (!st) st = g->stream;
     int rc = grz_alloc_outdegrees(g);
     if (rc) return rc;
-    GRZ_CK(g, cudaMemsetAsync(g->outdeg, 0, sizeof(double) * (V + 8), st));
+    GRZ_CK(g, cudaMemsetAsync(g->outdeg + V, 0, sizeof(double) * 8, st));  // the padding; k_degree_to_double writes the rest
     if (E > 0 && d_pull_pairs) {
         k_degree<<<grid_blocks_for(E), BT, 0, st>>>(d_pull_pairs, E, g->degree); GRZ_COUNT_LAUNCH(g);
         GRZ_CK(g, cudaGetLastError());

@@ -473,6 +473,14 @@ int grz_ingest_pull_derive(grz_graph* g, const uint64_t* pull, uint64_t E, const
     for (int b = 0; b < 3; ++b)
         if (b < 2 || passes > 1) IRC(grz_dev_alloc(g, (void**)&kbuf[b], sizeof(unsigned long long) * E));
     for (uint64_t r = 0; r < nslots; ++r) IRC(grz_dev_alloc(g, (void**)&slot[r], sizeof(ulonglong2) * tpc * STILE));
+    // 1. the first chunks start crossing the link as soon as their slots exist
+    if (host) {
+        ICK(grz_copy_stream(g));
+        cs = g->copy_stream;
+        ICK(cudaEventRecord(ev[2 * nchunks], st));  // after the slots' allocation
+        ICK(cudaStreamWaitEvent(cs, ev[2 * nchunks], 0));
+        for (uint64_t c = 0; c < nslots; ++c) ICK(copy_chunk(c));
+    }
     IRC(grz_dev_alloc(g, (void**)&rank, sizeof(uint32_t) * E));
     IRC(grz_dev_alloc(g, (void**)&hist, sizeof(uint32_t) * RBINS * ntiles));
     IRC(grz_dev_alloc(g, (void**)&start, sizeof(uint32_t) * (V + 1)));
@@ -488,14 +496,6 @@ int grz_ingest_pull_derive(grz_graph* g, const uint64_t* pull, uint64_t E, const
     ICK(cudaMemsetAsync(start, 0, sizeof(uint32_t) * (V + 1), st));
     ICK(cudaMemsetAsync(end, 0, sizeof(uint32_t) * (V + 1), st));
     ICK(cudaMemsetAsync(flags, 0, sizeof(unsigned) * 2, st));
-    // 1. the first chunks start crossing the link
-    if (host) {
-        ICK(grz_copy_stream(g));
-        cs = g->copy_stream;
-        ICK(cudaEventRecord(ev[2 * nchunks], st));  // after the slots' allocation
-        ICK(cudaStreamWaitEvent(cs, ev[2 * nchunks], 0));
-        for (uint64_t c = 0; c < nslots; ++c) ICK(copy_chunk(c));
-    }
     // 2. per chunk, once it is in: the first pass, its -pull vectors, its sort by source and its
     //    edges' ranks; its slot then takes the chunk nslots further on
     for (uint64_t c = 0; c < nchunks; ++c) {
@@ -535,27 +535,24 @@ int grz_ingest_pull_derive(grz_graph* g, const uint64_t* pull, uint64_t E, const
         ICK(cudaGetLastError());
         sorted = in - e0;
     }
-    // 3. the input checks, then the -pull list's offsets and index (its vectors are written)
-    ICK(cudaMemcpyAsync(flags_h, flags, sizeof(flags_h), cudaMemcpyDeviceToHost, st));
-    ICK(cudaMemcpyAsync(&kends[0], kbuf[0], sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-    ICK(cudaMemcpyAsync(&kends[1], kbuf[0] + (E - 1), sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-    ICK(cudaStreamSynchronize(st));
-    if (flags_h[0]) { rc = grz_set_error(g, GRZ_ERR_UNSORTED, "pull list is not grouped by destination in ascending order"); goto done; }
-    if (flags_h[1]) { rc = grz_set_error(g, GRZ_ERR_RANGE, "pull list holds a vertex ID >= V (%llu)", (unsigned long long)V); goto done; }
-    ICK(cudaMallocAsync((void**)&P->vindex, sizeof(uint64_t) * vi_count, st));
-    ICK(cudaMallocAsync((void**)&P->rowptr, sizeof(uint32_t) * (V + 1), st));
-    IRC(grz_build_list_from_bounds(g, P, nullptr, E, 1, start, end, kends[0] & 0xffffffffull, kends[1] & 0xffffffffull, nullptr,
-                                   st, pcap));
-    // 4. the -push list: offsets from the outdegrees (its run lengths), then every edge into its lane
+    // 3. after the last chunk: the input checks and the -push list's offsets (from the outdegrees,
+    //    its run lengths) on the graph's stream
     IRC(grz_dev_alloc(g, (void**)&cnt, sizeof(uint32_t) * (V + 1)));
     IRC(grz_dev_alloc(g, (void**)&tot, sizeof(uint32_t)));
     ICK(cudaMallocAsync((void**)&Q->vindex, sizeof(uint64_t) * vi_count, st));
     ICK(cudaMallocAsync((void**)&Q->rowptr, sizeof(uint32_t) * (V + 1), st));
+    ICK(cudaMallocAsync((void**)&P->vindex, sizeof(uint64_t) * vi_count, st));
+    ICK(cudaMallocAsync((void**)&P->rowptr, sizeof(uint32_t) * (V + 1), st));
+    ICK(cudaMemcpyAsync(flags_h, flags, sizeof(flags_h), cudaMemcpyDeviceToHost, st));
+    ICK(cudaMemcpyAsync(&kends[0], kbuf[0], sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    ICK(cudaMemcpyAsync(&kends[1], kbuf[0] + (E - 1), sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     k_run_vectors<<<blocks_of(V + 1), ST, 0, st>>>(g->degree, V, cnt); GRZ_COUNT_LAUNCH(g);
     ICK(cudaGetLastError());
     IRC(grz_exclusive_sum_u32(g, cnt, Q->rowptr, V + 1, tot));
     ICK(cudaMemcpyAsync(&nv32, tot, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     ICK(cudaStreamSynchronize(st));
+    if (flags_h[0]) { rc = grz_set_error(g, GRZ_ERR_UNSORTED, "pull list is not grouped by destination in ascending order"); goto done; }
+    if (flags_h[1]) { rc = grz_set_error(g, GRZ_ERR_RANGE, "pull list holds a vertex ID >= V (%llu)", (unsigned long long)V); goto done; }
     Q->nvec = nv32;
     ICK(cudaMallocAsync((void**)&Q->nbr, sizeof(uint4) * Q->nvec, st));
     ICK(cudaMallocAsync((void**)&Q->shared, sizeof(uint32_t) * Q->nvec, st));
@@ -571,6 +568,15 @@ int grz_ingest_pull_derive(grz_graph* g, const uint64_t* pull, uint64_t E, const
                                                                   Q->shared); GRZ_COUNT_LAUNCH(g);
         ICK(cudaGetLastError());
     }
+    // 4. meanwhile on the second stream: the -pull list's offsets and index (its vectors are
+    //    written) and the outdegrees as doubles
+    ICK(grz_copy_stream(g));
+    cs = g->copy_stream;
+    ICK(cudaEventRecord(ev[2 * nchunks], st));
+    ICK(cudaStreamWaitEvent(cs, ev[2 * nchunks], 0));
+    IRC(grz_build_list_from_bounds(g, P, nullptr, E, 1, start, end, kends[0] & 0xffffffffull, kends[1] & 0xffffffffull, nullptr,
+                                   cs, pcap));
+    IRC(grz_build_outdegrees(g, nullptr, E, cs));
     // the -push vertex index: its first and last shared vertices are those of its end vectors
     ICK(cudaMemcpyAsync(&qends[0], Q->shared, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     ICK(cudaMemcpyAsync(&qends[1], Q->shared + (Q->nvec - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
@@ -580,11 +586,10 @@ int grz_ingest_pull_derive(grz_graph* g, const uint64_t* pull, uint64_t E, const
     Q->vs = nullptr;
     k_run_vindex<<<blocks_of(vi_count), ST, 0, st>>>(g->degree, Q->rowptr, V, vi_count, qends[1], Q->vindex); GRZ_COUNT_LAUNCH(g);
     ICK(cudaGetLastError());
-    IRC(grz_build_outdegrees(g, nullptr, E));
 done:
 #undef ICK
 #undef IRC
-    // the temporaries are freed on the graph's stream once the copies into the slots are done too
+    // the temporaries are freed on the graph's stream once the second stream's work is done too
     if (cs && (cudaEventRecord(g->copy_ev[1], cs) != cudaSuccess || cudaStreamWaitEvent(st, g->copy_ev[1], 0) != cudaSuccess))
         cudaStreamSynchronize(cs);
     for (void* q : { (void*)kbuf[0], (void*)kbuf[1], (void*)kbuf[2], (void*)rank, (void*)hist, (void*)start, (void*)end, (void*)off,

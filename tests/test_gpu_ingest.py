@@ -295,3 +295,15 @@ def test_reload_with_same_vertex_count_keeps_buffers_and_results():
                     np.testing.assert_array_equal(pr_, pf)
                     np.testing.assert_array_equal(lr, lf)
                 np.testing.assert_array_equal(R.pagerank(8), F.pagerank(8))
+
+
+def test_ingest_chunks_tuning_bounds():
+    from grazelle import native
+    from grazelle.engine import Graph
+    with Graph(0) as G:
+        G.tune(ingest_chunks=64)
+        assert G.tuning()["ingest_chunks"] == 64
+        with pytest.raises(native.GrzError) as ei:
+            G.tune(ingest_chunks=65)
+        assert ei.value.code == -5
+        assert G.tuning()["ingest_chunks"] == 64

@@ -39,6 +39,7 @@ constexpr int RBITS = 8;
 constexpr int RBINS = 1 << RBITS;
 constexpr uint64_t CHUNK_EDGES = 1ull << 24;  // pairs per ingest chunk by default (GB300 sweep at 520M pairs:
 constexpr uint64_t AUTO_CHUNKS_MAX = 64;      // 8 chunks 45.4 ms, 24 43.7, 32-64 43.5; one chunk 65.1)
+constexpr int TAIL_SPLITS = 3;                // the last regular chunk is cut into halves, quarters, ...
 constexpr uint64_t STAGE_SLOTS = 3;           // device slots the chunks of pinned host pairs are copied into
 constexpr uint64_t PLACE_BLOCK_BYTES = 24ull << 20;  // -push vectors per placement block (L2: 126 MB)
 constexpr uint64_t PLACE_MAX_BLOCKS = 4096;
@@ -344,14 +345,14 @@ __global__ void k_src_ranks(const unsigned long long* __restrict__ keys, uint64_
 // chunk c's sorted keys whose source lies in block b or later (seg[c][nb] = the chunk's end), so
 // the edges of block b from every chunk are placed together and the partial-sector writes of the
 // chunks meet in L2 instead of in DRAM.
-__global__ void k_seg_bounds(const unsigned long long* __restrict__ keys, uint64_t E, uint64_t chunk_edges, uint32_t nchunks,
+__global__ void k_seg_bounds(const unsigned long long* __restrict__ keys, const uint64_t* __restrict__ cstart, uint32_t nchunks,
                              const uint32_t* __restrict__ rowptr, uint64_t V, uint64_t nvec, uint32_t nb,
                              uint64_t* __restrict__ seg)
 {
     const uint64_t i = (uint64_t)blockIdx.x * ST + threadIdx.x;
     if (i >= (uint64_t)nchunks * (nb + 1)) return;
     const uint32_t c = (uint32_t)(i / (nb + 1)), b = (uint32_t)(i % (nb + 1));
-    const uint64_t lo0 = (uint64_t)c * chunk_edges, hi0 = min(lo0 + chunk_edges, E);
+    const uint64_t lo0 = cstart[c], hi0 = cstart[c + 1];
     if (b == nb) { seg[i] = hi0; return; }
     // first source of the block: the smallest s with rowptr[s] >= b nvec / nb
     const uint64_t target = (uint64_t)b * nvec / nb;
@@ -435,7 +436,23 @@ int grz_ingest_pull_derive(grz_graph* g, const uint64_t* pull, uint64_t E, const
     if (nchunks == 0) nchunks = std::min<uint64_t>(AUTO_CHUNKS_MAX, std::max<uint64_t>(1, (E + CHUNK_EDGES - 1) / CHUNK_EDGES));
     nchunks = std::min<uint64_t>(nchunks, ntiles);
     const uint64_t tpc = (ntiles + nchunks - 1) / nchunks;  // tiles per chunk
-    nchunks = (ntiles + tpc - 1) / tpc;
+    // chunk c is tiles [ct[c], ct[c + 1]): tpc each, and the rest (at most tpc) in halves, so
+    // that the last chunk, whose work follows the link, is small
+    uint64_t ct[GRZ_INGEST_MAX_CHUNKS + TAIL_SPLITS + 2];
+    nchunks = 0;
+    {
+        uint64_t t = 0;
+        while (ntiles - t > tpc) { ct[nchunks++] = t; t += tpc; }
+        uint64_t rest = ntiles - t;
+        for (int k = 0; k < TAIL_SPLITS && rest > 1; ++k) {
+            const uint64_t piece = (rest + 1) / 2;
+            ct[nchunks++] = t;
+            t += piece;
+            rest -= piece;
+        }
+        ct[nchunks++] = t;
+        ct[nchunks] = ntiles;
+    }
     const uint64_t vi_count = V + 64;
     const ulonglong2* all = reinterpret_cast<const ulonglong2*>(pull);
     grz_list* P = &g->pull;
@@ -443,6 +460,7 @@ int grz_ingest_pull_derive(grz_graph* g, const uint64_t* pull, uint64_t E, const
     unsigned long long* kbuf[3] = { nullptr, nullptr, nullptr };  // input-order keys, then the sort's two buffers
     uint32_t *hist = nullptr, *start = nullptr, *end = nullptr, *off = nullptr, *rank = nullptr, *cnt = nullptr, *tot = nullptr;
     uint32_t *heads = nullptr, *carry = nullptr;
+    uint64_t* cstart = nullptr;  // first edge of each chunk, and E
     // the -pull list's vectors, numbered as they are written: at most E/4 + one partial vector per destination
     const uint64_t pcap = E / 4 + std::min<uint64_t>(V, E) + 1;
     unsigned* flags = nullptr;
@@ -452,14 +470,14 @@ int grz_ingest_pull_derive(grz_graph* g, const uint64_t* pull, uint64_t E, const
     uint32_t nv32 = 0;
     uint32_t qends[2] = { 0, 0 };
     // ev[c]: chunk c is in its slot; ev[nchunks + c]: its slot is free again; ev[2 nchunks]: set-up done
-    cudaEvent_t ev[2 * GRZ_INGEST_MAX_CHUNKS + 1] = {};
+    cudaEvent_t ev[2 * (GRZ_INGEST_MAX_CHUNKS + TAIL_SPLITS + 1) + 1] = {};
     int nev = 0;
     cudaStream_t cs = nullptr;
     const uint64_t nslots = host ? std::min<uint64_t>(nchunks, STAGE_SLOTS) : 0;
     ulonglong2* slot[STAGE_SLOTS] = {};
     const unsigned long long* sorted = nullptr;
     auto copy_chunk = [&](uint64_t c) -> cudaError_t {
-        const uint64_t e0 = c * tpc * STILE, n = std::min<uint64_t>(tpc * STILE, E - e0);
+        const uint64_t e0 = ct[c] * STILE, n = std::min<uint64_t>(ct[c + 1] * STILE, E) - e0;
         cudaError_t e = cudaSuccess;
         if (c >= nslots) e = cudaStreamWaitEvent(cs, ev[nchunks + c - nslots], 0);
         if (e == cudaSuccess) e = cudaMemcpyAsync(slot[c % nslots], host + 2 * e0, sizeof(ulonglong2) * n, cudaMemcpyHostToDevice, cs);
@@ -499,7 +517,7 @@ int grz_ingest_pull_derive(grz_graph* g, const uint64_t* pull, uint64_t E, const
     // 2. per chunk, once it is in: the first pass, its -pull vectors, its sort by source and its
     //    edges' ranks; its slot then takes the chunk nslots further on
     for (uint64_t c = 0; c < nchunks; ++c) {
-        const uint64_t t0 = c * tpc, nt = std::min<uint64_t>(tpc, ntiles - t0);
+        const uint64_t t0 = ct[c], nt = ct[c + 1] - t0;
         const uint64_t e0 = t0 * STILE, n = std::min<uint64_t>(nt * STILE, E - e0);
         uint32_t* h = hist + RBINS * t0;
         if (host) ICK(cudaStreamWaitEvent(st, ev[c], 0));
@@ -560,8 +578,13 @@ int grz_ingest_pull_derive(grz_graph* g, const uint64_t* pull, uint64_t E, const
         const uint64_t nb = std::min<uint64_t>(PLACE_MAX_BLOCKS, std::max<uint64_t>(1, Q->nvec * sizeof(uint4) / PLACE_BLOCK_BYTES));
         const uint64_t per = (E + nb * nchunks - 1) / (nb * nchunks);  // edges per (block, chunk) on average
         const uint64_t xs = std::max<uint64_t>(1, (per + PLACE_EDGES_PER_THREAD * ST - 1) / (PLACE_EDGES_PER_THREAD * ST));
+        uint64_t cs_h[GRZ_INGEST_MAX_CHUNKS + TAIL_SPLITS + 2];
+        for (uint64_t c = 0; c <= nchunks; ++c) cs_h[c] = std::min<uint64_t>(ct[c] * STILE, E);
         IRC(grz_dev_alloc(g, (void**)&seg, sizeof(uint64_t) * nchunks * (nb + 1)));
-        k_seg_bounds<<<blocks_of(nchunks * (nb + 1)), ST, 0, st>>>(sorted, E, tpc * STILE, (uint32_t)nchunks, Q->rowptr, V, Q->nvec,
+        IRC(grz_dev_alloc(g, (void**)&cstart, sizeof(uint64_t) * (nchunks + 1)));
+        ICK(cudaMemcpyAsync(cstart, cs_h, sizeof(uint64_t) * (nchunks + 1), cudaMemcpyHostToDevice, st));
+        ICK(cudaStreamSynchronize(st));  // cs_h is on this stack frame
+        k_seg_bounds<<<blocks_of(nchunks * (nb + 1)), ST, 0, st>>>(sorted, cstart, (uint32_t)nchunks, Q->rowptr, V, Q->nvec,
                                                                   (uint32_t)nb, seg); GRZ_COUNT_LAUNCH(g);
         k_push_place<<<(unsigned)(nb * nchunks * xs), ST, 0, st>>>(sorted, rank, seg, (uint32_t)nchunks, (uint32_t)nb, (uint32_t)xs,
                                                                   g->degree, Q->rowptr, reinterpret_cast<uint32_t*>(Q->nbr),
@@ -593,7 +616,7 @@ done:
     if (cs && (cudaEventRecord(g->copy_ev[1], cs) != cudaSuccess || cudaStreamWaitEvent(st, g->copy_ev[1], 0) != cudaSuccess))
         cudaStreamSynchronize(cs);
     for (void* q : { (void*)kbuf[0], (void*)kbuf[1], (void*)kbuf[2], (void*)rank, (void*)hist, (void*)start, (void*)end, (void*)off,
-                     (void*)cnt, (void*)tot, (void*)flags, (void*)seg, (void*)heads, (void*)carry })
+                     (void*)cnt, (void*)tot, (void*)flags, (void*)seg, (void*)heads, (void*)carry, (void*)cstart })
         grz_dev_free(g, q);
     for (void* q : slot) grz_dev_free(g, q);
     for (int i = 0; i < nev; ++i) cudaEventDestroy(ev[i]);

@@ -72,9 +72,11 @@ __device__ __forceinline__ uint32_t graph_of(const uint32_t* voff, uint32_t G, u
     return lo;
 }
 
-// initial PPR state: prop = one-hot(seed) / deg'; S = deg(seed) * prop(seed) per (graph, instance)
+// initial PPR state: prop = one-hot(seed) / deg'; S = deg(seed) * prop(seed) per (graph, instance).
+// The props are 4.124 fixed point (prop) or the doubles they are the exact conversions of (propd).
 __global__ void k_ppr_init(const uint32_t* __restrict__ seeds, uint32_t G, const double* __restrict__ inv_deg,
-                           const uint32_t* __restrict__ degree, u128* __restrict__ prop, u128* __restrict__ S)
+                           const uint32_t* __restrict__ degree, u128* __restrict__ prop, double* __restrict__ propd,
+                           u128* __restrict__ S)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= G * K) return;
@@ -83,7 +85,8 @@ __global__ void k_ppr_init(const uint32_t* __restrict__ seeds, uint32_t G, const
     u128 v = u128_zero();
     if (s != NONE) {
         const u128 p = fx_from_double(inv_deg[s]);
-        prop[(uint64_t)s * K + i] = p;
+        if (propd) propd[(uint64_t)s * K + i] = inv_deg[s];
+        else prop[(uint64_t)s * K + i] = p;
         v = u128_mul32(p, degree[s]);
     }
     S[t] = v;
@@ -111,6 +114,10 @@ constexpr int GCHUNK = 2;       // steps whose loads are issued together
 // chunk 1-8 and 4-8 blocks per SM: 99.8 ms per 256-instance run here, 102-163 ms elsewhere)
 constexpr int GATHER_RESIDENT = 6;
 
+// a gathered prop in fixed point: read as such, or converted (exactly) from the double it came from
+__device__ __forceinline__ u128 ld_prop(const u128* p) { return ldg_u128(p); }
+__device__ __forceinline__ u128 ld_prop(const double* p) { return fx_from_double(__ldg(p)); }
+
 __device__ __forceinline__ u128 shfl_u128(u128 v, int src)
 {
     u128 r;
@@ -119,8 +126,9 @@ __device__ __forceinline__ u128 shfl_u128(u128 v, int src)
     return r;
 }
 
+template <typename P>
 __global__ void __launch_bounds__(GT, GATHER_RESIDENT) k_ppr_gather(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv,
-                                                   uint64_t nvec, uint32_t V, const u128* __restrict__ prop,
+                                                   uint64_t nvec, uint32_t V, const P* __restrict__ prop,
                                                    u128* __restrict__ rowacc, u128* __restrict__ S_next, uint32_t nS)
 {
     if (blockIdx.x == 0)
@@ -149,7 +157,7 @@ __global__ void __launch_bounds__(GT, GATHER_RESIDENT) k_ppr_gather(const uint4*
                     const uint32_t ids[4] = { sv.x, sv.y, sv.z, sv.w };
 #pragma unroll
                     for (int l = 0; l < 4; ++l)
-                        if (ids[l] < V) val[j] = u128_add(val[j], ldg_u128(prop + (uint64_t)ids[l] * K + inst));
+                        if (ids[l] < V) val[j] = u128_add(val[j], ld_prop(prop + (uint64_t)ids[l] * K + inst));
                 }
             }
 #pragma unroll
@@ -213,7 +221,8 @@ __global__ void __launch_bounds__(GT, 3) k_ppr_apply(u128* __restrict__ rowacc, 
                                                      const uint32_t* __restrict__ voff_g, uint32_t G,
                                                      const uint32_t* __restrict__ seeds, double damping,
                                                      const u128* __restrict__ S_cur, u128* __restrict__ S_next,
-                                                     u128* __restrict__ prop_out, double* __restrict__ rank_out)
+                                                     u128* __restrict__ prop_out, double* __restrict__ propd_out,
+                                                     double* __restrict__ rank_out)
 {
     __shared__ uint32_t voff[MAX_GRAPHS + 1];
     __shared__ u128 s_part[APPLY_SLOTS * K];
@@ -262,14 +271,16 @@ __global__ void __launch_bounds__(GT, 3) k_ppr_apply(u128* __restrict__ rowacc, 
             const bool mass = (a[j].lo | a[j].hi) != 0;
             if (mass && ((cw[j] >> lv) & 1u)) rowacc[idx] = u128_zero();
             // rank' = fma(accum, d, [v == seed] * teleport); zero without mass (most vertices early on)
-            double rank = 0.0;
+            double rank = 0.0, pd = 0.0;
             u128 p = u128_zero();
             if (seed != NONE && (mass || v == seed)) {
                 rank = __fma_rn(fx_to_double(a[j]), damping, v == seed ? cseed : 0.0);
-                p = fx_from_double(__dmul_rn(rank, __ldg(inv_deg + v)));
+                pd = __dmul_rn(rank, __ldg(inv_deg + v));
+                p = fx_from_double(pd);
                 if (p.lo | p.hi) acc = u128_add(acc, u128_mul32(p, __ldg(degree + v)));
             }
-            *(reinterpret_cast<ulonglong2*>(prop_out) + idx) = make_ulonglong2(p.lo, p.hi);
+            if (propd_out) propd_out[idx] = pd;  // the gather converts it to p
+            else *(reinterpret_cast<ulonglong2*>(prop_out) + idx) = make_ulonglong2(p.lo, p.hi);
             if (rank_out) rank_out[idx] = rank;
         }
     }
@@ -404,6 +415,9 @@ struct grz_batch {
     uint32_t* d_seeds;                   // [G][K] union vertex IDs or NONE
     // PPR
     u128* prop[2];                       // [vertex][instance] 4.124 fixed point
+    double* propd[2];                    // the same props as the doubles they convert from exactly
+    int ppr_props;                       // tuning: 0 or 1 fixed point, 2 doubles
+    int ppr_dmode;                       // the captured loop gathers propd
     double* rank;
     u128* rowacc;
     uint32_t* cut;                       // [V/32] accumulators the apply clears (k_ppr_cutbits)
@@ -464,11 +478,12 @@ extern "C" int grz_batch_create(grz_batch** out, int device, void* stream)
 
 static void free_state(grz_batch* b)
 {
-    void* p[] = { b->d_voff, b->d_seeds, b->prop[0], b->prop[1], b->rank, b->rowacc, b->cut, b->S[0], b->S[1],
+    void* p[] = { b->d_voff, b->d_seeds, b->prop[0], b->prop[1], b->propd[0], b->propd[1], b->rank, b->rowacc, b->cut, b->S[0], b->S[1],
                   b->visited, b->frontier, b->next_words, b->level, b->ctl, b->iter };
     for (void* x : p) cudaFree(x);
     b->d_voff = b->d_seeds = nullptr;
     b->prop[0] = b->prop[1] = nullptr;
+    b->propd[0] = b->propd[1] = nullptr;
     b->rank = nullptr;
     b->rowacc = b->S[0] = b->S[1] = nullptr;
     b->cut = nullptr;
@@ -569,7 +584,7 @@ static int upload_seeds(grz_batch* b, const uint32_t* local, uint32_t k)
 }
 
 // the fixed-length PPR iteration loop as one CUDA graph (gather + apply per iteration)
-static int build_ppr_graph(grz_batch* b, uint32_t iterations, double damping)
+static int build_ppr_graph(grz_batch* b, uint32_t iterations, double damping, int dmode)
 {
     if (b->ppr_exec) { cudaGraphExecDestroy(b->ppr_exec); b->ppr_exec = nullptr; }
     grz_graph* u = b->u;
@@ -580,7 +595,9 @@ static int build_ppr_graph(grz_batch* b, uint32_t iterations, double damping)
     int rc = bck(b, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "begin capture");
     // the gather's unit is a warp tile of TV vectors; blocks beyond residency would only queue
     int gres = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gres, k_ppr_gather, GT, 0) != cudaSuccess || gres < 1) {
+    const cudaError_t oe = dmode ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gres, k_ppr_gather<double>, GT, 0)
+                                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gres, k_ppr_gather<u128>, GT, 0);
+    if (oe != cudaSuccess || gres < 1) {
         cudaGetLastError();
         gres = 1;
     }
@@ -590,9 +607,13 @@ static int build_ppr_graph(grz_batch* b, uint32_t iterations, double damping)
     const unsigned agrid = persistent_grid(b, (V + TV - 1) / TV, std::min(b->ppr_blocks, 3));
     int cur = 0;
     for (uint32_t it = 0; it < iterations && !rc; ++it) {
-        k_ppr_gather<<<ggrid, GT, 0, cs>>>(u->pull.nbr, u->pull.shared, u->pull.nvec, V, b->prop[cur], b->rowacc, b->S[cur ^ 1], G * K);
+        if (dmode)
+            k_ppr_gather<<<ggrid, GT, 0, cs>>>(u->pull.nbr, u->pull.shared, u->pull.nvec, V, b->propd[cur], b->rowacc, b->S[cur ^ 1], G * K);
+        else
+            k_ppr_gather<<<ggrid, GT, 0, cs>>>(u->pull.nbr, u->pull.shared, u->pull.nvec, V, b->prop[cur], b->rowacc, b->S[cur ^ 1], G * K);
         k_ppr_apply<<<agrid, GT, 0, cs>>>(b->rowacc, b->cut, u->inv_deg, u->degree, V, b->d_voff, G, b->d_seeds, damping, b->S[cur],
-                                         b->S[cur ^ 1], b->prop[cur ^ 1], it + 1 == iterations ? b->rank : nullptr);
+                                         b->S[cur ^ 1], b->prop[cur ^ 1], dmode ? b->propd[cur ^ 1] : nullptr,
+                                         it + 1 == iterations ? b->rank : nullptr);
         cur ^= 1;
         rc = bck(b, cudaGetLastError(), "ppr launch");
     }
@@ -605,6 +626,7 @@ static int build_ppr_graph(grz_batch* b, uint32_t iterations, double damping)
     b->ppr_iters = iterations;
     b->ppr_damping = damping;
     b->ppr_final = cur;
+    b->ppr_dmode = dmode;
     return GRZ_OK;
 }
 
@@ -631,10 +653,21 @@ extern "C" int grz_batch_ppr(grz_batch* b, const uint32_t* seeds, uint32_t k, ui
         k_ppr_cutbits<<<(unsigned)((V + 255) / 256), 256, 0, b->stream>>>(u->pull.rowptr, (uint32_t)V, b->cut);
         BCK(b, cudaGetLastError());
     }
+    // Doubles gathered instead of 16-byte fixed point only when chosen: each row of a source's 8
+    // instances is 64 bytes instead of 128, and the gather converts each double exactly to the
+    // fixed point the apply would have stored, so the sums and results are the same bit for bit.
+    // The gather is bound by L1TEX and instructions, not DRAM, so the conversions cost more than
+    // the halved rows save: GB300, the 32-graph batch (1.9 GB of fixed-point rows, 15x L2), 256
+    // instances x 20 iterations: 101 ms fixed point, 155 ms doubles.
+    const int dmode = b->ppr_props == 2;
+    if (dmode && !b->propd[0]) {
+        BCK(b, cudaMalloc((void**)&b->propd[0], sizeof(double) * V * K));
+        BCK(b, cudaMalloc((void**)&b->propd[1], sizeof(double) * V * K));
+    }
     int rc = upload_seeds(b, seeds, k);
     if (rc) return rc;
-    if (!b->ppr_exec || b->ppr_iters != iterations || b->ppr_damping != damping) {
-        rc = build_ppr_graph(b, iterations, damping);
+    if (!b->ppr_exec || b->ppr_iters != iterations || b->ppr_damping != damping || b->ppr_dmode != dmode) {
+        rc = build_ppr_graph(b, iterations, damping, dmode);
         if (rc) return rc;
     }
     cudaEvent_t e0, e1;
@@ -642,9 +675,11 @@ extern "C" int grz_batch_ppr(grz_batch* b, const uint32_t* seeds, uint32_t k, ui
     BCK(b, cudaEventCreate(&e1));
     cudaStream_t st = b->stream;
     rc = bck(b, cudaEventRecord(e0, st), "event");
-    if (!rc) rc = bck(b, cudaMemsetAsync(b->prop[0], 0, sizeof(u128) * V * K, st), "memset");
+    if (!rc && dmode) rc = bck(b, cudaMemsetAsync(b->propd[0], 0, sizeof(double) * V * K, st), "memset");
+    if (!rc && !dmode) rc = bck(b, cudaMemsetAsync(b->prop[0], 0, sizeof(u128) * V * K, st), "memset");
     if (!rc) {
-        k_ppr_init<<<(G * K + 255) / 256, 256, 0, st>>>(b->d_seeds, G, u->inv_deg, u->degree, b->prop[0], b->S[0]);
+        k_ppr_init<<<(G * K + 255) / 256, 256, 0, st>>>(b->d_seeds, G, u->inv_deg, u->degree, b->prop[0], dmode ? b->propd[0] : nullptr,
+                                                        b->S[0]);
         rc = bck(b, cudaGetLastError(), "ppr init");
     }
     if (!rc) rc = bck(b, cudaGraphLaunch(b->ppr_exec, st), "graph launch");
@@ -784,6 +819,11 @@ extern "C" int grz_batch_msbfs(grz_batch* b, const uint32_t* roots, uint32_t k, 
 extern "C" int grz_batch_tune_set(grz_batch* b, int param, int64_t value)
 {
     if (!b) return GRZ_ERR_ARG;
+    if (param == GRZ_BATCH_TUNE_PPR_PROPS) {
+        if (value < 0 || value > 2) return bset(b, GRZ_ERR_RANGE, "PPR props must be 0 (by size), 1 (fixed point) or 2 (doubles)");
+        b->ppr_props = (int)value;  // the next run captures its loop again if the mode changes
+        return GRZ_OK;
+    }
     if (value < 1 || value > 32) return bset(b, GRZ_ERR_RANGE, "blocks per SM must be 1..32");
     int* slot = param == GRZ_BATCH_TUNE_PPR_BLOCKS ? &b->ppr_blocks : (param == GRZ_BATCH_TUNE_BFS_BLOCKS ? &b->bfs_blocks : nullptr);
     if (!slot) return bset(b, GRZ_ERR_ARG, "unknown batch tuning parameter");
@@ -802,6 +842,7 @@ extern "C" int grz_batch_tune_get(const grz_batch* b, int param, int64_t* value)
     if (!b || !value) return GRZ_ERR_ARG;
     if (param == GRZ_BATCH_TUNE_PPR_BLOCKS) *value = b->ppr_blocks;
     else if (param == GRZ_BATCH_TUNE_BFS_BLOCKS) *value = b->bfs_blocks;
+    else if (param == GRZ_BATCH_TUNE_PPR_PROPS) *value = b->ppr_props;
     else return GRZ_ERR_ARG;
     return GRZ_OK;
 }

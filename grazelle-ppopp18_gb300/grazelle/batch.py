@@ -88,16 +88,19 @@ class Batch:
         self._ck(self.lib.grz_batch_msbfs(self.h, a.ctypes.data, k, out.ctypes.data if levels else None, C.byref(st)))
         return ([out[self.voff[g]:self.voff[g + 1]] for g in range(len(self.sizes))] if levels else None), st
 
-    def tune(self, ppr_blocks: int | None = None, bfs_blocks: int | None = None):
-        """Resident blocks per SM of the persistent batch kernels (results never depend on them)."""
-        for p, v in ((native.BATCH_TUNE_PPR_BLOCKS, ppr_blocks), (native.BATCH_TUNE_BFS_BLOCKS, bfs_blocks)):
+    def tune(self, ppr_blocks: int | None = None, bfs_blocks: int | None = None, ppr_props: int | None = None):
+        """Resident blocks per SM of the persistent batch kernels, and the props the PPR gather
+        reads (0 or 1 fixed point, 2 doubles); results never depend on them."""
+        for p, v in ((native.BATCH_TUNE_PPR_BLOCKS, ppr_blocks), (native.BATCH_TUNE_BFS_BLOCKS, bfs_blocks),
+                     (native.BATCH_TUNE_PPR_PROPS, ppr_props)):
             if v is not None:
                 self._ck(self.lib.grz_batch_tune_set(self.h, p, int(v)))
         return self
 
     def tuning(self) -> dict:
         out = {}
-        for k, p in (("ppr_blocks", native.BATCH_TUNE_PPR_BLOCKS), ("bfs_blocks", native.BATCH_TUNE_BFS_BLOCKS)):
+        for k, p in (("ppr_blocks", native.BATCH_TUNE_PPR_BLOCKS), ("bfs_blocks", native.BATCH_TUNE_BFS_BLOCKS),
+                     ("ppr_props", native.BATCH_TUNE_PPR_PROPS)):
             v = C.c_int64()
             self._ck(self.lib.grz_batch_tune_get(self.h, p, C.byref(v)))
             out[k] = v.value

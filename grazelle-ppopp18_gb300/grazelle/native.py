@@ -31,7 +31,7 @@ BATCH_K = 8
 LOAD_DERIVE_PUSH = 1
 TUNE_HUBS, TUNE_CC_CACHE, TUNE_CC_THREADS, TUNE_CC_GRID, TUNE_PR_GRID, TUNE_BFS_PULL_SCAN, TUNE_PR_PROPS = 0, 1, 2, 3, 4, 5, 6
 TUNE_INGEST_CHUNKS, TUNE_HUBS_LOADED = 7, 100
-BATCH_TUNE_PPR_BLOCKS, BATCH_TUNE_BFS_BLOCKS = 0, 1
+BATCH_TUNE_PPR_BLOCKS, BATCH_TUNE_BFS_BLOCKS, BATCH_TUNE_PPR_PROPS = 0, 1, 2
 FLAG_HOST_LOOP = 16  # grz_cc_run / grz_bfs_run: host round trip per iteration instead of one CUDA graph
 MLP_FEATURES, MLP_HIDDEN, MLP_PARAMS = 12, 32, 1505
 POLICY_THRESHOLD, POLICY_LEARNED = 0, 1

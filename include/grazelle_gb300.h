@@ -189,6 +189,7 @@ int grz_batch_msbfs(grz_batch* b, const uint32_t* roots, uint32_t k, int32_t* le
  * persistent PPR gather / apply and multi-source BFS pull kernels, 1..32 (default 8) */
 #define GRZ_BATCH_TUNE_PPR_BLOCKS 0
 #define GRZ_BATCH_TUNE_BFS_BLOCKS 1
+#define GRZ_BATCH_TUNE_PPR_PROPS 2   /* props the PPR gather reads: 0 (default) or 1 = 16-byte fixed point, 2 = 8-byte doubles converted on the gather (measured slower: the gather is not DRAM-bound); results identical */
 int grz_batch_tune_set(grz_batch* b, int param, int64_t value);
 int grz_batch_tune_get(const grz_batch* b, int param, int64_t* value);
 unsigned long long grz_batch_launch_count(const grz_batch* b);

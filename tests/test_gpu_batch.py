@@ -82,6 +82,28 @@ def test_ppr_replay_and_iteration_change(batch):
     assert np.abs(c[0][:, 1] - ref).sum() / np.abs(ref).sum() < 1e-12
 
 
+def test_ppr_gathered_prop_forms_agree(batch):
+    """The gather reads 16-byte fixed-point props or the doubles they convert from exactly: the
+    ranks are the same bit for bit, and the tuning switches between them on the next run."""
+    B, gs = batch
+    seeds = [pick(g, 8, 30 + i) for i, g in enumerate(gs)]
+    runs = {}
+    for props in (1, 2, 1, 0):
+        B.tune(ppr_props=props)
+        assert B.tuning()["ppr_props"] == props
+        runs.setdefault(props, []).append(B.ppr(seeds, iterations=9, damping=0.85)[0])
+    for x, y, z in zip(runs[1][0], runs[2][0], runs[1][1]):
+        np.testing.assert_array_equal(x, y)
+        np.testing.assert_array_equal(x, z)
+    for x, y in zip(runs[1][0], runs[0][0]):
+        np.testing.assert_array_equal(x, y)
+    g = gs[3]
+    ref = P.ppr(g.num_vertices, g.pull_order().pairs(), seeds[3][0], 9, 0.85)
+    assert np.abs(runs[2][0][3][:, 0] - ref).sum() / np.abs(ref).sum() < 1e-12
+    with pytest.raises(Exception):
+        B.tune(ppr_props=3)
+
+
 @pytest.mark.parametrize("k", [8, 5])
 def test_msbfs_levels_match_oracle(batch, k):
     B, gs = batch

@@ -40,7 +40,7 @@ def test_tune_batch_keeps_results():
         r0, _ = B.ppr(seeds, 6, 0.85)
         l0, _ = B.msbfs(seeds)
         rep = autotune.tune_batch(B, seeds, iterations=3, trials=1, blocks=(2, 8))
-        assert B.tuning() == {"ppr_blocks": rep["ppr_blocks"]["best"], "bfs_blocks": rep["bfs_blocks"]["best"]}
+        assert B.tuning() == {"ppr_blocks": rep["ppr_blocks"]["best"], "bfs_blocks": rep["bfs_blocks"]["best"], "ppr_props": 0}
         r1, _ = B.ppr(seeds, 6, 0.85)
         l1, _ = B.msbfs(seeds)
         for a, b in zip(r0, r1):

@@ -72,3 +72,35 @@ def test_fixed_point_sum_is_correctly_rounded():
     assert lib.grz_fixed_point_sum(bad.ctypes.data, 1, C.byref(out)) == -5
     over = np.full(5, 15.0)
     assert lib.grz_fixed_point_sum(over.ctypes.data, 5, C.byref(out)) == -5
+
+
+def _defines(path):
+    out = {}
+    for m in re.finditer(r"^#define (GRZ_\w+)\s+(-?\d+)u?\b", path.read_text(), flags=re.M):
+        out[m.group(1)] = int(m.group(2))
+    return out
+
+
+def test_constants_agree_across_headers_and_the_binding():
+    """The public header, the library's internal header and the Python binding give every shared
+    constant (error codes, flags, tuning parameters, load flags) the same value."""
+    from grazelle import native
+    pub = {}
+    for h in sorted((REPO / "include").glob("*.h")):
+        pub.update(_defines(h))
+    internal = _defines(REPO / "grazelle-ppopp18_gb300" / "csrc" / "grz_internal.cuh")
+    shared = sorted(set(pub) & set(internal))
+    assert len(shared) >= 20
+    for name in shared:
+        assert pub[name] == internal[name], name
+    checked = 0
+    for name, value in pub.items():
+        short = name[len("GRZ_"):]
+        for cand in (short, short.replace("FLAG_", "", 1) if short.startswith("FLAG_") and not short.endswith("HOST_LOOP") else None):
+            if cand and hasattr(native, cand) and isinstance(getattr(native, cand), int):
+                assert getattr(native, cand) == value, name
+                checked += 1
+                break
+    assert checked >= 15, checked
+    for code, label in native.ERRORS.items():
+        assert pub[label] == code, label

@@ -257,11 +257,6 @@ __global__ void __launch_bounds__(T) k_bfs_pull(const uint4* __restrict__ nbr, c
 
 constexpr uint32_t PUSH_TILE = 1024;
 
-__device__ __forceinline__ uint32_t vec_count(const uint32_t* __restrict__ rowptr, uint32_t u)
-{
-    return rowptr[u + 1] - rowptr[u];
-}
-
 // block-wide exclusive scan of two u32 values; returns the block totals through the references
 __device__ __forceinline__ void block_scan2(uint32_t& a, uint32_t& b, uint32_t& tot_a, uint32_t& tot_b, uint32_t* sa,
                                             uint32_t* sb)

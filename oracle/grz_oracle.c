@@ -559,7 +559,7 @@ void oracle_bfs(const uint64_t* pull_vec, uint64_t pull_nvec, const uint64_t* pu
     const uint64_t words = (V >> 6) + ((V & 63) ? 1 : 0);
     uint64_t* has = (uint64_t*)calloc(words + 1, sizeof(uint64_t));
     uint64_t* has_next = (uint64_t*)calloc(words + 1, sizeof(uint64_t));
-    uint64_t* wants = (uint64_t*)malloc(sizeof(uint64_t) * (words + 1));
+    uint64_t* wants = (uint64_t*)calloc(words + 1, sizeof(uint64_t));
     for (uint64_t w = 0; w < words; ++w) wants[w] = ~0ull;
     orc_set(has, 0);
     orc_clr(wants, 0);

@@ -158,7 +158,7 @@ int grz_read_levels(grz_graph* g, int64_t* host_levels, uint64_t capacity);
 #define GRZ_TUNE_PR_GRID 4      /* blocks of the persistent PageRank gather kernel (0 = SMs x resident blocks) */
 #define GRZ_TUNE_BFS_PULL_SCAN 5 /* BFS pull over the whole list: 0 = only the wanted destinations' vectors (compacted), 1 = scan every vector */
 #define GRZ_TUNE_PR_PROPS 6     /* props the PageRank gather reads, from the next grz_pr_init: 0 = by size (8-byte doubles when 16-byte fixed-point props exceed 6x L2), 1 = fixed point, 2 = doubles; results identical */
-#define GRZ_TUNE_INGEST_CHUNKS 7 /* chunks of the pull-only ingest, from the next load (0 = one per 2^24 pairs, <= 64): each chunk is processed while the next crosses the host link */
+#define GRZ_TUNE_INGEST_CHUNKS 7 /* chunks of the pull-only ingest, from the next load (0 = one per 2^24 pairs, <= 64; the last is cut into up to four smaller pieces): each chunk is processed while the next crosses the host link */
 #define GRZ_TUNE_HUBS_LOADED 100 /* read-only: hubs encoded in the loaded pull list */
 int grz_tune_set(grz_graph* g, int param, int64_t value);
 int grz_tune_get(const grz_graph* g, int param, int64_t* value);

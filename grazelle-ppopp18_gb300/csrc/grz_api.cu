@@ -652,7 +652,7 @@ extern "C" int grz_pr_init(grz_graph* g, double damping)
 extern "C" int grz_pr_iterate(grz_graph* g, uint32_t iterations)
 {
     if (!g) return GRZ_ERR_ARG;
-    if (!g->pr_fx[0]) return grz_set_error(g, GRZ_ERR_STATE, "grz_pr_init not called");
+    if (!grz_pr_live(g)) return grz_set_error(g, GRZ_ERR_STATE, "grz_pr_init not called since the graph was loaded");
     for (uint32_t i = 0; i < iterations; ++i) {
         int rc = grz_pr_fused_iteration(g, 0);
         if (rc) return rc;
@@ -663,7 +663,7 @@ extern "C" int grz_pr_iterate(grz_graph* g, uint32_t iterations)
 extern "C" int grz_pr_time_iterations(grz_graph* g, uint32_t iterations, float* ms_out)
 {
     if (!g || !ms_out) return GRZ_ERR_ARG;
-    if (!g->pr_fx[0]) return grz_set_error(g, GRZ_ERR_STATE, "grz_pr_init not called");
+    if (!grz_pr_live(g)) return grz_set_error(g, GRZ_ERR_STATE, "grz_pr_init not called since the graph was loaded");
     cudaEvent_t e0, e1;
     GRZ_CK(g, cudaEventCreate(&e0));
     GRZ_CK(g, cudaEventCreate(&e1));
@@ -684,6 +684,7 @@ extern "C" int grz_read_props(grz_graph* g, double* host, uint64_t cap)
     if (cap < g->V) return grz_set_error(g, GRZ_ERR_ARG, "capacity below V");
     GRZ_CK(g, cudaSetDevice(g->device));
     if (g->app == GRZ_APP_PAGERANK && g->pr_fx[0]) {
+        if (g->pr_lists_changed) return grz_set_error(g, GRZ_ERR_STATE, "grz_pr_init not called since the graph was loaded");
         int rc = grz_pr_props_to_double(g);
         if (rc) return rc;
     } else if (g->app != GRZ_APP_PAGERANK) {
@@ -762,7 +763,7 @@ extern "C" int grz_frontier_begin(grz_graph* g, int app, uint32_t root, int flag
 extern "C" int grz_frontier_next(grz_graph* g, int engine, int* engine_used, uint64_t* vote)
 {
     if (!g) return GRZ_ERR_ARG;
-    if (!g->fr.label) return grz_set_error(g, GRZ_ERR_STATE, "grz_frontier_begin not called");
+    if (!grz_frontier_live(g)) return grz_set_error(g, GRZ_ERR_STATE, "grz_frontier_begin not called since the graph was loaded");
     return grz_frontier_step(g, engine, engine_used, vote);
 }
 
@@ -778,7 +779,7 @@ extern "C" int grz_read_levels(grz_graph* g, int64_t* host, uint64_t cap)
 {
     if (!g || !host) return GRZ_ERR_ARG;
     if (cap < g->V) return grz_set_error(g, GRZ_ERR_ARG, "capacity below V");
-    if (!g->fr.level || g->fr.app != GRZ_APP_BREADTH_FIRST_SEARCH) return grz_set_error(g, GRZ_ERR_STATE, "no BFS result");
+    if (!grz_frontier_live(g) || g->fr.app != GRZ_APP_BREADTH_FIRST_SEARCH) return grz_set_error(g, GRZ_ERR_STATE, "no BFS result");
     uint32_t* tmp = (uint32_t*)malloc(sizeof(uint32_t) * (g->V ? g->V : 1));
     if (!tmp) return GRZ_ERR_NOMEM;
     cudaError_t e = cudaMemcpyAsync(tmp, g->fr.level, sizeof(uint32_t) * g->V, cudaMemcpyDeviceToHost, g->stream);

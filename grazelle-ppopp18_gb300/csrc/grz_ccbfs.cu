@@ -1027,7 +1027,7 @@ int grz_frontier_vertex_phase(grz_graph* g, uint64_t first, uint64_t count)
     (void)first;
     (void)count;
     grz_frontier_state& f = g->fr;
-    if (!f.label) return grz_set_error(g, GRZ_ERR_STATE, "frontier state not initialised");
+    if (!grz_frontier_live(g)) return grz_set_error(g, GRZ_ERR_STATE, "frontier state not initialised for the loaded graph");
     unsigned long long* t = f.has;
     f.has = f.has_next;
     f.has_next = t;
@@ -1038,7 +1038,7 @@ int grz_frontier_vertex_phase(grz_graph* g, uint64_t first, uint64_t count)
 // the phases.h entry points: one edge phase with a fresh vote, counted into the iteration total
 int grz_cc_phase(grz_graph* g, int pull, uint64_t first_vec, uint64_t count)
 {
-    if (!g->fr.label || g->fr.app != GRZ_APP_CONNECTED_COMPONENTS) {
+    if (!grz_frontier_live(g) || g->fr.app != GRZ_APP_CONNECTED_COMPONENTS) {
         int rc = grz_frontier_init(g, GRZ_APP_CONNECTED_COMPONENTS, 0, 0);
         if (rc) return rc;
     }
@@ -1047,7 +1047,7 @@ int grz_cc_phase(grz_graph* g, int pull, uint64_t first_vec, uint64_t count)
 
 int grz_bfs_phase(grz_graph* g, int pull, uint64_t first_vec, uint64_t count)
 {
-    if (!g->fr.label || g->fr.app != GRZ_APP_BREADTH_FIRST_SEARCH) {
+    if (!grz_frontier_live(g) || g->fr.app != GRZ_APP_BREADTH_FIRST_SEARCH) {
         int rc = grz_frontier_init(g, GRZ_APP_BREADTH_FIRST_SEARCH, 0, 0);
         if (rc) return rc;
     }
@@ -1155,7 +1155,7 @@ __global__ void __launch_bounds__(T) k_digest(const uint32_t* __restrict__ label
 int grz_frontier_digest(grz_graph* g, uint64_t* out3)
 {
     grz_frontier_state& f = g->fr;
-    if (!f.label) return grz_set_error(g, GRZ_ERR_STATE, "no CC/BFS result");
+    if (!grz_frontier_live(g)) return grz_set_error(g, GRZ_ERR_STATE, "no CC/BFS result for the loaded graph");
     int rc = grz_frontier_mail(g);
     if (rc) return rc;
     unsigned long long* d = nullptr;
@@ -1177,7 +1177,7 @@ int grz_frontier_digest(grz_graph* g, uint64_t* out3)
 int grz_frontier_props(grz_graph* g)
 {
     grz_frontier_state& f = g->fr;
-    if (!f.label) return grz_set_error(g, GRZ_ERR_STATE, "no CC/BFS result");
+    if (!grz_frontier_live(g)) return grz_set_error(g, GRZ_ERR_STATE, "no CC/BFS result for the loaded graph");
     k_u32_to_double<<<blocks_for(g->V), T, 0, g->stream>>>(f.label, g->V, g->prop, f.app == GRZ_APP_BREADTH_FIRST_SEARCH); GRZ_COUNT_LAUNCH(g);
     GRZ_CK(g, cudaGetLastError());
     return GRZ_OK;
@@ -1360,7 +1360,7 @@ void grz_frontier_run_prepare(grz_graph* g)
 int grz_frontier_run_graph(grz_graph* g, uint64_t* launches)
 {
     grz_frontier_state& f = g->fr;
-    if (!f.label) return grz_set_error(g, GRZ_ERR_STATE, "frontier state not initialised");
+    if (!grz_frontier_live(g)) return grz_set_error(g, GRZ_ERR_STATE, "frontier state not initialised for the loaded graph");
     if (!g->pull.nbr || !g->push.nbr || !g->pull.nvec || !g->push.nvec)
         return grz_set_error(g, GRZ_ERR_STATE, "the graph run needs both edge lists");
     int rc = grz_frontier_mail(g);

@@ -374,6 +374,12 @@ struct grz_graph {
 
 #define GRZ_COUNT_LAUNCH(g) ((g)->nlaunch++)
 
+// CC/BFS state that belongs to the loaded lists: a reload with the same V keeps the buffers
+// but marks them stale until grz_frontier_init rebuilds what depends on the lists
+static inline bool grz_frontier_live(const grz_graph* g) { return g->fr.label && !g->fr.lists_changed; }
+// PageRank state of the loaded lists (grz_pr_init since the last load)
+static inline bool grz_pr_live(const grz_graph* g) { return g->pr_fx[0] && !g->pr_lists_changed; }
+
 // The streamed device arrays of a graph (vector lists, row pointers, degrees, the edge pairs of a
 // load, temporaries) come from its device's stream-ordered pool, allocated and freed on the
 // graph's stream.  The pool keeps freed memory (its release threshold is raised once per device

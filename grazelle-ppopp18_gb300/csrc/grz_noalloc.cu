@@ -121,6 +121,8 @@ __global__ void __launch_bounds__(NA_T) k_na_apply(const u128* __restrict__ acc,
 }
 
 // Resolves the device addresses of the scratch arrays for the current device, once per device.
+// The addresses are kept for the life of the process: a caller that resets the device
+// (cudaDeviceReset) and then calls again is not supported.
 int na_setup(int dev, u128** acc, u128** part)
 {
     std::lock_guard<std::mutex> lk(g_na_mutex);
@@ -148,6 +150,9 @@ extern "C" int grz_pr_step_noalloc(const void* vectors, uint64_t num_vectors, ui
     if (!vectors || num_vectors == 0 || num_vectors > 0xffffffffull || !props_in || !outdeg || !props_out) return GRZ_ERR_ARG;
     if (!(damping >= 0.0 && damping <= 1.0)) return GRZ_ERR_ARG;
     if (((uintptr_t)vectors & 31) != 0) return GRZ_ERR_ARG;
+    // props_out is written while other blocks still gather props_in: the two ranges must not overlap
+    const uintptr_t in0 = (uintptr_t)props_in, out0 = (uintptr_t)props_out, nb = (uintptr_t)(sizeof(double) * num_vertices);
+    if (in0 < out0 + nb && out0 < in0 + nb) return GRZ_ERR_ARG;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES) {
         cudaGetLastError();

@@ -345,6 +345,17 @@ __global__ void k_src_ranks(const unsigned long long* __restrict__ keys, uint64_
 // chunk c's sorted keys whose source lies in block b or later (seg[c][nb] = the chunk's end), so
 // the edges of block b from every chunk are placed together and the partial-sector writes of the
 // chunks meet in L2 instead of in DRAM.
+// the chunks' first edges, passed by value so that no host buffer has to outlive the launch
+struct ChunkStarts {
+    uint64_t v[GRZ_INGEST_MAX_CHUNKS + TAIL_SPLITS + 2];
+};
+
+__global__ void k_chunk_starts(ChunkStarts cs, uint32_t n, uint64_t* __restrict__ out)
+{
+    const uint32_t i = threadIdx.x;
+    if (i < n) out[i] = cs.v[i];
+}
+
 __global__ void k_seg_bounds(const unsigned long long* __restrict__ keys, const uint64_t* __restrict__ cstart, uint32_t nchunks,
                              const uint32_t* __restrict__ rowptr, uint64_t V, uint64_t nvec, uint32_t nb,
                              uint64_t* __restrict__ seg)
@@ -578,12 +589,12 @@ int grz_ingest_pull_derive(grz_graph* g, const uint64_t* pull, uint64_t E, const
         const uint64_t nb = std::min<uint64_t>(PLACE_MAX_BLOCKS, std::max<uint64_t>(1, Q->nvec * sizeof(uint4) / PLACE_BLOCK_BYTES));
         const uint64_t per = (E + nb * nchunks - 1) / (nb * nchunks);  // edges per (block, chunk) on average
         const uint64_t xs = std::max<uint64_t>(1, (per + PLACE_EDGES_PER_THREAD * ST - 1) / (PLACE_EDGES_PER_THREAD * ST));
-        uint64_t cs_h[GRZ_INGEST_MAX_CHUNKS + TAIL_SPLITS + 2];
-        for (uint64_t c = 0; c <= nchunks; ++c) cs_h[c] = std::min<uint64_t>(ct[c] * STILE, E);
+        ChunkStarts cs_h;
+        for (uint64_t c = 0; c <= nchunks; ++c) cs_h.v[c] = std::min<uint64_t>(ct[c] * STILE, E);
         IRC(grz_dev_alloc(g, (void**)&seg, sizeof(uint64_t) * nchunks * (nb + 1)));
         IRC(grz_dev_alloc(g, (void**)&cstart, sizeof(uint64_t) * (nchunks + 1)));
-        ICK(cudaMemcpyAsync(cstart, cs_h, sizeof(uint64_t) * (nchunks + 1), cudaMemcpyHostToDevice, st));
-        ICK(cudaStreamSynchronize(st));  // cs_h is on this stack frame
+        static_assert(GRZ_INGEST_MAX_CHUNKS + TAIL_SPLITS + 2 <= 128, "one block writes the chunk starts");
+        k_chunk_starts<<<1, 128, 0, st>>>(cs_h, (uint32_t)(nchunks + 1), cstart); GRZ_COUNT_LAUNCH(g);
         k_seg_bounds<<<blocks_of(nchunks * (nb + 1)), ST, 0, st>>>(sorted, cstart, (uint32_t)nchunks, Q->rowptr, V, Q->nvec,
                                                                   (uint32_t)nb, seg); GRZ_COUNT_LAUNCH(g);
         k_push_place<<<(unsigned)(nb * nchunks * xs), ST, 0, st>>>(sorted, rank, seg, (uint32_t)nchunks, (uint32_t)nb, (uint32_t)xs,

@@ -621,7 +621,7 @@ extern "C" int grz_frontier_last_features(grz_graph* g, float* host, uint64_t ca
 extern "C" int grz_frontier_features(grz_graph* g, float* host, uint64_t cap, int* policy_choice)
 {
     if (!g || !host || cap < (uint64_t)NF) return GRZ_ERR_ARG;
-    if (!g->fr.label) return grz_set_error(g, GRZ_ERR_STATE, "grz_frontier_begin not called");
+    if (!grz_frontier_live(g)) return grz_set_error(g, GRZ_ERR_STATE, "grz_frontier_begin not called");
     uint64_t v = 0;
     int pull = 0;
     const int rc = grz_switch_decide(g, g->fr.has, g->fr.vote_host, g->fr.iter + 1, &v, &pull, host);
@@ -633,7 +633,7 @@ extern "C" int grz_frontier_features(grz_graph* g, float* host, uint64_t cap, in
 // snapshot / restore of the CC/BFS state, to time both engines from the same state
 extern "C" int grz_frontier_snapshot(grz_graph* g)
 {
-    if (!g || !g->fr.label) return GRZ_ERR_STATE;
+    if (!g || !grz_frontier_live(g)) return GRZ_ERR_STATE;
     grz_frontier_state& f = g->fr;
     const uint64_t V = g->V, W = (V >> 6) + 2;
     const uint64_t need = sizeof(uint32_t) * (V + 1) * 2 + sizeof(unsigned long long) * W * 3;
@@ -658,7 +658,7 @@ extern "C" int grz_frontier_snapshot(grz_graph* g)
 
 extern "C" int grz_frontier_restore(grz_graph* g)
 {
-    if (!g || !g->fr.label || !g->fr.snap) return GRZ_ERR_STATE;
+    if (!g || !grz_frontier_live(g) || !g->fr.snap) return GRZ_ERR_STATE;
     grz_frontier_state& f = g->fr;
     const uint64_t V = g->V, W = (V >> 6) + 2;
     const char* p = (const char*)f.snap;
@@ -677,7 +677,7 @@ extern "C" int grz_frontier_restore(grz_graph* g)
 // learned switch trains on)
 extern "C" int grz_frontier_next_timed(grz_graph* g, int engine, int* engine_used, uint64_t* vote, float* edge_ms)
 {
-    if (!g || !g->fr.label) return GRZ_ERR_STATE;
+    if (!g || !grz_frontier_live(g)) return GRZ_ERR_STATE;
     grz_frontier_state& f = g->fr;
     if (!f.ev[0]) {
         GRZ_CK(g, cudaEventCreate(&f.ev[0]));

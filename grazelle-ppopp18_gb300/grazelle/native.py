@@ -12,6 +12,8 @@ from pathlib import Path
 from . import build as _build
 
 GRZ_OK = 0
+GRZ_ERR_ARG, GRZ_ERR_CUDA, GRZ_ERR_NOMEM, GRZ_ERR_UNSORTED = -1, -2, -3, -4
+GRZ_ERR_RANGE, GRZ_ERR_STATE, GRZ_ERR_IO, GRZ_ERR_TIMEOUT = -5, -6, -7, -8
 ERRORS = {
     -1: "GRZ_ERR_ARG", -2: "GRZ_ERR_CUDA", -3: "GRZ_ERR_NOMEM", -4: "GRZ_ERR_UNSORTED",
     -5: "GRZ_ERR_RANGE", -6: "GRZ_ERR_STATE", -7: "GRZ_ERR_IO", -8: "GRZ_ERR_TIMEOUT",

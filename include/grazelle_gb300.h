@@ -269,12 +269,14 @@ unsigned long long grz_launch_count(const grz_graph* g);
  *                grz_graph_info_t.pull_list_device; num_vectors of them
  *   props_in     double[V] on the device: rank / outdegree', as the reference stores props
  *   outdeg       double[V] on the device: outdegree from the -pull list
- *   props_out    double[V] on the device: the props after one iteration (may not alias props_in)
+ *   props_out    double[V] on the device: the props after one iteration; must not overlap
+ *                props_in (GRZ_ERR_ARG)
  *   stream       cudaStream_t to run on (NULL = the legacy default stream)
  * Returns GRZ_ERR_RANGE if num_vertices is 0 or above GRZ_NOALLOC_MAX_VERTICES, GRZ_ERR_ARG
  * for a bad argument, GRZ_ERR_CUDA if a launch fails.
  * The first call on a device resolves the scratch array's device address (cudaGetSymbolAddress)
- * for that device, so make that first call before capturing a stream.  Every call shares the
+ * for that device, so make that first call before capturing a stream.  The address is kept until
+ * the process exits: calling again after cudaDeviceReset is not supported.  Every call shares the
  * one array and clears the part it needs when it starts, so calls that overlap on the GPU (on
  * different streams, or from different host threads) race with each other: order them. */
 int grz_pr_step_noalloc(const void* vectors, uint64_t num_vectors, uint64_t num_vertices, const double* props_in,

@@ -23,7 +23,12 @@ This script does not run the reference's Makefile.  Instead it:
 It only builds where the reference does: x86-64 with AVX2
 (include/versioninfo.h:33-47).  Elsewhere it says so and exits 0.
 
-Usage: python oracle/build_ref.py [--ref /root/reference] [--variant NAME ...]
+Usage: python oracle/build_ref.py [--ref DIR] [--variant NAME ...]
+
+The reference tree is DIR, else the environment variable GRZ_REFERENCE, else
+the one place this recipe knows it is mounted read-only (``KNOWN_TREE``).  When
+none of them holds the reference the recipe says so and exits 0 (nothing else
+needs the binaries: the committed fixtures under tests/golden/ were made by them).
 """
 from __future__ import annotations
 
@@ -38,6 +43,15 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
+KNOWN_TREE = "/root/reference"
+
+
+def locate(explicit: str | None = None) -> Path | None:
+    """The reference tree: the explicit path, GRZ_REFERENCE, or KNOWN_TREE; None if absent."""
+    for cand in (explicit, os.environ.get("GRZ_REFERENCE"), KNOWN_TREE):
+        if cand and (Path(cand) / "source" / "main.c").exists():
+            return Path(cand)
+    return None
 
 # variant name -> (ALGORITHM, EXPERIMENTS); mirrors the Makefile's figure targets minus TSX (Makefile:277-355)
 VARIANTS = {
@@ -199,17 +213,17 @@ def reference_buildable() -> tuple[bool, str]:
 
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None, help="reference tree (default: GRZ_REFERENCE, then KNOWN_TREE)")
     ap.add_argument("--variant", action="append")
     ap.add_argument("-j", type=int, default=os.cpu_count() or 4)
     a = ap.parse_args(argv)
-    ref = Path(a.ref)
     ok, why = reference_buildable()
     if not ok:
         print("build_ref: skipped:", why)
         return 0
-    if not (ref / "source" / "main.c").exists():
-        print("build_ref: skipped: reference tree not found at", ref)
+    ref = locate(a.ref)
+    if ref is None:
+        print("build_ref: skipped: no reference tree (give --ref DIR or set GRZ_REFERENCE)")
         return 0
     names = a.variant or list(VARIANTS)
     for n in names:

@@ -307,3 +307,41 @@ def test_ingest_chunks_tuning_bounds():
             G.tune(ingest_chunks=65)
         assert ei.value.code == -5
         assert G.tuning()["ingest_chunks"] == 64
+
+
+def test_calls_out_of_order_after_a_reload_are_rejected():
+    """A reload with the same V keeps the CC/BFS and PageRank buffers, but their contents belong
+    to the graph loaded before.  Until grz_frontier_begin / grz_pr_init runs for the new lists,
+    every call that would read or advance that state returns GRZ_ERR_STATE, also when the new
+    -push list has more vectors than the push tiles were sized for, and launches nothing."""
+    import ctypes as C
+    from grazelle import graphgen as gg, native
+    from grazelle.engine import Graph
+    small, big = gg.rmat(13, 4, seed=3, symmetric=True), gg.rmat(13, 32, seed=4, symmetric=True)
+    assert small.num_vertices == big.num_vertices
+    with Graph(0) as R:
+        R.load_pairs(small.num_vertices, small.pull_order().pairs(), small.push_order().pairs())
+        R.connected_components()
+        R.pagerank(2)
+        R.load_pairs(big.num_vertices, big.pull_order().pairs(), big.push_order().pairs())
+        lib, h = R.lib, R.h
+        V = big.num_vertices
+        before = R.launch_count()
+        eng, vote = C.c_int(), C.c_uint64()
+        assert lib.grz_frontier_next(h, -1, C.byref(eng), C.byref(vote)) == native.GRZ_ERR_STATE
+        lv = np.zeros(V, dtype=np.int64)
+        assert lib.grz_read_levels(h, lv.ctypes.data_as(C.c_void_p), V) == native.GRZ_ERR_STATE
+        dg = (C.c_uint64 * 3)()
+        assert lib.grz_result_digest(h, dg) == native.GRZ_ERR_STATE
+        assert lib.grz_frontier_snapshot(h) == native.GRZ_ERR_STATE
+        assert lib.grz_pr_iterate(h, 1) == native.GRZ_ERR_STATE
+        ms = C.c_float()
+        assert lib.grz_pr_time_iterations(h, 1, C.byref(ms)) == native.GRZ_ERR_STATE
+        props = np.zeros(V, dtype=np.float64)
+        assert lib.grz_read_props(h, props.ctypes.data_as(C.c_void_p), V) == native.GRZ_ERR_STATE
+        assert R.launch_count() == before
+        # after the initialisations the graph gives a fresh graph's results
+        with Graph(0) as F:
+            F.load_pairs(V, big.pull_order().pairs(), big.push_order().pairs())
+            np.testing.assert_array_equal(R.connected_components(), F.connected_components())
+            np.testing.assert_array_equal(R.pagerank(3), F.pagerank(3))

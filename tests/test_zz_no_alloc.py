@@ -62,3 +62,15 @@ def test_noalloc_step_rejects_oversized_graphs():
     assert rc == -5  # GRZ_ERR_RANGE, before any device work
     assert lib.grz_pr_step_noalloc(C.c_void_p(32), 1, 0, C.c_void_p(8), C.c_void_p(8), C.c_double(0.875),
                                    C.c_void_p(8), None) == -5
+
+
+def test_noalloc_step_rejects_overlapping_props():
+    """props_out is written while other blocks still read props_in, so overlapping ranges are
+    refused with GRZ_ERR_ARG before any device work (the pointers are never dereferenced)."""
+    from grazelle import native
+    lib = native.load()
+    V = 64
+    for base_in, base_out in ((4096, 4096), (4096, 4096 + 8 * (V - 1)), (4096 + 8, 4096)):
+        rc = lib.grz_pr_step_noalloc(C.c_void_p(32), 1, V, C.c_void_p(base_in), C.c_void_p(8), C.c_double(0.875),
+                                     C.c_void_p(base_out), None)
+        assert rc == native.GRZ_ERR_ARG, (base_in, base_out)

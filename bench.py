@@ -303,10 +303,17 @@ def run_native(a):
     # profiling on.  The event pairs need host-launched kernels, so CC/BFS run their host loop
     # here (the same kernels as the graph the headline region launches).
     G.profile(True)
+    recs, first_pull = [], []
     with Timer(torch, stream) as tprof:
         for i in range(a.steps):
             step(i)
-    recs = G.profile_read()
+            r = G.profile_read()
+            recs += r
+            # the first pull launch of a CC run is the full pass over every vector (the converged-
+            # destination skip starts in the next iteration)
+            fp = [ms for k, ms in r if k == "cc_pull"]
+            if fp:
+                first_pull.append(fp[0])
     G.profile(False)
     ks = kernel_stats(recs)
     dominant = max(ks.items(), key=lambda kv: kv[1]["total_ms"])[0] if ks else None
@@ -316,14 +323,19 @@ def run_native(a):
     alg = {"pr_gather": 8 * E + 16 * V, "cc_pull": 8 * E + 16 * V + V // 4, "bfs_pull": 8 * E + 16 * V + V // 4}
     roof = None
     if dominant:
-        mean_s = ks[dominant]["mean_ms"] * 1e-3
+        mean_ms = ks[dominant]["mean_ms"]
+        region = "profiled pass of the same %d steps" % a.steps
+        if dominant == "cc_pull" and first_pull:
+            mean_ms = sum(first_pull) / len(first_pull)
+            region += ", first (full-pass) pull launch of each run"
+        mean_s = mean_ms * 1e-3
         if dominant in alg:
             achieved = alg[dominant] / mean_s / 1e9
             roof = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": hbm, "peak_kind": hbm_kind,
                     "unit": "GB/s", "frac": round(achieved / hbm, 4), "algorithmic_bytes": alg[dominant],
-                    "mean_launch_ms": round(ks[dominant]["mean_ms"], 4),
+                    "mean_launch_ms": round(mean_ms, 4),
                     "share_of_profiled_pass": round(ks[dominant]["total_ms"] / tprof.ms, 4),
-                    "region": "profiled pass of the same %d steps" % a.steps,
+                    "region": region,
                     "traffic": profile_traffic(dominant, "%s%d" % (wl, scale))}
 
     # end to end through the C ABI from pinned host buffers
@@ -351,8 +363,14 @@ def run_native(a):
     if rank == 0 and not a.no_apps and wl == "cc" and not lean:
         apps = extra_apps(a, G, g, torch, stream, hbm, hbm_kind)
     cpu = None
+    parity = {}
     if rank == 0 and not a.no_cpu and not lean:
-        cpu = cpu_baseline(wl, g, pull, push, scale, sample=True)
+        cpu, ref_out = cpu_baseline(wl, g, pull, push, scale, sample=True)
+        if wl == "cc":
+            # the labels of the last e2e step (read back through the C ABI) against the CPU run's
+            parity["cc_labels_exact"] = bool(np.array_equal(d2h, ref_out[:V]))
+            parity["cc_labels_checked"] = "all %d vertices, the GPU run of the last e2e step against the OpenMP restatement" % V
+        del ref_out
     elif rank == 0 and lean:
         cpu = {"value": None, "unit": "GTEPS", "cores": os.cpu_count(), "kind": "port",
                "sample": "not run: the CPU restatement's layout of a graph this size does not fit a bounded sample"}
@@ -371,8 +389,12 @@ def run_native(a):
                    "l2": "inputs larger than L2 (%.1f GB of edge vectors)" % (G.info().pull_vectors * 20 / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU", "autotuned": tuned},
         "roofline": roof, "kernels": {k: {"n": v["n"], "mean_us": round(v["mean_ms"] * 1e3, 2)} for k, v in ks.items()},
-        "e2e": e2e, "gpu_launches": int(launches), "clocks": clk.summary(), "cpu_baseline": cpu, "apps": apps,
+        "e2e": e2e, "gpu_launches": int(launches), "clocks": clk.summary(), "cpu_baseline": cpu, "parity": parity,
+        "apps": apps,
     }
+    for name, app in apps.items():
+        if isinstance(app, dict) and "parity" in app:
+            parity[name] = app["parity"]
     print(json.dumps(line), flush=True)
 
 
@@ -405,16 +427,32 @@ def extra_apps(a, G_cc, g_cc, torch, stream, hbm, hbm_kind):
     cc["learned_speedup"] = round(cc["threshold"]["ms_per_run"] / cc["learned"]["ms_per_run"], 4)
     out["cc_switch"] = cc
     if a.bfs_scale:
-        out["bfs_switch"] = bfs_switch_study(a, torch, stream, net, dev)
+        out["bfs_switch"] = bfs_switch_study(a, torch, stream, net, dev, hbm, hbm_kind)
     if not a.no_batch:
         out["batch"] = batch_study(a, torch, stream, dev)
-    # PageRank
-    g, pull, push = make_graph("pr", 20, a.seed)
+    if a.stress_scale:
+        out["stress"] = stress_study(a, torch, stream, dev, hbm, hbm_kind)
+    out["pagerank"] = pagerank_study(a, torch, stream, hbm, hbm_kind)
+    return out
+
+
+def pagerank_study(a, torch, stream, hbm, hbm_kind, scale=20):
+    """PageRank on R-MAT `scale` (16 pull iterations, d = 0.875, FP64 props): device-resident
+    GTEPS, the gather kernel's roofline, e2e through the C ABI (the -pull pairs from pinned host
+    memory, layout build, 16 iterations, props back), the OpenMP restatement on the host cores,
+    and parity of the props with the serial oracle (relative L1, bound 1e-12)."""
+    from grazelle.engine import Graph
+    from oracle import oracle as O
+    g, pull, push = make_graph("pr", scale, a.seed)
     V, E = g.num_vertices, g.num_edges
+    res = {"workload": "pr-rmat%d, 16 iterations, d=0.875" % scale, "V": V, "E": E}
+    pin_pull = torch.from_numpy(pull.view(np.int64)).pin_memory()
+    d2h_t = torch.zeros(V, dtype=torch.float64).pin_memory()
+    d2h = d2h_t.numpy()
+    n = max(2, a.steps // 2)
     with Graph(torch.cuda.current_device(), stream=stream.cuda_stream) as G:
         G.load_pairs(V, pull, push)
         G.pr_init(0.875).pr_iterate(16)
-        n = max(1, a.steps // 2)
         with Timer(torch, stream) as tp:
             for _ in range(n):
                 G.pr_init(0.875).pr_iterate(16)
@@ -424,37 +462,105 @@ def extra_apps(a, G_cc, g_cc, torch, stream, hbm, hbm_kind):
         G.sync()
         ks = kernel_stats(G.profile_read())
         G.profile(False)
+        props = G.pr_init(0.875).pr_iterate(16).props()
         alg = 8 * E + 16 * V
         gm = ks.get("pr_gather", {}).get("mean_ms", 0)
         it_ms = tp.ms / (16 * n)
-        out["pagerank"] = {"workload": "pr-rmat20, 16 iterations, d=0.875", "gteps": round(E * 16 * n / (tp.ms * 1e-3) / 1e9, 3),
-                           "us_per_iteration": round(it_ms * 1e3, 2),
-                           "roofline_iteration": {"achieved": round(alg / (it_ms * 1e-3) / 1e9, 1), "peak": hbm,
-                                                  "peak_kind": hbm_kind, "frac": round(alg / (it_ms * 1e-3) / 1e9 / hbm, 4),
-                                                  "algorithmic_bytes": alg},
-                           "kernels_us": {k: round(v["mean_ms"] * 1e3, 2) for k, v in ks.items()},
-                           "gather_roofline_frac": round(alg / (gm * 1e-3) / 1e9 / hbm, 4) if gm else None}
+        res.update({"gteps": round(E * 16 * n / (tp.ms * 1e-3) / 1e9, 3), "us_per_iteration": round(it_ms * 1e3, 2),
+                    "kernels_us": {k: round(v["mean_ms"] * 1e3, 2) for k, v in ks.items()}})
+        res["roofline"] = {"bound": "hbm", "kernel": "pr_gather", "algorithmic_bytes": alg,
+                           "achieved": round(alg / (gm * 1e-3) / 1e9, 1) if gm else None, "peak": hbm, "peak_kind": hbm_kind,
+                           "unit": "GB/s", "frac": round(alg / (gm * 1e-3) / 1e9 / hbm, 4) if gm else None,
+                           "mean_launch_us": round(gm * 1e3, 2),
+                           "iteration_frac": round(alg / (it_ms * 1e-3) / 1e9 / hbm, 4),
+                           "traffic": profile_traffic("pr_gather", "pr%d" % scale)}
+        # e2e: the -pull pairs cross the link each step (PageRank pull needs no -push list)
+        for _ in range(2):
+            G.load_pointers(V, E, pin_pull.data_ptr(), None)
+            G.pr_init(0.875).pr_iterate(16)
+            G.lib.grz_read_props(G.h, d2h.ctypes.data, V)
+        with Timer(torch, stream) as te:
+            for _ in range(n):
+                G.load_pointers(V, E, pin_pull.data_ptr(), None)
+                G.pr_init(0.875).pr_iterate(16)
+                G.lib.grz_read_props(G.h, d2h.ctypes.data, V)
+        res["e2e"] = {"value": round(E * 16 * n / (te.ms * 1e-3) / 1e9, 3), "unit": "GTEPS", "h2d_bytes_per_step": int(pull.nbytes),
+                      "d2h_bytes_per_step": int(d2h.nbytes), "ms_per_step": round(te.ms / n, 3),
+                      "ingest": "the -pull pairs (the pull engine needs no -push list)"}
+        e2e_err = O.relative_l1(d2h, props[:V])
+    L = O.layout(V, pull, push)
+    ref = O.pr_pull(L, 16, 0.875)[:V]
+    del L
+    res["parity"] = {"props_rel_l1_vs_oracle": O.relative_l1(props[:V], ref), "bound": 1e-12,
+                     "e2e_props_equal_resident": e2e_err == 0.0}
+    res["parity"]["ok"] = res["parity"]["props_rel_l1_vs_oracle"] < 1e-12 and res["parity"]["e2e_props_equal_resident"]
+    cpu, _ = cpu_baseline("pr", g, pull, push, scale, sample=True)
+    res["cpu_baseline"] = cpu
+    return res
+
+
+def bfs_kernel_rooflines(G, roots, outdeg, indeg, hbm, hbm_kind):
+    """Algorithmic bytes over CUDA-event time of the BFS edge kernels, from profiled host-loop
+    runs: iteration k's push reads the frontier F = {level k-1}: 8 x (out-edges of F) + 8|F| +
+    16|U|, U = {level k} the updates; its pull reads every vector of the wanted destinations W
+    (unvisited, with in-edges): 8 x (in-edges of W) + 8|W| + 16|U| (the reference's pull scans
+    them all; the kernel's early exit reads fewer)."""
+    agg = {"bfs_pull": [0, 0.0, 0], "bfs_push": [0, 0.0, 0]}
+    G.profile(True)
+    for r in roots:
+        G.bfs_run(r)
+        recs = [(k, ms) for k, ms in G.profile_read() if k in agg]
+        lv = G.levels()
+        nl = int(lv.max()) + 2
+        key = np.where(lv < 0, nl, lv)  # unreached last
+        cnt = np.bincount(key, minlength=nl + 1)
+        out_by = np.bincount(key, weights=outdeg, minlength=nl + 1)
+        has_in = indeg > 0
+        w_cnt = np.bincount(key, weights=has_in.astype(np.float64), minlength=nl + 1)
+        in_by = np.bincount(key, weights=indeg, minlength=nl + 1)
+        for i, (kind, ms) in enumerate(recs):
+            k = i + 1  # iteration k visits level k
+            upd = cnt[k] if k < nl else 0
+            if kind == "bfs_push":
+                b = 8 * out_by[k - 1] + 8 * cnt[k - 1] + 16 * upd
+            else:
+                b = 8 * in_by[k:].sum() + 8 * w_cnt[k:].sum() + 16 * upd
+            agg[kind][0] += 1
+            agg[kind][1] += ms
+            agg[kind][2] += int(b)
+    G.profile(False)
+    out = {}
+    for kind, (n, ms, b) in agg.items():
+        if n:
+            gbs = b / (ms * 1e-3) / 1e9
+            out[kind] = {"launches": n, "total_ms": round(ms, 3), "algorithmic_bytes": b, "achieved": round(gbs, 1),
+                         "peak": hbm, "peak_kind": hbm_kind, "unit": "GB/s", "frac": round(gbs / hbm, 4)}
     return out
 
 
-def bfs_switch_study(a, torch, stream, net, dev):
+def bfs_switch_study(a, torch, stream, net, dev, hbm=None, hbm_kind=None):
     """BFS on a directed R-MAT (default scale 26, edge factor 16) from 64 seeded non-isolated
     roots under the threshold rule and the learned switch: GTEPS from the device time of each
     run, identical levels checked by an on-device digest, and the edge-phase regret of both
-    policies against the best engine per iteration on 4 of the roots."""
+    policies against the best engine per iteration on 4 of the roots.  Also: parity of 4 roots
+    (levels equal to the oracle's, parents a legal BFS tree), the BFS kernels' rooflines, e2e
+    through the C ABI (the -pull pairs from pinned host memory, the -push list derived on the
+    device, 64 roots, a digest read back per root) and the OpenMP restatement on the host."""
     from grazelle import graphgen as gg
     from grazelle import native
     from grazelle import switch as sw
     from grazelle.engine import Graph
+    from oracle import oracle as O
     t0 = time.time()
     g = gg.rmat(a.bfs_scale, 16, seed=a.seed + 26)
     V, E = g.num_vertices, g.num_edges
     roots = pick_roots(g, 64, seed=a.seed + 64)
+    pull, push = g.pull_order().pairs(), g.push_order().pairs()
+    del g
     log("bfs graph: scale %d V=%d E=%d (%.1fs)" % (a.bfs_scale, V, E, time.time() - t0))
     res = {"workload": "bfs-rmat%d (directed), %d roots" % (a.bfs_scale, len(roots)), "V": V, "E": E}
     with Graph(dev, stream=stream.cuda_stream) as G:
-        G.load_pairs(V, g.pull_order().pairs(), g.push_order().pairs())
-        del g
+        G.load_pairs(V, pull, push)
         digests = {}
         for name, policy, mlp in (("threshold", native.POLICY_THRESHOLD, None), ("learned", native.POLICY_LEARNED, net)):
             G.set_policy(policy, mlp)
@@ -472,9 +578,20 @@ def bfs_switch_study(a, torch, stream, net, dev):
             digests[name] = dg
             res[name] = {"ms_total": round(ms, 3), "ms_per_root": round(ms / len(roots), 4),
                          "gteps": round(teps / (ms * 1e-3) / 1e9, 3), "pull_iterations": npull, "push_iterations": npush}
-        G.set_policy(native.POLICY_THRESHOLD)
         res["identical_levels"] = digests["threshold"] == digests["learned"]
         res["learned_speedup"] = round(res["threshold"]["ms_total"] / res["learned"]["ms_total"], 4)
+        # parity: 4 roots under the learned switch against the oracle's levels, parents a legal tree
+        chk = roots[:4]
+        ref = O.bfs_levels_multi(push, V, chk)
+        lv_ok, tree_ok = True, True
+        for k, r in enumerate(chk):
+            par, lv = G.bfs(r)
+            lv_ok &= bool(np.array_equal(lv, ref[k]))
+            tree_ok &= O.bfs_check_tree(push, V, r, lv, par.astype(np.int64)) == 0
+        del ref
+        res["parity"] = {"roots_checked": len(chk), "levels_exact": lv_ok, "parents_legal_bfs_tree": tree_ok,
+                         "policies_identical_levels_64_roots": res["identical_levels"], "ok": lv_ok and tree_ok and res["identical_levels"]}
+        G.set_policy(native.POLICY_THRESHOLD)
         d = sw.Samples()
         d.extend(sw.collect(G, native.APP_BREADTH_FIRST_SEARCH, roots[:4]))
         e = sw.edge_totals(d, net)
@@ -482,6 +599,140 @@ def bfs_switch_study(a, torch, stream, net, dev):
                                             "best_per_iteration_ms": round(e["best_ms"], 4), "iterations": e["iterations"],
                                             "learned_regret": round(e["learned_ms"] / e["best_ms"] - 1, 4),
                                             "threshold_regret": round(e["threshold_ms"] / e["best_ms"] - 1, 4)}
+        if hbm:
+            outdeg = np.bincount(pull[0::2].astype(np.int64), minlength=V).astype(np.float64)
+            indeg = np.bincount(pull[1::2].astype(np.int64), minlength=V).astype(np.float64)
+            res["roofline"] = bfs_kernel_rooflines(G, roots[:4], outdeg, indeg, hbm, hbm_kind)
+            del outdeg, indeg
+        # e2e through the C ABI: load from pinned -pull pairs, 64 roots under the learned switch
+        G.set_policy(native.POLICY_LEARNED, net)
+        pin_pull = torch.from_numpy(pull.view(np.int64)).pin_memory()
+
+        def e2e_step():
+            G.load_pull_derive_push(V, E, pin_pull.data_ptr())
+            u = 0
+            for r in roots:
+                G.bfs_run(r)
+                u += G.digest()[1]
+            return u
+        e2e_step()
+        with Timer(torch, stream) as te:
+            units = e2e_step()
+        res["e2e"] = {"value": round(units / (te.ms * 1e-3) / 1e9, 3), "unit": "GTEPS", "h2d_bytes_per_step": int(pull.nbytes),
+                      "d2h_bytes_per_step": 24 * len(roots), "ms_per_step": round(te.ms, 3),
+                      "step": "load of the -pull pairs (the -push list derived on the device), 64 BFS runs under the "
+                              "learned switch, each run's digest (reached vertices, reached edges, level checksum) read back"}
+        del pin_pull
+        G.set_policy(native.POLICY_THRESHOLD)
+    if not a.no_cpu:
+        cpu, _ = cpu_baseline("bfs", None, pull, push, a.bfs_scale, sample=True, V=V)
+        res["cpu_baseline"] = cpu
+    return res
+
+
+def stress_study(a, torch, stream, dev, hbm, hbm_kind):
+    """Large power-law stress (directed R-MAT 27 by default, V = 2^27, E ~ 2.1e9, held in HBM):
+    PageRank (16 pull iterations, d = 0.875) and CC to convergence on the same graph.  Only the
+    -pull pairs stay on the host; the library derives the -push list on the device.  Reports
+    device-resident GTEPS, the pull kernels' rooflines (the PageRank gather also against the
+    gather-inclusive 8E + 8E + 16V, since the gathered props exceed L2), e2e through the C ABI,
+    and parity: one PageRank iteration on a seeded sample of 10^5 destinations recomputed on
+    the host in FP64 from the pairs, and all CC labels against the host's label propagation
+    over the pairs."""
+    from grazelle.engine import Graph
+    from oracle import oracle as O
+    scale = a.stress_scale
+    t0 = time.time()
+    V, E, pull = make_graph_lean("pr", scale, a.seed, True)
+    log("stress graph: scale %d V=%d E=%d (%.1fs)" % (scale, V, E, time.time() - t0))
+    res = {"workload": "rmat%d directed: pr 16 iterations d=0.875, cc to convergence" % scale, "V": V, "E": E}
+    pin_pull = torch.from_numpy(pull.view(np.int64)).pin_memory()
+    n = 2
+    with Graph(dev, stream=stream.cuda_stream) as G:
+        G.load_pull_derive_push(V, E, pin_pull.data_ptr())
+        # PageRank
+        G.pr_init(0.875).pr_iterate(16)
+        with Timer(torch, stream) as tp:
+            for _ in range(n):
+                G.pr_init(0.875).pr_iterate(16)
+        G.profile(True)
+        G.pr_init(0.875).pr_iterate(16)
+        G.sync()
+        ks = kernel_stats(G.profile_read())
+        G.profile(False)
+        gm = ks.get("pr_gather", {}).get("mean_ms", 0)
+        alg, alg_g = 8 * E + 16 * V, 16 * E + 16 * V
+        pr = {"gteps": round(E * 16 * n / (tp.ms * 1e-3) / 1e9, 3), "ms_per_iteration": round(tp.ms / (16 * n), 3),
+              "kernels_us": {k: round(v["mean_ms"] * 1e3, 1) for k, v in ks.items()}}
+        if gm:
+            pr["roofline"] = {"bound": "hbm", "kernel": "pr_gather", "mean_launch_ms": round(gm, 3), "peak": hbm,
+                              "peak_kind": hbm_kind, "unit": "GB/s",
+                              "algorithmic_bytes": alg, "achieved": round(alg / (gm * 1e-3) / 1e9, 1),
+                              "frac": round(alg / (gm * 1e-3) / 1e9 / hbm, 4),
+                              "gather_inclusive_bytes": alg_g, "gather_inclusive_achieved": round(alg_g / (gm * 1e-3) / 1e9, 1),
+                              "gather_inclusive_frac": round(alg_g / (gm * 1e-3) / 1e9 / hbm, 4)}
+        # parity: one iteration at a seeded sample of destinations
+        rng = np.random.default_rng(a.seed + 27)
+        smp = np.sort(rng.choice(V, size=100000, replace=False)).astype(np.uint64)
+        p1 = G.pr_init(0.875).pr_iterate(1).props()
+        t1 = time.time()
+        ref = O.pr_sample_iteration(pull, V, smp, 0.875)
+        err = O.relative_l1(p1[smp.astype(np.int64)], ref)
+        pr["parity"] = {"destinations_sampled": int(smp.shape[0]), "iterations": 1, "rel_l1": err, "bound": 1e-12,
+                        "ok": err < 1e-12, "check_s": round(time.time() - t1, 1)}
+        del p1, ref
+        # CC on the same (directed) graph
+        G.cc_run()
+        ms, its = [], None
+        for _ in range(n):
+            st = G.cc_run()
+            ms.append(st.ms)
+            its = (st.iterations, st.pull_iterations, st.push_iterations)
+        G.profile(True)
+        G.cc_run()
+        recs = G.profile_read()
+        G.profile(False)
+        fp = [m for k, m in recs if k == "cc_pull"]
+        cc = {"gteps": round(E * its[0] / (np.mean(ms) * 1e-3) / 1e9, 3), "ms_per_run": round(float(np.mean(ms)), 3),
+              "iterations_pull_push": list(its),
+              "kernels_us": {k: round(v["mean_ms"] * 1e3, 1) for k, v in kernel_stats(recs).items()}}
+        if fp:
+            b = 8 * E + 16 * V + V // 4
+            cc["roofline"] = {"bound": "hbm", "kernel": "cc_pull", "launch": "first (full-pass) pull of the run",
+                              "mean_launch_ms": round(fp[0], 3), "algorithmic_bytes": b,
+                              "achieved": round(b / (fp[0] * 1e-3) / 1e9, 1), "peak": hbm, "peak_kind": hbm_kind,
+                              "unit": "GB/s", "frac": round(b / (fp[0] * 1e-3) / 1e9 / hbm, 4)}
+        lab = G.props()
+        # e2e: load + 16 PageRank iterations + props back; load + CC + labels back
+        d2h = torch.zeros(V, dtype=torch.float64).pin_memory().numpy()
+        with Timer(torch, stream) as te:
+            G.load_pull_derive_push(V, E, pin_pull.data_ptr())
+            G.pr_init(0.875).pr_iterate(16)
+            G.lib.grz_read_props(G.h, d2h.ctypes.data, V)
+        pr["e2e"] = {"value": round(E * 16 / (te.ms * 1e-3) / 1e9, 3), "unit": "GTEPS", "h2d_bytes_per_step": int(pull.nbytes),
+                     "d2h_bytes_per_step": int(d2h.nbytes), "ms_per_step": round(te.ms, 3)}
+        with Timer(torch, stream) as te:
+            G.load_pull_derive_push(V, E, pin_pull.data_ptr())
+            st = G.cc_run()
+            G.lib.grz_read_props(G.h, d2h.ctypes.data, V)
+        cc["e2e"] = {"value": round(E * st.iterations / (te.ms * 1e-3) / 1e9, 3), "unit": "GTEPS",
+                     "h2d_bytes_per_step": int(pull.nbytes), "d2h_bytes_per_step": int(d2h.nbytes), "ms_per_step": round(te.ms, 3)}
+        e2e_same = bool(np.array_equal(d2h, lab))
+        del d2h
+    del pin_pull
+    t1 = time.time()
+    ref = O.cc_min_labels(pull, V)
+    ok = bool(np.array_equal(lab, ref.astype(np.float64)))
+    cc["parity"] = {"labels_checked": V, "labels_exact": ok, "e2e_labels_equal_resident": e2e_same, "ok": ok and e2e_same,
+                    "check": "label propagation over the -pull pairs on the host (oracle_cc_min_labels)",
+                    "check_s": round(time.time() - t1, 1)}
+    del ref, lab, pull
+    res["pagerank"] = pr
+    res["cc"] = cc
+    res["parity"] = {"ok": pr["parity"]["ok"] and cc["parity"]["ok"]}
+    res["cpu_baseline"] = {"value": None, "unit": "GTEPS", "cores": os.cpu_count(), "kind": "port",
+                           "sample": "not run: the CPU restatement's vector layout of a graph this size does not fit a "
+                                     "bounded sample; the parity checks above run on the host from the pairs"}
     return res
 
 
@@ -503,10 +754,9 @@ def batch_graphs(seed: int):
 def batch_study(a, torch, stream, dev):
     """256 personalized-PageRank instances (8 seeds per graph, 20 iterations, d = 0.85, FP64
     ranks) and 256 BFS instances (8 roots per graph) over the 32 graphs, each run one CUDA graph
-    launch of the batch; every instance of two graphs checked against the CPU oracles."""
+    launch of the batch; every instance of every graph checked against the CPU oracles."""
     from grazelle.batch import Batch
     from oracle import oracle as O
-    from oracle import ppr as P
     t0 = time.time()
     gs = batch_graphs(a.seed)
     E_tot = sum(g.num_edges for _, g in gs)
@@ -551,15 +801,19 @@ def batch_study(a, torch, stream, dev):
                 reached += int(deg[lv[:, i] >= 0].sum())
         res["msbfs"] = {"instances": n_inst, "ms": round(bfs_ms, 3), "iterations": st.iterations,
                         "gteps": round(reached / (bfs_ms * 1e-3) / 1e9, 2)}
+        # every instance of every graph against the oracles (C, OpenMP): PPR within 1e-12
+        # relative L1 of oracle/ppr.py's definition, BFS levels exactly
+        t2 = time.time()
         worst, exact = 0.0, True
-        for gi in (0, 1):
-            g = gs[gi][1]
+        for gi, (_, g) in enumerate(gs):
             pull, push = g.pull_order().pairs(), g.push_order().pairs()
-            for i, s in enumerate(seeds[gi]):
-                ref = P.ppr(g.num_vertices, pull, s, 20, 0.85)
-                worst = max(worst, float(np.abs(ranks[gi][:, i] - ref).sum() / np.abs(ref).sum()))
-                exact &= bool(np.array_equal(levels[gi][:, i].astype(np.int64), O.bfs_levels(push, g.num_vertices, s)))
-        res["parity_sample"] = {"ppr_max_rel_l1": worst, "bfs_levels_exact": exact, "graphs_checked": [gs[0][0], gs[1][0]]}
+            ref = O.ppr_multi(g.num_vertices, pull, seeds[gi], 20, 0.85)
+            refl = O.bfs_levels_multi(push, g.num_vertices, seeds[gi])
+            for i in range(len(seeds[gi])):
+                worst = max(worst, O.relative_l1(ranks[gi][:, i], ref[:, i]))
+                exact &= bool(np.array_equal(levels[gi][:, i].astype(np.int64), refl[i]))
+        res["parity"] = {"graphs_checked": len(gs), "instances_checked": n_inst, "ppr_max_rel_l1": worst, "ppr_bound": 1e-12,
+                         "bfs_levels_exact": exact, "ok": worst < 1e-12 and exact, "check_s": round(time.time() - t2, 1)}
         res["gpu_launches_per_run"] = {"ppr": 1 + 2 * 20, "msbfs": 1 + 3 * st.iterations}
     return res
 
@@ -585,42 +839,47 @@ def run_batch(a):
 
 # ---------------------------------------------------------------------------------------------- CPU
 
-def cpu_baseline(wl, g, pull, push, scale, sample=True, threads=0, steps=1):
+def cpu_baseline(wl, g, pull, push, scale, sample=True, threads=0, steps=1, V=None):
     """The reference's algorithm on the host cores.  The reference binary runs only on x86-64
     with AVX2, so this uses oracle/'s OpenMP restatement with the same work-unit scheme;
-    `kind` says which."""
+    `kind` says which.  Returns (baseline record, the last run's props as the reference stores
+    them: PageRank rank/outdeg', CC labels, BFS parents)."""
     from oracle import oracle as O
+    V = g.num_vertices if g is not None else V
     t0 = time.time()
-    L = O.layout(g.num_vertices, pull, push)
+    L = O.layout(V, pull, push)
     build_s = time.time() - t0
     cores = os.cpu_count() or 1
     vals = []
     n_used = 0
     it_total = 0
+    out = None
     for _ in range(steps):
         t = time.time()
         if wl == "pr":
             iters = 4 if sample else 16
-            O.pr_pull(L, iters, 0.875, units=32 * cores, threads=threads, multithreaded=True)
+            out = O.pr_pull(L, iters, 0.875, units=32 * cores, threads=threads, multithreaded=True)
             units = L.E * iters
             it_total = iters
         elif wl == "cc":
-            lab, it, n_used = O.frontier_mt(L, 1, 0, threads=threads)
+            out, it, n_used = O.frontier_mt(L, 1, 0, threads=threads)
             units = L.E * int(it[0])
             it_total = int(it[0])
         else:
-            par, it, n_used = O.frontier_mt(L, 2, 0, threads=threads)
-            reached = par >= 0
+            out, it, n_used = O.frontier_mt(L, 2, 0, threads=threads)
+            reached = out >= 0
             reached[0] = True
             units = int(L.outdeg[reached].sum())
             it_total = int(it[0])
         dt = time.time() - t
         vals.append(units / dt / 1e9)
-    return {"value": round(max(vals), 4), "unit": "GTEPS", "cores": threads or cores, "kind": "port",
-            "sample": "%s on the same graph, %d iteration(s) per run, best of %d, OpenMP restatement with the "
-                      "reference's work units (oracle/grz_oracle.c); layout build %.1fs not timed" % (
-                          {"pr": "PageRank pull", "cc": "CC to convergence", "bfs": "BFS from root 0"}[wl], it_total,
-                          steps, build_s)}
+    del L
+    rec = {"value": round(max(vals), 4), "unit": "GTEPS", "cores": threads or cores, "kind": "port",
+           "sample": "%s on the same graph, %d iteration(s) per run, best of %d, OpenMP restatement with the "
+                     "reference's work units (oracle/grz_oracle.c); layout build %.1fs not timed" % (
+                         {"pr": "PageRank pull", "cc": "CC to convergence", "bfs": "BFS from root 0"}[wl], it_total,
+                         steps, build_s)}
+    return rec, out
 
 
 def run_reference(a):
@@ -632,7 +891,7 @@ def run_reference(a):
     g, pull, push = make_graph(wl, scale, a.seed, a.directed)
     for _ in range(a.warmup):
         pass  # the CPU run has no warm-up state beyond the layout, which is built once
-    res = cpu_baseline(wl, g, pull, push, scale, sample=False, steps=max(1, a.steps))
+    res, _ = cpu_baseline(wl, g, pull, push, scale, sample=False, steps=max(1, a.steps))
     line = {
         "impl": "reference", "metric": "GTEPS (%s, E x iterations / time)" % {"cc": "connected components", "pr": "pagerank pull",
                                                                                "bfs": "bfs"}[wl],
@@ -658,6 +917,8 @@ def main():
     ap.add_argument("--no-apps", action="store_true")
     ap.add_argument("--bfs-scale", type=int, default=26, help="R-MAT scale of the BFS switch study (0: skip)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched PPR / multi-source BFS study")
+    ap.add_argument("--stress-scale", type=int, default=27,
+                    help="R-MAT scale of the large power-law stress study, PageRank and CC on a directed graph (0: skip)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the default kernel shapes (no autotuning pass)")
     ap.add_argument("--lean", action="store_true", help="host keeps only the -pull pairs (default from scale 26)")

@@ -100,34 +100,88 @@ struct VoteCfg {
 // ---------------------------------------------------------------------------------------------
 // CC pull
 
+// Smallest label written by a CC iteration, for the next iteration's converged-destination
+// skip.  Iteration k adds ((k << 32) | ~m) into word k & 1 with atomicMax, m the smallest label
+// it wrote; the words are never reset: a tag other than k - 1 means "unknown" and the reader
+// does not skip.  Why the skip is exact: after a complete iteration (a pull over the
+// whole list, or a push from the whole frontier) every destination d holds at most the labels
+// its sources had when d was last evaluated, so only a source that changed since can lower d.
+// Every such change happened in iteration k - 1 (earlier ones were evaluated or pushed in
+// k - 1) or happens during iteration k (recorded in HasInfo*, handled in k + 1).  A change in
+// k - 1 wrote a label >= m(k - 1); so if label[d] <= m(k - 1), iteration k cannot lower d.
+// Iteration 1 follows the initial state, in which every vertex counts as changed: no skip.
+__device__ __forceinline__ bool cc_prev_min(const unsigned long long* __restrict__ chg, uint32_t k, uint32_t* m)
+{
+    if (k < 2) return false;
+    const unsigned long long w = chg[(k - 1) & 1];
+    if ((uint32_t)(w >> 32) != k - 1) return false;
+    *m = ~(uint32_t)w;
+    return true;
+}
+
+// block-wide minimum of one value per thread, then one tagged atomicMax (threadIdx.x 0 only)
+template <int BT>
+__device__ __forceinline__ void cc_record_min(uint32_t my_min, uint32_t* red32, unsigned long long* __restrict__ chg, uint32_t k)
+{
+    my_min = __reduce_min_sync(0xffffffffu, my_min);
+    if ((threadIdx.x & 31) == 0) red32[threadIdx.x >> 5] = my_min;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        uint32_t x = threadIdx.x < BT / 32 ? red32[threadIdx.x] : INF;
+        x = __reduce_min_sync(0xffffffffu, x);
+        if (threadIdx.x == 0 && x != INF) atomicMax(chg + (k & 1), ((unsigned long long)k << 32) | (unsigned long long)(~x));
+    }
+}
+
 // Persistent, BT threads per block, one thread per vector per tile of BT vectors.  The labels
 // of the first `ncache` hub slots are copied into shared memory when the block starts; lanes
 // that name them read shared memory instead of gathering through L1 (in a power-law graph most
 // lanes).  Those copies may fall behind the in-place updates of this phase, which the
 // reference's asynchronous CAS loop allows as well: a label only ever decreases, every value
 // read is one the source really had, and an iteration that changes nothing is still a fixpoint.
+// Iteration k (epoch_dev, else epoch) skips destinations whose label is at most the smallest
+// label written in iteration k - 1 (cc_prev_min; only with use_prev, i.e. when k - 1 was a
+// complete iteration): it reads their destination and label, not their vectors.  R-MAT's
+// hubs have the smallest IDs, so after the first iteration most of the giant component holds
+// label 0 and the second pull reads little more than the destinations.
 template <int BT>
 __global__ void __launch_bounds__(BT) k_cc_pull(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv, uint64_t first,
                                                 uint64_t nvec, uint32_t V, uint32_t* __restrict__ label,
                                                 const uint32_t* __restrict__ hub_vid, uint32_t nhub, uint32_t ncache,
                                                 unsigned long long* __restrict__ has_next, VoteCfg vc,
-                                                unsigned long long* __restrict__ vote)
+                                                unsigned long long* __restrict__ vote, unsigned long long* __restrict__ chg,
+                                                uint32_t epoch, const uint32_t* __restrict__ epoch_dev, int use_prev)
 {
     extern __shared__ uint32_t s_hub[];
     __shared__ unsigned long long red[BT / 32];
+    __shared__ uint32_t red32[BT / 32];
     for (uint32_t k = threadIdx.x; k < ncache; k += BT) s_hub[k] = label[__ldg(hub_vid + k)];
+    const uint32_t ep = epoch_dev ? *epoch_dev : epoch;
+    uint32_t mprev = 0;
+    const bool skip = use_prev && cc_prev_min(chg, ep, &mprev);
     __syncthreads();
     const int lane = threadIdx.x & 31;
     unsigned long long my_vote = 0;
+    uint32_t my_min = INF;
     const uint64_t ntiles = (nvec + BT - 1) / BT;
     for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const uint64_t i = t * BT + threadIdx.x;
         const uint64_t v = first + i;
         const bool live = i < nvec;
-        uint32_t key = INF, m = INF;
-        if (live) {
+        uint32_t key = INF, m = INF, labd = INF;
+        bool need = live;
+        if (skip) {
+            // skip mode: the destination's label decides whether the vector is read at all
+            if (live) {
+                key = __ldcs(dstv + v);
+                labd = label[key];
+                need = labd > mprev;
+            }
+            if (!__any_sync(0xffffffffu, need)) continue;  // warp-uniform
+        }
+        if (need) {
             const uint4 s = __ldcs(nbr + v);
-            key = __ldcs(dstv + v);
+            if (!skip) key = __ldcs(dstv + v);
             const uint32_t x[4] = { s.x, s.y, s.z, s.w };
             uint32_t val[4];
 #pragma unroll
@@ -154,14 +208,17 @@ __global__ void __launch_bounds__(BT) k_cc_pull(const uint4* __restrict__ nbr, c
             const uint32_t o = __shfl_up_sync(0xffffffffu, m, off);
             if (lane - off >= segstart) m = min(m, o);
         }
-        if (live && tail && m != INF && m < label[key]) {
+        if (live && tail && m != INF && m < (skip ? labd : label[key])) {
             const uint32_t old = atomicMin(label + key, m);
-            if (m < old && bit_set_first(has_next, key)) my_vote += vc.of(key);
+            if (m < old) {
+                my_min = min(my_min, m);
+                if (bit_set_first(has_next, key)) my_vote += vc.of(key);
+            }
         }
     }
     for (int o = 16; o > 0; o >>= 1) my_vote += __shfl_down_sync(0xffffffffu, my_vote, o);
     if (lane == 0) red[threadIdx.x >> 5] = my_vote;
-    __syncthreads();
+    cc_record_min<BT>(my_min, red32, chg, ep);  // (contains the __syncthreads the vote sum needs)
     if (threadIdx.x < 32) {
         unsigned long long x = threadIdx.x < BT / 32 ? red[threadIdx.x] : 0ull;
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
@@ -443,9 +500,13 @@ __global__ void __launch_bounds__(T) k_push_expand(const uint32_t* __restrict__ 
                                                    uint32_t V, uint32_t* __restrict__ label,
                                                    unsigned long long* __restrict__ has_next, const unsigned long long* __restrict__ wants,
                                                    uint32_t* __restrict__ cand32, uint32_t* __restrict__ touched,
-                                                   uint32_t* __restrict__ ntouched, VoteCfg vc, unsigned long long* __restrict__ vote)
+                                                   uint32_t* __restrict__ ntouched, VoteCfg vc, unsigned long long* __restrict__ vote,
+                                                   unsigned long long* __restrict__ chg, uint32_t epoch,
+                                                   const uint32_t* __restrict__ epoch_dev)
 {
     __shared__ uint32_t s_src[PUSH_TILE + 1];
+    __shared__ uint32_t red32[T / 32];
+    uint32_t my_min = INF;  // CC: the smallest label written (cc_prev_min of the next iteration)
     __shared__ uint32_t s_off[PUSH_TILE + 1];
     __shared__ uint32_t s_delta[PUSH_TILE + 1];
     __shared__ unsigned long long red[T / 32];
@@ -499,7 +560,10 @@ __global__ void __launch_bounds__(T) k_push_expand(const uint32_t* __restrict__ 
                     const uint32_t d = ids[l];
                     if (d < V && msg < label[d]) {
                         const uint32_t old = atomicMin(label + d, msg);
-                        if (msg < old && bit_set_first(has_next, d)) my_vote += vc.of(d);
+                        if (msg < old) {
+                            my_min = min(my_min, msg);
+                            if (bit_set_first(has_next, d)) my_vote += vc.of(d);
+                        }
                     }
                 }
             }
@@ -509,6 +573,7 @@ __global__ void __launch_bounds__(T) k_push_expand(const uint32_t* __restrict__ 
     if (!IsBfs) {
         my_vote = block_sum_u64(my_vote, red);
         if (threadIdx.x == 0) vote_add(vote, my_vote);
+        cc_record_min<T>(my_min, red32, chg, epoch_dev ? *epoch_dev : epoch);
     }
 }
 
@@ -796,6 +861,7 @@ static int ensure_frontier_state(grz_graph* g)
     GRZ_CK(g, cudaMalloc((void**)&f.cand32, sizeof(uint32_t) * (V + 1)));
     GRZ_CK(g, cudaMalloc((void**)&f.counters, sizeof(uint32_t) * 8));
     GRZ_CK(g, cudaMalloc((void**)&f.vote, sizeof(unsigned long long) * GRZ_VOTE_SLOTS * GRZ_VOTE_STRIDE));
+    GRZ_CK(g, cudaMalloc((void**)&f.chg, sizeof(unsigned long long) * 2));
     return frontier_list_state(g);
 }
 
@@ -848,6 +914,10 @@ int grz_frontier_init(grz_graph* g, int app, int flags, uint32_t root)
         k_cc_init<<<blocks_for(V + 1), T, 0, st>>>(f.label, V); GRZ_COUNT_LAUNCH(g);
         k_bitmap_init<<<blocks_for(W), T, 0, st>>>(f.has, W, V, 1); GRZ_COUNT_LAUNCH(g);      // HasInfo = all (execution_cc.c:66-73)
         k_bitmap_init<<<blocks_for(W), T, 0, st>>>(f.wants, W, V, 1); GRZ_COUNT_LAUNCH(g);
+        // before iteration 1 every vertex counts as changed, the smallest label being 0 (tag 0)
+        const unsigned long long chg0[2] = { 0x00000000ffffffffull, 0ull };
+        memcpy(f.mail_chg, chg0, sizeof(chg0));
+        GRZ_CK(g, cudaMemcpyAsync(f.chg, f.mail_chg, sizeof(chg0), cudaMemcpyHostToDevice, st));
         f.vote_host = 0;
         if (!(flags & GRZ_FLAG_WITHOUT_OUTDEG)) f.vote_host += g->E;     // execution_cc.c:106-112
         if (!(flags & GRZ_FLAG_WITHOUT_COUNT)) f.vote_host += V;
@@ -926,8 +996,12 @@ static int launch_cc_pull_bt(grz_graph* g, uint64_t first, uint64_t count, const
     const uint64_t tiles = (count + BT - 1) / BT;
     uint64_t grid = g->tune.cc_grid ? g->tune.cc_grid : (uint64_t)g->num_sms * resident;
     grid = std::max<uint64_t>(1, std::min<uint64_t>(grid, tiles));
+    // the skip needs every earlier iteration to have been complete (the whole list, or the whole
+    // frontier): true for the driver loops, not for calls of the phases.h entry points
+    const int use_prev = !f.phase_api && first == 0 && count == g->pull.nvec;
     k_cc_pull<BT><<<(unsigned)grid, BT, smem, g->stream>>>(g->pull.nbr, g->pull.shared, first, count, (uint32_t)g->V, f.label,
-                                                          g->pull.hub_vid, g->pull.nhub, ncache, f.has_next, vc, f.vote); GRZ_COUNT_LAUNCH(g);
+                                                          g->pull.hub_vid, g->pull.nhub, ncache, f.has_next, vc, f.vote, f.chg,
+                                                          f.iter, f.level_dev, use_prev); GRZ_COUNT_LAUNCH(g);
     return GRZ_OK;
 }
 
@@ -1007,14 +1081,16 @@ static int edge_phase(grz_graph* g, int pull, uint64_t first, uint64_t count)
         const unsigned grid = (unsigned)g->num_sms * 8;
         if (bfs) {
             k_push_expand<true><<<grid, T, 0, st>>>(f.frontier, f.voff, f.vdelta, f.tile_first, f.counters, g->push.nbr, V, f.label,
-                                                    f.has_next, f.wants, f.cand32, f.touched, f.counters + 1, vc, f.vote); GRZ_COUNT_LAUNCH(g);
+                                                    f.has_next, f.wants, f.cand32, f.touched, f.counters + 1, vc, f.vote,
+                                                    nullptr, 0, nullptr); GRZ_COUNT_LAUNCH(g);
             grz_prof_end(g);
             grz_prof_begin(g, GRZ_PROF_BFS_VISIT);
             k_bfs_visit<false><<<visit_grid(g), T, 0, st>>>(f.touched, f.counters + 1, f.cand64, f.cand32, f.label, f.level,
                                                              f.iter, f.level_dev, f.wants, f.has_next, vc, f.vote, V); GRZ_COUNT_LAUNCH(g);
         } else {
             k_push_expand<false><<<grid, T, 0, st>>>(f.frontier, f.voff, f.vdelta, f.tile_first, f.counters, g->push.nbr, V, f.label,
-                                                     f.has_next, f.wants, f.cand32, f.touched, f.counters + 1, vc, f.vote); GRZ_COUNT_LAUNCH(g);
+                                                     f.has_next, f.wants, f.cand32, f.touched, f.counters + 1, vc, f.vote,
+                                                     f.chg, f.iter, f.level_dev); GRZ_COUNT_LAUNCH(g);
         }
         grz_prof_end(g);
     }
@@ -1042,7 +1118,14 @@ int grz_cc_phase(grz_graph* g, int pull, uint64_t first_vec, uint64_t count)
         int rc = grz_frontier_init(g, GRZ_APP_CONNECTED_COMPONENTS, 0, 0);
         if (rc) return rc;
     }
-    return edge_phase(g, pull, first_vec, count);
+    // the caller may pass any vector range: no converged-destination skip, and none later in
+    // this state either (the tag 2^32 - 1 never matches; grz_frontier_init starts over)
+    g->fr.phase_api = 1;
+    const int rc = edge_phase(g, pull, first_vec, count);
+    g->fr.phase_api = 0;
+    if (rc) return rc;
+    GRZ_CK(g, cudaMemsetAsync(g->fr.chg, 0xff, 2 * sizeof(unsigned long long), g->stream));
+    return GRZ_OK;
 }
 
 int grz_bfs_phase(grz_graph* g, int pull, uint64_t first_vec, uint64_t count)
@@ -1196,7 +1279,7 @@ void grz_frontier_park(grz_graph* g)
 void grz_frontier_free(grz_graph* g)
 {
     grz_frontier_state& f = g->fr;
-    void* ptrs[] = { f.label, f.level, f.has, f.has_next, f.wants, f.nonempty_push, f.nonempty_pull, f.frontier, f.voff, f.vdelta, f.tile_first,
+    void* ptrs[] = { f.label, f.level, f.has, f.has_next, f.wants, f.nonempty_push, f.nonempty_pull, f.frontier, f.voff, f.vdelta, f.tile_first, f.chg,
                      f.fr_part, f.touched, f.cand64, f.cand32,
                      f.counters, f.vote, f.sw_out, f.snap };
     for (void* p : ptrs) cudaFree(p);

@@ -292,6 +292,9 @@ struct grz_frontier_state {
     uint32_t* cand32;                // BFS push: smallest source per destination
     uint32_t* counters;              // [0] frontier size, [1] touched count
     unsigned long long* vote;        // GRZ_VOTE_SLOTS * GRZ_VOTE_STRIDE
+    unsigned long long* chg;         // CC: smallest label written per iteration, tagged (2 words, grz_ccbfs.cu)
+    unsigned long long mail_chg[2];  // host copy of the initial chg words (outlives the async copy)
+    int phase_api;                   // an edge phase of the phases.h entry points is running
     // engine policy
     int policy;                      // GRZ_POLICY_*
     grz_mlp* mlp;

@@ -862,3 +862,213 @@ int oracle_frontier_mt(const uint64_t* pull_vec, uint64_t pull_nvec, const uint6
     free(has); free(has_next); free(wants);
     return threads;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Batched personalized PageRank and multi-root BFS levels (checkers)          */
+/* ------------------------------------------------------------------------- */
+
+/*
+ * K personalized PageRank instances on one graph, the serial definition of
+ * oracle/ppr.py with the instances side by side: the reference's PageRank
+ * iteration (edge pull source/phase_edge_pull_pr.asm:45-171, vertex phase
+ * source/phase_vertex_pr.asm:75-134) with the teleport term and the dangling
+ * mass sent to the seed:
+ *   prop[u]  = rank[u] / deg'(u)   (deg' = outdegree, or V when 0)
+ *   accum[v] = sum over in-edges (u, v) of prop[u], in the -pull file's order
+ *   S        = sum over v of accum[v]
+ *   rank'[v] = d * accum[v] + [v == seed] * (d * (1 - S) + (1 - d))
+ * from rank = one-hot(seed).  pull_pairs is the -pull list (sorted by
+ * destination).  ranks is [V][K]; seeds[k] >= V leaves column k at zero.
+ * OpenMP over destinations; S is summed per thread, then over threads.
+ */
+void oracle_ppr_multi(const uint64_t* pull_pairs, uint64_t E, uint64_t V, const uint32_t* seeds, uint32_t K,
+                      uint32_t iters, double d, int threads, double* ranks)
+{
+    uint64_t* off = (uint64_t*)calloc(V + 1, sizeof(uint64_t));
+    double* degp = (double*)malloc(sizeof(double) * (V ? V : 1));
+    double* prop = (double*)malloc(sizeof(double) * (V ? V : 1) * K);
+    double* S = (double*)calloc(K, sizeof(double));
+    for (uint64_t v = 0; v < V; ++v) degp[v] = 0.0;
+    for (uint64_t e = 0; e < E; ++e) {
+        degp[pull_pairs[2 * e]] += 1.0;
+        off[pull_pairs[2 * e + 1] + 1]++;
+    }
+    for (uint64_t v = 0; v < V; ++v) {
+        off[v + 1] += off[v];
+        if (degp[v] == 0.0) degp[v] = (double)V;
+    }
+    memset(ranks, 0, sizeof(double) * V * K);
+    for (uint32_t k = 0; k < K; ++k)
+        if (seeds[k] < V) ranks[(uint64_t)seeds[k] * K + k] = 1.0;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#endif
+    for (uint32_t it = 0; it < iters; ++it) {
+        for (uint32_t k = 0; k < K; ++k) S[k] = 0.0;
+#pragma omp parallel
+        {
+            double* Sl = (double*)calloc(K, sizeof(double));
+#pragma omp for schedule(static)
+            for (uint64_t v = 0; v < V; ++v)
+                for (uint32_t k = 0; k < K; ++k) prop[v * K + k] = ranks[v * K + k] / degp[v];
+#pragma omp for schedule(dynamic, 4096)
+            for (uint64_t v = 0; v < V; ++v) {
+                double acc[64];
+                for (uint32_t k = 0; k < K; ++k) acc[k] = 0.0;
+                for (uint64_t e = off[v]; e < off[v + 1]; ++e) {
+                    const double* p = prop + pull_pairs[2 * e] * K;
+                    for (uint32_t k = 0; k < K; ++k) acc[k] += p[k];
+                }
+                for (uint32_t k = 0; k < K; ++k) {
+                    Sl[k] += acc[k];
+                    ranks[v * K + k] = d * acc[k];
+                }
+            }
+#pragma omp critical
+            for (uint32_t k = 0; k < K; ++k) S[k] += Sl[k];
+            free(Sl);
+        }
+        for (uint32_t k = 0; k < K; ++k)
+            if (seeds[k] < V) ranks[(uint64_t)seeds[k] * K + k] += d * (1.0 - S[k]) + (1.0 - d);
+    }
+    free(S); free(prop); free(degp); free(off);
+}
+
+/*
+ * BFS levels from n roots over the -push pairs (the CSR is built once, the
+ * roots run on parallel threads): level[r * V + v], -1 if unreachable.
+ */
+void oracle_bfs_levels_multi(const uint64_t* push_pairs, uint64_t E, uint64_t V, const uint64_t* roots, uint32_t n,
+                             int threads, int64_t* level)
+{
+    uint64_t* off = (uint64_t*)calloc(V + 1, sizeof(uint64_t));
+    for (uint64_t e = 0; e < E; ++e) off[push_pairs[2 * e] + 1]++;
+    for (uint64_t v = 0; v < V; ++v) off[v + 1] += off[v];
+    uint64_t* adj = (uint64_t*)malloc(sizeof(uint64_t) * (E ? E : 1));
+    uint64_t* fill = (uint64_t*)malloc(sizeof(uint64_t) * (V ? V : 1));
+    memcpy(fill, off, sizeof(uint64_t) * V);
+    for (uint64_t e = 0; e < E; ++e) adj[fill[push_pairs[2 * e]]++] = push_pairs[2 * e + 1];
+    free(fill);
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1)
+    for (uint32_t r = 0; r < n; ++r) {
+        int64_t* lv = level + (uint64_t)r * V;
+        uint64_t* q = (uint64_t*)malloc(sizeof(uint64_t) * (V ? V : 1));
+        uint64_t qh = 0, qt = 0;
+        for (uint64_t v = 0; v < V; ++v) lv[v] = -1;
+        lv[roots[r]] = 0;
+        q[qt++] = roots[r];
+        while (qh < qt) {
+            const uint64_t u = q[qh++];
+            for (uint64_t k = off[u]; k < off[u + 1]; ++k) {
+                const uint64_t w = adj[k];
+                if (lv[w] < 0) { lv[w] = lv[u] + 1; q[qt++] = w; }
+            }
+        }
+        free(q);
+    }
+    free(adj); free(off);
+}
+
+/*
+ * Connected Components labels straight from the -pull pairs (sorted by
+ * destination), for graphs whose vector lists would not fit a bounded host
+ * sample: label[v] = the smallest vertex ID that reaches v (v included),
+ * which is the fixpoint the reference's CC reaches on a directed or
+ * symmetric graph (pull: label[d] = min over its sources and itself,
+ * source/phase_edge_pull_cc.asm:183-233; push: CAS-min into the
+ * destinations, source/phase_edge_push_cc.asm:130-225; the vertex IDs are the
+ * initial labels, source/execution_cc.c:66-90).  Sweeps of in-place
+ * min-propagation over the destination ranges (OpenMP, relaxed atomic reads
+ * and writes: labels only decrease) until a sweep changes nothing.  Returns
+ * the number of sweeps.
+ */
+uint32_t oracle_cc_min_labels(const uint64_t* pull_pairs, uint64_t E, uint64_t V, int threads, uint32_t* label)
+{
+    for (uint64_t v = 0; v < V; ++v) label[v] = (uint32_t)v;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#endif
+    /* chunk boundaries on destination changes, so that one thread owns each destination */
+    const uint64_t nch = E / 65536 + 1;
+    uint64_t* cut = (uint64_t*)malloc(sizeof(uint64_t) * (nch + 1));
+    for (uint64_t c = 0; c <= nch; ++c) {
+        uint64_t e = E * c / nch;
+        while (e > 0 && e < E && pull_pairs[2 * e + 1] == pull_pairs[2 * (e - 1) + 1]) ++e;
+        cut[c] = e;
+    }
+    uint32_t sweeps = 0;
+    for (;;) {
+        uint64_t changed = 0;
+        ++sweeps;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : changed)
+        for (uint64_t c = 0; c < nch; ++c) {
+            uint64_t e = cut[c];
+            const uint64_t end = cut[c + 1];
+            while (e < end) {
+                const uint64_t d = pull_pairs[2 * e + 1];
+                uint32_t m = __atomic_load_n(&label[d], __ATOMIC_RELAXED);
+                const uint32_t m0 = m;
+                for (; e < end && pull_pairs[2 * e + 1] == d; ++e) {
+                    const uint32_t x = __atomic_load_n(&label[pull_pairs[2 * e]], __ATOMIC_RELAXED);
+                    if (x < m) m = x;
+                }
+                if (m < m0) {
+                    __atomic_store_n(&label[d], m, __ATOMIC_RELAXED);
+                    ++changed;
+                }
+            }
+        }
+        if (!changed) break;
+    }
+    free(cut);
+    return sweeps;
+}
+
+/*
+ * One PageRank iteration from the initial props, checked on a sample of
+ * destinations only, straight from the -pull pairs (sorted by destination):
+ * for graphs whose vector lists would not fit a bounded host sample.
+ *   prop0[u] = (1/V) / deg'(u)                 source/execution_pr.c:85-88
+ *   accum[v] = sum over v's in-edges of prop0  source/phase_edge_pull_pr.asm:45-171
+ *   S        = sum over u of prop0[u] * outdeg(u)   (= sum of all accumulators)
+ *   prop1[v] = ((accum[v] + (1-S)/V) * d + (1-d)/V) / deg'(v)   source/phase_vertex_pr.asm:75-134
+ * deg' = outdegree from the -pull pairs, or V when 0.  samples[] are
+ * destinations; out[i] is prop1[samples[i]] (a binary search finds each
+ * destination's edges).
+ */
+void oracle_pr_sample_iteration(const uint64_t* pull_pairs, uint64_t E, uint64_t V, double d, int threads,
+                                const uint64_t* samples, uint64_t n, double* out)
+{
+    uint32_t* deg = (uint32_t*)calloc(V ? V : 1, sizeof(uint32_t));
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#endif
+#pragma omp parallel for schedule(static)
+    for (uint64_t e = 0; e < E; ++e) __atomic_fetch_add(&deg[pull_pairs[2 * e]], 1u, __ATOMIC_RELAXED);
+    const double dV = (double)V;
+    double S = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : S)
+    for (uint64_t u = 0; u < V; ++u)
+        if (deg[u]) S += ((1.0 / dV) / (double)deg[u]) * (double)deg[u];
+    const double G = (1.0 - S) / dV;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (uint64_t i = 0; i < n; ++i) {
+        const uint64_t v = samples[i];
+        uint64_t lo = 0, hi = E;  /* first edge with destination >= v */
+        while (lo < hi) {
+            const uint64_t mid = lo + (hi - lo) / 2;
+            if (pull_pairs[2 * mid + 1] < v) lo = mid + 1; else hi = mid;
+        }
+        double acc = 0.0;
+        for (uint64_t e = lo; e < E && pull_pairs[2 * e + 1] == v; ++e) {
+            const uint64_t u = pull_pairs[2 * e];
+            acc += (1.0 / dV) / (double)deg[u];  /* a source of an edge has deg >= 1 */
+        }
+        const double dp = deg[v] ? (double)deg[v] : dV;
+        out[i] = ((acc + G) * d + (1.0 - d) / dV) / dp;
+    }
+    free(deg);
+}

@@ -75,6 +75,13 @@ def lib():
         L.oracle_frontier_mt.argtypes = [_u64p, C.c_uint64, _u64p, _u64p, C.c_uint64, _u64p, _f64p, C.c_uint64, C.c_uint64,
                                          C.c_int, C.c_int, C.c_int, _f64p, _u64p]
         L.oracle_bfs_levels.argtypes = [_u64p, C.c_uint64, C.c_uint64, C.c_uint64, _i64p]
+        L.oracle_ppr_multi.argtypes = [_u64p, C.c_uint64, C.c_uint64, np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS"),
+                                       C.c_uint32, C.c_uint32, C.c_double, C.c_int, _f64p]
+        L.oracle_bfs_levels_multi.argtypes = [_u64p, C.c_uint64, C.c_uint64, _u64p, C.c_uint32, C.c_int, _i64p]
+        L.oracle_cc_min_labels.restype = C.c_uint32
+        L.oracle_cc_min_labels.argtypes = [_u64p, C.c_uint64, C.c_uint64, C.c_int,
+                                           np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")]
+        L.oracle_pr_sample_iteration.argtypes = [_u64p, C.c_uint64, C.c_uint64, C.c_double, C.c_int, _u64p, C.c_uint64, _f64p]
         L.oracle_bfs_check_tree.restype = C.c_uint64
         L.oracle_bfs_check_tree.argtypes = [_u64p, C.c_uint64, C.c_uint64, C.c_uint64, _i64p, _i64p]
         _lib = L
@@ -184,6 +191,42 @@ def bfs_levels(push_pairs: np.ndarray, V: int, root: int = 0) -> np.ndarray:
     lv = np.zeros(V, dtype=np.int64)
     lib().oracle_bfs_levels(np.ascontiguousarray(push_pairs, dtype=np.uint64), push_pairs.shape[0] // 2, V, root, lv)
     return lv
+
+
+def bfs_levels_multi(push_pairs: np.ndarray, V: int, roots, threads: int = 0) -> np.ndarray:
+    """BFS levels from several roots at once (one CSR, the roots on parallel threads): [n, V]."""
+    r = np.ascontiguousarray(np.asarray(roots, dtype=np.uint64))
+    lv = np.zeros((r.shape[0], V), dtype=np.int64)
+    lib().oracle_bfs_levels_multi(np.ascontiguousarray(push_pairs, dtype=np.uint64), push_pairs.shape[0] // 2, V, r,
+                                  r.shape[0], threads, lv)
+    return lv
+
+
+def ppr_multi(V: int, pull_pairs: np.ndarray, seeds, iterations: int, damping: float, threads: int = 0) -> np.ndarray:
+    """Personalized PageRank of several seeds side by side (oracle/ppr.py's definition, in C with
+    OpenMP): ranks [V, K]; a seed >= V leaves its column zero."""
+    s = np.ascontiguousarray(np.asarray(seeds, dtype=np.uint32))
+    assert 0 < s.shape[0] <= 64
+    out = np.zeros((V, s.shape[0]), dtype=np.float64)
+    lib().oracle_ppr_multi(np.ascontiguousarray(pull_pairs, dtype=np.uint64), pull_pairs.shape[0] // 2, V, s, s.shape[0],
+                           iterations, damping, threads, out)
+    return out
+
+
+def cc_min_labels(pull_pairs: np.ndarray, V: int, threads: int = 0) -> np.ndarray:
+    """CC labels from the -pull pairs alone: the smallest vertex ID reaching each vertex (uint32[V])."""
+    lab = np.zeros(V, dtype=np.uint32)
+    lib().oracle_cc_min_labels(np.ascontiguousarray(pull_pairs, dtype=np.uint64), pull_pairs.shape[0] // 2, V, threads, lab)
+    return lab
+
+
+def pr_sample_iteration(pull_pairs: np.ndarray, V: int, samples, damping: float = 0.875, threads: int = 0) -> np.ndarray:
+    """PageRank props after one iteration from the initial props, at the sampled destinations only."""
+    smp = np.ascontiguousarray(np.asarray(samples, dtype=np.uint64))
+    out = np.zeros(smp.shape[0], dtype=np.float64)
+    lib().oracle_pr_sample_iteration(np.ascontiguousarray(pull_pairs, dtype=np.uint64), pull_pairs.shape[0] // 2, V, damping,
+                                     threads, smp, smp.shape[0], out)
+    return out
 
 
 def bfs_check_tree(push_pairs: np.ndarray, V: int, root: int, level: np.ndarray, parent: np.ndarray) -> int:

@@ -109,3 +109,27 @@ def test_oracle_detects_planted_error(case):
     p[len(p) // 2] *= 1.0 + 1e-9
     assert not np.array_equal(p.view(np.uint64), rec["pr_n1"].view(np.uint64))
     assert O.relative_l1(p, rec["pr_n1"]) > 0
+
+
+def test_cc_min_labels_from_pairs_equal_the_reference_labels():
+    """The pairs-based CC check used at sizes beyond a host layout gives the reference's labels
+    bit for bit on every golden graph (directed and symmetric)."""
+    for name in golden_names():
+        rec, g = load_golden(name)
+        lab = O.cc_min_labels(g.pull_order().pairs(), g.num_vertices, threads=4)
+        np.testing.assert_array_equal(lab.astype(np.float64), rec["cc_labels"][:g.num_vertices], err_msg=name)
+
+
+def test_pagerank_sample_iteration_matches_the_oracle():
+    """The sampled one-iteration PageRank check used at R-MAT 27 agrees with the pinned oracle's
+    first iteration at the sampled destinations (1e-14 relative; only the S sum order differs),
+    including destinations without in-edges and dangling sources."""
+    for name in ("rmat10_s12", "isolated_root70", "tiny13"):
+        rec, g = load_golden(name)
+        V = g.num_vertices
+        pull = g.pull_order().pairs()
+        L = O.layout(V, pull, g.push_order().pairs())
+        ref = O.pr_pull(L, 1, 0.875)[:V]
+        smp = np.arange(0, V, 3, dtype=np.uint64)
+        got = O.pr_sample_iteration(pull, V, smp, 0.875, threads=3)
+        assert O.relative_l1(got, ref[smp.astype(np.int64)]) < 1e-14, name

@@ -52,3 +52,30 @@ def test_ppr_properties():
     mean = P.pagerank_mean_of_ppr(V, pull, 3, 0.85)
     cols = np.mean([P.ppr(V, pull, s, 3, 0.85) for s in range(V)], axis=0)
     assert np.abs(mean - cols).max() < 1e-14
+
+
+def test_multi_seed_ppr_matches_the_serial_oracle():
+    """The C multi-seed PPR (the bench's check of all 32 batch graphs) equals oracle/ppr.py seed
+    by seed within 1e-13 relative L1 (only the order of the S sum differs); a seed >= V leaves
+    its column zero."""
+    from grazelle import graphgen as gg
+    for g in (gg.rmat(11, seed=5), gg.erdos_renyi(1500, 6, seed=2)):
+        V, pull = g.num_vertices, g.pull_order().pairs()
+        seeds = [0, 7, V - 1, 0xffffffff, 123]
+        R = O.ppr_multi(V, pull, seeds, 20, 0.85, threads=4)
+        for k, s in enumerate(seeds):
+            if s >= V:
+                assert not R[:, k].any()
+                continue
+            ref = P.ppr(V, pull, s, 20, 0.85)
+            assert O.relative_l1(R[:, k], ref) < 1e-13
+
+
+def test_multi_root_bfs_levels_match_single_root():
+    from grazelle import graphgen as gg
+    g = gg.rmat(12, seed=9)
+    V, push = g.num_vertices, g.push_order().pairs()
+    roots = [0, 3, 77, V - 1]
+    L = O.bfs_levels_multi(push, V, roots, threads=3)
+    for k, r in enumerate(roots):
+        np.testing.assert_array_equal(L[k], O.bfs_levels(push, V, r))

@@ -751,7 +751,19 @@ def batch_graphs(seed: int):
     return out
 
 
-def batch_study(a, torch, stream, dev):
+def assign_graphs(edges, world: int):
+    """Splits the batch's graphs over `world` ranks: longest first, each to the rank with the
+    fewest edges so far (ties to the lower rank).  Returns the sorted graph indices per rank."""
+    load = [0] * world
+    out = [[] for _ in range(world)]
+    for i in sorted(range(len(edges)), key=lambda j: (-edges[j], j)):
+        r = min(range(world), key=lambda k: (load[k], k))
+        out[r].append(i)
+        load[r] += edges[i]
+    return [sorted(x) for x in out]
+
+
+def batch_study(a, torch, stream, dev, graph_ids=None):
     """256 personalized-PageRank instances (8 seeds per graph, 20 iterations, d = 0.85, FP64
     ranks) and 256 BFS instances (8 roots per graph) over the 32 graphs, each run one CUDA graph
     launch of the batch; every instance of every graph checked against the CPU oracles."""
@@ -759,9 +771,12 @@ def batch_study(a, torch, stream, dev):
     from oracle import oracle as O
     t0 = time.time()
     gs = batch_graphs(a.seed)
+    seeds = [pick_roots(g, 8, seed=a.seed + 7 * i) for i, (_, g) in enumerate(gs)]
+    if graph_ids is not None:
+        gs = [gs[i] for i in graph_ids]
+        seeds = [seeds[i] for i in graph_ids]
     E_tot = sum(g.num_edges for _, g in gs)
     log("batch graphs: %d, E=%d (%.1fs)" % (len(gs), E_tot, time.time() - t0))
-    seeds = [pick_roots(g, 8, seed=a.seed + 7 * i) for i, (_, g) in enumerate(gs)]
     res = {"workload": "32 graphs (R-MAT 14-22, ER degree 4-64), 256 PPR x 20 iterations + 256 BFS",
            "graphs": len(gs), "edges": E_tot}
     with Batch(dev, stream=stream.cuda_stream) as B:
@@ -801,6 +816,20 @@ def batch_study(a, torch, stream, dev):
                 reached += int(deg[lv[:, i] >= 0].sum())
         res["msbfs"] = {"instances": n_inst, "ms": round(bfs_ms, 3), "iterations": st.iterations,
                         "gteps": round(reached / (bfs_ms * 1e-3) / 1e9, 2)}
+        # both in one CUDA graph launch, the two loops side by side (results equal the separate
+        # runs': tests/test_gpu_batch.py)
+        B.run(seeds, seeds, 20, 0.85, results=False)
+        tots, sps, sbs = [], [], []
+        for _ in range(max(1, a.steps)):
+            _, _, sp, sb, tot = B.run(seeds, seeds, 20, 0.85, results=False)
+            tots.append(tot)
+            sps.append(sp.ms)
+            sbs.append(sb.ms)
+        one = float(np.median(tots))
+        res["one_launch"] = {"ms": round(one, 3), "ppr_branch_ms": round(float(np.median(sps)), 3),
+                             "bfs_branch_ms": round(float(np.median(sbs)), 3), "separate_ms": round(ppr_ms + bfs_ms, 3),
+                             "gteps_ppr_plus_bfs": round((upd + reached) / (one * 1e-3) / 1e9, 2), "launches_per_run": 1}
+        res["units"] = {"ppr_updates": upd, "bfs_reached_edges": reached}
         # every instance of every graph against the oracles (C, OpenMP): PPR within 1e-12
         # relative L1 of oracle/ppr.py's definition, BFS levels exactly
         t2 = time.time()
@@ -819,21 +848,35 @@ def batch_study(a, torch, stream, dev):
 
 
 def run_batch(a):
-    """The batched workload on its own: 256 PPR and 256 BFS instances over 32 graphs, one CUDA
-    graph launch per run.  Value: PPR edge-instance updates per second (GTEPS).  Under torchrun
-    every rank runs its own replica of the batch; rank 0 reports its own numbers."""
+    """The batched workload on its own: 256 PPR and 256 BFS instances over 32 graphs.  Value:
+    PPR edge-instance updates plus BFS reached edges per second of the one-launch run (GTEPS).
+    Under torchrun the 32 graphs (and their instances) are split over the ranks
+    (assign_graphs); units are summed and the slowest rank's time is taken."""
     import torch
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
     stream = torch.cuda.Stream()
-    res = batch_study(a, torch, stream, local)
+    ids = None
+    if world > 1:
+        edges = [g.num_edges for _, g in batch_graphs(a.seed)]
+        ids = assign_graphs(edges, world)[rank]
+    res = batch_study(a, torch, stream, local, graph_ids=ids)
+    units = res["units"]["ppr_updates"] + res["units"]["bfs_reached_edges"]
+    u_all, ms = combine_ranks(units, res["one_launch"]["ms"], dist)
+    if dist:
+        dist.barrier()
     if rank != 0:
         return
-    line = {"metric": "GTEPS (batched personalized PageRank, edge-instance updates / time)", "value": res["ppr"]["gteps"],
-            "unit": "GTEPS", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup, "ms_per_step": res["ppr"]["ms"],
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u128 fixed point + f64",
-            "data": "synthetic (seeded R-MAT and Erdos-Renyi)", "config": {"workload": res["workload"]}, "batch": res}
+    line = {"metric": "GTEPS (batched personalized PageRank and multi-source BFS, edge-instance updates / time)",
+            "value": round(u_all / (ms * 1e-3) / 1e9, 2), "unit": "GTEPS", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "strong" if world > 1 else "weak", "vs_baseline": None,
+            "dtype": "u128 fixed point + f64", "data": "synthetic (seeded R-MAT and Erdos-Renyi)",
+            "config": {"workload": res["workload"], "graphs_per_rank": "split over ranks" if world > 1 else "all"}, "batch": res}
     print(json.dumps(line), flush=True)
 
 

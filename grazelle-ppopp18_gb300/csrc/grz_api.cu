@@ -8,6 +8,7 @@
 #include <sys/stat.h>
 #include <unistd.h>
 
+#include <chrono>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -18,6 +19,8 @@
 // grz_pr.cu
 int grz_pr_init_state(grz_graph* g, double damping);
 int grz_pr_fused_iteration(grz_graph* g, int write_double_props);
+int grz_pr_use_persistent(const grz_graph* g);
+int grz_pr_persistent_iterations(grz_graph* g, uint32_t iters);
 int grz_pr_props_to_double(grz_graph* g);
 
 int grz_set_error(grz_graph* g, int code, const char* fmt, ...)
@@ -221,6 +224,16 @@ void grz_prof_end(grz_graph* g)
     grz_prof* p = g->prof;
     if (!p || !p->on || p->n >= GRZ_PROF_MAX) return;
     cudaEventRecord(p->ev[p->n][1], g->stream);
+    p->direct_ms[p->n] = -1.0f;
+    p->n++;
+}
+
+void grz_prof_direct(grz_graph* g, int kind, float ms)
+{
+    grz_prof* p = g->prof;
+    if (!p || !p->on || p->n >= GRZ_PROF_MAX) return;
+    p->kind[p->n] = kind;
+    p->direct_ms[p->n] = ms;
     p->n++;
 }
 
@@ -246,7 +259,8 @@ extern "C" int grz_profile_read(grz_graph* g, int* kinds, float* ms, int capacit
     for (int i = 0; i < n; ++i) {
         kinds[i] = p->kind[i];
         ms[i] = 0.0f;
-        cudaEventElapsedTime(&ms[i], p->ev[i][0], p->ev[i][1]);
+        if (p->direct_ms[i] >= 0.0f) ms[i] = p->direct_ms[i];
+        else cudaEventElapsedTime(&ms[i], p->ev[i][0], p->ev[i][1]);
     }
     p->n = 0;
     return n;
@@ -273,6 +287,8 @@ extern "C" void grz_graph_destroy(grz_graph* g)
     free_graph_data(g);
     cudaStreamSynchronize(g->stream);
     if (g->stats_dev) cudaFree(g->stats_dev);
+    if (g->pr_bar) cudaFree(g->pr_bar);
+    if (g->pr_bar_host) cudaFreeHost(g->pr_bar_host);
     if (g->copy_stream) {
         cudaStreamDestroy(g->copy_stream);
         cudaEventDestroy(g->copy_ev[0]);
@@ -653,6 +669,8 @@ extern "C" int grz_pr_iterate(grz_graph* g, uint32_t iterations)
 {
     if (!g) return GRZ_ERR_ARG;
     if (!grz_pr_live(g)) return grz_set_error(g, GRZ_ERR_STATE, "grz_pr_init not called since the graph was loaded");
+    GRZ_CK(g, cudaSetDevice(g->device));
+    if (grz_pr_use_persistent(g)) return grz_pr_persistent_iterations(g, iterations);
     for (uint32_t i = 0; i < iterations; ++i) {
         int rc = grz_pr_fused_iteration(g, 0);
         if (rc) return rc;
@@ -669,7 +687,9 @@ extern "C" int grz_pr_time_iterations(grz_graph* g, uint32_t iterations, float* 
     GRZ_CK(g, cudaEventCreate(&e1));
     int rc = GRZ_OK;
     cudaEventRecord(e0, g->stream);
-    for (uint32_t i = 0; i < iterations && rc == GRZ_OK; ++i) rc = grz_pr_fused_iteration(g, 0);
+    if (grz_pr_use_persistent(g)) rc = grz_pr_persistent_iterations(g, iterations);
+    else
+        for (uint32_t i = 0; i < iterations && rc == GRZ_OK; ++i) rc = grz_pr_fused_iteration(g, 0);
     cudaEventRecord(e1, g->stream);
     if (rc == GRZ_OK) rc = grz_cuda_check(g, cudaEventSynchronize(e1), "event sync");
     if (rc == GRZ_OK) cudaEventElapsedTime(ms_out, e0, e1);
@@ -721,15 +741,28 @@ static int frontier_run(grz_graph* g, int app, uint32_t root, int flags, grz_run
     if (graph) {
         rc = grz_frontier_run_graph(g, nullptr);
     } else {
+        // the same bounds as the graph run's decision kernel, checked between iterations
+        const uint64_t max_it = g->tune.run_max_iterations ? g->tune.run_max_iterations : g->V + 2;
+        const double limit_s = g->tune.run_limit_us ? g->tune.run_limit_us * 1e-6 : 300.0;
+        const auto t0 = std::chrono::steady_clock::now();
         for (;;) {
             int engine = -1;
             uint64_t vote = 0;
             rc = grz_frontier_step(g, -1, &engine, &vote);
             if (rc <= 0) break;
+            if (g->fr.iter >= max_it) {
+                rc = grz_set_error(g, GRZ_ERR_TIMEOUT, "no convergence within %llu iterations", (unsigned long long)max_it);
+                break;
+            }
+            if (std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() > limit_s) {
+                rc = grz_set_error(g, GRZ_ERR_TIMEOUT, "run stopped by its time bound (%.0f ms)", limit_s * 1e3);
+                break;
+            }
         }
     }
     cudaEventRecord(e1, g->stream);
     if (rc == 0) rc = grz_cuda_check(g, cudaEventSynchronize(e1), "run");
+    if (rc == 0 && g->tune.pull_staging) rc = grz_frontier_check_waits(g);
     if (rc == 0 && stats) {
         memset(stats, 0, sizeof(*stats));
         stats->iterations = g->fr.iter;
@@ -832,6 +865,30 @@ extern "C" int grz_tune_set(grz_graph* g, int param, int64_t value)
         if (value > GRZ_INGEST_MAX_CHUNKS) return grz_set_error(g, GRZ_ERR_RANGE, "at most %d ingest chunks", GRZ_INGEST_MAX_CHUNKS);
         g->tune.ingest_chunks = (uint32_t)value;
         return GRZ_OK;
+    case GRZ_TUNE_PR_PERSISTENT:
+        if (value > 3) return grz_set_error(g, GRZ_ERR_ARG, "PageRank iteration form must be 0 (default), 1 (two kernels), 2 or 3 (persistent, 6 or 8 blocks per SM)");
+        g->tune.pr_persistent = (uint32_t)value;
+        return GRZ_OK;
+    case GRZ_TUNE_PR_WAIT_LIMIT_US:
+        if (value > 60000000) return grz_set_error(g, GRZ_ERR_RANGE, "barrier wait limit above 60 s");
+        g->tune.pr_wait_limit_us = (uint32_t)value;
+        return GRZ_OK;
+    case GRZ_TUNE_PR_WITHHOLD:
+        if (value > (1 << 20)) return GRZ_ERR_RANGE;
+        g->tune.pr_withhold = (uint32_t)value;
+        return GRZ_OK;
+    case GRZ_TUNE_RUN_MAX_ITERATIONS:
+        if (value > 0xfffffff0ll) return GRZ_ERR_RANGE;
+        g->tune.run_max_iterations = (uint32_t)value;
+        return GRZ_OK;
+    case GRZ_TUNE_PULL_STAGING:
+        if (value > 1) return grz_set_error(g, GRZ_ERR_ARG, "pull staging must be 0 (loads) or 1 (bulk copies)");
+        g->tune.pull_staging = (uint32_t)value;
+        return GRZ_OK;
+    case GRZ_TUNE_RUN_LIMIT_US:
+        if (value > 3600000000ll) return grz_set_error(g, GRZ_ERR_RANGE, "run time bound above one hour");
+        g->tune.run_limit_us = (uint32_t)value;
+        return GRZ_OK;
     default:
         return grz_set_error(g, GRZ_ERR_ARG, "unknown tuning parameter %d", param);
     }
@@ -849,6 +906,12 @@ extern "C" int grz_tune_get(const grz_graph* g, int param, int64_t* value)
     case GRZ_TUNE_BFS_PULL_SCAN: *value = g->tune.bfs_pull_scan; return GRZ_OK;
     case GRZ_TUNE_PR_PROPS: *value = g->tune.pr_props; return GRZ_OK;
     case GRZ_TUNE_INGEST_CHUNKS: *value = g->tune.ingest_chunks; return GRZ_OK;
+    case GRZ_TUNE_PR_PERSISTENT: *value = g->tune.pr_persistent; return GRZ_OK;
+    case GRZ_TUNE_PR_WAIT_LIMIT_US: *value = g->tune.pr_wait_limit_us; return GRZ_OK;
+    case GRZ_TUNE_PR_WITHHOLD: *value = g->tune.pr_withhold; return GRZ_OK;
+    case GRZ_TUNE_RUN_MAX_ITERATIONS: *value = g->tune.run_max_iterations; return GRZ_OK;
+    case GRZ_TUNE_RUN_LIMIT_US: *value = g->tune.run_limit_us; return GRZ_OK;
+    case GRZ_TUNE_PULL_STAGING: *value = g->tune.pull_staging; return GRZ_OK;
     case GRZ_TUNE_HUBS_LOADED: *value = g->pull.nhub; return GRZ_OK;
     default: return GRZ_ERR_ARG;
     }

@@ -296,9 +296,10 @@ __global__ void __launch_bounds__(GT, 3) k_ppr_apply(u128* __restrict__ rowacc, 
 // multi-source BFS
 
 __global__ void k_msbfs_init(const uint32_t* __restrict__ roots, uint32_t n, uint8_t* __restrict__ visited,
-                             uint8_t* __restrict__ frontier, int32_t* __restrict__ level)
+                             uint8_t* __restrict__ frontier, int32_t* __restrict__ level, uint32_t* __restrict__ iter)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0 && iter) *iter = 1;  // the first iteration
     if (t >= n) return;
     const uint32_t r = roots[t];
     if (r == NONE) return;
@@ -434,6 +435,13 @@ struct grz_batch {
     unsigned long long* ctl;             // changed, iterations, bound hit
     uint32_t* iter;
     cudaGraphExec_t bfs_exec;
+    // PPR and BFS together: one graph whose two branches run the two loops side by side
+    uint32_t* d_roots;                   // [G][K] BFS roots of the combined run
+    cudaGraphExec_t run_exec;
+    uint32_t run_iters;
+    double run_damping;
+    int run_dmode;
+    cudaEvent_t run_ev[4];               // PPR start / end, BFS start / end (recorded inside the graph)
     int ppr_blocks, bfs_blocks;          // resident blocks per SM of the persistent kernels
     void* mail;                          // pinned host read-back
     char err[256];
@@ -478,10 +486,10 @@ extern "C" int grz_batch_create(grz_batch** out, int device, void* stream)
 
 static void free_state(grz_batch* b)
 {
-    void* p[] = { b->d_voff, b->d_seeds, b->prop[0], b->prop[1], b->propd[0], b->propd[1], b->rank, b->rowacc, b->cut, b->S[0], b->S[1],
+    void* p[] = { b->d_voff, b->d_seeds, b->d_roots, b->prop[0], b->prop[1], b->propd[0], b->propd[1], b->rank, b->rowacc, b->cut, b->S[0], b->S[1],
                   b->visited, b->frontier, b->next_words, b->level, b->ctl, b->iter };
     for (void* x : p) cudaFree(x);
-    b->d_voff = b->d_seeds = nullptr;
+    b->d_voff = b->d_seeds = b->d_roots = nullptr;
     b->prop[0] = b->prop[1] = nullptr;
     b->propd[0] = b->propd[1] = nullptr;
     b->rank = nullptr;
@@ -494,7 +502,8 @@ static void free_state(grz_batch* b)
     b->iter = nullptr;
     if (b->ppr_exec) cudaGraphExecDestroy(b->ppr_exec);
     if (b->bfs_exec) cudaGraphExecDestroy(b->bfs_exec);
-    b->ppr_exec = b->bfs_exec = nullptr;
+    if (b->run_exec) cudaGraphExecDestroy(b->run_exec);
+    b->ppr_exec = b->bfs_exec = b->run_exec = nullptr;
 }
 
 extern "C" void grz_batch_destroy(grz_batch* b)
@@ -503,6 +512,8 @@ extern "C" void grz_batch_destroy(grz_batch* b)
     cudaSetDevice(b->device);
     free_state(b);
     if (b->mail) cudaFreeHost(b->mail);
+    if (b->run_ev[0])
+        for (cudaEvent_t e : b->run_ev) cudaEventDestroy(e);
     grz_graph_destroy(b->u);
     delete b;
 }
@@ -553,6 +564,7 @@ extern "C" int grz_batch_build(grz_batch* b)
     BCK(b, cudaMalloc((void**)&b->d_voff, sizeof(uint32_t) * (G + 1)));
     BCK(b, cudaMemcpy(b->d_voff, b->voff.data(), sizeof(uint32_t) * (G + 1), cudaMemcpyHostToDevice));
     BCK(b, cudaMalloc((void**)&b->d_seeds, sizeof(uint32_t) * G * K));
+    BCK(b, cudaMalloc((void**)&b->d_roots, sizeof(uint32_t) * G * K));
     if (!b->mail) BCK(b, cudaMallocHost(&b->mail, 64));
     return GRZ_OK;
 }
@@ -567,8 +579,9 @@ extern "C" int grz_batch_info(const grz_batch* b, uint64_t* graphs, uint64_t* ve
     return GRZ_OK;
 }
 
-static int upload_seeds(grz_batch* b, const uint32_t* local, uint32_t k)
+static int upload_seeds(grz_batch* b, const uint32_t* local, uint32_t k, uint32_t* dst = nullptr)
 {
+    if (!dst) dst = b->d_seeds;
     const uint32_t G = (uint32_t)b->Vg.size();
     std::vector<uint32_t> s((size_t)G * K, NONE);
     for (uint32_t g = 0; g < G; ++g)
@@ -578,21 +591,18 @@ static int upload_seeds(grz_batch* b, const uint32_t* local, uint32_t k)
             if (x >= b->Vg[g]) return bset(b, GRZ_ERR_ARG, "seed or root outside its graph");
             s[(size_t)g * K + i] = b->voff[g] + x;
         }
-    BCK(b, cudaMemcpyAsync(b->d_seeds, s.data(), sizeof(uint32_t) * s.size(), cudaMemcpyHostToDevice, b->stream));
+    BCK(b, cudaMemcpyAsync(dst, s.data(), sizeof(uint32_t) * s.size(), cudaMemcpyHostToDevice, b->stream));
     BCK(b, cudaStreamSynchronize(b->stream));
     return GRZ_OK;
 }
 
-// the fixed-length PPR iteration loop as one CUDA graph (gather + apply per iteration)
-static int build_ppr_graph(grz_batch* b, uint32_t iterations, double damping, int dmode)
+// Enqueues the fixed-length PPR loop (gather + apply per iteration) on cs, which is capturing.
+// Returns the prop buffer the last iteration wrote.
+static int enqueue_ppr_chain(grz_batch* b, cudaStream_t cs, uint32_t iterations, double damping, int dmode, const uint32_t* seeds,
+                             int* final_cur)
 {
-    if (b->ppr_exec) { cudaGraphExecDestroy(b->ppr_exec); b->ppr_exec = nullptr; }
     grz_graph* u = b->u;
     const uint32_t V = (uint32_t)u->V, G = (uint32_t)b->Vg.size();
-    cudaStream_t cs = nullptr;
-    BCK(b, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-    cudaGraph_t graph = nullptr;
-    int rc = bck(b, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "begin capture");
     // the gather's unit is a warp tile of TV vectors; blocks beyond residency would only queue
     int gres = 0;
     const cudaError_t oe = dmode ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gres, k_ppr_gather<double>, GT, 0)
@@ -606,17 +616,32 @@ static int build_ppr_graph(grz_batch* b, uint32_t iterations, double damping, in
     // 3 blocks per SM fit the apply's registers (8 tiles of accumulators per thread in flight)
     const unsigned agrid = persistent_grid(b, (V + TV - 1) / TV, std::min(b->ppr_blocks, 3));
     int cur = 0;
-    for (uint32_t it = 0; it < iterations && !rc; ++it) {
+    for (uint32_t it = 0; it < iterations; ++it) {
         if (dmode)
             k_ppr_gather<<<ggrid, GT, 0, cs>>>(u->pull.nbr, u->pull.shared, u->pull.nvec, V, b->propd[cur], b->rowacc, b->S[cur ^ 1], G * K);
         else
             k_ppr_gather<<<ggrid, GT, 0, cs>>>(u->pull.nbr, u->pull.shared, u->pull.nvec, V, b->prop[cur], b->rowacc, b->S[cur ^ 1], G * K);
-        k_ppr_apply<<<agrid, GT, 0, cs>>>(b->rowacc, b->cut, u->inv_deg, u->degree, V, b->d_voff, G, b->d_seeds, damping, b->S[cur],
+        k_ppr_apply<<<agrid, GT, 0, cs>>>(b->rowacc, b->cut, u->inv_deg, u->degree, V, b->d_voff, G, seeds, damping, b->S[cur],
                                          b->S[cur ^ 1], b->prop[cur ^ 1], dmode ? b->propd[cur ^ 1] : nullptr,
                                          it + 1 == iterations ? b->rank : nullptr);
         cur ^= 1;
-        rc = bck(b, cudaGetLastError(), "ppr launch");
+        const int rc = bck(b, cudaGetLastError(), "ppr launch");
+        if (rc) return rc;
     }
+    *final_cur = cur;
+    return GRZ_OK;
+}
+
+// the fixed-length PPR iteration loop as one CUDA graph (gather + apply per iteration)
+static int build_ppr_graph(grz_batch* b, uint32_t iterations, double damping, int dmode)
+{
+    if (b->ppr_exec) { cudaGraphExecDestroy(b->ppr_exec); b->ppr_exec = nullptr; }
+    cudaStream_t cs = nullptr;
+    BCK(b, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t graph = nullptr;
+    int cur = 0;
+    int rc = bck(b, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "begin capture");
+    if (!rc) rc = enqueue_ppr_chain(b, cs, iterations, damping, dmode, b->d_seeds, &cur);
     const cudaError_t e = cudaStreamEndCapture(cs, &graph);
     if (!rc) rc = bck(b, e, "end capture");
     if (!rc) rc = bck(b, cudaGraphInstantiate(&b->ppr_exec, graph, 0), "instantiate");
@@ -630,14 +655,9 @@ static int build_ppr_graph(grz_batch* b, uint32_t iterations, double damping, in
     return GRZ_OK;
 }
 
-// k seeds per graph (local vertex IDs, NONE = unused instance), `iterations` PPR iterations;
-// ranks out as [union vertex][k] (graph g's vertex v at row voff[g] + v)
-extern "C" int grz_batch_ppr(grz_batch* b, const uint32_t* seeds, uint32_t k, uint32_t iterations, double damping,
-                             double* ranks_out, grz_run_stats_t* stats)
+// the PPR state (props, ranks, accumulators, straddle bits), allocated on first use
+static int ppr_alloc(grz_batch* b, int dmode)
 {
-    if (!b || !seeds || k == 0 || k > (uint32_t)K || iterations == 0 || !(damping >= 0.0 && damping <= 1.0)) return GRZ_ERR_ARG;
-    if (!b->d_seeds) return bset(b, GRZ_ERR_STATE, "grz_batch_build not called");
-    BCK(b, cudaSetDevice(b->device));
     grz_graph* u = b->u;
     const uint64_t V = u->V;
     const uint32_t G = (uint32_t)b->Vg.size();
@@ -653,6 +673,24 @@ extern "C" int grz_batch_ppr(grz_batch* b, const uint32_t* seeds, uint32_t k, ui
         k_ppr_cutbits<<<(unsigned)((V + 255) / 256), 256, 0, b->stream>>>(u->pull.rowptr, (uint32_t)V, b->cut);
         BCK(b, cudaGetLastError());
     }
+    if (dmode && !b->propd[0]) {
+        BCK(b, cudaMalloc((void**)&b->propd[0], sizeof(double) * V * K));
+        BCK(b, cudaMalloc((void**)&b->propd[1], sizeof(double) * V * K));
+    }
+    return GRZ_OK;
+}
+
+// k seeds per graph (local vertex IDs, NONE = unused instance), `iterations` PPR iterations;
+// ranks out as [union vertex][k] (graph g's vertex v at row voff[g] + v)
+extern "C" int grz_batch_ppr(grz_batch* b, const uint32_t* seeds, uint32_t k, uint32_t iterations, double damping,
+                             double* ranks_out, grz_run_stats_t* stats)
+{
+    if (!b || !seeds || k == 0 || k > (uint32_t)K || iterations == 0 || !(damping >= 0.0 && damping <= 1.0)) return GRZ_ERR_ARG;
+    if (!b->d_seeds) return bset(b, GRZ_ERR_STATE, "grz_batch_build not called");
+    BCK(b, cudaSetDevice(b->device));
+    grz_graph* u = b->u;
+    const uint64_t V = u->V;
+    const uint32_t G = (uint32_t)b->Vg.size();
     // Doubles gathered instead of 16-byte fixed point only when chosen: each row of a source's 8
     // instances is 64 bytes instead of 128, and the gather converts each double exactly to the
     // fixed point the apply would have stored, so the sums and results are the same bit for bit.
@@ -660,11 +698,9 @@ extern "C" int grz_batch_ppr(grz_batch* b, const uint32_t* seeds, uint32_t k, ui
     // the halved rows save: GB300, the 32-graph batch (1.9 GB of fixed-point rows, 15x L2), 256
     // instances x 20 iterations: 101 ms fixed point, 155 ms doubles.
     const int dmode = b->ppr_props == 2;
-    if (dmode && !b->propd[0]) {
-        BCK(b, cudaMalloc((void**)&b->propd[0], sizeof(double) * V * K));
-        BCK(b, cudaMalloc((void**)&b->propd[1], sizeof(double) * V * K));
-    }
-    int rc = upload_seeds(b, seeds, k);
+    int rc = ppr_alloc(b, dmode);
+    if (rc) return rc;
+    rc = upload_seeds(b, seeds, k);
     if (rc) return rc;
     if (!b->ppr_exec || b->ppr_iters != iterations || b->ppr_damping != damping || b->ppr_dmode != dmode) {
         rc = build_ppr_graph(b, iterations, damping, dmode);
@@ -705,23 +741,20 @@ extern "C" int grz_batch_ppr(grz_batch* b, const uint32_t* seeds, uint32_t k, ui
     return rc;
 }
 
-// the BFS loop as one CUDA graph: WHILE (a bit changed) { pull; vertex pass; decide }
-static int build_bfs_graph(grz_batch* b)
+// Adds to `graph`, after `deps`, the BFS loop: WHILE (a bit changed) { pull; vertex pass; decide }.
+static int add_bfs_loop(grz_batch* b, cudaGraph_t graph, const cudaGraphNode_t* deps, size_t ndeps, cudaGraphNode_t* node_out)
 {
-    if (b->bfs_exec) { cudaGraphExecDestroy(b->bfs_exec); b->bfs_exec = nullptr; }
     grz_graph* u = b->u;
     const uint32_t V = (uint32_t)u->V;
-    cudaGraph_t top = nullptr;
-    BCK(b, cudaGraphCreate(&top, 0));
     cudaGraphConditionalHandle loop = 0;
-    int rc = bck(b, cudaGraphConditionalHandleCreate(&loop, top, 1, cudaGraphCondAssignDefault), "handle");
+    int rc = bck(b, cudaGraphConditionalHandleCreate(&loop, graph, 1, cudaGraphCondAssignDefault), "handle");
     cudaGraphNodeParams p = {};
     p.type = cudaGraphNodeTypeConditional;
     p.conditional.handle = loop;
     p.conditional.type = cudaGraphCondTypeWhile;
     p.conditional.size = 1;
     cudaGraphNode_t node = nullptr;
-    if (!rc) rc = bck(b, cudaGraphAddNode(&node, top, nullptr, nullptr, 0, &p), "while node");
+    if (!rc) rc = bck(b, cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &p), "while node");
     cudaStream_t cs = nullptr;
     if (!rc) rc = bck(b, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "stream");
     if (!rc) rc = bck(b, cudaStreamBeginCaptureToGraph(cs, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
@@ -739,10 +772,120 @@ static int build_bfs_graph(grz_batch* b)
         if (!rc) rc = bck(b, e, "end capture");
     }
     if (cs) cudaStreamDestroy(cs);
+    *node_out = node;
+    return rc;
+}
+
+// the BFS loop as one CUDA graph
+static int build_bfs_graph(grz_batch* b)
+{
+    if (b->bfs_exec) { cudaGraphExecDestroy(b->bfs_exec); b->bfs_exec = nullptr; }
+    cudaGraph_t top = nullptr;
+    BCK(b, cudaGraphCreate(&top, 0));
+    cudaGraphNode_t node = nullptr;
+    int rc = add_bfs_loop(b, top, nullptr, 0, &node);
     if (!rc) rc = bck(b, cudaGraphInstantiate(&b->bfs_exec, top, 0), "instantiate");
     cudaGraphDestroy(top);
     if (rc) b->bfs_exec = nullptr;
     return rc;
+}
+
+// the multi-source BFS state, allocated on first use
+static int bfs_alloc(grz_batch* b)
+{
+    const uint64_t V = b->u->V;
+    const uint64_t Vw = (V + 3) / 4 * 4;
+    if (!b->visited) {
+        BCK(b, cudaMalloc((void**)&b->visited, Vw));
+        BCK(b, cudaMalloc((void**)&b->frontier, Vw));
+        BCK(b, cudaMalloc((void**)&b->next_words, Vw));
+        BCK(b, cudaMalloc((void**)&b->level, sizeof(int32_t) * V * K));
+        BCK(b, cudaMalloc((void**)&b->ctl, sizeof(unsigned long long) * 4));
+        BCK(b, cudaMalloc((void**)&b->iter, sizeof(uint32_t)));
+    }
+    return GRZ_OK;
+}
+
+// the last node of the work captured so far on cs (one node), then ends the capture
+static int end_capture_sink(grz_batch* b, cudaStream_t cs, cudaGraphNode_t* sink)
+{
+    cudaStreamCaptureStatus st;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t n = 0;
+    const cudaError_t e = cudaStreamGetCaptureInfo(cs, &st, nullptr, nullptr, &deps, nullptr, &n);
+    const cudaGraphNode_t last = (e == cudaSuccess && n == 1) ? deps[0] : nullptr;
+    cudaGraph_t out = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(cs, &out);
+    if (e != cudaSuccess) return bck(b, e, "capture info");
+    if (e2 != cudaSuccess) return bck(b, e2, "end capture");
+    if (sink) {
+        if (!last) return bset(b, GRZ_ERR_STATE, "captured work does not end in one node");
+        *sink = last;
+    }
+    return GRZ_OK;
+}
+
+// PPR and multi-source BFS as one CUDA graph with two independent branches, each from its initial
+// state to its results: branch 1 the PPR loop (d_seeds), branch 2 the BFS loop (d_roots).  Event
+// records at both ends of each branch time them inside the one launch.
+static int build_run_graph(grz_batch* b, uint32_t iterations, double damping, int dmode)
+{
+    if (b->run_exec) { cudaGraphExecDestroy(b->run_exec); b->run_exec = nullptr; }
+    if (!b->run_ev[0])
+        for (cudaEvent_t& e : b->run_ev) BCK(b, cudaEventCreate(&e));
+    grz_graph* u = b->u;
+    const uint64_t V = u->V;
+    const uint64_t Vw = (V + 3) / 4 * 4;
+    const uint32_t G = (uint32_t)b->Vg.size();
+    cudaGraph_t top = nullptr;
+    BCK(b, cudaGraphCreate(&top, 0));
+    cudaStream_t cs = nullptr;
+    int rc = bck(b, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "stream");
+    int cur = 0;
+    // branch 1: PPR
+    if (!rc) rc = bck(b, cudaStreamBeginCaptureToGraph(cs, top, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal), "capture");
+    if (!rc) {
+        cudaEventRecord(b->run_ev[0], cs);
+        if (dmode) cudaMemsetAsync(b->propd[0], 0, sizeof(double) * V * K, cs);
+        else cudaMemsetAsync(b->prop[0], 0, sizeof(u128) * V * K, cs);
+        k_ppr_init<<<(G * K + 255) / 256, 256, 0, cs>>>(b->d_seeds, G, u->inv_deg, u->degree, b->prop[0], dmode ? b->propd[0] : nullptr,
+                                                        b->S[0]);
+        rc = bck(b, cudaGetLastError(), "ppr init");
+        if (!rc) rc = enqueue_ppr_chain(b, cs, iterations, damping, dmode, b->d_seeds, &cur);
+        cudaEventRecord(b->run_ev[1], cs);
+        const int rc2 = end_capture_sink(b, cs, nullptr);
+        if (!rc) rc = rc2;
+    }
+    // branch 2: BFS (no dependency on branch 1)
+    cudaGraphNode_t init = nullptr, loop = nullptr;
+    if (!rc) rc = bck(b, cudaStreamBeginCaptureToGraph(cs, top, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal), "capture");
+    if (!rc) {
+        cudaEventRecord(b->run_ev[2], cs);
+        cudaMemsetAsync(b->visited, 0, Vw, cs);
+        cudaMemsetAsync(b->frontier, 0, Vw, cs);
+        cudaMemsetAsync(b->next_words, 0, Vw, cs);
+        cudaMemsetAsync(b->level, 0xff, sizeof(int32_t) * V * K, cs);
+        cudaMemsetAsync(b->ctl, 0, sizeof(unsigned long long) * 4, cs);
+        k_msbfs_init<<<(G * K + 255) / 256, 256, 0, cs>>>(b->d_roots, G * K, b->visited, b->frontier, b->level, b->iter);
+        rc = bck(b, cudaGetLastError(), "bfs init");
+        const int rc2 = end_capture_sink(b, cs, &init);
+        if (!rc) rc = rc2;
+    }
+    if (!rc) rc = add_bfs_loop(b, top, &init, 1, &loop);
+    if (!rc) rc = bck(b, cudaStreamBeginCaptureToGraph(cs, top, &loop, nullptr, 1, cudaStreamCaptureModeThreadLocal), "capture");
+    if (!rc) {
+        cudaEventRecord(b->run_ev[3], cs);
+        rc = end_capture_sink(b, cs, nullptr);
+    }
+    if (cs) cudaStreamDestroy(cs);
+    if (!rc) rc = bck(b, cudaGraphInstantiate(&b->run_exec, top, 0), "instantiate");
+    cudaGraphDestroy(top);
+    if (rc) { b->run_exec = nullptr; return rc; }
+    b->run_iters = iterations;
+    b->run_damping = damping;
+    b->run_dmode = dmode;
+    b->ppr_final = cur;
+    return GRZ_OK;
 }
 
 // k roots per graph (local IDs, NONE = unused instance); levels out as [union vertex][k]
@@ -756,15 +899,9 @@ extern "C" int grz_batch_msbfs(grz_batch* b, const uint32_t* roots, uint32_t k, 
     const uint64_t V = u->V;
     const uint32_t G = (uint32_t)b->Vg.size();
     const uint64_t Vw = (V + 3) / 4 * 4;
-    if (!b->visited) {
-        BCK(b, cudaMalloc((void**)&b->visited, Vw));
-        BCK(b, cudaMalloc((void**)&b->frontier, Vw));
-        BCK(b, cudaMalloc((void**)&b->next_words, Vw));
-        BCK(b, cudaMalloc((void**)&b->level, sizeof(int32_t) * V * K));
-        BCK(b, cudaMalloc((void**)&b->ctl, sizeof(unsigned long long) * 4));
-        BCK(b, cudaMalloc((void**)&b->iter, sizeof(uint32_t)));
-    }
-    int rc = upload_seeds(b, roots, k);
+    int rc = bfs_alloc(b);
+    if (rc) return rc;
+    rc = upload_seeds(b, roots, k);
     if (rc) return rc;
     if (!b->bfs_exec) {
         rc = build_bfs_graph(b);
@@ -786,7 +923,7 @@ extern "C" int grz_batch_msbfs(grz_batch* b, const uint32_t* roots, uint32_t k, 
         rc = bck(b, cudaMemcpyAsync(b->iter, b->mail, sizeof(uint32_t), cudaMemcpyHostToDevice, st), "H2D");
     }
     if (!rc) {
-        k_msbfs_init<<<(G * K + 255) / 256, 256, 0, st>>>(b->d_seeds, G * K, b->visited, b->frontier, b->level);
+        k_msbfs_init<<<(G * K + 255) / 256, 256, 0, st>>>(b->d_seeds, G * K, b->visited, b->frontier, b->level, nullptr);
         rc = bck(b, cudaGetLastError(), "bfs init");
     }
     if (!rc) rc = bck(b, cudaGraphLaunch(b->bfs_exec, st), "graph launch");
@@ -802,8 +939,8 @@ extern "C" int grz_batch_msbfs(grz_batch* b, const uint32_t* roots, uint32_t k, 
     if (!rc) rc = bck(b, cudaStreamSynchronize(st), "run");
     unsigned long long c[3];
     memcpy(c, b->mail, sizeof(c));
-    if (!rc && c[2] == 1) rc = bset(b, GRZ_ERR_STATE, "BFS did not converge within V + 1 iterations");
-    if (!rc && c[2] == 2) rc = bset(b, GRZ_ERR_STATE, "BFS stopped by its time bound");
+    if (!rc && c[2] == 1) rc = bset(b, GRZ_ERR_TIMEOUT, "BFS did not converge within V + 1 iterations");
+    if (!rc && c[2] == 2) rc = bset(b, GRZ_ERR_TIMEOUT, "BFS stopped by its time bound");
     if (!rc && stats) {
         memset(stats, 0, sizeof(*stats));
         stats->iterations = (uint32_t)c[1] + 1;  // the last iteration found nothing new
@@ -813,6 +950,78 @@ extern "C" int grz_batch_msbfs(grz_batch* b, const uint32_t* roots, uint32_t k, 
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     u->nlaunch += 1 + 3ull * (c[1] + 1);
+    return rc;
+}
+
+// PPR (seeds, k per graph, `iterations`) and multi-source BFS (roots, kb per graph) in one CUDA
+// graph launch: the two loops run side by side as independent branches of one graph, each from
+// its initial state.  Results and per-branch device times as grz_batch_ppr / grz_batch_msbfs;
+// *total_ms is the launch's device time.
+extern "C" int grz_batch_run(grz_batch* b, const uint32_t* seeds, uint32_t k, uint32_t iterations, double damping,
+                             const uint32_t* roots, uint32_t kb, double* ranks_out, int32_t* levels_out,
+                             grz_run_stats_t* ppr_stats, grz_run_stats_t* bfs_stats, float* total_ms)
+{
+    if (!b || !seeds || !roots || k == 0 || k > (uint32_t)K || kb == 0 || kb > (uint32_t)K || iterations == 0 ||
+        !(damping >= 0.0 && damping <= 1.0))
+        return GRZ_ERR_ARG;
+    if (!b->d_seeds) return bset(b, GRZ_ERR_STATE, "grz_batch_build not called");
+    BCK(b, cudaSetDevice(b->device));
+    grz_graph* u = b->u;
+    const uint64_t V = u->V;
+    const int dmode = b->ppr_props == 2;
+    int rc = ppr_alloc(b, dmode);
+    if (!rc) rc = bfs_alloc(b);
+    if (!rc) rc = upload_seeds(b, seeds, k, b->d_seeds);
+    if (!rc) rc = upload_seeds(b, roots, kb, b->d_roots);
+    if (rc) return rc;
+    if (!b->run_exec || b->run_iters != iterations || b->run_damping != damping || b->run_dmode != dmode) {
+        rc = build_run_graph(b, iterations, damping, dmode);
+        if (rc) return rc;
+    }
+    cudaStream_t st = b->stream;
+    cudaEvent_t e0, e1;
+    BCK(b, cudaEventCreate(&e0));
+    BCK(b, cudaEventCreate(&e1));
+    rc = bck(b, cudaEventRecord(e0, st), "event");
+    if (!rc) rc = bck(b, cudaGraphLaunch(b->run_exec, st), "graph launch");
+    if (!rc) rc = bck(b, cudaEventRecord(e1, st), "event");
+    if (!rc) rc = bck(b, cudaMemcpyAsync(b->mail, b->ctl, sizeof(unsigned long long) * 3, cudaMemcpyDeviceToHost, st), "D2H");
+    if (!rc && ranks_out) {
+        if (k == (uint32_t)K) {
+            rc = bck(b, cudaMemcpyAsync(ranks_out, b->rank, sizeof(double) * V * K, cudaMemcpyDeviceToHost, st), "D2H");
+        } else {
+            rc = bck(b, cudaMemcpy2DAsync(ranks_out, sizeof(double) * k, b->rank, sizeof(double) * K, sizeof(double) * k, V,
+                                          cudaMemcpyDeviceToHost, st), "D2H");
+        }
+    }
+    if (!rc && levels_out) {
+        if (kb == (uint32_t)K)
+            rc = bck(b, cudaMemcpyAsync(levels_out, b->level, sizeof(int32_t) * V * K, cudaMemcpyDeviceToHost, st), "D2H");
+        else
+            rc = bck(b, cudaMemcpy2DAsync(levels_out, sizeof(int32_t) * kb, b->level, sizeof(int32_t) * K, sizeof(int32_t) * kb, V,
+                                          cudaMemcpyDeviceToHost, st), "D2H");
+    }
+    if (!rc) rc = bck(b, cudaStreamSynchronize(st), "run");
+    unsigned long long c[3];
+    memcpy(c, b->mail, sizeof(c));
+    if (!rc && c[2] == 1) rc = bset(b, GRZ_ERR_TIMEOUT, "BFS did not converge within V + 1 iterations");
+    if (!rc && c[2] == 2) rc = bset(b, GRZ_ERR_TIMEOUT, "BFS stopped by its time bound");
+    if (!rc) {
+        if (ppr_stats) {
+            memset(ppr_stats, 0, sizeof(*ppr_stats));
+            ppr_stats->iterations = ppr_stats->pull_iterations = iterations;
+            cudaEventElapsedTime(&ppr_stats->ms, b->run_ev[0], b->run_ev[1]);
+        }
+        if (bfs_stats) {
+            memset(bfs_stats, 0, sizeof(*bfs_stats));
+            bfs_stats->iterations = bfs_stats->pull_iterations = (uint32_t)c[1] + 1;
+            cudaEventElapsedTime(&bfs_stats->ms, b->run_ev[2], b->run_ev[3]);
+        }
+        if (total_ms) cudaEventElapsedTime(total_ms, e0, e1);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    u->nlaunch += 2 + 2ull * iterations + 1 + 3ull * (c[1] + 1);
     return rc;
 }
 
@@ -833,6 +1042,7 @@ extern "C" int grz_batch_tune_set(grz_batch* b, int param, int64_t value)
         cudaSetDevice(b->device);
         if (param == GRZ_BATCH_TUNE_PPR_BLOCKS && b->ppr_exec) { cudaGraphExecDestroy(b->ppr_exec); b->ppr_exec = nullptr; }
         if (param == GRZ_BATCH_TUNE_BFS_BLOCKS && b->bfs_exec) { cudaGraphExecDestroy(b->bfs_exec); b->bfs_exec = nullptr; }
+        if (b->run_exec) { cudaGraphExecDestroy(b->run_exec); b->run_exec = nullptr; }
     }
     return GRZ_OK;
 }

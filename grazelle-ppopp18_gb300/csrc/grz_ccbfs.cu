@@ -32,6 +32,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "grz_internal.cuh"
 
@@ -144,32 +145,89 @@ __device__ __forceinline__ void cc_record_min(uint32_t my_min, uint32_t* red32, 
 // complete iteration): it reads their destination and label, not their vectors.  R-MAT's
 // hubs have the smallest IDs, so after the first iteration most of the giant component holds
 // label 0 and the second pull reads little more than the destinations.
+// double-buffered staging of the edge stream in shared memory (the bulk-copy form)
 template <int BT>
+struct CCStage {
+    uint4 nbr[2][BT];
+    uint32_t dst[2][BT];
+    unsigned long long bar[2];
+};
+struct CCNoStage {};
+
+template <int BT, bool BULK>
 __global__ void __launch_bounds__(BT) k_cc_pull(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv, uint64_t first,
                                                 uint64_t nvec, uint32_t V, uint32_t* __restrict__ label,
                                                 const uint32_t* __restrict__ hub_vid, uint32_t nhub, uint32_t ncache,
                                                 unsigned long long* __restrict__ has_next, VoteCfg vc,
                                                 unsigned long long* __restrict__ vote, unsigned long long* __restrict__ chg,
-                                                uint32_t epoch, const uint32_t* __restrict__ epoch_dev, int use_prev)
+                                                uint32_t epoch, const uint32_t* __restrict__ epoch_dev, int use_prev,
+                                                unsigned* __restrict__ err)
 {
     extern __shared__ uint32_t s_hub[];
     __shared__ unsigned long long red[BT / 32];
     __shared__ uint32_t red32[BT / 32];
+    __shared__ __align__(16) typename std::conditional<BULK, CCStage<BT>, CCNoStage>::type stg;
     for (uint32_t k = threadIdx.x; k < ncache; k += BT) s_hub[k] = label[__ldg(hub_vid + k)];
     const uint32_t ep = epoch_dev ? *epoch_dev : epoch;
     uint32_t mprev = 0;
     const bool skip = use_prev && cc_prev_min(chg, ep, &mprev);
-    __syncthreads();
     const int lane = threadIdx.x & 31;
     unsigned long long my_vote = 0;
     uint32_t my_min = INF;
     const uint64_t ntiles = (nvec + BT - 1) / BT;
-    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const uint64_t nfull = nvec / BT;  // tiles the bulk copies serve (whole tiles only)
+    // The bulk form copies each whole tile's vectors and destinations into shared memory on the
+    // copy engine, two tiles ahead, so the SM's load path serves only the label gathers.  Not in
+    // skip mode (it reads most vectors' destinations only) nor for a vector sub-range.
+    const bool bulk = BULK && !skip && first == 0;
+    unsigned par = 0u;  // bit j: the parity stage j waits for next
+    if constexpr (BULK) {
+        if (bulk && threadIdx.x == 0) {
+            mbar_init(&stg.bar[0], 1);
+            mbar_init(&stg.bar[1], 1);
+            mbar_fence_init();
+            for (int j = 0; j < 2; ++j) {
+                const uint64_t t = blockIdx.x + (uint64_t)j * gridDim.x;
+                if (t < nfull) {
+                    mbar_arrive_expect_tx(&stg.bar[j], BT * (sizeof(uint4) + sizeof(uint32_t)));
+                    bulk_copy_g2s(stg.nbr[j], nbr + t * BT, BT * sizeof(uint4), &stg.bar[j]);
+                    bulk_copy_g2s(stg.dst[j], dstv + t * BT, BT * sizeof(uint32_t), &stg.bar[j]);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    uint64_t j = 0;
+    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++j) {
         const uint64_t i = t * BT + threadIdx.x;
         const uint64_t v = first + i;
         const bool live = i < nvec;
         uint32_t key = INF, m = INF, labd = INF;
         bool need = live;
+        bool staged = false;
+        uint4 sv = make_uint4(INF, INF, INF, INF);
+        if constexpr (BULK) {
+            if (bulk && t < nfull) {
+                const int st = (int)(j & 1);
+                const bool ok = mbar_wait_bounded(&stg.bar[st], (par >> st) & 1u);
+                if (__syncthreads_or(!ok)) {
+                    if (threadIdx.x == 0) atomicExch(err, 1u);
+                    return;
+                }
+                par ^= 1u << st;
+                sv = stg.nbr[st][threadIdx.x];
+                key = stg.dst[st][threadIdx.x];
+                staged = true;
+                __syncthreads();  // every thread has read the stage
+                const uint64_t tn = t + 2ull * gridDim.x;
+                if (threadIdx.x == 0 && tn < nfull) {
+                    fence_proxy_async_smem();
+                    mbar_arrive_expect_tx(&stg.bar[st], BT * (sizeof(uint4) + sizeof(uint32_t)));
+                    bulk_copy_g2s(stg.nbr[st], nbr + tn * BT, BT * sizeof(uint4), &stg.bar[st]);
+                    bulk_copy_g2s(stg.dst[st], dstv + tn * BT, BT * sizeof(uint32_t), &stg.bar[st]);
+                }
+            }
+        }
         if (skip) {
             // skip mode: the destination's label decides whether the vector is read at all
             if (live) {
@@ -180,9 +238,9 @@ __global__ void __launch_bounds__(BT) k_cc_pull(const uint4* __restrict__ nbr, c
             if (!__any_sync(0xffffffffu, need)) continue;  // warp-uniform
         }
         if (need) {
-            const uint4 s = __ldcs(nbr + v);
-            if (!skip) key = __ldcs(dstv + v);
-            const uint32_t x[4] = { s.x, s.y, s.z, s.w };
+            const uint4 s4 = staged ? sv : __ldcs(nbr + v);
+            if (!skip && !staged) key = __ldcs(dstv + v);
+            const uint32_t x[4] = { s4.x, s4.y, s4.z, s4.w };
             uint32_t val[4];
 #pragma unroll
             for (int l = 0; l < 4; ++l) {
@@ -862,6 +920,7 @@ static int ensure_frontier_state(grz_graph* g)
     GRZ_CK(g, cudaMalloc((void**)&f.counters, sizeof(uint32_t) * 8));
     GRZ_CK(g, cudaMalloc((void**)&f.vote, sizeof(unsigned long long) * GRZ_VOTE_SLOTS * GRZ_VOTE_STRIDE));
     GRZ_CK(g, cudaMalloc((void**)&f.chg, sizeof(unsigned long long) * 2));
+    GRZ_CK(g, cudaMalloc((void**)&f.dev_err, sizeof(unsigned)));
     return frontier_list_state(g);
 }
 
@@ -909,7 +968,9 @@ int grz_frontier_init(grz_graph* g, int app, int flags, uint32_t root)
     f.npull = f.npush = 0;
     f.last_engine = 1;
     f.next_pull = 1;
+    f.cc_partial = 0;
     cudaStream_t st = g->stream;
+    GRZ_CK(g, cudaMemsetAsync(f.dev_err, 0, sizeof(unsigned), st));
     if (app == GRZ_APP_CONNECTED_COMPONENTS) {
         k_cc_init<<<blocks_for(V + 1), T, 0, st>>>(f.label, V); GRZ_COUNT_LAUNCH(g);
         k_bitmap_init<<<blocks_for(W), T, 0, st>>>(f.has, W, V, 1); GRZ_COUNT_LAUNCH(g);      // HasInfo = all (execution_cc.c:66-73)
@@ -964,53 +1025,61 @@ static unsigned visit_grid(const grz_graph* g)
     return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(blocks_for((g->V + 3) / 4), (uint64_t)g->num_sms * 8));
 }
 
-// Shared-memory opt-in and resident blocks per SM of the CC pull kernel, per device and block size.
-template <int BT>
+// Shared-memory opt-in and resident blocks per SM of the CC pull kernel, per device, block size
+// and staging form.
+template <int BT, bool BULK>
 static int cc_pull_config(grz_graph* g, size_t smem, int* resident)
 {
     static int configured[64] = {};
-    const int bit = BT == 256 ? 1 : (BT == 512 ? 2 : 4);
+    const int bit = (BT == 256 ? 1 : (BT == 512 ? 2 : 4)) << (BULK ? 3 : 0);
     if (g->device < 0 || g->device >= 64) return GRZ_ERR_ARG;
     if (!(configured[g->device] & bit)) {
         cudaFuncAttributes fa;
         int optin = 0;
-        GRZ_CK(g, cudaFuncGetAttributes(&fa, k_cc_pull<BT>));
+        GRZ_CK(g, cudaFuncGetAttributes(&fa, k_cc_pull<BT, BULK>));
         GRZ_CK(g, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, g->device));
-        GRZ_CK(g, cudaFuncSetAttribute(k_cc_pull<BT>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+        GRZ_CK(g, cudaFuncSetAttribute(k_cc_pull<BT, BULK>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
         configured[g->device] |= bit;
     }
-    GRZ_CK(g, cudaOccupancyMaxActiveBlocksPerMultiprocessor(resident, k_cc_pull<BT>, BT, smem));
+    GRZ_CK(g, cudaOccupancyMaxActiveBlocksPerMultiprocessor(resident, k_cc_pull<BT, BULK>, BT, smem));
     if (*resident < 1) return grz_set_error(g, GRZ_ERR_ARG, "CC pull: %d threads with %zu bytes of shared memory do not fit", BT, smem);
     return GRZ_OK;
 }
 
 template <int BT>
+static int cc_pull_config_any(grz_graph* g, size_t smem, int* resident)
+{
+    return g->tune.pull_staging ? cc_pull_config<BT, true>(g, smem, resident) : cc_pull_config<BT, false>(g, smem, resident);
+}
+
+template <int BT, bool BULK>
 static int launch_cc_pull_bt(grz_graph* g, uint64_t first, uint64_t count, const VoteCfg& vc)
 {
     grz_frontier_state& f = g->fr;
     const uint32_t ncache = std::min<uint32_t>(g->tune.cc_cache, g->pull.nhub);
     const size_t smem = sizeof(uint32_t) * ncache;
     int resident = 0;
-    int rc = cc_pull_config<BT>(g, smem, &resident);
+    int rc = cc_pull_config<BT, BULK>(g, smem, &resident);
     if (rc) return rc;
     const uint64_t tiles = (count + BT - 1) / BT;
     uint64_t grid = g->tune.cc_grid ? g->tune.cc_grid : (uint64_t)g->num_sms * resident;
     grid = std::max<uint64_t>(1, std::min<uint64_t>(grid, tiles));
     // the skip needs every earlier iteration to have been complete (the whole list, or the whole
-    // frontier): true for the driver loops, not for calls of the phases.h entry points
-    const int use_prev = !f.phase_api && first == 0 && count == g->pull.nvec;
-    k_cc_pull<BT><<<(unsigned)grid, BT, smem, g->stream>>>(g->pull.nbr, g->pull.shared, first, count, (uint32_t)g->V, f.label,
-                                                          g->pull.hub_vid, g->pull.nhub, ncache, f.has_next, vc, f.vote, f.chg,
-                                                          f.iter, f.level_dev, use_prev); GRZ_COUNT_LAUNCH(g);
+    // frontier): true for the driver loops, not once a phases.h call covered part of the list
+    const int use_prev = !f.cc_partial && first == 0 && count == g->pull.nvec;
+    k_cc_pull<BT, BULK><<<(unsigned)grid, BT, smem, g->stream>>>(g->pull.nbr, g->pull.shared, first, count, (uint32_t)g->V, f.label,
+                                                                g->pull.hub_vid, g->pull.nhub, ncache, f.has_next, vc, f.vote, f.chg,
+                                                                f.iter, f.level_dev, use_prev, f.dev_err); GRZ_COUNT_LAUNCH(g);
     return GRZ_OK;
 }
 
 static int launch_cc_pull(grz_graph* g, uint64_t first, uint64_t count, const VoteCfg& vc)
 {
+    const bool b = g->tune.pull_staging != 0;
     switch (g->tune.cc_threads) {
-    case 256: return launch_cc_pull_bt<256>(g, first, count, vc);
-    case 1024: return launch_cc_pull_bt<1024>(g, first, count, vc);
-    default: return launch_cc_pull_bt<512>(g, first, count, vc);
+    case 256: return b ? launch_cc_pull_bt<256, true>(g, first, count, vc) : launch_cc_pull_bt<256, false>(g, first, count, vc);
+    case 1024: return b ? launch_cc_pull_bt<1024, true>(g, first, count, vc) : launch_cc_pull_bt<1024, false>(g, first, count, vc);
+    default: return b ? launch_cc_pull_bt<512, true>(g, first, count, vc) : launch_cc_pull_bt<512, false>(g, first, count, vc);
     }
 }
 
@@ -1118,13 +1187,16 @@ int grz_cc_phase(grz_graph* g, int pull, uint64_t first_vec, uint64_t count)
         int rc = grz_frontier_init(g, GRZ_APP_CONNECTED_COMPONENTS, 0, 0);
         if (rc) return rc;
     }
-    // the caller may pass any vector range: no converged-destination skip, and none later in
-    // this state either (the tag 2^32 - 1 never matches; grz_frontier_init starts over)
-    g->fr.phase_api = 1;
+    // An edge phase per call, numbered like the driver loops' iterations.  A pull over part of
+    // the list leaves the converged-destination skip off for the rest of this state (the tag
+    // 2^32 - 1 never matches; grz_frontier_init starts over).
+    grz_frontier_state& f = g->fr;
+    const bool whole = !pull || (first_vec == 0 && count == g->pull.nvec);
+    if (!whole) f.cc_partial = 1;
+    f.iter++;
     const int rc = edge_phase(g, pull, first_vec, count);
-    g->fr.phase_api = 0;
     if (rc) return rc;
-    GRZ_CK(g, cudaMemsetAsync(g->fr.chg, 0xff, 2 * sizeof(unsigned long long), g->stream));
+    if (f.cc_partial) GRZ_CK(g, cudaMemsetAsync(f.chg, 0xff, 2 * sizeof(unsigned long long), g->stream));
     return GRZ_OK;
 }
 
@@ -1181,6 +1253,19 @@ int grz_frontier_step(grz_graph* g, int engine, int* engine_out, uint64_t* vote_
     if (v == 0) return 0;
     rc = grz_frontier_vertex_phase(g, 0, g->V);
     return rc ? rc : 1;
+}
+
+// GRZ_ERR_TIMEOUT if a bounded device-side wait of an edge phase gave up since grz_frontier_init
+// (synchronises the stream)
+int grz_frontier_check_waits(grz_graph* g)
+{
+    grz_frontier_state& f = g->fr;
+    if (!f.dev_err) return GRZ_OK;
+    unsigned e = 0;
+    GRZ_CK(g, cudaMemcpyAsync(&e, f.dev_err, sizeof(e), cudaMemcpyDeviceToHost, g->stream));
+    GRZ_CK(g, cudaStreamSynchronize(g->stream));
+    if (e) return grz_set_error(g, GRZ_ERR_TIMEOUT, "an edge phase's wait for its staged vectors ran out");
+    return GRZ_OK;
 }
 
 // the pinned host buffer the per-iteration read-backs go through
@@ -1279,7 +1364,7 @@ void grz_frontier_park(grz_graph* g)
 void grz_frontier_free(grz_graph* g)
 {
     grz_frontier_state& f = g->fr;
-    void* ptrs[] = { f.label, f.level, f.has, f.has_next, f.wants, f.nonempty_push, f.nonempty_pull, f.frontier, f.voff, f.vdelta, f.tile_first, f.chg,
+    void* ptrs[] = { f.label, f.level, f.has, f.has_next, f.wants, f.nonempty_push, f.nonempty_pull, f.frontier, f.voff, f.vdelta, f.tile_first, f.chg, f.dev_err,
                      f.fr_part, f.touched, f.cand64, f.cand32,
                      f.counters, f.vote, f.sw_out, f.snap };
     for (void* p : ptrs) cudaFree(p);
@@ -1458,8 +1543,8 @@ int grz_frontier_run_graph(grz_graph* g, uint64_t* launches)
     if (!same) {
         int resident = 0;
         const size_t smem = sizeof(uint32_t) * std::min<uint32_t>(g->tune.cc_cache, g->pull.nhub);
-        rc = g->tune.cc_threads == 256 ? cc_pull_config<256>(g, smem, &resident)
-             : (g->tune.cc_threads == 1024 ? cc_pull_config<1024>(g, smem, &resident) : cc_pull_config<512>(g, smem, &resident));
+        rc = g->tune.cc_threads == 256 ? cc_pull_config_any<256>(g, smem, &resident)
+             : (g->tune.cc_threads == 1024 ? cc_pull_config_any<1024>(g, smem, &resident) : cc_pull_config_any<512>(g, smem, &resident));
         if (!rc) rc = build_run_graph(g);
         if (rc) return rc;
     }
@@ -1469,8 +1554,9 @@ int grz_frontier_run_graph(grz_graph* g, uint64_t* launches)
     c.level = f.iter + 1;
     c.last_engine = (uint32_t)f.last_engine;
     c.vote = f.vote_host;
-    c.max_level = (uint32_t)std::min<uint64_t>(g->V + 2, 0xfffffff0ull) + f.iter;
-    c.limit_ns = 300ull * 1000000000ull;
+    const uint64_t max_it = g->tune.run_max_iterations ? g->tune.run_max_iterations : std::min<uint64_t>(g->V + 2, 0xfffffff0ull);
+    c.max_level = (uint32_t)std::min<uint64_t>(max_it + f.iter, 0xfffffff0ull);
+    c.limit_ns = g->tune.run_limit_us ? (unsigned long long)g->tune.run_limit_us * 1000ull : 300ull * 1000000000ull;
     grz_switch_policy_ctl(g, &c);
     memcpy(f.mail, &c, sizeof(c));
     GRZ_CK(g, cudaMemcpyAsync(f.ctl, f.mail, sizeof(c), cudaMemcpyHostToDevice, g->stream));
@@ -1479,8 +1565,20 @@ int grz_frontier_run_graph(grz_graph* g, uint64_t* launches)
     GRZ_CK(g, cudaMemcpyAsync(f.mail, f.ctl, sizeof(c), cudaMemcpyDeviceToHost, g->stream));
     GRZ_CK(g, cudaStreamSynchronize(g->stream));
     memcpy(&c, f.mail, sizeof(c));
-    if (c.overrun == 1) return grz_set_error(g, GRZ_ERR_STATE, "no convergence within %u iterations", c.max_level);
-    if (c.overrun) return grz_set_error(g, GRZ_ERR_STATE, "run stopped by its time bound");
+    if (c.overrun) {
+        // the loop stopped before convergence: the state is left as the last iteration made it
+        // (a later grz_frontier_begin, grz_cc_run or grz_bfs_run starts over)
+        f.iter += c.npull + c.npush;
+        f.npull += c.npull;
+        f.npush += c.npush;
+        if ((c.npull + c.npush) % 2 == 0 && c.npull + c.npush > 0) {
+            unsigned long long* t = f.has;
+            f.has = f.has_next;
+            f.has_next = t;
+        }
+        if (c.overrun == 1) return grz_set_error(g, GRZ_ERR_TIMEOUT, "no convergence within %u iterations", c.max_level);
+        return grz_set_error(g, GRZ_ERR_TIMEOUT, "run stopped by its time bound (%llu us)", c.limit_ns / 1000ull);
+    }
     const uint32_t n = c.npull + c.npush;
     f.iter += n;
     f.npull += c.npull;

@@ -171,6 +171,61 @@ __device__ __forceinline__ u128 u128_shfl_down(u128 v, int off)
 }
 
 // ----------------------------------------------------------------------------------------------
+// Bulk copies global -> shared memory on the copy engine (cp.async.bulk, completion counted on an
+// mbarrier in shared memory).  Addresses and sizes must be multiples of 16 bytes.  Waits are
+// bounded (iterations and %globaltimer): a wait that runs out returns false.
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// makes initialised mbarriers visible to the copy engine (the async proxy)
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+// orders this thread's earlier shared-memory accesses before later bulk copies into the same bytes
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait_parity(unsigned long long* bar, unsigned parity)
+{
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+// waits for the phase with the given parity to complete; false when the wait ran out (1 s)
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity)
+{
+    if (mbar_try_wait_parity(bar, parity)) return true;
+    unsigned long long t0;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    for (unsigned i = 0; i < (1u << 24); ++i) {
+        if (mbar_try_wait_parity(bar, parity)) return true;
+        unsigned long long t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        if (t - t0 > 1000000000ull) break;
+    }
+    return false;
+}
+
+// ----------------------------------------------------------------------------------------------
 // graph context
 
 struct grz_list {
@@ -232,6 +287,12 @@ struct grz_mlp;
 #define GRZ_TUNE_BFS_PULL_SCAN 5
 #define GRZ_TUNE_PR_PROPS 6
 #define GRZ_TUNE_INGEST_CHUNKS 7
+#define GRZ_TUNE_PR_PERSISTENT 8
+#define GRZ_TUNE_PR_WAIT_LIMIT_US 9
+#define GRZ_TUNE_PR_WITHHOLD 10
+#define GRZ_TUNE_RUN_MAX_ITERATIONS 11
+#define GRZ_TUNE_RUN_LIMIT_US 12
+#define GRZ_TUNE_PULL_STAGING 13
 #define GRZ_TUNE_HUBS_LOADED 100
 
 // kernel shapes chosen per graph (grz_tune_set; the autotuner searches them)
@@ -244,6 +305,12 @@ struct grz_tuning {
     uint32_t bfs_pull_scan;  // 1: BFS pull scans every vector; 0: only the wanted destinations' (compacted)
     uint32_t pr_props;     // props the PageRank gather reads: 0 by size, 1 fixed point, 2 doubles
     uint32_t ingest_chunks;  // chunks of the pull-only ingest (0: by edge count)
+    uint32_t pr_persistent;  // PageRank iterations: 0 by default rule, 1 two kernels each, 2 one cooperative launch
+    uint32_t pr_wait_limit_us;  // bound of one grid-barrier wait of the persistent kernel (0: 2 s)
+    uint32_t pr_withhold;    // tests: block + 1 whose first barrier arrival is withheld (0: none)
+    uint32_t run_max_iterations;  // CC/BFS iteration bound (0: V + 2)
+    uint32_t run_limit_us;   // CC/BFS time bound of a run in microseconds (0: 300 s)
+    uint32_t pull_staging;   // CC pull's edge stream: 0 plain streaming loads, 1 bulk copies into shared memory
 };
 
 // Device control block of a CC/BFS run executed as one CUDA graph (grz_ccbfs.cu): the
@@ -294,7 +361,8 @@ struct grz_frontier_state {
     unsigned long long* vote;        // GRZ_VOTE_SLOTS * GRZ_VOTE_STRIDE
     unsigned long long* chg;         // CC: smallest label written per iteration, tagged (2 words, grz_ccbfs.cu)
     unsigned long long mail_chg[2];  // host copy of the initial chg words (outlives the async copy)
-    int phase_api;                   // an edge phase of the phases.h entry points is running
+    int cc_partial;                  // a phases.h pull covered part of the list: no converged-destination skip
+    unsigned* dev_err;               // set by an edge phase whose bounded wait gave up
     // engine policy
     int policy;                      // GRZ_POLICY_*
     grz_mlp* mlp;
@@ -346,6 +414,8 @@ struct grz_graph {
     int pr_rowacc_stale;  // fused iterations cleared only the straddling accumulators
     int pr_lists_changed; // the PageRank arrays were kept across a reload with the same V
     uint32_t pr_nparts[2];  // partials in each half of pr_sum
+    void* pr_bar;         // grid barrier and phase timer of the persistent PageRank kernel (device)
+    void* pr_bar_host;    // pinned read-back of its error word and phase times
     double* pr_d[2];      // double[V+1]: the props as doubles, gathered instead of pr_fx in pr_dmode
     int pr_dmode;         // fused iterations gather pr_d
     int pr_fx_stale;      // pr_fx[pr_cur] is behind pr_d[pr_cur]
@@ -430,8 +500,11 @@ struct grz_prof {
     int n;
     int kind[GRZ_PROF_MAX];
     cudaEvent_t ev[GRZ_PROF_MAX][2];
+    float direct_ms[GRZ_PROF_MAX];  // >= 0: a duration measured on the device (%globaltimer), no events
     int created;
 };
+// a record whose duration the device measured itself (phases of a persistent kernel)
+void grz_prof_direct(grz_graph* g, int kind, float ms);
 
 // host helpers (grz_api.cu)
 int grz_set_error(grz_graph* g, int code, const char* fmt, ...);
@@ -454,6 +527,7 @@ int grz_engine_threshold(const grz_graph* g, uint64_t vote);
 int grz_read_vote(grz_graph* g, uint64_t* out);
 int grz_frontier_mail(grz_graph* g);
 int grz_frontier_run_graph(grz_graph* g, uint64_t* launches);
+int grz_frontier_check_waits(grz_graph* g);
 void grz_frontier_run_prepare(grz_graph* g);
 int grz_frontier_digest(grz_graph* g, uint64_t* out3);
 int grz_switch_max_degree(grz_graph* g);

@@ -47,6 +47,22 @@ __device__ __forceinline__ u128 ld_fx(const u128* p, uint32_t i)
 __device__ __forceinline__ u128 ld_prop(const u128* p, uint32_t i) { return ld_fx(p, i); }
 __device__ __forceinline__ u128 ld_prop(const double* p, uint32_t i) { return fx_from_double(__ldg(p + i)); }
 
+// The same through the coherent path (ld.global, L1-cached): for the persistent kernel, whose
+// apply phase rewrites the props that a later gather phase of the same launch reads, which the
+// read-only (non-coherent) path does not allow.
+__device__ __forceinline__ u128 ld_prop_coh(const u128* p, uint32_t i)
+{
+    u128 r;
+    asm volatile("ld.global.v2.u64 {%0, %1}, [%2];" : "=l"(r.lo), "=l"(r.hi) : "l"(p + i));
+    return r;
+}
+__device__ __forceinline__ u128 ld_prop_coh(const double* p, uint32_t i)
+{
+    double x;
+    asm volatile("ld.global.f64 %0, [%1];" : "=d"(x) : "l"(p + i));
+    return fx_from_double(x);
+}
+
 // per-iteration constants handed from the gather kernel to the apply kernel
 struct PRConst {
     const u128* part_in;  // per-block partial sums whose total is S_k (exact)
@@ -76,29 +92,37 @@ __device__ __forceinline__ u128 u128_shfl_up(u128 v, int off)
 // u128 fixed point, or double (converted exactly to fixed point after the load).
 __device__ __forceinline__ u128 block_reduce_u128(u128 s, u128* red);
 
-template <typename P>
-__global__ void __launch_bounds__(PR_THREADS) k_pr_gather(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv,
-                                                          uint64_t first, uint64_t nvec, uint64_t list_nvec,
-                                                          const P* __restrict__ prop_fx, uint32_t V, u128* __restrict__ rowacc,
-                                                          const uint32_t* __restrict__ hub_vid, uint32_t nhub, const PRConst pc)
+// shared memory of the gather's block combine
+struct GatherSmem {
+    static constexpr int NW = PR_THREADS / 32;
+    uint32_t key[2][NW];
+    u128 sum[2][NW];
+    uint32_t flag[2][NW];  // bit0 present, bit1 head real, bit2 tail real
+    u128 red[NW];
+};
+
+// once per iteration (block 0 of the gather): S_k from the previous apply's per-block partials,
+// then K = G*d + (1-d)/V with G = (1 - S_k)/V
+__device__ __forceinline__ void pr_publish_K(const PRConst& pc, u128* red)
 {
-    constexpr int NW = PR_THREADS / 32;
-    __shared__ uint32_t s_key[2][NW];
-    __shared__ u128 s_sum[2][NW];
-    __shared__ uint32_t s_flag[2][NW];  // bit0 present, bit1 head real, bit2 tail real
-    __shared__ u128 red[NW];
-    if (pc.K_out && blockIdx.x == 0) {
-        // once per iteration: S_k from the previous apply's per-block partials, then
-        // K = G*d + (1-d)/V with G = (1 - S_k)/V
-        u128 S = u128_zero();
-        for (uint32_t b = threadIdx.x; b < pc.nparts; b += PR_THREADS) S = u128_add(S, pc.part_in[b]);
-        S = block_reduce_u128(S, red);
-        if (threadIdx.x == 0) *pc.K_out = __fma_rn((1.0 - fx_to_double(S)) / pc.nverts, pc.damping, pc.c);
-    }
+    u128 S = u128_zero();
+    for (uint32_t b = threadIdx.x; b < pc.nparts; b += PR_THREADS) S = u128_add(S, pc.part_in[b]);
+    S = block_reduce_u128(S, red);
+    if (threadIdx.x == 0) *pc.K_out = __fma_rn((1.0 - fx_to_double(S)) / pc.nverts, pc.damping, pc.c);
+}
+
+// The gather over tiles blockIdx.x, blockIdx.x + nblocks, ... of PR_THREADS vectors.
+template <typename P, bool COH>
+__device__ __forceinline__ void pr_gather_tiles(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv, uint64_t first,
+                                                uint64_t nvec, uint64_t list_nvec, const P* __restrict__ prop_fx, uint32_t V,
+                                                u128* __restrict__ rowacc, const uint32_t* __restrict__ hub_vid, uint32_t nhub,
+                                                uint32_t block, uint32_t nblocks, GatherSmem& sm)
+{
+    constexpr int NW = GatherSmem::NW;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t ntiles = (nvec + PR_THREADS - 1) / PR_THREADS;
-    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        if (lane < 2) s_flag[lane][warp] = 0;
+    for (uint64_t tile = block; tile < ntiles; tile += nblocks) {
+        if (lane < 2) sm.flag[lane][warp] = 0;
         const uint64_t i = tile * PR_THREADS + threadIdx.x;
         const uint64_t v = first + i;
         const bool live = i < nvec;
@@ -107,10 +131,12 @@ __global__ void __launch_bounds__(PR_THREADS) k_pr_gather(const uint4* __restric
         if (live) {
             const uint4 s = __ldcs(nbr + v);
             key = __ldcs(dstv + v);
-            const u128 g0 = ld_prop(prop_fx, min(grz_hub_decode(s.x, hub_vid, nhub), V));
-            const u128 g1 = ld_prop(prop_fx, min(grz_hub_decode(s.y, hub_vid, nhub), V));
-            const u128 g2 = ld_prop(prop_fx, min(grz_hub_decode(s.z, hub_vid, nhub), V));
-            const u128 g3 = ld_prop(prop_fx, min(grz_hub_decode(s.w, hub_vid, nhub), V));
+            const uint32_t i0 = min(grz_hub_decode(s.x, hub_vid, nhub), V), i1 = min(grz_hub_decode(s.y, hub_vid, nhub), V);
+            const uint32_t i2 = min(grz_hub_decode(s.z, hub_vid, nhub), V), i3 = min(grz_hub_decode(s.w, hub_vid, nhub), V);
+            const u128 g0 = COH ? ld_prop_coh(prop_fx, i0) : ld_prop(prop_fx, i0);
+            const u128 g1 = COH ? ld_prop_coh(prop_fx, i1) : ld_prop(prop_fx, i1);
+            const u128 g2 = COH ? ld_prop_coh(prop_fx, i2) : ld_prop(prop_fx, i2);
+            const u128 g3 = COH ? ld_prop_coh(prop_fx, i3) : ld_prop(prop_fx, i3);
             val = u128_add(u128_add(g2, g3), u128_add(g0, g1));
         }
         uint32_t prevkey = __shfl_up_sync(0xffffffffu, key, 1);
@@ -138,9 +164,9 @@ __global__ void __launch_bounds__(PR_THREADS) k_pr_gather(const uint4* __restric
             } else {
                 // open on the left (slot 0) or on the right only (slot 1): combined across the block below
                 const int slot = (segstart == 0 && !head_real) ? 0 : 1;
-                s_key[slot][warp] = key;
-                s_sum[slot][warp] = val;
-                s_flag[slot][warp] = 1u | (head_real ? 2u : 0u) | (tail ? 4u : 0u);
+                sm.key[slot][warp] = key;
+                sm.sum[slot][warp] = val;
+                sm.flag[slot][warp] = 1u | (head_real ? 2u : 0u) | (tail ? 4u : 0u);
             }
         }
         __syncthreads();
@@ -152,23 +178,34 @@ __global__ void __launch_bounds__(PR_THREADS) k_pr_gather(const uint4* __restric
             uint32_t ok = 0;
             u128 os = u128_zero();
             for (int w = 0; w < NW; ++w) {
-                const uint32_t f0 = s_flag[0][w];
+                const uint32_t f0 = sm.flag[0][w];
                 if (f0 & 1u) {
-                    if (!open) { open = true; open_head = false; ok = s_key[0][w]; os = u128_zero(); }
-                    os = u128_add(os, s_sum[0][w]);
+                    if (!open) { open = true; open_head = false; ok = sm.key[0][w]; os = u128_zero(); }
+                    os = u128_add(os, sm.sum[0][w]);
                     if (f0 & 4u) {
                         if (open_head) __stcg(reinterpret_cast<ulonglong2*>(rowacc) + ok, make_ulonglong2(os.lo, os.hi));
                         else if (os.lo | os.hi) u128_atomic_add(rowacc + ok, os);
                         open = false;
                     }
                 }
-                const uint32_t f1 = s_flag[1][w];
-                if (f1 & 1u) { open = true; open_head = (f1 & 2u) != 0; ok = s_key[1][w]; os = s_sum[1][w]; }
+                const uint32_t f1 = sm.flag[1][w];
+                if (f1 & 1u) { open = true; open_head = (f1 & 2u) != 0; ok = sm.key[1][w]; os = sm.sum[1][w]; }
             }
             if (open && (os.lo | os.hi)) u128_atomic_add(rowacc + ok, os);
         }
         __syncthreads();  // the walk has read this tile's pieces
     }
+}
+
+template <typename P>
+__global__ void __launch_bounds__(PR_THREADS) k_pr_gather(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv,
+                                                          uint64_t first, uint64_t nvec, uint64_t list_nvec,
+                                                          const P* __restrict__ prop_fx, uint32_t V, u128* __restrict__ rowacc,
+                                                          const uint32_t* __restrict__ hub_vid, uint32_t nhub, const PRConst pc)
+{
+    __shared__ GatherSmem sm;
+    if (pc.K_out && blockIdx.x == 0) pr_publish_K(pc, sm.red);
+    pr_gather_tiles<P, false>(nbr, dstv, first, nvec, list_nvec, prop_fx, V, rowacc, hub_vid, nhub, blockIdx.x, gridDim.x, sm);
 }
 
 __device__ __forceinline__ u128 block_reduce_u128(u128 s, u128* red)
@@ -199,22 +236,22 @@ __device__ __forceinline__ u128 block_reduce_u128(u128 s, u128* red)
 constexpr int PR_APPLY_U = 8;
 constexpr int PR_APPLY_RESIDENT = 3;  // blocks per SM that the launch bounds fit
 
-__global__ void __launch_bounds__(PR_THREADS, PR_APPLY_RESIDENT) k_pr_apply(u128* __restrict__ rowacc, const uint32_t* __restrict__ cut,
-                                                                            const double* __restrict__ inv_deg,
-                                                                            const uint32_t* __restrict__ degree, uint64_t V,
-                                                                            const double* __restrict__ Kp, u128* __restrict__ part_out,
-                                                                            double damping, u128* __restrict__ prop_fx,
-                                                                            double* __restrict__ prop_d, double* __restrict__ prop_out)
+// the apply over vertices block*PR_THREADS + tid, strided by nblocks*PR_THREADS, U vertices per
+// thread loaded before any is stored; returns the block's partial of S' (valid in thread 0;
+// every thread of the block must call it)
+template <int U>
+__device__ __forceinline__ u128 pr_apply_range(u128* __restrict__ rowacc, const uint32_t* __restrict__ cut,
+                                               const double* __restrict__ inv_deg, const uint32_t* __restrict__ degree, uint64_t V,
+                                               double sK, double damping, u128* __restrict__ prop_fx, double* __restrict__ prop_d,
+                                               double* __restrict__ prop_out, uint32_t block, uint32_t nblocks, u128* red)
 {
-    __shared__ u128 red[PR_THREADS / 32];
-    const double sK = *Kp;
-    const uint64_t stride = (uint64_t)gridDim.x * PR_THREADS;
+    const uint64_t stride = (uint64_t)nblocks * PR_THREADS;
     u128 s = u128_zero();
-    for (uint64_t base = (uint64_t)blockIdx.x * PR_THREADS + threadIdx.x; base < V; base += stride * PR_APPLY_U) {
-        ulonglong2 a[PR_APPLY_U];
-        uint32_t cw[PR_APPLY_U];
+    for (uint64_t base = (uint64_t)block * PR_THREADS + threadIdx.x; base < V; base += stride * U) {
+        ulonglong2 a[U];
+        uint32_t cw[U];
 #pragma unroll
-        for (int j = 0; j < PR_APPLY_U; ++j) {
+        for (int j = 0; j < U; ++j) {
             const uint64_t v = base + (uint64_t)j * stride;
             a[j] = make_ulonglong2(0ull, 0ull);
             cw[j] = 0;
@@ -224,7 +261,7 @@ __global__ void __launch_bounds__(PR_THREADS, PR_APPLY_RESIDENT) k_pr_apply(u128
             }
         }
 #pragma unroll
-        for (int j = 0; j < PR_APPLY_U; ++j) {
+        for (int j = 0; j < U; ++j) {
             const uint64_t v = base + (uint64_t)j * stride;
             if (v >= V) break;
             if ((a[j].x | a[j].y) && ((cw[j] >> (v & 31)) & 1u))
@@ -240,8 +277,156 @@ __global__ void __launch_bounds__(PR_THREADS, PR_APPLY_RESIDENT) k_pr_apply(u128
             s = u128_add(s, u128_mul32(pf, __ldg(degree + v)));
         }
     }
-    s = block_reduce_u128(s, red);
+    return block_reduce_u128(s, red);
+}
+
+__global__ void __launch_bounds__(PR_THREADS, PR_APPLY_RESIDENT) k_pr_apply(u128* __restrict__ rowacc, const uint32_t* __restrict__ cut,
+                                                                            const double* __restrict__ inv_deg,
+                                                                            const uint32_t* __restrict__ degree, uint64_t V,
+                                                                            const double* __restrict__ Kp, u128* __restrict__ part_out,
+                                                                            double damping, u128* __restrict__ prop_fx,
+                                                                            double* __restrict__ prop_d, double* __restrict__ prop_out)
+{
+    __shared__ u128 red[PR_THREADS / 32];
+    const u128 s = pr_apply_range<PR_APPLY_U>(rowacc, cut, inv_deg, degree, V, *Kp, damping, prop_fx, prop_d, prop_out, blockIdx.x, gridDim.x,
+                                  red);
     if (threadIdx.x == 0) part_out[blockIdx.x] = s;  // summed by the next gather kernel's block 0
+}
+
+// ---------------------------------------------------------------------------------------------
+// Persistent form: all iterations in one cooperative launch, gather and apply separated by a
+// grid-wide barrier (the reference's pull phase -> threads_barrier -> perform_vertex_phase_pr,
+// source/phase_vertex_pr.asm:190-285, barrier source/threads.asm:181-204).  Every wait of the
+// barrier is bounded: past the deadline (%globaltimer) a block sets the error word and every
+// block returns at its next barrier, so a launch always ends and the host reads the error.
+
+struct PRBar {
+    unsigned int count;     // arrivals at the current barrier
+    unsigned int gen;       // barriers completed
+    unsigned int err;       // 1: a wait ran out
+    unsigned int where;     // the barrier (1-based) whose wait ran out
+    unsigned long long gather_ns[64];  // per iteration, block 0's view: gather phase (the barrier included)
+    unsigned long long apply_ns[64];   // apply phase
+};
+
+constexpr unsigned long long PR_BAR_SPIN_MAX = 1ull << 26;  // iteration bound of one wait (besides the deadline)
+
+__device__ __forceinline__ unsigned long long pr_now_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// true when every block arrived; false when a wait gave up (or another block's did).
+// `withhold` leaves this block's arrival out (host-side fault injection for the tests).
+__device__ __forceinline__ bool pr_grid_barrier(PRBar* bar, unsigned nblocks, unsigned long long limit_ns, unsigned idx, bool withhold)
+{
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        volatile unsigned int* vgen = &bar->gen;
+        volatile unsigned int* verr = &bar->err;
+        const unsigned int g0 = *vgen;
+        __threadfence();
+        if (*verr) {
+            ok = 0;
+        } else if (!withhold && atomicAdd(&bar->count, 1u) + 1u == nblocks) {
+            bar->count = 0u;
+            __threadfence();
+            atomicAdd(&bar->gen, 1u);
+        } else {
+            const unsigned long long t0 = pr_now_ns();
+            for (unsigned long long spin = 0; *vgen == g0; ++spin) {
+                if (*verr) { ok = 0; break; }
+                if (spin >= PR_BAR_SPIN_MAX || pr_now_ns() - t0 > limit_ns) {
+                    if (atomicExch(&bar->err, 1u) == 0u) bar->where = idx;
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+struct PRPersist {
+    const uint4* nbr;
+    const uint32_t* dstv;
+    uint64_t nvec;
+    uint32_t V;
+    const uint32_t* hub_vid;
+    uint32_t nhub;
+    u128* rowacc;
+    const uint32_t* cut;
+    const double* inv_deg;
+    const uint32_t* degree;
+    u128* fx[2];            // props, fixed point (ping-pong)
+    double* d[2];           // props, doubles (ping-pong; gathered in doubles mode)
+    int dmode;
+    int cur;                // which buffer holds the current props
+    u128* sum[2];           // per-block partials of S (ping-pong)
+    uint32_t nparts0;       // partials in sum[sum_cur] at the start
+    int sum_cur;
+    double* K;
+    double damping, c, nverts;
+    uint32_t iters;
+    double* prop_out;       // reference-format doubles after the last iteration, or null
+    PRBar* bar;
+    unsigned long long limit_ns;
+    int withhold_block;     // -1: none
+    int time_phases;        // block 0 records the phase durations into bar
+};
+
+// registers bounded so that MINB blocks of 256 threads stay resident per SM (the gather wants as
+// many random loads in flight as possible: 6 leaves the apply unspilled, 8 is the two-kernel
+// gather's occupancy); the apply loads 2 vertices per thread ahead
+constexpr int PR_PERSIST_APPLY_U = 2;
+
+template <typename P, int MINB>
+__global__ void __launch_bounds__(PR_THREADS, MINB) k_pr_persistent(const PRPersist q)
+{
+    __shared__ GatherSmem sm;
+    const unsigned nb = gridDim.x;
+    unsigned bi = 0;
+    int cur = q.cur, sc = q.sum_cur;
+    uint32_t nparts = q.nparts0;
+    for (uint32_t it = 0; it < q.iters; ++it) {
+        const unsigned long long t0 = (q.time_phases && blockIdx.x == 0 && threadIdx.x == 0) ? pr_now_ns() : 0ull;
+        if (blockIdx.x == 0) {
+            PRConst pc;
+            pc.part_in = q.sum[sc];
+            pc.nparts = nparts;
+            pc.K_out = q.K;
+            pc.damping = q.damping;
+            pc.c = q.c;
+            pc.nverts = q.nverts;
+            pr_publish_K(pc, sm.red);
+        }
+        const P* props = q.dmode ? (const P*)q.d[cur] : (const P*)q.fx[cur];
+        pr_gather_tiles<P, true>(q.nbr, q.dstv, 0, q.nvec, q.nvec, props, q.V, q.rowacc, q.hub_vid, q.nhub, blockIdx.x, nb, sm);
+        if (!pr_grid_barrier(q.bar, nb, q.limit_ns, ++bi, (int)blockIdx.x == q.withhold_block)) return;
+        const unsigned long long t1 = (q.time_phases && blockIdx.x == 0 && threadIdx.x == 0) ? pr_now_ns() : 0ull;
+        const double sK = *(volatile double*)q.K;
+        const u128 s = pr_apply_range<PR_PERSIST_APPLY_U>(q.rowacc, q.cut, q.inv_deg, q.degree, q.V, sK, q.damping, q.fx[cur ^ 1],
+                                      q.dmode ? q.d[cur ^ 1] : nullptr, it + 1 == q.iters ? q.prop_out : nullptr, blockIdx.x, nb,
+                                      sm.red);
+        if (threadIdx.x == 0) q.sum[sc ^ 1][blockIdx.x] = s;
+        if (!pr_grid_barrier(q.bar, nb, q.limit_ns, ++bi, false)) return;
+        if (q.time_phases && blockIdx.x == 0 && threadIdx.x == 0 && it < 64) {
+            const unsigned long long t2 = pr_now_ns();
+            q.bar->gather_ns[it] = t1 - t0;
+            q.bar->apply_ns[it] = t2 - t1;
+        }
+        cur ^= 1;
+        sc ^= 1;
+        nparts = nb;
+    }
 }
 
 // bit j of word t: vertex 32t + j has pull vectors in two or more gather tiles of PR_THREADS
@@ -498,6 +683,115 @@ int grz_pr_fused_iteration(grz_graph* g, int write_double_props)
     g->pr_cur ^= 1;
     g->pr_sum_cur = k ^ 1;
     g->pr_iters_done++;
+    return GRZ_OK;
+}
+
+// resident blocks per SM of the persistent kernel (a cooperative launch needs them all resident)
+template <typename P, int MINB>
+static int pr_persistent_resident(grz_graph* g)
+{
+    static int resident[64] = {};
+    if (g->device < 0 || g->device >= 64) return 1;
+    if (!resident[g->device]) {
+        int r = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_pr_persistent<P, MINB>, PR_THREADS, 0) != cudaSuccess || r < 1) {
+            cudaGetLastError();
+            r = 1;
+        }
+        resident[g->device] = r;
+    }
+    return resident[g->device];
+}
+
+// Whether grz_pr_iterate runs its iterations in one persistent launch.  Measured on GB300 (R-MAT
+// 20, 16 iterations): two kernels 93 us per iteration, the persistent kernel (6 blocks per SM)
+// 109 us: its gather must read the props through the coherent path (its apply rewrites them in
+// the same launch) and holds fewer blocks per SM.  Two kernels stay the default.
+int grz_pr_use_persistent(const grz_graph* g) { return g->tune.pr_persistent >= 2; }
+
+// `iters` PageRank iterations (gather + apply each) in one cooperative launch.  Synchronises the
+// graph's stream to read the barrier's error word.  A wait that runs out returns GRZ_ERR_TIMEOUT
+// and leaves the PageRank state uninitialised (grz_pr_init starts over).
+int grz_pr_persistent_iterations(grz_graph* g, uint32_t iters)
+{
+    if (iters == 0 || g->V == 0) return GRZ_OK;
+    if (!g->pr_bar) {
+        GRZ_CK(g, cudaMalloc(&g->pr_bar, sizeof(PRBar)));
+        GRZ_CK(g, cudaMallocHost(&g->pr_bar_host, sizeof(PRBar)));
+    }
+    int rc = g->pr_dmode ? pr_sync_d(g) : pr_sync_fx(g);
+    if (rc) return rc;
+    const bool eight = g->tune.pr_persistent == 3;
+    const int resident = eight ? (g->pr_dmode ? pr_persistent_resident<double, 8>(g) : pr_persistent_resident<u128, 8>(g))
+                               : (g->pr_dmode ? pr_persistent_resident<double, 6>(g) : pr_persistent_resident<u128, 6>(g));
+    uint64_t want = g->tune.pr_grid ? g->tune.pr_grid : (uint64_t)g->num_sms * resident;
+    want = std::min<uint64_t>(want, (uint64_t)g->num_sms * resident);  // co-resident
+    const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(want, blocks_for(g->V)));  // partial slots
+    const uint32_t stride = blocks_for(g->V) + 1;
+    const bool timing = g->prof && g->prof->on;
+    PRPersist q;
+    memset(&q, 0, sizeof(q));
+    q.nbr = g->pull.nbr;
+    q.dstv = g->pull.shared;
+    q.nvec = g->pull.nvec;
+    q.V = (uint32_t)g->V;
+    q.hub_vid = g->pull.hub_vid;
+    q.nhub = g->pull.nhub;
+    q.rowacc = g->pr_rowacc;
+    q.cut = g->pr_cut;
+    q.inv_deg = g->inv_deg;
+    q.degree = g->degree;
+    q.fx[0] = g->pr_fx[0];
+    q.fx[1] = g->pr_fx[1];
+    q.d[0] = g->pr_d[0];
+    q.d[1] = g->pr_d[1];
+    q.dmode = g->pr_dmode;
+    q.cur = g->pr_cur;
+    q.sum[0] = g->pr_sum;
+    q.sum[1] = g->pr_sum + stride;
+    q.sum_cur = g->pr_sum_cur;
+    q.nparts0 = g->pr_nparts[g->pr_sum_cur];
+    q.K = g->pr_K;
+    q.damping = g->pr_damping;
+    q.nverts = (double)g->V;
+    q.c = (1.0 - g->pr_damping) / q.nverts;
+    q.iters = iters;
+    q.prop_out = nullptr;
+    q.bar = (PRBar*)g->pr_bar;
+    q.limit_ns = (unsigned long long)(g->tune.pr_wait_limit_us ? g->tune.pr_wait_limit_us : 2000000u) * 1000ull;
+    q.withhold_block = (int)g->tune.pr_withhold - 1;
+    q.time_phases = timing ? 1 : 0;
+    GRZ_CK(g, cudaMemsetAsync(g->pr_bar, 0, 4 * sizeof(unsigned int), g->stream));
+    void* args[] = { &q };
+    const void* fn = eight ? (g->pr_dmode ? (const void*)k_pr_persistent<double, 8> : (const void*)k_pr_persistent<u128, 8>)
+                           : (g->pr_dmode ? (const void*)k_pr_persistent<double, 6> : (const void*)k_pr_persistent<u128, 6>);
+    GRZ_CK(g, cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(PR_THREADS), args, 0, g->stream));
+    GRZ_COUNT_LAUNCH(g);
+    const size_t rb = timing ? sizeof(PRBar) : 4 * sizeof(unsigned int);
+    GRZ_CK(g, cudaMemcpyAsync(g->pr_bar_host, g->pr_bar, rb, cudaMemcpyDeviceToHost, g->stream));
+    GRZ_CK(g, cudaStreamSynchronize(g->stream));
+    const PRBar* hb = (const PRBar*)g->pr_bar_host;
+    if (hb->err) {
+        // the iteration stopped part-way: the accumulators and props are inconsistent
+        GRZ_CK(g, cudaMemsetAsync(g->pr_rowacc, 0, sizeof(u128) * (g->V + 1), g->stream));
+        g->pr_rowacc_stale = 0;
+        g->pr_lists_changed = 1;
+        return grz_set_error(g, GRZ_ERR_TIMEOUT, "PageRank grid barrier %u: a wait ran out after %u us", hb->where,
+                             g->tune.pr_wait_limit_us ? g->tune.pr_wait_limit_us : 2000000u);
+    }
+    if (timing)
+        for (uint32_t i = 0; i < iters && i < 64; ++i) {
+            grz_prof_direct(g, GRZ_PROF_PR_GATHER, (float)(hb->gather_ns[i] * 1e-6));
+            grz_prof_direct(g, GRZ_PROF_PR_APPLY, (float)(hb->apply_ns[i] * 1e-6));
+        }
+    if (iters & 1) {
+        g->pr_cur ^= 1;
+        g->pr_sum_cur ^= 1;
+    }
+    g->pr_nparts[g->pr_sum_cur] = grid;
+    g->pr_fx_stale = g->pr_dmode;
+    g->pr_rowacc_stale = 1;
+    g->pr_iters_done += iters;
     return GRZ_OK;
 }
 

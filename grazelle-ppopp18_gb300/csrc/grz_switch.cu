@@ -81,20 +81,30 @@ constexpr int SW_U64 = 5;
 // MLP forward pass of one sample by one warp, lane j computing hidden unit j.  Same operation
 // order as mlp_forward, so the logit equals grz_mlp_predict's.  f: NF features, h: NH scratch
 // (both shared); every lane returns the logit.
-__device__ float mlp_logit_warp(const float* params, const float* f, float* h, int lane)
+// One warp, lane j = hidden unit j, the weights in registers: lane j loads its own rows of W1 and
+// W2 straight from global memory (all loads issued together, one L2 round trip), and the hidden
+// activations pass between lanes by shuffles.  The operation order is mlp_forward's, so the
+// logit equals grz_mlp_predict's bit for bit.
+__device__ float mlp_logit_warp(const float* __restrict__ params, const float* f, int lane)
 {
-    float s = params[OFF_B1 + lane];
-    for (int k = 0; k < NF; ++k) s = fmaf(params[OFF_W1 + lane * NF + k], f[k], s);
-    h[lane] = relu(s);
-    __syncwarp();
-    s = params[OFF_B2 + lane];
-    for (int k = 0; k < NH; ++k) s = fmaf(params[OFF_W2 + lane * NH + k], h[k], s);
-    __syncwarp();
-    h[lane] = relu(s);
-    __syncwarp();
-    float z = params[OFF_B3];
-    for (int k = 0; k < NH; ++k) z = fmaf(params[OFF_W3 + k], h[k], z);
-    __syncwarp();
+    float w1[NF], w2[NH];
+#pragma unroll
+    for (int k = 0; k < NF; ++k) w1[k] = __ldg(params + OFF_W1 + lane * NF + k);
+#pragma unroll
+    for (int k = 0; k < NH; ++k) w2[k] = __ldg(params + OFF_W2 + lane * NH + k);
+    const float b1 = __ldg(params + OFF_B1 + lane), b2 = __ldg(params + OFF_B2 + lane);
+    const float w3 = __ldg(params + OFF_W3 + lane), b3 = __ldg(params + OFF_B3);
+    float s = b1;
+#pragma unroll
+    for (int k = 0; k < NF; ++k) s = fmaf(w1[k], f[k], s);
+    const float h1 = relu(s);
+    s = b2;
+#pragma unroll
+    for (int k = 0; k < NH; ++k) s = fmaf(w2[k], __shfl_sync(0xffffffffu, h1, k), s);
+    const float h2 = relu(s);
+    float z = b3;
+#pragma unroll
+    for (int k = 0; k < NH; ++k) z = fmaf(__shfl_sync(0xffffffffu, w3, k), __shfl_sync(0xffffffffu, h2, k), z);
     return z;
 }
 
@@ -129,10 +139,6 @@ __global__ void __launch_bounds__(T) k_features_decide(FeatIn in, const float* _
     __shared__ unsigned s_pf[T / 32], s_pw[T / 32];
     __shared__ bool s_last;
     __shared__ float f[NF];
-    __shared__ float h[NH];
-    __shared__ float sp[NP];
-    if (use_mlp)
-        for (int k = threadIdx.x; k < NP; k += T) sp[k] = __ldg(params + k);  // staged while counting
     unsigned pf = 0, pw = 0;
     for (uint64_t w = (uint64_t)blockIdx.x * T + threadIdx.x; w < in.words; w += (uint64_t)gridDim.x * T) {
         pf += __popcll(in.frontier[w]);
@@ -166,7 +172,7 @@ __global__ void __launch_bounds__(T) k_features_decide(FeatIn in, const float* _
     __syncwarp();
     int pull;
     if (use_mlp) {
-        pull = mlp_logit_warp(sp, f, h, lane) > 0.f ? 1 : 0;
+        pull = mlp_logit_warp(params, f, lane) > 0.f ? 1 : 0;
     } else {
         pull = (double)vote > threshold ? 1 : 0;
     }
@@ -201,14 +207,9 @@ __global__ void __launch_bounds__(T) k_run_decide(RunIn in, grz_runctl* __restri
     __shared__ unsigned s_pf[T / 32], s_pw[T / 32];
     __shared__ bool s_last;
     __shared__ float f[NF];
-    __shared__ float h[NH];
-    __shared__ float sp[NP];
     if (!in.initial && !*(volatile uint32_t*)&ctl->running) return;
     const FeatIn& fi = in.feat;
-    // every block stages the MLP parameters (6 KB) while it counts; only the last block uses them
     const float* params = ctl->params;
-    if (params && ctl->force < 0)
-        for (int i = threadIdx.x; i < NP; i += T) sp[i] = __ldg(params + i);
     unsigned pf = 0, pw = 0;
     for (uint64_t w = (uint64_t)blockIdx.x * T + threadIdx.x; w < fi.words; w += (uint64_t)gridDim.x * T) {
         pf += __popcll(fi.frontier[w]);
@@ -266,8 +267,10 @@ __global__ void __launch_bounds__(T) k_run_decide(RunIn in, grz_runctl* __restri
     int pull;
     if (ctl->force >= 0) {
         pull = ctl->force;
+    } else if (!running) {
+        pull = 0;  // the loop stops: no next engine to choose
     } else if (params) {
-        pull = mlp_logit_warp(sp, f, h, lane) > 0.f ? 1 : 0;
+        pull = mlp_logit_warp(params, f, lane) > 0.f ? 1 : 0;
     } else {
         pull = (double)vote > ctl->threshold ? 1 : 0;
     }

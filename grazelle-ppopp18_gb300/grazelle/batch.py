@@ -88,6 +88,21 @@ class Batch:
         self._ck(self.lib.grz_batch_msbfs(self.h, a.ctypes.data, k, out.ctypes.data if levels else None, C.byref(st)))
         return ([out[self.voff[g]:self.voff[g + 1]] for g in range(len(self.sizes))] if levels else None), st
 
+    def run(self, seeds, roots, iterations: int = 20, damping: float = 0.85, results: bool = True):
+        """PPR from `seeds` and multi-source BFS from `roots` in one CUDA graph launch (the two loops
+        run side by side).  Returns (ranks or None, levels or None, PPR RunStats, BFS RunStats,
+        total device ms of the launch)."""
+        a, k = self._ids(seeds)
+        r, kb = self._ids(roots)
+        ranks = np.zeros((self.voff[-1], k), dtype=np.float64) if results else None
+        levels = np.zeros((self.voff[-1], kb), dtype=np.int32) if results else None
+        sp, sb, tot = native.RunStats(), native.RunStats(), C.c_float()
+        self._ck(self.lib.grz_batch_run(self.h, a.ctypes.data, k, iterations, C.c_double(damping), r.ctypes.data, kb,
+                                        ranks.ctypes.data if results else None, levels.ctypes.data if results else None,
+                                        C.byref(sp), C.byref(sb), C.byref(tot)))
+        split = (lambda x: [x[self.voff[g]:self.voff[g + 1]] for g in range(len(self.sizes))]) if results else (lambda x: None)
+        return split(ranks), split(levels), sp, sb, tot.value
+
     def tune(self, ppr_blocks: int | None = None, bfs_blocks: int | None = None, ppr_props: int | None = None):
         """Resident blocks per SM of the persistent batch kernels, and the props the PPR gather
         reads (0 or 1 fixed point, 2 doubles); results never depend on them."""

@@ -70,11 +70,15 @@ class Graph:
 
     def tune(self, **kw):
         """Set kernel shapes: hubs=, cc_cache=, cc_threads=, cc_grid=, pr_grid=, bfs_pull_scan=, pr_props=,
-        ingest_chunks= (results never depend on them; hubs and ingest_chunks take effect at the next
-        load)."""
+        ingest_chunks=, pr_persistent= (results never depend on them; hubs and ingest_chunks take effect
+        at the next load), and the bounds of the device-side waits: pr_wait_limit_us=, run_max_iterations=,
+        run_limit_us= (pr_withhold= injects a barrier fault for tests)."""
         keys = {"hubs": native.TUNE_HUBS, "cc_cache": native.TUNE_CC_CACHE, "cc_threads": native.TUNE_CC_THREADS,
                 "cc_grid": native.TUNE_CC_GRID, "pr_grid": native.TUNE_PR_GRID, "bfs_pull_scan": native.TUNE_BFS_PULL_SCAN,
-                "pr_props": native.TUNE_PR_PROPS, "ingest_chunks": native.TUNE_INGEST_CHUNKS}
+                "pr_props": native.TUNE_PR_PROPS, "ingest_chunks": native.TUNE_INGEST_CHUNKS,
+                "pr_persistent": native.TUNE_PR_PERSISTENT, "pr_wait_limit_us": native.TUNE_PR_WAIT_LIMIT_US,
+                "pr_withhold": native.TUNE_PR_WITHHOLD, "run_max_iterations": native.TUNE_RUN_MAX_ITERATIONS,
+                "run_limit_us": native.TUNE_RUN_LIMIT_US, "pull_staging": native.TUNE_PULL_STAGING}
         for k, v in kw.items():
             self._ck(self.lib.grz_tune_set(self.h, keys[k], int(v)))
         return self
@@ -84,7 +88,9 @@ class Graph:
         for k, p in (("hubs", native.TUNE_HUBS), ("cc_cache", native.TUNE_CC_CACHE), ("cc_threads", native.TUNE_CC_THREADS),
                      ("cc_grid", native.TUNE_CC_GRID), ("pr_grid", native.TUNE_PR_GRID),
                      ("bfs_pull_scan", native.TUNE_BFS_PULL_SCAN), ("pr_props", native.TUNE_PR_PROPS),
-                     ("ingest_chunks", native.TUNE_INGEST_CHUNKS),
+                     ("ingest_chunks", native.TUNE_INGEST_CHUNKS), ("pr_persistent", native.TUNE_PR_PERSISTENT),
+                     ("pr_wait_limit_us", native.TUNE_PR_WAIT_LIMIT_US), ("pr_withhold", native.TUNE_PR_WITHHOLD),
+                     ("run_max_iterations", native.TUNE_RUN_MAX_ITERATIONS), ("run_limit_us", native.TUNE_RUN_LIMIT_US), ("pull_staging", native.TUNE_PULL_STAGING),
                      ("hubs_loaded", native.TUNE_HUBS_LOADED)):
             v = C.c_int64()
             self._ck(self.lib.grz_tune_get(self.h, p, C.byref(v)))

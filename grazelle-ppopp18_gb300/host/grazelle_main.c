@@ -27,9 +27,24 @@
 #include <string.h>
 #include <time.h>
 
+#include <unistd.h>
+
 #include "grazelle_phases.h"
 
 #define VERSION "1.0.1-ppopp18-gb300"
+
+#ifdef EXPERIMENT_ITERATION_PROFILE
+/* the frontier column of the per-iteration profile (source/main.c:43-55) */
+#if defined(EXPERIMENT_THRESHOLD_WITHOUT_OUTDEGREES) && defined(EXPERIMENT_THRESHOLD_WITHOUT_COUNT)
+#error "Cannot profile iterations with both outdegrees and count disabled for engine selection."
+#elif defined(EXPERIMENT_THRESHOLD_WITHOUT_OUTDEGREES)
+#define PROFILE_FRONTIER_COLUMN "HasInfo Vertices / Total Vertices"
+#elif defined(EXPERIMENT_THRESHOLD_WITHOUT_COUNT)
+#define PROFILE_FRONTIER_COLUMN "HasInfo Edges / Total Edges"
+#else
+#define PROFILE_FRONTIER_COLUMN "HasInfo (Vertices + Edges) / Total Edges"
+#endif
+#endif
 
 #if defined(BREADTH_FIRST_SEARCH)
 #define APP GRZ_APP_BREADTH_FIRST_SEARCH
@@ -163,6 +178,15 @@ static double now_ms(void)
     return (double)t.tv_sec * 1e3 + (double)t.tv_nsec / 1e6;
 }
 
+#ifdef EXPERIMENT_ITERATION_PROFILE
+static uint64_t now_ns(void)
+{
+    struct timespec t;
+    clock_gettime(CLOCK_MONOTONIC, &t);
+    return (uint64_t)t.tv_sec * 1000000000ull + (uint64_t)t.tv_nsec;
+}
+#endif
+
 static void gpu_or_die(int rc, grz_graph* g, const char* what)
 {
     if (rc == GRZ_OK) return;
@@ -240,6 +264,14 @@ static void execution_impl(grz_graph* g, const grz_graph_info_t* info, const opt
     uint64_t converge_vote = 0;
     gpu_or_die(grz_frontier_current_vote(g, &converge_vote, NULL), g, "initial vote");
     (void)o;
+#ifdef EXPERIMENT_ITERATION_PROFILE
+    /* execution_bfs.c:127-139, execution_cc.c: the vote over the edges (the vertices without outdegrees) */
+#ifdef EXPERIMENT_THRESHOLD_WITHOUT_OUTDEGREES
+    const double profile_comparator = (double)info->num_vertices;
+#else
+    const double profile_comparator = (double)info->num_edges;
+#endif
+#endif
 #ifdef EXPERIMENT_ITERATION_STATS
     gpu_or_die(grz_stats_enable(g, 1), g, "iteration stats");
 #endif
@@ -254,6 +286,10 @@ static void execution_impl(grz_graph* g, const grz_graph_info_t* info, const opt
 #else
         const int use_pull = converge_vote > info->num_edges / 5;
 #endif
+#ifdef EXPERIMENT_ITERATION_PROFILE
+        const double profile_frontier = (double)converge_vote / profile_comparator;
+        const uint64_t profile_t0 = now_ns();
+#endif
         phase_op_reset_global_accum();
         if (use_pull) {
             iterations_pull += 1;
@@ -263,6 +299,13 @@ static void execution_impl(grz_graph* g, const grz_graph_info_t* info, const opt
             perform_edge_push_phase(push_list, info->push_vectors);
         }
         phase_op_write_global_accum_to_buf(reduce_buffer);
+#ifdef EXPERIMENT_ITERATION_PROFILE
+        /* source/execution_bfs.c:172-215: one row per iteration; the edge phase in nanoseconds of
+           wall time (the GPU finished it before the vote came back), not TSC cycles */
+        gpu_or_die(grz_sync(g), g, "edge phase");
+        fprintf(stderr, "%llu,%s,%llu,%.10lf\n", (unsigned long long)total_iterations, use_pull ? "Pull" : "Push",
+                (unsigned long long)(now_ns() - profile_t0), profile_frontier);
+#endif
         converge_vote = phase_op_combine_global_var_from_buf(reduce_buffer);
 #ifdef EXPERIMENT_ITERATION_STATS
         stats_record(g, total_iterations - 1);
@@ -313,6 +356,25 @@ int main(int argc, char** argv)
         }
     }
 #endif
+    /* graphdata.c:435-470 (one node: every vertex), then main.c:73-89 */
+    printf("Vertices:  assigned using in-edge list\n");
+    printf("Vertices:  node %u gets %llu vertices (%llu to %llu, %.2lf%% of total)\n", 0u, (unsigned long long)info.num_vertices,
+           0ull, (unsigned long long)(info.num_vertices - 1), 100.0);
+    {
+        uint64_t threads = o.threads;
+        if (threads == 0) {
+            const long n = sysconf(_SC_NPROCESSORS_ONLN);
+            threads = n > 0 ? (uint64_t)n : 1;
+        }
+        const uint64_t units = o.granularity ? info.pull_vectors / o.granularity : threads << 5;
+        if (units == 0) {
+            printf("Unable to set requested scheduler granularity because the graph is too small.\n");
+            grz_graph_destroy(g);
+            return 1;
+        }
+        printf("Scheduler: total units = %llu, vectors per unit = %llu\n", (unsigned long long)units,
+               (unsigned long long)(info.pull_vectors / units));
+    }
     printf("Loading graph took %.2lfms.\n", now_ms() - t_load);
 #ifdef EXPERIMENT_MODEL_LONG_VECTORS
     printf("Not executing application, since this was a modelling experiment.\n");
@@ -324,6 +386,9 @@ int main(int argc, char** argv)
 #endif
     gpu_or_die(grz_phases_bind(g, APP), g, "bind");
     printf("Starting execution.\n");
+#ifdef EXPERIMENT_ITERATION_PROFILE
+    fprintf(stderr, "Iteration,Selected Engine,Edge Phase Execution Time (ns),%s\n", PROFILE_FRONTIER_COLUMN);
+#endif
     const double t0 = now_ms();
     execution_impl(g, &info, &o);
     gpu_or_die(grz_sync(g), g, "execution");

@@ -159,6 +159,12 @@ int grz_read_levels(grz_graph* g, int64_t* host_levels, uint64_t capacity);
 #define GRZ_TUNE_BFS_PULL_SCAN 5 /* BFS pull over the whole list: 0 = only the wanted destinations' vectors (compacted), 1 = scan every vector */
 #define GRZ_TUNE_PR_PROPS 6     /* props the PageRank gather reads, from the next grz_pr_init: 0 = by size (8-byte doubles when 16-byte fixed-point props exceed 6x L2), 1 = fixed point, 2 = doubles; results identical */
 #define GRZ_TUNE_INGEST_CHUNKS 7 /* chunks of the pull-only ingest, from the next load (0 = one per 2^24 pairs, <= 64; the last is cut into up to four smaller pieces): each chunk is processed while the next crosses the host link */
+#define GRZ_TUNE_PR_PERSISTENT 8 /* form of grz_pr_iterate: 0 = default (two kernels), 1 = two kernels per iteration (gather, apply), 2 or 3 = every iteration in one cooperative launch (6 or 8 blocks per SM) whose phases are separated by a grid barrier with bounded waits (the call then waits for the iterations) */
+#define GRZ_TUNE_PULL_STAGING 13 /* CC pull's edge stream: 0 = streaming loads, 1 = bulk copies (cp.async.bulk) into shared memory, two tiles ahead; results identical */
+#define GRZ_TUNE_PR_WAIT_LIMIT_US 9 /* bound of one grid-barrier wait of the persistent PageRank kernel in microseconds (0 = 2 s); a wait that runs out makes grz_pr_iterate return GRZ_ERR_TIMEOUT and leaves PageRank uninitialised */
+#define GRZ_TUNE_PR_WITHHOLD 10  /* fault injection for tests: block + 1 of the persistent PageRank kernel that never arrives at its first barrier (0 = none) */
+#define GRZ_TUNE_RUN_MAX_ITERATIONS 11 /* CC/BFS iteration bound (0 = V + 2): a run that has not converged by then returns GRZ_ERR_TIMEOUT */
+#define GRZ_TUNE_RUN_LIMIT_US 12  /* CC/BFS time bound of a run in microseconds (0 = 300 s), checked after each iteration: GRZ_ERR_TIMEOUT */
 #define GRZ_TUNE_HUBS_LOADED 100 /* read-only: hubs encoded in the loaded pull list */
 int grz_tune_set(grz_graph* g, int param, int64_t value);
 int grz_tune_get(const grz_graph* g, int param, int64_t* value);
@@ -185,6 +191,13 @@ int grz_batch_info(const grz_batch* b, uint64_t* graphs, uint64_t* vertices, uin
 int grz_batch_ppr(grz_batch* b, const uint32_t* seeds, uint32_t k, uint32_t iterations, double damping,
                   double* ranks_out, grz_run_stats_t* stats);
 int grz_batch_msbfs(grz_batch* b, const uint32_t* roots, uint32_t k, int32_t* levels_out, grz_run_stats_t* stats);
+/* Both at once: PPR from `seeds` ([graphs][k]) and multi-source BFS from `roots` ([graphs][kb]) in one
+ * CUDA graph launch whose two branches run the two loops side by side.  Results as the two calls
+ * above (either output may be NULL); ppr_stats / bfs_stats time each branch inside the launch,
+ * *total_ms the launch. */
+int grz_batch_run(grz_batch* b, const uint32_t* seeds, uint32_t k, uint32_t iterations, double damping, const uint32_t* roots,
+                  uint32_t kb, double* ranks_out, int32_t* levels_out, grz_run_stats_t* ppr_stats, grz_run_stats_t* bfs_stats,
+                  float* total_ms);
 /* kernel shapes of a batch (results never depend on them): resident blocks per SM of the
  * persistent PPR gather / apply and multi-source BFS pull kernels, 1..32 (default 8) */
 #define GRZ_BATCH_TUNE_PPR_BLOCKS 0

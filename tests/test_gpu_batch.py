@@ -146,3 +146,29 @@ def test_bad_inputs():
         B.add_graph(g.num_vertices, g.pull_order().pairs()).build()
         with pytest.raises(native.GrzError):
             B.ppr([[g.num_vertices + 5]])  # seed outside its graph
+
+
+@pytest.mark.parametrize("props", [0, 2])
+def test_ppr_and_bfs_in_one_launch_match_the_separate_runs(batch, props):
+    """grz_batch_run: PPR and multi-source BFS as two branches of one CUDA graph launch give
+    exactly the results of the separate calls (the same kernels), with different seeds and roots
+    and uneven instance counts, twice in a row (the graph is replayed from its initial state)."""
+    B, gs = batch
+    B.tune(ppr_props=props)
+    seeds = [pick(g, 8, 40 + i) for i, g in enumerate(gs)]
+    roots = [pick(g, 5, 80 + i) for i, g in enumerate(gs)]
+    seeds[2] = seeds[2][:3]
+    r_sep, _ = B.ppr(seeds, iterations=12, damping=0.85)
+    l_sep, st_b = B.msbfs(roots)
+    for _ in range(2):
+        ranks, levels, sp, sb, tot = B.run(seeds, roots, iterations=12, damping=0.85)
+        for a, b in zip(ranks, r_sep):
+            np.testing.assert_array_equal(a, b)
+        for a, b in zip(levels, l_sep):
+            np.testing.assert_array_equal(a, b)
+        assert sp.iterations == 12 and sb.iterations == st_b.iterations
+        assert 0 < sp.ms <= tot * 1.01 and 0 < sb.ms <= tot * 1.01
+    for g, lv, rt in zip(gs, levels, roots):
+        for i, r in enumerate(rt):
+            np.testing.assert_array_equal(lv[:, i].astype(np.int64), O.bfs_levels(g.push_order().pairs(), g.num_vertices, r))
+    B.tune(ppr_props=0)

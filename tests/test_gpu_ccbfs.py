@@ -295,3 +295,52 @@ def test_profiler_off_restores_the_graph_run():
             G.cc_run()
             counts.append(G.launch_count() - l0)
     assert counts[0] == counts[1]
+
+
+@pytest.mark.parametrize("host_loop", [False, True])
+def test_run_bounds_return_timeout_and_leave_the_graph_usable(host_loop):
+    """The iteration and time bounds of a CC/BFS run (the decision kernel's in a graph run, the
+    host's in the host loop) stop a run that has not converged with GRZ_ERR_TIMEOUT; the next run
+    with the default bounds gives the oracle's labels and levels."""
+    from grazelle import graphgen as gg, native
+    from grazelle.engine import Graph
+    g = gg.rmat(14, seed=31, symmetric=True)
+    V = g.num_vertices
+    pull, push = g.pull_order().pairs(), g.push_order().pairs()
+    flags = native.FLAG_HOST_LOOP if host_loop else 0
+    L = O.layout(V, pull, push)
+    with Graph(0) as G:
+        G.load_pairs(V, pull, push)
+        G.tune(run_max_iterations=1)
+        st = native.RunStats()
+        assert G.lib.grz_cc_run(G.h, flags, C.byref(st)) == native.GRZ_ERR_TIMEOUT
+        assert b"iterations" in G.lib.grz_graph_last_error(G.h)
+        assert G.lib.grz_bfs_run(G.h, 0, flags, C.byref(st)) == native.GRZ_ERR_TIMEOUT
+        G.tune(run_max_iterations=0, run_limit_us=1)
+        assert G.lib.grz_cc_run(G.h, flags, C.byref(st)) == native.GRZ_ERR_TIMEOUT
+        assert b"time bound" in G.lib.grz_graph_last_error(G.h)
+        G.tune(run_limit_us=0)
+        np.testing.assert_array_equal(G.connected_components(flags), O.cc(L)[0])
+        np.testing.assert_array_equal(G.bfs(0, flags)[1], O.bfs_levels(push, V, 0))
+
+
+@pytest.mark.parametrize("threads", [256, 512, 1024])
+def test_bulk_staged_pull_gives_the_same_labels(threads):
+    """The CC pull with its edge stream staged by bulk copies (cp.async.bulk into shared memory,
+    two tiles ahead, mbarrier completion with bounded waits) gives the oracle's labels under every
+    block size, in the graph run and the host loop, including a list whose last tile is partial
+    (served by plain loads)."""
+    from grazelle import graphgen as gg, native
+    from grazelle.engine import Graph
+    g = gg.rmat(15, seed=41, symmetric=True)
+    V = g.num_vertices
+    pull, push = g.pull_order().pairs(), g.push_order().pairs()
+    L = O.layout(V, pull, push)
+    ref = O.cc(L)[0]
+    with Graph(0) as G:
+        G.load_pairs(V, pull, push)
+        assert G.info().pull_vectors % threads != 0 or threads == 256
+        G.tune(pull_staging=1, cc_threads=threads)
+        np.testing.assert_array_equal(G.connected_components(), ref)
+        np.testing.assert_array_equal(G.connected_components(native.FLAG_HOST_LOOP), ref)
+        np.testing.assert_array_equal(G.connected_components(native.FLAG_FORCE_PULL), ref)

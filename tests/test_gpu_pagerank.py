@@ -212,3 +212,66 @@ def test_phase_api_continues_fused_double_gather_iterations():
         assert lib.grz_phases_last_status() == 0
         mixed = G.props()
     np.testing.assert_array_equal(mixed.view(np.uint64), ref.view(np.uint64))
+
+
+@pytest.mark.parametrize("props", [1, 2])
+def test_persistent_iterations_bit_identical_to_two_kernels(props):
+    """All iterations in one cooperative launch (gather and apply separated by a grid barrier)
+    give exactly the props of the two-kernel iterations, for fixed-point and double gathers, on
+    graphs whose destinations straddle tiles and with hub encoding, also when a call continues
+    from the state an earlier call left (odd counts switch the ping-pong buffers)."""
+    from grazelle import graphgen as gg
+    from grazelle.engine import Graph
+    for g, hubs in ((gg.rmat(16, seed=21), 0), (gg.rmat(14, 8, seed=22, symmetric=True), 512), (gg.erdos_renyi(3000, 5, seed=4), 0)):
+        V = g.num_vertices
+        pull, push = g.pull_order().pairs(), g.push_order().pairs()
+        out = {}
+        for mode in (1, 2):
+            with Graph(0) as G:
+                G.tune(pr_persistent=mode, pr_props=props, hubs=hubs)
+                G.load_pairs(V, pull, push)
+                G.pr_init(0.85).pr_iterate(3).pr_iterate(10)
+                out[mode] = G.props()
+        np.testing.assert_array_equal(out[1], out[2])
+        L = O.layout(V, pull, push)
+        assert O.relative_l1(out[2], O.pr_pull(L, 13, damping=0.85)) < PR_TOL
+
+
+def test_persistent_barrier_wait_runs_out_and_the_graph_recovers():
+    """A block that never arrives at the first grid barrier (injected on the host side) makes the
+    other blocks' bounded waits run out: grz_pr_iterate returns GRZ_ERR_TIMEOUT, PageRank is
+    left uninitialised (GRZ_ERR_STATE), and after grz_pr_init the same graph gives the oracle's
+    props.  Nothing faults or hangs: every wait has a time and an iteration bound."""
+    from grazelle import graphgen as gg, native
+    from grazelle.engine import Graph
+    g = gg.rmat(14, seed=23)
+    V = g.num_vertices
+    pull, push = g.pull_order().pairs(), g.push_order().pairs()
+    with Graph(0) as G:
+        G.load_pairs(V, pull, push)
+        G.tune(pr_persistent=2, pr_wait_limit_us=20000, pr_withhold=1)
+        G.pr_init(0.875)
+        assert G.lib.grz_pr_iterate(G.h, 4) == native.GRZ_ERR_TIMEOUT
+        assert b"barrier 1" in G.lib.grz_graph_last_error(G.h)
+        assert G.lib.grz_pr_iterate(G.h, 1) == native.GRZ_ERR_STATE
+        G.tune(pr_withhold=0)
+        p = G.pagerank(16, damping=0.875)
+    L = O.layout(V, pull, push)
+    assert O.relative_l1(p, O.pr_pull(L, 16, damping=0.875)) < PR_TOL
+
+
+def test_persistent_phase_times_reach_the_profiler():
+    from grazelle import graphgen as gg
+    from grazelle.engine import Graph
+    g = gg.rmat(15, seed=24)
+    with Graph(0) as G:
+        G.load_pairs(g.num_vertices, g.pull_order().pairs(), g.push_order().pairs())
+        G.tune(pr_persistent=2)
+        G.pr_init(0.875)
+        G.profile(True)
+        G.pr_iterate(5)
+        recs = G.profile_read()
+        G.profile(False)
+    kinds = [k for k, _ in recs]
+    assert kinds == ["pr_gather", "pr_apply"] * 5
+    assert all(ms > 0 for _, ms in recs)

@@ -36,33 +36,52 @@ def test_exit_codes_without_gpu(app, tmp_path):
     assert v.returncode == 0 and "ppopp18" in v.stdout
 
 
+def reference_output_file(app, rec, V):
+    """The bytes graph_data_write_ranks_to_file (source/graphdata.c:1119-1138) writes from the
+    reference's own props (the golden fixture, single-thread run): PageRank "%llu %.5le" of
+    prop * deg', CC and BFS "%llu %.0lf" of the prop.  Python's %-formatting of a double is
+    correctly rounded, as glibc's printf is, so the text is the reference's byte for byte."""
+    if app == "pr":
+        od = rec["outdeg"][:V]
+        vals = rec["pr_n1"][:V] * np.where(od == 0.0, float(V), od)
+        return "".join("%d %.5e\n" % (i, x) for i, x in enumerate(vals))
+    vals = rec["cc_labels"][:V] if app == "cc" else rec["bfs_parents"][:V]
+    return "".join("%d %.0f\n" % (i, x) for i, x in enumerate(vals))
+
+
 @pytest.mark.gpu
+@pytest.mark.parametrize("name", ["rmat10_s12", "rmat10_sym_s21", "tiny13", "isolated_root70", "star_chain1001", "er2000_d8_s31"])
 @pytest.mark.parametrize("app", ["pr", "cc", "bfs"])
-def test_driver_output_matches_reference(app, tmp_path):
+def test_driver_output_file_is_the_reference_file(app, name, tmp_path):
+    """The -o file equals, byte for byte, the one the reference writes on the same graph (16
+    PageRank iterations); the stdout carries the reference's load, scheduler and statistics
+    lines (source/graphdata.c:435-470, source/main.c:73-145)."""
     from grazelle import graphgen as gg
-    rec, g = load_golden("rmat10_s12")
+    rec, g = load_golden(name)
+    V = g.num_vertices
     base = str(tmp_path / "g")
     gg.write_grazelle(g, base)
     out = tmp_path / "out.txt"
-    r = run([exe(app), "-i", base, "-N", "16", "-o", str(out)])
+    r = run([exe(app), "-i", base, "-N", "16", "-n", "4", "-o", str(out)])
     assert r.returncode == 0, r.stdout + r.stderr
+    assert out.read_text() == reference_output_file(app, rec, V)
+    lines = r.stdout.splitlines()
+    nvec = int(rec["pull_nvec"])
+    assert "Vertices:  assigned using in-edge list" in lines
+    assert "Vertices:  node 0 gets %d vertices (0 to %d, 100.00%% of total)" % (V, V - 1) in lines
+    assert "Scheduler: total units = 128, vectors per unit = %d" % (nvec // 128) in lines
+    assert lines.index("Scheduler: total units = 128, vectors per unit = %d" % (nvec // 128)) < \
+        [i for i, l in enumerate(lines) if l.startswith("Loading graph took")][0]
     assert "EXECUTION STATISTICS" in r.stdout
-    vals = np.loadtxt(out)
-    assert vals.shape == (g.num_vertices, 2)
-    np.testing.assert_array_equal(vals[:, 0], np.arange(g.num_vertices))
     if app == "pr":
-        od = np.where(rec["outdeg"] == 0, g.num_vertices, rec["outdeg"])
-        ranks = rec["pr_n1"] * od
-        np.testing.assert_allclose(vals[:, 1], ranks, rtol=1e-5)   # %.5le in the file
         assert "PageRank Sum              = 1.0000000000" in r.stdout or "PageRank Sum              = 0.9999999999" in r.stdout
-    elif app == "cc":
-        np.testing.assert_array_equal(vals[:, 1], rec["cc_labels"])
-        assert "Total Iterations" in r.stdout
-    else:
-        np.testing.assert_array_equal(vals[:, 1], rec["bfs_parents"])
+    elif app == "bfs":
         it = rec["bfs_iters"]
         assert "Total Iterations          = %d" % it[0] in r.stdout
         assert "Pull-Based Iterations     = %d" % it[1] in r.stdout
+    # -s: a granularity the graph is too small for (main.c:77-86)
+    r = run([exe(app), "-i", base, "-s", str(nvec + 1)])
+    assert r.returncode == 1 and "Unable to set requested scheduler granularity because the graph is too small." in r.stdout
 
 
 @pytest.mark.gpu
@@ -113,3 +132,44 @@ def test_driver_experiments_iteration_stats_and_long_vectors(tmp_path):
         n = int(np.sum((indeg + lanes - 1) // lanes))
         assert "In-edges:  VL%d: created %d vectors" % (lanes, n) in r.stdout
     assert "Not executing application" in r.stdout and "EXECUTION STATISTICS" not in r.stdout
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("app,flags", [("cc", []), ("bfs", []), ("bfs", ["THRESHOLD_WITHOUT_COUNT"]), ("cc", ["THRESHOLD_WITHOUT_OUTDEGREES"])])
+def test_driver_iteration_profile(app, flags, tmp_path):
+    """EXPERIMENT_ITERATION_PROFILE (source/main.c:43-55,110-112, source/execution_bfs.c:127-215):
+    a CSV on stderr with one row per iteration: its number, the engine, the edge phase's time
+    (nanoseconds here, TSC cycles in the reference) and the vote it was chosen on over E (over V
+    without outdegrees).  The engines and the first row's ratio follow the reference's rule."""
+    from grazelle import build
+    from grazelle import graphgen as gg
+    rec, g = load_golden("rmat10_sym_s21")
+    V, E = g.num_vertices, g.num_edges
+    base = str(tmp_path / "g")
+    gg.write_grazelle(g, base)
+    build.build()
+    r = run([str(build.build_driver(app, ["ITERATION_PROFILE"] + flags)), "-i", base])
+    assert r.returncode == 0, r.stdout + r.stderr
+    err = r.stderr.splitlines()
+    col = {(): "HasInfo (Vertices + Edges) / Total Edges", ("THRESHOLD_WITHOUT_COUNT",): "HasInfo Edges / Total Edges",
+           ("THRESHOLD_WITHOUT_OUTDEGREES",): "HasInfo Vertices / Total Vertices"}[tuple(flags)]
+    assert err[0] == "Iteration,Selected Engine,Edge Phase Execution Time (ns)," + col
+    rows = [l.split(",") for l in err[1:] if l and l[0].isdigit()]
+    stat = {l.split("=")[0].strip(): int(l.split("=")[1]) for l in r.stdout.splitlines()
+            if "Iterations" in l and "=" in l}
+    assert len(rows) == stat["Total Iterations"]
+    assert sum(1 for x in rows if x[1] == "Pull") == stat["Pull-Based Iterations"]
+    assert [int(x[0]) for x in rows] == list(range(1, len(rows) + 1))
+    assert all(int(x[2]) > 0 for x in rows)
+    outdeg = rec["outdeg"][:V]
+    if app == "cc":
+        v0 = (V if "THRESHOLD_WITHOUT_COUNT" not in flags else 0) + (E if "THRESHOLD_WITHOUT_OUTDEGREES" not in flags else 0)
+    else:
+        v0 = (1 if "THRESHOLD_WITHOUT_COUNT" not in flags else 0) + (int(outdeg[0]) if "THRESHOLD_WITHOUT_OUTDEGREES" not in flags else 0)
+    comparator = V if "THRESHOLD_WITHOUT_OUTDEGREES" in flags else E
+    assert abs(float(rows[0][3]) - v0 / comparator) <= 1e-10  # printed with 10 decimals
+    thr = V // 2 if "THRESHOLD_WITHOUT_OUTDEGREES" in flags else E // 5
+    for x in rows:
+        vote = float(x[3]) * comparator  # the vote the engine was chosen on (10 decimals of the ratio)
+        if abs(vote - thr) > 1.0:
+            assert (x[1] == "Pull") == (vote > thr)

@@ -248,6 +248,8 @@ def run_native(a):
         else:
             G.load_pointers(V, E, pin_pull.data_ptr(), pin_push.data_ptr())
 
+    if a.pr_props:
+        G.tune(pr_props=a.pr_props)
     load()
     hbm, hbm_kind = measured_hbm()
     # kernel shapes for this graph, chosen by timing (outside every timed region)
@@ -256,6 +258,7 @@ def run_native(a):
         from grazelle import autotune
         tuned = autotune.tune_cc(G, device=local) if wl in ("cc", "bfs") else autotune.tune_pr(G, device=local)
         tuned.pop("trials", None)
+        tuned["gain"] = round(tuned["default_ms"] / tuned["best_ms"], 4) if tuned.get("default_ms") else None
 
     def barrier():
         if dist:
@@ -452,6 +455,12 @@ def pagerank_study(a, torch, stream, hbm, hbm_kind, scale=20):
     n = max(2, a.steps // 2)
     with Graph(torch.cuda.current_device(), stream=stream.cuda_stream) as G:
         G.load_pairs(V, pull, push)
+        if not a.no_tune:
+            from grazelle import autotune
+            t = autotune.tune_pr(G, device=torch.cuda.current_device())
+            res["autotuned"] = {"best": t["best"], "best_ms": round(t["best_ms"], 4),
+                                "default_ms": round(t["default_ms"], 4) if t["default_ms"] else None,
+                                "candidates": t["candidates"], "objective": t["objective"]}
         G.pr_init(0.875).pr_iterate(16)
         with Timer(torch, stream) as tp:
             for _ in range(n):
@@ -967,6 +976,8 @@ def main():
     ap.add_argument("--lean", action="store_true", help="host keeps only the -pull pairs (default from scale 26)")
     ap.add_argument("--ingest", choices=["pull", "both"], default="pull",
                     help="e2e input: the -pull pairs (the library derives the -push list) or both lists")
+    ap.add_argument("--pr-props", type=int, default=0, choices=[0, 1, 2],
+                    help="props the PageRank gather reads: 0 by size, 1 fixed point, 2 doubles (results identical)")
     ap.add_argument("--directed", action="store_true", help="CC/BFS on the directed R-MAT (no symmetrisation), as the scale-27 stress configuration")
     a = ap.parse_args()
     if a.warmup < 3:

@@ -381,6 +381,14 @@ __global__ void __launch_bounds__(256) k_msbfs_vertex(unsigned* __restrict__ nex
     if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(changed, cnt);
 }
 
+// %globaltimer into *out (one thread): the branch timers of the combined PPR + BFS graph
+__global__ void k_stamp(unsigned long long* __restrict__ out)
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    *out = t;
+}
+
 // end of a BFS iteration: stop when no bit changed or the bound is reached; next iteration number
 __global__ void k_msbfs_decide(unsigned long long* __restrict__ ctl, uint32_t* __restrict__ iter, uint32_t max_iter,
                                cudaGraphConditionalHandle loop)
@@ -441,7 +449,7 @@ struct grz_batch {
     uint32_t run_iters;
     double run_damping;
     int run_dmode;
-    cudaEvent_t run_ev[4];               // PPR start / end, BFS start / end (recorded inside the graph)
+    unsigned long long* stamps;          // PPR start / end, BFS start / end (%globaltimer, written inside the graph)
     int ppr_blocks, bfs_blocks;          // resident blocks per SM of the persistent kernels
     void* mail;                          // pinned host read-back
     char err[256];
@@ -486,10 +494,11 @@ extern "C" int grz_batch_create(grz_batch** out, int device, void* stream)
 
 static void free_state(grz_batch* b)
 {
-    void* p[] = { b->d_voff, b->d_seeds, b->d_roots, b->prop[0], b->prop[1], b->propd[0], b->propd[1], b->rank, b->rowacc, b->cut, b->S[0], b->S[1],
+    void* p[] = { b->d_voff, b->d_seeds, b->d_roots, b->stamps, b->prop[0], b->prop[1], b->propd[0], b->propd[1], b->rank, b->rowacc, b->cut, b->S[0], b->S[1],
                   b->visited, b->frontier, b->next_words, b->level, b->ctl, b->iter };
     for (void* x : p) cudaFree(x);
     b->d_voff = b->d_seeds = b->d_roots = nullptr;
+    b->stamps = nullptr;
     b->prop[0] = b->prop[1] = nullptr;
     b->propd[0] = b->propd[1] = nullptr;
     b->rank = nullptr;
@@ -512,8 +521,7 @@ extern "C" void grz_batch_destroy(grz_batch* b)
     cudaSetDevice(b->device);
     free_state(b);
     if (b->mail) cudaFreeHost(b->mail);
-    if (b->run_ev[0])
-        for (cudaEvent_t e : b->run_ev) cudaEventDestroy(e);
+
     grz_graph_destroy(b->u);
     delete b;
 }
@@ -831,8 +839,7 @@ static int end_capture_sink(grz_batch* b, cudaStream_t cs, cudaGraphNode_t* sink
 static int build_run_graph(grz_batch* b, uint32_t iterations, double damping, int dmode)
 {
     if (b->run_exec) { cudaGraphExecDestroy(b->run_exec); b->run_exec = nullptr; }
-    if (!b->run_ev[0])
-        for (cudaEvent_t& e : b->run_ev) BCK(b, cudaEventCreate(&e));
+    if (!b->stamps) BCK(b, cudaMalloc((void**)&b->stamps, 4 * sizeof(unsigned long long)));
     grz_graph* u = b->u;
     const uint64_t V = u->V;
     const uint64_t Vw = (V + 3) / 4 * 4;
@@ -845,14 +852,14 @@ static int build_run_graph(grz_batch* b, uint32_t iterations, double damping, in
     // branch 1: PPR
     if (!rc) rc = bck(b, cudaStreamBeginCaptureToGraph(cs, top, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal), "capture");
     if (!rc) {
-        cudaEventRecord(b->run_ev[0], cs);
+        k_stamp<<<1, 1, 0, cs>>>(b->stamps + 0);
         if (dmode) cudaMemsetAsync(b->propd[0], 0, sizeof(double) * V * K, cs);
         else cudaMemsetAsync(b->prop[0], 0, sizeof(u128) * V * K, cs);
         k_ppr_init<<<(G * K + 255) / 256, 256, 0, cs>>>(b->d_seeds, G, u->inv_deg, u->degree, b->prop[0], dmode ? b->propd[0] : nullptr,
                                                         b->S[0]);
         rc = bck(b, cudaGetLastError(), "ppr init");
         if (!rc) rc = enqueue_ppr_chain(b, cs, iterations, damping, dmode, b->d_seeds, &cur);
-        cudaEventRecord(b->run_ev[1], cs);
+        k_stamp<<<1, 1, 0, cs>>>(b->stamps + 1);
         const int rc2 = end_capture_sink(b, cs, nullptr);
         if (!rc) rc = rc2;
     }
@@ -860,7 +867,7 @@ static int build_run_graph(grz_batch* b, uint32_t iterations, double damping, in
     cudaGraphNode_t init = nullptr, loop = nullptr;
     if (!rc) rc = bck(b, cudaStreamBeginCaptureToGraph(cs, top, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal), "capture");
     if (!rc) {
-        cudaEventRecord(b->run_ev[2], cs);
+        k_stamp<<<1, 1, 0, cs>>>(b->stamps + 2);
         cudaMemsetAsync(b->visited, 0, Vw, cs);
         cudaMemsetAsync(b->frontier, 0, Vw, cs);
         cudaMemsetAsync(b->next_words, 0, Vw, cs);
@@ -874,8 +881,10 @@ static int build_run_graph(grz_batch* b, uint32_t iterations, double damping, in
     if (!rc) rc = add_bfs_loop(b, top, &init, 1, &loop);
     if (!rc) rc = bck(b, cudaStreamBeginCaptureToGraph(cs, top, &loop, nullptr, 1, cudaStreamCaptureModeThreadLocal), "capture");
     if (!rc) {
-        cudaEventRecord(b->run_ev[3], cs);
-        rc = end_capture_sink(b, cs, nullptr);
+        k_stamp<<<1, 1, 0, cs>>>(b->stamps + 3);
+        rc = bck(b, cudaGetLastError(), "stamp");
+        const int rc2 = end_capture_sink(b, cs, nullptr);
+        if (!rc) rc = rc2;
     }
     if (cs) cudaStreamDestroy(cs);
     if (!rc) rc = bck(b, cudaGraphInstantiate(&b->run_exec, top, 0), "instantiate");
@@ -986,6 +995,8 @@ extern "C" int grz_batch_run(grz_batch* b, const uint32_t* seeds, uint32_t k, ui
     if (!rc) rc = bck(b, cudaGraphLaunch(b->run_exec, st), "graph launch");
     if (!rc) rc = bck(b, cudaEventRecord(e1, st), "event");
     if (!rc) rc = bck(b, cudaMemcpyAsync(b->mail, b->ctl, sizeof(unsigned long long) * 3, cudaMemcpyDeviceToHost, st), "D2H");
+    if (!rc) rc = bck(b, cudaMemcpyAsync((unsigned long long*)b->mail + 4, b->stamps, 4 * sizeof(unsigned long long),
+                                         cudaMemcpyDeviceToHost, st), "D2H");
     if (!rc && ranks_out) {
         if (k == (uint32_t)K) {
             rc = bck(b, cudaMemcpyAsync(ranks_out, b->rank, sizeof(double) * V * K, cudaMemcpyDeviceToHost, st), "D2H");
@@ -1007,15 +1018,16 @@ extern "C" int grz_batch_run(grz_batch* b, const uint32_t* seeds, uint32_t k, ui
     if (!rc && c[2] == 1) rc = bset(b, GRZ_ERR_TIMEOUT, "BFS did not converge within V + 1 iterations");
     if (!rc && c[2] == 2) rc = bset(b, GRZ_ERR_TIMEOUT, "BFS stopped by its time bound");
     if (!rc) {
+        const unsigned long long* ts = (const unsigned long long*)b->mail + 4;
         if (ppr_stats) {
             memset(ppr_stats, 0, sizeof(*ppr_stats));
             ppr_stats->iterations = ppr_stats->pull_iterations = iterations;
-            cudaEventElapsedTime(&ppr_stats->ms, b->run_ev[0], b->run_ev[1]);
+            ppr_stats->ms = (float)((double)(ts[1] - ts[0]) * 1e-6);
         }
         if (bfs_stats) {
             memset(bfs_stats, 0, sizeof(*bfs_stats));
             bfs_stats->iterations = bfs_stats->pull_iterations = (uint32_t)c[1] + 1;
-            cudaEventElapsedTime(&bfs_stats->ms, b->run_ev[2], b->run_ev[3]);
+            bfs_stats->ms = (float)((double)(ts[3] - ts[2]) * 1e-6);
         }
         if (total_ms) cudaEventElapsedTime(total_ms, e0, e1);
     }

@@ -1,9 +1,10 @@
 """Autotuner: kernel shapes chosen per loaded graph (or batch) by timing them on the device.
 
 The knobs (include/grazelle_gb300.h, GRZ_TUNE_* and GRZ_BATCH_TUNE_*) change only speed:
-block size and persistent grid of the CC pull kernel, persistent grid of the PageRank gather,
-resident blocks per SM of the batch kernels, and the optional hub-source encoding.  Each
-candidate is timed with the library's CUDA-event kernel profiler (or the run statistics), the
+block size, persistent grid and edge-stream staging of the CC pull kernel, the PageRank
+iteration's form (two kernels or one persistent launch) and gather grid, resident blocks per SM
+of the batch kernels, and the optional hub-source encoding.  Each candidate is timed on the
+device (the run statistics' or CUDA-event times of the whole run or iteration sequence), the
 median of a few trials is kept, and the fastest candidate is applied.  The default shape is
 always one of the candidates, so tuning never makes a kernel slower than the default by more
 than the measurement noise.
@@ -36,53 +37,71 @@ def _kernel_ms(G, kind: str, run, trials: int) -> float:
     return statistics.median(vals) if vals else float("inf")
 
 
-def tune_cc(G, trials: int = 3, threads=(256, 512, 1024), grids_per_sm=(0, 1, 2, 4), caches=(0,), device: int = 0) -> dict:
-    """CC pull kernel: block size x persistent grid (x hub-label cache when hubs are loaded).
-    Times the pull edge phase of a full CC run with the pull engine forced."""
+def _median_ms(run, trials: int) -> float:
+    return statistics.median(run() for _ in range(trials))
+
+
+def tune_cc(G, trials: int = 3, threads=(256, 512, 1024), grids_per_sm=(0, 1, 2, 4), caches=(0,), stagings=(0, 1),
+            device: int = 0) -> dict:
+    """CC: pull-kernel block size x persistent grid x edge-stream staging (streaming loads or bulk
+    copies into shared memory) (x hub-label cache when hubs are loaded).  The objective is the
+    whole run to convergence (one CUDA graph launch, device time), which is what the knobs are
+    for: the first pull scans every vector, the later ones skip converged destinations."""
     sms = _sms(device)
     start = G.tuning()
-    flags = native.FORCE_PULL | native.FLAG_HOST_LOOP
 
     def run():
-        G.cc_run(flags)
+        return G.cc_run().ms
 
     run()  # warm-up
     trials_out = []
     for th in threads:
         for gps in grids_per_sm:
-            for cache in caches:
-                if cache and start["hubs_loaded"] == 0:
-                    continue
-                G.tune(cc_threads=th, cc_grid=gps * sms, cc_cache=cache)
-                ms = _kernel_ms(G, "cc_pull", run, trials)
-                trials_out.append({"cc_threads": th, "cc_grid": gps * sms, "cc_cache": cache, "ms": ms})
+            for stg in stagings:
+                for cache in caches:
+                    if cache and start["hubs_loaded"] == 0:
+                        continue
+                    G.tune(cc_threads=th, cc_grid=gps * sms, cc_cache=cache, pull_staging=stg)
+                    run()  # the run graph is captured again for a new shape
+                    trials_out.append({"cc_threads": th, "cc_grid": gps * sms, "cc_cache": cache, "pull_staging": stg,
+                                       "ms": _median_ms(run, trials)})
+    keys = ("cc_threads", "cc_grid", "cc_cache", "pull_staging")
     default = next((t for t in trials_out if t["cc_threads"] == start["cc_threads"] and t["cc_grid"] == start["cc_grid"]
-                    and t["cc_cache"] == (start["cc_cache"] if start["hubs_loaded"] else 0)), None)
+                    and t["cc_cache"] == (start["cc_cache"] if start["hubs_loaded"] else 0)
+                    and t["pull_staging"] == start["pull_staging"]), None)
     best = min(trials_out, key=lambda t: t["ms"])
-    G.tune(cc_threads=best["cc_threads"], cc_grid=best["cc_grid"], cc_cache=best["cc_cache"])
-    return {"kernel": "cc_pull", "best": {k: best[k] for k in ("cc_threads", "cc_grid", "cc_cache")},
+    G.tune(**{k: best[k] for k in keys})
+    return {"objective": "cc run to convergence", "best": {k: best[k] for k in keys},
             "best_ms": best["ms"], "default_ms": default["ms"] if default else None, "candidates": len(trials_out),
             "trials": trials_out}
 
 
-def tune_pr(G, trials: int = 3, grids_per_sm=(0, 1, 2, 4, 8), iterations: int = 4, device: int = 0) -> dict:
-    """PageRank gather: persistent grid.  Times `iterations` fused iterations."""
+def tune_pr(G, trials: int = 3, grids_per_sm=(0, 1, 2, 4, 8), forms=(1, 2, 3), iterations: int = 8, device: int = 0) -> dict:
+    """PageRank: the iteration's form (two kernels, or one persistent cooperative launch with 6
+    or 8 blocks per SM) x the gather's persistent grid.  The objective is the device time of
+    `iterations` iterations."""
     sms = _sms(device)
     start = G.tuning()
 
     def run():
-        G.pr_init(0.875).pr_iterate(iterations)
+        G.pr_init(0.875)
+        return G.pr_time(iterations)
 
     run()
     trials_out = []
-    for gps in grids_per_sm:
-        G.tune(pr_grid=gps * sms)
-        trials_out.append({"pr_grid": gps * sms, "ms": _kernel_ms(G, "pr_gather", run, trials)})
-    default = next((t for t in trials_out if t["pr_grid"] == start["pr_grid"]), None)
+    for form in forms:
+        for gps in grids_per_sm:
+            G.tune(pr_persistent=form, pr_grid=gps * sms)
+            run()
+            trials_out.append({"pr_persistent": form, "pr_grid": gps * sms, "ms": _median_ms(run, trials)})
+    default_form = start["pr_persistent"] or 1
+    default = next((t for t in trials_out if t["pr_grid"] == start["pr_grid"] and t["pr_persistent"] == default_form), None)
     best = min(trials_out, key=lambda t: t["ms"])
-    G.tune(pr_grid=best["pr_grid"])
-    return {"kernel": "pr_gather", "best": {"pr_grid": best["pr_grid"]}, "best_ms": best["ms"],
-            "default_ms": default["ms"] if default else None, "candidates": len(trials_out), "trials": trials_out}
+    G.tune(pr_persistent=best["pr_persistent"], pr_grid=best["pr_grid"])
+    return {"objective": "%d PageRank iterations" % iterations, "best": {"pr_persistent": best["pr_persistent"],
+                                                                       "pr_grid": best["pr_grid"]},
+            "best_ms": best["ms"], "default_ms": default["ms"] if default else None, "candidates": len(trials_out),
+            "trials": trials_out}
 
 
 def tune_batch(B, seeds, iterations: int = 5, trials: int = 2, blocks=(2, 4, 8, 16)) -> dict:

@@ -18,12 +18,14 @@ def test_tune_cc_and_pr_keep_results():
         lab0 = G.connected_components()
         pr0 = G.pagerank(5)
         rep = autotune.tune_cc(G, trials=2, threads=(256, 512), grids_per_sm=(0, 1))
-        assert rep["candidates"] == 4
+        assert rep["candidates"] == 8
         assert rep["best_ms"] <= rep["default_ms"]
         t = G.tuning()
-        assert t["cc_threads"] == rep["best"]["cc_threads"] and t["cc_grid"] == rep["best"]["cc_grid"]
+        assert all(t[k] == v for k, v in rep["best"].items())
         rep2 = autotune.tune_pr(G, trials=2, grids_per_sm=(0, 2))
-        assert G.tuning()["pr_grid"] == rep2["best"]["pr_grid"]
+        assert rep2["candidates"] == 6 and rep2["best_ms"] <= rep2["default_ms"]
+        t = G.tuning()
+        assert t["pr_grid"] == rep2["best"]["pr_grid"] and t["pr_persistent"] == rep2["best"]["pr_persistent"]
         np.testing.assert_array_equal(G.connected_components(), lab0)
         np.testing.assert_array_equal(G.pagerank(5), pr0)
 

@@ -343,4 +343,4 @@ def test_bulk_staged_pull_gives_the_same_labels(threads):
         G.tune(pull_staging=1, cc_threads=threads)
         np.testing.assert_array_equal(G.connected_components(), ref)
         np.testing.assert_array_equal(G.connected_components(native.FLAG_HOST_LOOP), ref)
-        np.testing.assert_array_equal(G.connected_components(native.FLAG_FORCE_PULL), ref)
+        np.testing.assert_array_equal(G.connected_components(native.FORCE_PULL), ref)

@@ -250,6 +250,9 @@ def run_native(a):
 
     if a.pr_props:
         G.tune(pr_props=a.pr_props)
+    for kv in a.tune:
+        k, v = kv.split("=", 1)
+        G.tune(**{k: int(v)})
     load()
     hbm, hbm_kind = measured_hbm()
     # kernel shapes for this graph, chosen by timing (outside every timed region)
@@ -976,6 +979,8 @@ def main():
     ap.add_argument("--lean", action="store_true", help="host keeps only the -pull pairs (default from scale 26)")
     ap.add_argument("--ingest", choices=["pull", "both"], default="pull",
                     help="e2e input: the -pull pairs (the library derives the -push list) or both lists")
+    ap.add_argument("--tune", action="append", default=[], metavar="KNOB=VALUE",
+                    help="kernel-shape knob applied before the load (grazelle.engine.Graph.tune), e.g. pull_staging=1; repeatable")
     ap.add_argument("--pr-props", type=int, default=0, choices=[0, 1, 2],
                     help="props the PageRank gather reads: 0 by size, 1 fixed point, 2 doubles (results identical)")
     ap.add_argument("--directed", action="store_true", help="CC/BFS on the directed R-MAT (no symmetrisation), as the scale-27 stress configuration")

@@ -123,6 +123,13 @@ static void free_graph_data(grz_graph* g, uint64_t next_V = ~0ull)
         g->pr_fx[0] = g->pr_fx[1] = nullptr; g->pr_sum = nullptr; g->pr_K = nullptr; g->pr_rowacc = nullptr;
         g->pr_cut = nullptr;
     }
+    grz_dev_free(g, g->seg_nbr);
+    grz_dev_free(g, g->seg_dst);
+    g->seg_nbr = nullptr;
+    g->seg_dst = nullptr;
+    g->seg_bits = 0;
+    g->nseg = 0;
+    g->pr_segmode = 0;
     g->pr_dmode = g->pr_fx_stale = g->pr_d_stale = 0;
     g->outdeg = nullptr; g->degree = nullptr; g->inv_deg = nullptr;
     g->pr_rowacc_stale = 0;
@@ -885,6 +892,15 @@ extern "C" int grz_tune_set(grz_graph* g, int param, int64_t value)
         if (value > 1) return grz_set_error(g, GRZ_ERR_ARG, "pull staging must be 0 (loads) or 1 (bulk copies)");
         g->tune.pull_staging = (uint32_t)value;
         return GRZ_OK;
+    case GRZ_TUNE_PR_BLOCKS:
+        if (value != 0 && value != 6 && value != 8) return grz_set_error(g, GRZ_ERR_ARG, "PageRank gather shape must be 0, 6 or 8 blocks per SM");
+        g->tune.pr_blocks = (uint32_t)value;
+        return GRZ_OK;
+    case GRZ_TUNE_PR_SEGMENT_BITS:
+        if (value > 31 || (value > 1 && value < 8))
+            return grz_set_error(g, GRZ_ERR_ARG, "PageRank segment bits must be 0 (by size), 1 (none) or 8..31");
+        g->tune.pr_segment_bits = (uint32_t)value;  // from the next grz_pr_init
+        return GRZ_OK;
     case GRZ_TUNE_RUN_LIMIT_US:
         if (value > 3600000000ll) return grz_set_error(g, GRZ_ERR_RANGE, "run time bound above one hour");
         g->tune.run_limit_us = (uint32_t)value;
@@ -912,6 +928,8 @@ extern "C" int grz_tune_get(const grz_graph* g, int param, int64_t* value)
     case GRZ_TUNE_RUN_MAX_ITERATIONS: *value = g->tune.run_max_iterations; return GRZ_OK;
     case GRZ_TUNE_RUN_LIMIT_US: *value = g->tune.run_limit_us; return GRZ_OK;
     case GRZ_TUNE_PULL_STAGING: *value = g->tune.pull_staging; return GRZ_OK;
+    case GRZ_TUNE_PR_SEGMENT_BITS: *value = g->tune.pr_segment_bits; return GRZ_OK;
+    case GRZ_TUNE_PR_BLOCKS: *value = g->tune.pr_blocks; return GRZ_OK;
     case GRZ_TUNE_HUBS_LOADED: *value = g->pull.nhub; return GRZ_OK;
     default: return GRZ_ERR_ARG;
     }

@@ -248,6 +248,7 @@ struct grz_list {
 #define GRZ_HUB_BASE 0x80000000u
 #define GRZ_HUB_MAX 49152u
 #define GRZ_INGEST_MAX_CHUNKS 64
+#define GRZ_PR_MAX_SEGMENTS 256
 
 #define GRZ_BATCH_K 8  // instances per graph of a batch (grz_batch.cu)
 
@@ -293,6 +294,8 @@ struct grz_mlp;
 #define GRZ_TUNE_RUN_MAX_ITERATIONS 11
 #define GRZ_TUNE_RUN_LIMIT_US 12
 #define GRZ_TUNE_PULL_STAGING 13
+#define GRZ_TUNE_PR_SEGMENT_BITS 14
+#define GRZ_TUNE_PR_BLOCKS 15
 #define GRZ_TUNE_HUBS_LOADED 100
 
 // kernel shapes chosen per graph (grz_tune_set; the autotuner searches them)
@@ -311,6 +314,8 @@ struct grz_tuning {
     uint32_t run_max_iterations;  // CC/BFS iteration bound (0: V + 2)
     uint32_t run_limit_us;   // CC/BFS time bound of a run in microseconds (0: 300 s)
     uint32_t pull_staging;   // CC pull's edge stream: 0 plain streaming loads, 1 bulk copies into shared memory
+    uint32_t pr_segment_bits;  // PageRank source segments: 0 by size, 1 none, b in [8, 31]: 2^b sources per segment
+    uint32_t pr_blocks;   // PageRank gather's register shape: 0 or 8 (32 registers, 8 blocks per SM), 6 (38, no spill)
 };
 
 // Device control block of a CC/BFS run executed as one CUDA graph (grz_ccbfs.cu): the
@@ -414,6 +419,15 @@ struct grz_graph {
     int pr_rowacc_stale;  // fused iterations cleared only the straddling accumulators
     int pr_lists_changed; // the PageRank arrays were kept across a reload with the same V
     uint32_t pr_nparts[2];  // partials in each half of pr_sum
+    // source-segmented pull lists (grz_pr.cu): vectors of the edges whose source lies in segment s
+    // (sources [s << seg_bits, (s + 1) << seg_bits)), grouped by destination, concatenated in
+    // segment order; built at grz_pr_init when the gathered props exceed L2
+    uint32_t seg_bits;    // 0: not built
+    uint32_t nseg;
+    uint64_t seg_first[GRZ_PR_MAX_SEGMENTS + 1];
+    uint4* seg_nbr;
+    uint32_t* seg_dst;
+    int pr_segmode;       // fused iterations gather segment by segment
     void* pr_bar;         // grid barrier and phase timer of the persistent PageRank kernel (device)
     void* pr_bar_host;    // pinned read-back of its error word and phase times
     double* pr_d[2];      // double[V+1]: the props as doubles, gathered instead of pr_fx in pr_dmode

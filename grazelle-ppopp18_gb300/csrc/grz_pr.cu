@@ -26,6 +26,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <vector>
 
 #include "grz_internal.cuh"
 
@@ -112,7 +113,22 @@ __device__ __forceinline__ void pr_publish_K(const PRConst& pc, u128* red)
 }
 
 // The gather over tiles blockIdx.x, blockIdx.x + nblocks, ... of PR_THREADS vectors.
-template <typename P, bool COH>
+// ADD: the accumulators already hold the sums of earlier launches (source segments); a destination
+// owned by one warp or block is added by a plain read-modify-write, one cut by a tile edge atomically.
+__device__ __forceinline__ void rowacc_put(u128* rowacc, uint32_t key, u128 val, bool add)
+{
+    ulonglong2* p = reinterpret_cast<ulonglong2*>(rowacc) + key;
+    if (add) {
+        const ulonglong2 o = __ldcg(p);
+        u128 a;
+        a.lo = o.x;
+        a.hi = o.y;
+        val = u128_add(val, a);
+    }
+    __stcg(p, make_ulonglong2(val.lo, val.hi));
+}
+
+template <typename P, bool COH, bool ADD = false>
 __device__ __forceinline__ void pr_gather_tiles(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv, uint64_t first,
                                                 uint64_t nvec, uint64_t list_nvec, const P* __restrict__ prop_fx, uint32_t V,
                                                 u128* __restrict__ rowacc, const uint32_t* __restrict__ hub_vid, uint32_t nhub,
@@ -120,12 +136,14 @@ __device__ __forceinline__ void pr_gather_tiles(const uint4* __restrict__ nbr, c
 {
     constexpr int NW = GatherSmem::NW;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint64_t ntiles = (nvec + PR_THREADS - 1) / PR_THREADS;
-    for (uint64_t tile = block; tile < ntiles; tile += nblocks) {
+    // vector indices stay below 2^32 (the lists' limit), so the index arithmetic is 32-bit
+    const uint32_t ntiles = (uint32_t)((nvec + PR_THREADS - 1) / PR_THREADS);
+    const uint32_t first32 = (uint32_t)first, nvec32 = (uint32_t)nvec, list32 = (uint32_t)list_nvec;
+    for (uint32_t tile = block; tile < ntiles; tile += nblocks) {
         if (lane < 2) sm.flag[lane][warp] = 0;
-        const uint64_t i = tile * PR_THREADS + threadIdx.x;
-        const uint64_t v = first + i;
-        const bool live = i < nvec;
+        const uint32_t i = tile * PR_THREADS + threadIdx.x;
+        const uint32_t v = first32 + i;
+        const bool live = i < nvec32;
         uint32_t key = 0xffffffffu;
         u128 val = u128_zero();
         if (live) {
@@ -144,7 +162,7 @@ __device__ __forceinline__ void pr_gather_tiles(const uint4* __restrict__ nbr, c
         // neighbours across the warp edge come from the whole list, so a destination cut by the edge of
         // a caller's vector range is also added atomically, from both sides
         if (lane == 0) prevkey = (live && v > 0) ? __ldg(dstv + v - 1) : 0xfffffffeu;
-        if (lane == 31) nextkey = (live && v + 1 < list_nvec) ? __ldg(dstv + v + 1) : 0xfffffffeu;
+        if (lane == 31) nextkey = (live && v + 1 < list32) ? __ldg(dstv + v + 1) : 0xfffffffeu;
         const bool head = key != prevkey;  // the previous vector has another destination
         const bool tail = key != nextkey;  // the next vector has another destination
         const unsigned real_heads = __ballot_sync(0xffffffffu, head);
@@ -160,7 +178,7 @@ __device__ __forceinline__ void pr_gather_tiles(const uint4* __restrict__ nbr, c
             const bool head_real = (real_heads >> segstart) & 1u;
             if (tail && head_real) {
                 // every vector of this destination is in this warp
-                __stcg(reinterpret_cast<ulonglong2*>(rowacc) + key, make_ulonglong2(val.lo, val.hi));
+                rowacc_put(rowacc, key, val, ADD);
             } else {
                 // open on the left (slot 0) or on the right only (slot 1): combined across the block below
                 const int slot = (segstart == 0 && !head_real) ? 0 : 1;
@@ -183,7 +201,7 @@ __device__ __forceinline__ void pr_gather_tiles(const uint4* __restrict__ nbr, c
                     if (!open) { open = true; open_head = false; ok = sm.key[0][w]; os = u128_zero(); }
                     os = u128_add(os, sm.sum[0][w]);
                     if (f0 & 4u) {
-                        if (open_head) __stcg(reinterpret_cast<ulonglong2*>(rowacc) + ok, make_ulonglong2(os.lo, os.hi));
+                        if (open_head) rowacc_put(rowacc, ok, os, ADD);
                         else if (os.lo | os.hi) u128_atomic_add(rowacc + ok, os);
                         open = false;
                     }
@@ -197,15 +215,17 @@ __device__ __forceinline__ void pr_gather_tiles(const uint4* __restrict__ nbr, c
     }
 }
 
-template <typename P>
-__global__ void __launch_bounds__(PR_THREADS) k_pr_gather(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv,
+// MINB resident blocks per SM asked of the compiler: 8 keeps 32 registers (the most gathers in
+// flight; a 16-byte spill of the fixed-point form), 1 lets it take 38 (no spill, 6 blocks per SM)
+template <typename P, bool ADD = false, int MINB = 8>
+__global__ void __launch_bounds__(PR_THREADS, MINB) k_pr_gather(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv,
                                                           uint64_t first, uint64_t nvec, uint64_t list_nvec,
                                                           const P* __restrict__ prop_fx, uint32_t V, u128* __restrict__ rowacc,
                                                           const uint32_t* __restrict__ hub_vid, uint32_t nhub, const PRConst pc)
 {
     __shared__ GatherSmem sm;
     if (pc.K_out && blockIdx.x == 0) pr_publish_K(pc, sm.red);
-    pr_gather_tiles<P, false>(nbr, dstv, first, nvec, list_nvec, prop_fx, V, rowacc, hub_vid, nhub, blockIdx.x, gridDim.x, sm);
+    pr_gather_tiles<P, false, ADD>(nbr, dstv, first, nvec, list_nvec, prop_fx, V, rowacc, hub_vid, nhub, blockIdx.x, gridDim.x, sm);
 }
 
 __device__ __forceinline__ u128 block_reduce_u128(u128 s, u128* red)
@@ -240,7 +260,7 @@ constexpr int PR_APPLY_RESIDENT = 3;  // blocks per SM that the launch bounds fi
 // thread loaded before any is stored; returns the block's partial of S' (valid in thread 0;
 // every thread of the block must call it)
 template <int U>
-__device__ __forceinline__ u128 pr_apply_range(u128* __restrict__ rowacc, const uint32_t* __restrict__ cut,
+__device__ __forceinline__ u128 pr_apply_range(u128* __restrict__ rowacc, const uint32_t* __restrict__ cut, bool clear_all,
                                                const double* __restrict__ inv_deg, const uint32_t* __restrict__ degree, uint64_t V,
                                                double sK, double damping, u128* __restrict__ prop_fx, double* __restrict__ prop_d,
                                                double* __restrict__ prop_out, uint32_t block, uint32_t nblocks, u128* red)
@@ -257,14 +277,14 @@ __device__ __forceinline__ u128 pr_apply_range(u128* __restrict__ rowacc, const 
             cw[j] = 0;
             if (v < V) {
                 a[j] = __ldcs(reinterpret_cast<const ulonglong2*>(rowacc) + v);
-                cw[j] = __ldg(cut + (v >> 5));
+                cw[j] = clear_all ? 0u : __ldg(cut + (v >> 5));
             }
         }
 #pragma unroll
         for (int j = 0; j < U; ++j) {
             const uint64_t v = base + (uint64_t)j * stride;
             if (v >= V) break;
-            if ((a[j].x | a[j].y) && ((cw[j] >> (v & 31)) & 1u))
+            if ((a[j].x | a[j].y) && (clear_all || ((cw[j] >> (v & 31)) & 1u)))
                 *(reinterpret_cast<ulonglong2*>(rowacc) + v) = make_ulonglong2(0ull, 0ull);
             u128 acc;
             acc.lo = a[j].x;
@@ -281,14 +301,14 @@ __device__ __forceinline__ u128 pr_apply_range(u128* __restrict__ rowacc, const 
 }
 
 __global__ void __launch_bounds__(PR_THREADS, PR_APPLY_RESIDENT) k_pr_apply(u128* __restrict__ rowacc, const uint32_t* __restrict__ cut,
-                                                                            const double* __restrict__ inv_deg,
+                                                                            int clear_all, const double* __restrict__ inv_deg,
                                                                             const uint32_t* __restrict__ degree, uint64_t V,
                                                                             const double* __restrict__ Kp, u128* __restrict__ part_out,
                                                                             double damping, u128* __restrict__ prop_fx,
                                                                             double* __restrict__ prop_d, double* __restrict__ prop_out)
 {
     __shared__ u128 red[PR_THREADS / 32];
-    const u128 s = pr_apply_range<PR_APPLY_U>(rowacc, cut, inv_deg, degree, V, *Kp, damping, prop_fx, prop_d, prop_out, blockIdx.x, gridDim.x,
+    const u128 s = pr_apply_range<PR_APPLY_U>(rowacc, cut, clear_all != 0, inv_deg, degree, V, *Kp, damping, prop_fx, prop_d, prop_out, blockIdx.x, gridDim.x,
                                   red);
     if (threadIdx.x == 0) part_out[blockIdx.x] = s;  // summed by the next gather kernel's block 0
 }
@@ -413,7 +433,7 @@ __global__ void __launch_bounds__(PR_THREADS, MINB) k_pr_persistent(const PRPers
         if (!pr_grid_barrier(q.bar, nb, q.limit_ns, ++bi, (int)blockIdx.x == q.withhold_block)) return;
         const unsigned long long t1 = (q.time_phases && blockIdx.x == 0 && threadIdx.x == 0) ? pr_now_ns() : 0ull;
         const double sK = *(volatile double*)q.K;
-        const u128 s = pr_apply_range<PR_PERSIST_APPLY_U>(q.rowacc, q.cut, q.inv_deg, q.degree, q.V, sK, q.damping, q.fx[cur ^ 1],
+        const u128 s = pr_apply_range<PR_PERSIST_APPLY_U>(q.rowacc, q.cut, false, q.inv_deg, q.degree, q.V, sK, q.damping, q.fx[cur ^ 1],
                                       q.dmode ? q.d[cur ^ 1] : nullptr, it + 1 == q.iters ? q.prop_out : nullptr, blockIdx.x, nb,
                                       sm.red);
         if (threadIdx.x == 0) q.sum[sc ^ 1][blockIdx.x] = s;
@@ -441,6 +461,126 @@ __global__ void k_pr_cutbits(const uint32_t* __restrict__ rowptr, uint64_t V, ui
     }
     const unsigned m = __ballot_sync(0xffffffffu, c);
     if ((threadIdx.x & 31) == 0 && v < V) cut[v >> 5] = m;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Source-segmented pull lists.  A destination's in-edges are its vectors' lanes in order, sorted
+// by source (the -pull order), so the edges from source segment s form one run of lanes
+// [a_s, b_s).  Segment s's list has ceil((b_s - a_s) / 4) vectors per destination, grouped by
+// destination in ascending order; the segment lists are concatenated in segment order.
+
+// source of lane L of a destination whose vectors start at r0
+__device__ __forceinline__ uint32_t lane_src(const uint32_t* __restrict__ nbr32, uint32_t r0, uint32_t L)
+{
+    return __ldg(nbr32 + (uint64_t)r0 * 4 + L);
+}
+
+// valid lanes of the destination with vectors [r0, r1) (only its last vector can be partial)
+__device__ __forceinline__ uint32_t dst_lanes(const uint4* __restrict__ nbr, uint32_t r0, uint32_t r1)
+{
+    const uint4 t = __ldg(nbr + r1 - 1);
+    return 4 * (r1 - r0 - 1) + (t.x != GRZ_INVALID_ID) + (t.y != GRZ_INVALID_ID) + (t.z != GRZ_INVALID_ID) + (t.w != GRZ_INVALID_ID);
+}
+
+// first lane in [lo, hi) whose source is >= key, else hi
+__device__ __forceinline__ uint32_t lane_lower_bound(const uint32_t* __restrict__ nbr32, uint32_t r0, uint32_t lo, uint32_t hi,
+                                                     uint64_t key)
+{
+    while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        if ((uint64_t)lane_src(nbr32, r0, mid) < key) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// first lane at or after p + 1 whose source is >= key (lane p's source is below key): galloping,
+// then a binary search, so a run of n lanes costs O(log n) reads
+__device__ __forceinline__ uint32_t lane_gallop(const uint32_t* __restrict__ nbr32, uint32_t r0, uint32_t p, uint32_t L, uint64_t key)
+{
+    uint32_t lo = p + 1, step = 1, hi = p + 1;
+    while (hi < L && (uint64_t)lane_src(nbr32, r0, hi) < key) {
+        lo = hi + 1;
+        step <<= 1;
+        hi = (p + step < L) ? p + step : L;
+    }
+    return lane_lower_bound(nbr32, r0, lo, hi < L ? hi : L, key);
+}
+
+// vectors of every (segment, destination): cnt[s * (V + 1) + d]; entries of empty pairs stay 0
+__global__ void k_seg_count(const uint4* __restrict__ nbr, const uint32_t* __restrict__ rowptr, uint32_t V, uint32_t bits,
+                            uint32_t* __restrict__ cnt)
+{
+    const uint32_t* nbr32 = reinterpret_cast<const uint32_t*>(nbr);
+    for (uint64_t d = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; d < V; d += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t r0 = __ldg(rowptr + d), r1 = __ldg(rowptr + d + 1);
+        if (r0 == r1) continue;
+        const uint32_t L = dst_lanes(nbr, r0, r1);
+        uint32_t p = 0;
+        while (p < L) {
+            const uint32_t sg = lane_src(nbr32, r0, p) >> bits;
+            const uint32_t q = lane_gallop(nbr32, r0, p, L, (uint64_t)(sg + 1) << bits);
+            cnt[(uint64_t)sg * (V + 1) + d] = (q - p + 3) / 4;
+            p = q;
+        }
+    }
+}
+
+// run of one (segment, destination) pair too long for one thread: written by a whole block
+struct SegBig {
+    uint32_t d, a, b, out;  // destination, lanes [a, b), first output vector (within the segment)
+};
+constexpr uint32_t SEG_BIG_VECTORS = 32;
+
+__device__ __forceinline__ void seg_write_vector(const uint32_t* __restrict__ nbr32, uint32_t r0, uint32_t a, uint32_t b, uint32_t j,
+                                                 uint32_t d, uint4* __restrict__ out_nbr, uint32_t* __restrict__ out_dst, uint64_t o)
+{
+    const uint32_t L0 = a + 4 * j;
+    uint4 v;
+    v.x = L0 + 0 < b ? lane_src(nbr32, r0, L0 + 0) : GRZ_INVALID_ID;
+    v.y = L0 + 1 < b ? lane_src(nbr32, r0, L0 + 1) : GRZ_INVALID_ID;
+    v.z = L0 + 2 < b ? lane_src(nbr32, r0, L0 + 2) : GRZ_INVALID_ID;
+    v.w = L0 + 3 < b ? lane_src(nbr32, r0, L0 + 3) : GRZ_INVALID_ID;
+    out_nbr[o] = v;
+    out_dst[o] = d;
+}
+
+// segment sg: each destination with a run writes its vectors at base + off[d]; runs of more than
+// SEG_BIG_VECTORS vectors are listed for k_seg_write_big instead
+__global__ void k_seg_write(const uint4* __restrict__ nbr, const uint32_t* __restrict__ rowptr, uint32_t V, uint32_t bits, uint32_t sg,
+                            const uint32_t* __restrict__ off, uint64_t base, uint4* __restrict__ out_nbr, uint32_t* __restrict__ out_dst,
+                            SegBig* __restrict__ big, uint32_t* __restrict__ nbig)
+{
+    const uint32_t* nbr32 = reinterpret_cast<const uint32_t*>(nbr);
+    for (uint64_t d = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; d < V; d += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t o0 = __ldg(off + d), n = __ldg(off + d + 1) - o0;
+        if (n == 0) continue;
+        const uint32_t r0 = __ldg(rowptr + d), r1 = __ldg(rowptr + d + 1);
+        const uint32_t L = dst_lanes(nbr, r0, r1);
+        const uint32_t a = lane_lower_bound(nbr32, r0, 0, L, (uint64_t)sg << bits);
+        const uint32_t b = lane_lower_bound(nbr32, r0, a, L, (uint64_t)(sg + 1) << bits);
+        if (n > SEG_BIG_VECTORS) {
+            const uint32_t k = atomicAdd(nbig, 1u);
+            SegBig e;
+            e.d = (uint32_t)d; e.a = a; e.b = b; e.out = o0;
+            big[k] = e;
+            continue;
+        }
+        for (uint32_t j = 0; j < n; ++j) seg_write_vector(nbr32, r0, a, b, j, (uint32_t)d, out_nbr, out_dst, base + o0 + j);
+    }
+}
+
+__global__ void k_seg_write_big(const uint4* __restrict__ nbr, const uint32_t* __restrict__ rowptr, const SegBig* __restrict__ big,
+                                const uint32_t* __restrict__ nbig, uint64_t base, uint4* __restrict__ out_nbr, uint32_t* __restrict__ out_dst)
+{
+    const uint32_t* nbr32 = reinterpret_cast<const uint32_t*>(nbr);
+    const uint32_t m = *nbig;
+    for (uint32_t k = blockIdx.x; k < m; k += gridDim.x) {
+        const SegBig e = big[k];
+        const uint32_t r0 = __ldg(rowptr + e.d);
+        const uint32_t n = (e.b - e.a + 3) / 4;
+        for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) seg_write_vector(nbr32, r0, e.a, e.b, j, e.d, out_nbr, out_dst, base + e.out + j);
+    }
 }
 
 // Edge-pull phase alone (the phases.h boundary): accumulators as doubles plus their exact sum
@@ -548,6 +688,8 @@ int grz_pr_rowacc_clean(grz_graph* g)
     return GRZ_OK;
 }
 
+static int pr_build_segments(grz_graph* g, uint32_t bits);
+
 int grz_pr_prepare(grz_graph* g)
 {
     const uint64_t V = g->V;
@@ -583,12 +725,103 @@ int grz_pr_prepare(grz_graph* g)
     // 27 413 vs 371 ms.
     const int pick = g->tune.pr_props;
     g->pr_dmode = pick == 2 || (pick == 0 && (uint64_t)sizeof(u128) * V > 6ull * (uint64_t)g->l2_bytes);
+    // Source segments when even the double props are far larger than L2 (or when chosen): each
+    // segment's props (8 bytes x 2^bits) mostly stay in L2 while its edges stream, instead of one
+    // random DRAM sector per gathered prop.  Segment props of about the size of L2 are best: on
+    // GB300 at R-MAT 27 (16 iterations) the gather took 23.2 ms unsegmented and 17.8 / 18.1 /
+    // 19.0 / 20.5 ms with 2^24 / 2^23 / 2^22 / 2^21 sources per segment (128 MB of props for
+    // 2^24 against 126 MB of L2); smaller segments add more (segment, destination)
+    // read-modify-writes and partial vectors than they save.  Needs sources in ascending order
+    // along each destination's lanes, which hub encoding breaks.
+    uint32_t bits = 0;
+    const uint32_t sb = g->tune.pr_segment_bits;
+    if (sb >= 8) {
+        bits = sb;
+    } else if (sb == 0 && (uint64_t)sizeof(double) * V > 4ull * (uint64_t)g->l2_bytes) {
+        bits = 8;
+        while ((8ull << (bits + 1)) <= (uint64_t)g->l2_bytes * 5 / 4) ++bits;
+    }
+    while (bits && ((V + (1ull << bits) - 1) >> bits) > GRZ_PR_MAX_SEGMENTS) ++bits;
+    g->pr_segmode = 0;
+    if (bits && g->pull.nhub == 0 && g->pull.nvec) {
+        const int rc = pr_build_segments(g, bits);
+        if (rc) return rc;
+        g->pr_segmode = 1;
+        g->pr_dmode = 1;  // the segments gather the props as doubles
+    }
     if (g->pr_dmode && !g->pr_d[0]) {
         GRZ_CK(g, cudaMalloc((void**)&g->pr_d[0], sizeof(double) * (V + 1)));
         GRZ_CK(g, cudaMalloc((void**)&g->pr_d[1], sizeof(double) * (V + 1)));
         GRZ_CK(g, cudaMemsetAsync(g->pr_d[0], 0, sizeof(double) * (V + 1), g->stream));
         GRZ_CK(g, cudaMemsetAsync(g->pr_d[1], 0, sizeof(double) * (V + 1), g->stream));
     }
+    return GRZ_OK;
+}
+
+// Builds the source-segmented pull lists with 2^bits sources per segment (once per lists and bits).
+static int pr_build_segments(grz_graph* g, uint32_t bits)
+{
+    if (g->seg_nbr && g->seg_bits == bits) return GRZ_OK;
+    grz_dev_free(g, g->seg_nbr);
+    grz_dev_free(g, g->seg_dst);
+    g->seg_nbr = nullptr;
+    g->seg_dst = nullptr;
+    g->seg_bits = 0;
+    const uint64_t V = g->V;
+    const uint32_t nseg = (uint32_t)((V + (1ull << bits) - 1) >> bits);
+    if (nseg == 0 || nseg > GRZ_PR_MAX_SEGMENTS) return grz_set_error(g, GRZ_ERR_RANGE, "%u source segments (at most %d)", nseg, GRZ_PR_MAX_SEGMENTS);
+    cudaStream_t st = g->stream;
+    uint32_t *cnt = nullptr, *tot = nullptr, *nbig = nullptr;
+    SegBig* big = nullptr;
+    const uint64_t ncnt = (uint64_t)nseg * (V + 1);
+    int rc = grz_dev_alloc(g, (void**)&cnt, sizeof(uint32_t) * ncnt);
+    if (!rc) rc = grz_dev_alloc(g, (void**)&tot, sizeof(uint32_t) * (nseg + 1));
+    if (!rc) rc = grz_cuda_check(g, cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * ncnt, st), "memset");
+    const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(blocks_for(V), (uint64_t)g->num_sms * 8));
+    if (!rc) {
+        k_seg_count<<<grid, PR_THREADS, 0, st>>>(g->pull.nbr, g->pull.rowptr, (uint32_t)V, bits, cnt); GRZ_COUNT_LAUNCH(g);
+        rc = grz_cuda_check(g, cudaGetLastError(), "k_seg_count");
+    }
+    for (uint32_t sg = 0; sg < nseg && !rc; ++sg)
+        rc = grz_exclusive_sum_u32_on(g, cnt + (uint64_t)sg * (V + 1), cnt + (uint64_t)sg * (V + 1), V + 1, tot + sg, st);
+    std::vector<uint32_t> th(nseg);
+    if (!rc) rc = grz_cuda_check(g, cudaMemcpyAsync(th.data(), tot, sizeof(uint32_t) * nseg, cudaMemcpyDeviceToHost, st), "D2H");
+    if (!rc) rc = grz_cuda_check(g, cudaStreamSynchronize(st), "segment counts");
+    uint64_t total = 0, maxn = 0;
+    if (!rc) {
+        for (uint32_t sg = 0; sg < nseg; ++sg) {
+            g->seg_first[sg] = total;
+            total += th[sg];
+            maxn = std::max<uint64_t>(maxn, th[sg]);
+        }
+        g->seg_first[nseg] = total;
+        if (total >= 0xffffffffull) rc = grz_set_error(g, GRZ_ERR_RANGE, "segmented lists of %llu vectors", (unsigned long long)total);
+    }
+    if (!rc) rc = grz_dev_alloc(g, (void**)&g->seg_nbr, sizeof(uint4) * std::max<uint64_t>(total, 1));
+    if (!rc) rc = grz_dev_alloc(g, (void**)&g->seg_dst, sizeof(uint32_t) * std::max<uint64_t>(total, 1));
+    // long runs: at most one per SEG_BIG_VECTORS + 1 vectors of a segment
+    if (!rc) rc = grz_dev_alloc(g, (void**)&big, sizeof(SegBig) * (maxn / (SEG_BIG_VECTORS + 1) + 1));
+    if (!rc) rc = grz_dev_alloc(g, (void**)&nbig, sizeof(uint32_t));
+    for (uint32_t sg = 0; sg < nseg && !rc; ++sg) {
+        if (!th[sg]) continue;
+        rc = grz_cuda_check(g, cudaMemsetAsync(nbig, 0, sizeof(uint32_t), st), "memset");
+        if (rc) break;
+        k_seg_write<<<grid, PR_THREADS, 0, st>>>(g->pull.nbr, g->pull.rowptr, (uint32_t)V, bits, sg, cnt + (uint64_t)sg * (V + 1),
+                                                 g->seg_first[sg], g->seg_nbr, g->seg_dst, big, nbig); GRZ_COUNT_LAUNCH(g);
+        k_seg_write_big<<<(unsigned)g->num_sms * 4, PR_THREADS, 0, st>>>(g->pull.nbr, g->pull.rowptr, big, nbig, g->seg_first[sg],
+                                                                        g->seg_nbr, g->seg_dst); GRZ_COUNT_LAUNCH(g);
+        rc = grz_cuda_check(g, cudaGetLastError(), "k_seg_write");
+    }
+    for (void* q : { (void*)cnt, (void*)tot, (void*)big, (void*)nbig }) grz_dev_free(g, q);
+    if (rc) {
+        grz_dev_free(g, g->seg_nbr);
+        grz_dev_free(g, g->seg_dst);
+        g->seg_nbr = nullptr;
+        g->seg_dst = nullptr;
+        return rc;
+    }
+    g->seg_bits = bits;
+    g->nseg = nseg;
     return GRZ_OK;
 }
 
@@ -614,14 +847,14 @@ int grz_pr_init_state(grz_graph* g, double damping)
 }
 
 // resident blocks per SM of the gather kernel (its grid is persistent: SMs x resident)
-template <typename P>
+template <typename P, bool ADD, int MINB>
 static int pr_gather_resident(grz_graph* g)
 {
     static int resident[64] = {};
     if (g->device < 0 || g->device >= 64) return 1;
     if (!resident[g->device]) {
         int r = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_pr_gather<P>, PR_THREADS, 0) != cudaSuccess || r < 1) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_pr_gather<P, ADD, MINB>, PR_THREADS, 0) != cudaSuccess || r < 1) {
             cudaGetLastError();
             r = 1;
         }
@@ -630,18 +863,55 @@ static int pr_gather_resident(grz_graph* g)
     return resident[g->device];
 }
 
+// one gather launch over vectors [first, first + count) of a list of list_nvec vectors
+template <typename P, bool ADD>
+static void pr_gather_launch(grz_graph* g, const uint4* nbr, const uint32_t* dstv, uint64_t first, uint64_t count, uint64_t list_nvec,
+                             const P* props, const uint32_t* hub_vid, uint32_t nhub, const PRConst& pc)
+{
+    const bool wide = g->tune.pr_blocks == 6;  // the 38-register shape
+    const uint64_t res = wide ? pr_gather_resident<P, ADD, 1>(g) : pr_gather_resident<P, ADD, 8>(g);
+    const uint64_t want = g->tune.pr_grid ? g->tune.pr_grid : (uint64_t)g->num_sms * res;
+    const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(blocks_for(count), want));
+    if (wide)
+        k_pr_gather<P, ADD, 1><<<grid, PR_THREADS, 0, g->stream>>>(nbr, dstv, first, count, list_nvec, props, (uint32_t)g->V, g->pr_rowacc,
+                                                                   hub_vid, nhub, pc);
+    else
+        k_pr_gather<P, ADD, 8><<<grid, PR_THREADS, 0, g->stream>>>(nbr, dstv, first, count, list_nvec, props, (uint32_t)g->V, g->pr_rowacc,
+                                                                   hub_vid, nhub, pc);
+    GRZ_COUNT_LAUNCH(g);
+}
+
 template <typename P>
 static int pr_gather(grz_graph* g, uint64_t first, uint64_t count, const PRConst& pc, const P* props)
 {
     if (count == 0) return GRZ_OK;
-    const uint64_t want = g->tune.pr_grid ? g->tune.pr_grid : (uint64_t)g->num_sms * pr_gather_resident<P>(g);
-    const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>(blocks_for(count), want));
     grz_prof_begin(g, GRZ_PROF_PR_GATHER);
-    k_pr_gather<P><<<(unsigned)grid, PR_THREADS, 0, g->stream>>>(g->pull.nbr, g->pull.shared, first, count, g->pull.nvec,
-                                                                    props, (uint32_t)g->V, g->pr_rowacc, g->pull.hub_vid,
-                                                                    g->pull.nhub, pc); GRZ_COUNT_LAUNCH(g);
+    pr_gather_launch<P, false>(g, g->pull.nbr, g->pull.shared, first, count, g->pull.nvec, props, g->pull.hub_vid, g->pull.nhub, pc);
     grz_prof_end(g);
     return grz_cuda_check(g, cudaGetLastError(), "k_pr_gather");
+}
+
+// The gather over the source segments in order, each adding into the accumulators (which the
+// apply of segmented iterations leaves all zero).  One profiler record spans all segments.
+static int pr_gather_segments(grz_graph* g, const PRConst& pc0, const double* props)
+{
+    grz_prof_begin(g, GRZ_PROF_PR_GATHER);
+    bool first = true;
+    for (uint32_t sg = 0; sg < g->nseg; ++sg) {
+        const uint64_t a = g->seg_first[sg], n = g->seg_first[sg + 1] - a;
+        if (n == 0) continue;
+        PRConst pc = pc0;
+        if (!first) pc.K_out = nullptr;  // the iteration's constant once
+        first = false;
+        pr_gather_launch<double, true>(g, g->seg_nbr, g->seg_dst, a, n, g->seg_first[g->nseg], props, nullptr, 0u, pc);
+    }
+    if (first) {
+        // no edges at all: the constant still has to be published
+        k_pr_gather<double, true><<<1, PR_THREADS, 0, g->stream>>>(g->seg_nbr, g->seg_dst, 0, 0, 0, props, (uint32_t)g->V, g->pr_rowacc,
+                                                                   nullptr, 0u, pc0); GRZ_COUNT_LAUNCH(g);
+    }
+    grz_prof_end(g);
+    return grz_cuda_check(g, cudaGetLastError(), "k_pr_gather (segments)");
 }
 
 // one PageRank iteration: edge-pull gather + vertex phase (two kernels)
@@ -659,7 +929,10 @@ int grz_pr_fused_iteration(grz_graph* g, int write_double_props)
     pc.c = (1.0 - g->pr_damping) / dV;
     pc.nverts = dV;
     int rc = GRZ_OK;
-    if (g->pr_dmode) {
+    if (g->pr_segmode) {
+        rc = pr_sync_d(g);
+        if (rc == GRZ_OK) rc = pr_gather_segments(g, pc, (const double*)g->pr_d[g->pr_cur]);
+    } else if (g->pr_dmode) {
         rc = pr_sync_d(g);
         if (rc == GRZ_OK) rc = pr_gather(g, 0, g->pull.nvec, pc, (const double*)g->pr_d[g->pr_cur]);
     } else {
@@ -671,7 +944,7 @@ int grz_pr_fused_iteration(grz_graph* g, int write_double_props)
     const uint64_t agrid = std::max<uint64_t>(1, std::min<uint64_t>((g->V + (uint64_t)PR_THREADS * PR_APPLY_U - 1) /
                                                                         ((uint64_t)PR_THREADS * PR_APPLY_U),
                                                                     (uint64_t)g->num_sms * PR_APPLY_RESIDENT));
-    k_pr_apply<<<(unsigned)agrid, PR_THREADS, 0, g->stream>>>(g->pr_rowacc, g->pr_cut, g->inv_deg, g->degree, g->V, g->pr_K,
+    k_pr_apply<<<(unsigned)agrid, PR_THREADS, 0, g->stream>>>(g->pr_rowacc, g->pr_cut, g->pr_segmode, g->inv_deg, g->degree, g->V, g->pr_K,
                                                               g->pr_sum + (size_t)(k ^ 1) * stride, g->pr_damping, g->pr_fx[g->pr_cur ^ 1],
                                                               g->pr_dmode ? g->pr_d[g->pr_cur ^ 1] : nullptr,
                                                               write_double_props ? g->prop : nullptr); GRZ_COUNT_LAUNCH(g);
@@ -707,7 +980,7 @@ static int pr_persistent_resident(grz_graph* g)
 // 20, 16 iterations): two kernels 93 us per iteration, the persistent kernel (6 blocks per SM)
 // 109 us: its gather must read the props through the coherent path (its apply rewrites them in
 // the same launch) and holds fewer blocks per SM.  Two kernels stay the default.
-int grz_pr_use_persistent(const grz_graph* g) { return g->tune.pr_persistent >= 2; }
+int grz_pr_use_persistent(const grz_graph* g) { return g->tune.pr_persistent >= 2 && !g->pr_segmode; }
 
 // `iters` PageRank iterations (gather + apply each) in one cooperative launch.  Synchronises the
 // graph's stream to read the barrier's error word.  A wait that runs out returns GRZ_ERR_TIMEOUT

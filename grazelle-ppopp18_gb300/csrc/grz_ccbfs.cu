@@ -171,6 +171,9 @@ __global__ void __launch_bounds__(BT) k_cc_pull(const uint4* __restrict__ nbr, c
     const uint32_t ep = epoch_dev ? *epoch_dev : epoch;
     uint32_t mprev = 0;
     const bool skip = use_prev && cc_prev_min(chg, ep, &mprev);
+    // use_prev 2: a source-segment pass, which runs only when the skip is off (the full pass);
+    // use_prev 3: the pass over the whole list that runs only when it is on (the grid agrees)
+    if ((use_prev == 2 && skip) || (use_prev == 3 && !skip)) return;
     const int lane = threadIdx.x & 31;
     unsigned long long my_vote = 0;
     uint32_t my_min = INF;
@@ -959,6 +962,10 @@ int grz_frontier_init(grz_graph* g, int app, int flags, uint32_t root)
     if (!g->outdeg) return grz_set_error(g, GRZ_ERR_STATE, "no graph loaded");
     int rc = ensure_frontier_state(g);
     if (rc) return rc;
+    if (app == GRZ_APP_CONNECTED_COMPONENTS && g->tune.cc_segments == 2) {
+        rc = grz_pr_ensure_segments(g, 1);
+        if (rc) return rc;
+    }
     const uint64_t V = g->V, W = words_of(V);
     grz_frontier_state& f = g->fr;
     f.app = app;
@@ -1025,6 +1032,13 @@ static unsigned visit_grid(const grz_graph* g)
     return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(blocks_for((g->V + 3) / 4), (uint64_t)g->num_sms * 8));
 }
 
+// Whether the CC pull's full pass reads the source-segmented lists (built by grz_pr_init, or by
+// grz_frontier_init under GRZ_TUNE_CC_SEGMENTS = 2); they need a pull list without hub encoding.
+static bool cc_use_segments(const grz_graph* g)
+{
+    return g->tune.cc_segments != 1 && g->seg_nbr && g->nseg && g->pull.nhub == 0;
+}
+
 // Shared-memory opt-in and resident blocks per SM of the CC pull kernel, per device, block size
 // and staging form.
 template <int BT, bool BULK>
@@ -1066,10 +1080,28 @@ static int launch_cc_pull_bt(grz_graph* g, uint64_t first, uint64_t count, const
     grid = std::max<uint64_t>(1, std::min<uint64_t>(grid, tiles));
     // the skip needs every earlier iteration to have been complete (the whole list, or the whole
     // frontier): true for the driver loops, not once a phases.h call covered part of the list
-    const int use_prev = !f.cc_partial && first == 0 && count == g->pull.nvec;
+    const bool whole = !f.cc_partial && first == 0 && count == g->pull.nvec;
+    if (whole && cc_use_segments(g)) {
+        // The full pass (no skip yet) reads the source-segmented lists, so that each segment's
+        // labels stay in L2 while its edges stream; the pass with the skip reads the whole list
+        // (it reads destinations, not sources).  Which of them does the work is decided on the
+        // device, so one captured run graph holds both.
+        for (uint32_t sg = 0; sg < g->nseg; ++sg) {
+            const uint64_t a = g->seg_first[sg], n = g->seg_first[sg + 1] - a;
+            if (n == 0) continue;
+            const uint64_t sgrid = std::max<uint64_t>(1, std::min<uint64_t>(grid, (n + BT - 1) / BT));
+            k_cc_pull<BT, false><<<(unsigned)sgrid, BT, 0, g->stream>>>(g->seg_nbr, g->seg_dst, a, n, (uint32_t)g->V, f.label, nullptr,
+                                                                       0u, 0u, f.has_next, vc, f.vote, f.chg, f.iter, f.level_dev, 2,
+                                                                       f.dev_err); GRZ_COUNT_LAUNCH(g);
+        }
+        k_cc_pull<BT, BULK><<<(unsigned)grid, BT, smem, g->stream>>>(g->pull.nbr, g->pull.shared, first, count, (uint32_t)g->V, f.label,
+                                                                    g->pull.hub_vid, g->pull.nhub, ncache, f.has_next, vc, f.vote, f.chg,
+                                                                    f.iter, f.level_dev, 3, f.dev_err); GRZ_COUNT_LAUNCH(g);
+        return GRZ_OK;
+    }
     k_cc_pull<BT, BULK><<<(unsigned)grid, BT, smem, g->stream>>>(g->pull.nbr, g->pull.shared, first, count, (uint32_t)g->V, f.label,
                                                                 g->pull.hub_vid, g->pull.nhub, ncache, f.has_next, vc, f.vote, f.chg,
-                                                                f.iter, f.level_dev, use_prev, f.dev_err); GRZ_COUNT_LAUNCH(g);
+                                                                f.iter, f.level_dev, whole ? 1 : 0, f.dev_err); GRZ_COUNT_LAUNCH(g);
     return GRZ_OK;
 }
 
@@ -1510,6 +1542,7 @@ static int build_run_graph(grz_graph* g)
     f.run_key[0] = f.app;
     f.run_key[1] = f.flags;
     f.run_tune = g->tune;
+    f.run_seg = cc_use_segments(g) ? g->seg_nbr : nullptr;
     return GRZ_OK;
 }
 
@@ -1539,7 +1572,8 @@ int grz_frontier_run_graph(grz_graph* g, uint64_t* launches)
     rc = grz_switch_max_degree(g);
     if (rc) return rc;
     const bool same = f.run_exec && f.run_bm[0] == f.has && f.run_bm[1] == f.has_next && f.run_key[0] == f.app &&
-                      f.run_key[1] == f.flags && !memcmp(&f.run_tune, &g->tune, sizeof(g->tune));
+                      f.run_key[1] == f.flags && !memcmp(&f.run_tune, &g->tune, sizeof(g->tune)) &&
+                      f.run_seg == (cc_use_segments(g) ? g->seg_nbr : nullptr);
     if (!same) {
         int resident = 0;
         const size_t smem = sizeof(uint32_t) * std::min<uint32_t>(g->tune.cc_cache, g->pull.nhub);

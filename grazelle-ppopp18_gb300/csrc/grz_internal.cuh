@@ -296,6 +296,7 @@ struct grz_mlp;
 #define GRZ_TUNE_PULL_STAGING 13
 #define GRZ_TUNE_PR_SEGMENT_BITS 14
 #define GRZ_TUNE_PR_BLOCKS 15
+#define GRZ_TUNE_CC_SEGMENTS 16
 #define GRZ_TUNE_HUBS_LOADED 100
 
 // kernel shapes chosen per graph (grz_tune_set; the autotuner searches them)
@@ -316,6 +317,7 @@ struct grz_tuning {
     uint32_t pull_staging;   // CC pull's edge stream: 0 plain streaming loads, 1 bulk copies into shared memory
     uint32_t pr_segment_bits;  // PageRank source segments: 0 by size, 1 none, b in [8, 31]: 2^b sources per segment
     uint32_t pr_blocks;   // PageRank gather's register shape: 0 or 8 (32 registers, 8 blocks per SM), 6 (38, no spill)
+    uint32_t cc_segments; // CC full pull over the source segments: 0 when built, 1 never, 2 build them by size
 };
 
 // Device control block of a CC/BFS run executed as one CUDA graph (grz_ccbfs.cu): the
@@ -386,6 +388,7 @@ struct grz_frontier_state {
     unsigned long long* run_bm[2];   // the HasInfo buffers in the graph's even-iteration roles
     int run_key[2];                  // app, flags of the captured graph
     grz_tuning run_tune;             // kernel shapes of the captured graph
+    const uint4* run_seg;            // source-segmented lists the captured graph reads (or null)
     // snapshot for timing both engines from one state
     void* snap;
     uint64_t snap_bytes;
@@ -542,6 +545,9 @@ int grz_read_vote(grz_graph* g, uint64_t* out);
 int grz_frontier_mail(grz_graph* g);
 int grz_frontier_run_graph(grz_graph* g, uint64_t* launches);
 int grz_frontier_check_waits(grz_graph* g);
+// builds the source-segmented pull lists by the size rule of grz_pr_init (grz_pr.cu); `force`:
+// also below the size threshold, with the tuned or the default segment size
+int grz_pr_ensure_segments(grz_graph* g, int force);
 void grz_frontier_run_prepare(grz_graph* g);
 int grz_frontier_digest(grz_graph* g, uint64_t* out3);
 int grz_switch_max_degree(grz_graph* g);

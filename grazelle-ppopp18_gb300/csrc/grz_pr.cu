@@ -690,6 +690,31 @@ int grz_pr_rowacc_clean(grz_graph* g)
 
 static int pr_build_segments(grz_graph* g, uint32_t bits);
 
+// Sources per segment (log2) of the segmented lists, 0 for none: the tuned size, else, when the
+// double props exceed 4x L2 (or `force`), the largest segment whose props are at most 1.25x L2
+// (see grz_pr_prepare); never more than GRZ_PR_MAX_SEGMENTS segments.
+static uint32_t pr_segment_bits(const grz_graph* g, int force)
+{
+    const uint64_t V = g->V;
+    uint32_t bits = 0;
+    const uint32_t sb = g->tune.pr_segment_bits;
+    if (sb >= 8) {
+        bits = sb;
+    } else if (sb == 0 && (force || (uint64_t)sizeof(double) * V > 4ull * (uint64_t)g->l2_bytes)) {
+        bits = 8;
+        while ((8ull << (bits + 1)) <= (uint64_t)g->l2_bytes * 5 / 4) ++bits;
+    }
+    while (bits && ((V + (1ull << bits) - 1) >> bits) > GRZ_PR_MAX_SEGMENTS) ++bits;
+    return bits;
+}
+
+int grz_pr_ensure_segments(grz_graph* g, int force)
+{
+    const uint32_t bits = pr_segment_bits(g, force);
+    if (!bits || g->pull.nhub || !g->pull.nvec) return GRZ_OK;
+    return pr_build_segments(g, bits);
+}
+
 int grz_pr_prepare(grz_graph* g)
 {
     const uint64_t V = g->V;
@@ -733,15 +758,7 @@ int grz_pr_prepare(grz_graph* g)
     // 2^24 against 126 MB of L2); smaller segments add more (segment, destination)
     // read-modify-writes and partial vectors than they save.  Needs sources in ascending order
     // along each destination's lanes, which hub encoding breaks.
-    uint32_t bits = 0;
-    const uint32_t sb = g->tune.pr_segment_bits;
-    if (sb >= 8) {
-        bits = sb;
-    } else if (sb == 0 && (uint64_t)sizeof(double) * V > 4ull * (uint64_t)g->l2_bytes) {
-        bits = 8;
-        while ((8ull << (bits + 1)) <= (uint64_t)g->l2_bytes * 5 / 4) ++bits;
-    }
-    while (bits && ((V + (1ull << bits) - 1) >> bits) > GRZ_PR_MAX_SEGMENTS) ++bits;
+    const uint32_t bits = pr_segment_bits(g, 0);
     g->pr_segmode = 0;
     if (bits && g->pull.nhub == 0 && g->pull.nvec) {
         const int rc = pr_build_segments(g, bits);

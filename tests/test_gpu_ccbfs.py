@@ -344,3 +344,32 @@ def test_bulk_staged_pull_gives_the_same_labels(threads):
         np.testing.assert_array_equal(G.connected_components(), ref)
         np.testing.assert_array_equal(G.connected_components(native.FLAG_HOST_LOOP), ref)
         np.testing.assert_array_equal(G.connected_components(native.FORCE_PULL), ref)
+
+
+def test_cc_full_pull_over_source_segments():
+    """The CC run's full pull over the source-segmented lists (each segment's labels stay in L2;
+    the later pulls with the converged-destination skip read the whole list, the device choosing
+    which pass works) gives the oracle's labels: lists built for CC (GRZ_TUNE_CC_SEGMENTS = 2),
+    lists left by grz_pr_init, in the graph run and the host loop, and the same labels with the
+    segments turned off."""
+    from grazelle import graphgen as gg, native
+    from grazelle.engine import Graph
+    for g in (gg.rmat(14, 16, seed=71, symmetric=True), gg.rmat(14, 8, seed=72)):
+        V = g.num_vertices
+        pull, push = g.pull_order().pairs(), g.push_order().pairs()
+        ref = O.cc(O.layout(V, pull, push))[0]
+        with Graph(0) as G:
+            G.tune(cc_segments=2, pr_segment_bits=9)
+            G.load_pairs(V, pull, push)
+            np.testing.assert_array_equal(G.connected_components(), ref)
+            np.testing.assert_array_equal(G.connected_components(native.FLAG_HOST_LOOP), ref)
+            np.testing.assert_array_equal(G.connected_components(native.WITHOUT_COUNT), ref)
+            G.tune(cc_segments=1)
+            np.testing.assert_array_equal(G.connected_components(), ref)
+        with Graph(0) as G:
+            G.tune(pr_segment_bits=10)
+            G.load_pairs(V, pull, push)
+            np.testing.assert_array_equal(G.connected_components(), ref)   # no segments yet
+            G.pagerank(2)                                                 # builds them
+            np.testing.assert_array_equal(G.connected_components(), ref)   # the run graph is captured again
+            np.testing.assert_array_equal(G.bfs(0)[1], O.bfs_levels(push, V, 0))

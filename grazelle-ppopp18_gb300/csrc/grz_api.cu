@@ -896,10 +896,6 @@ extern "C" int grz_tune_set(grz_graph* g, int param, int64_t value)
         if (value > 2) return grz_set_error(g, GRZ_ERR_ARG, "CC segments must be 0 (when built), 1 (never) or 2 (build them)");
         g->tune.cc_segments = (uint32_t)value;
         return GRZ_OK;
-    case GRZ_TUNE_PR_BLOCKS:
-        if (value != 0 && value != 6 && value != 8) return grz_set_error(g, GRZ_ERR_ARG, "PageRank gather shape must be 0, 6 or 8 blocks per SM");
-        g->tune.pr_blocks = (uint32_t)value;
-        return GRZ_OK;
     case GRZ_TUNE_PR_SEGMENT_BITS:
         if (value > 31 || (value > 1 && value < 8))
             return grz_set_error(g, GRZ_ERR_ARG, "PageRank segment bits must be 0 (by size), 1 (none) or 8..31");
@@ -933,7 +929,6 @@ extern "C" int grz_tune_get(const grz_graph* g, int param, int64_t* value)
     case GRZ_TUNE_RUN_LIMIT_US: *value = g->tune.run_limit_us; return GRZ_OK;
     case GRZ_TUNE_PULL_STAGING: *value = g->tune.pull_staging; return GRZ_OK;
     case GRZ_TUNE_PR_SEGMENT_BITS: *value = g->tune.pr_segment_bits; return GRZ_OK;
-    case GRZ_TUNE_PR_BLOCKS: *value = g->tune.pr_blocks; return GRZ_OK;
     case GRZ_TUNE_CC_SEGMENTS: *value = g->tune.cc_segments; return GRZ_OK;
     case GRZ_TUNE_HUBS_LOADED: *value = g->pull.nhub; return GRZ_OK;
     default: return GRZ_ERR_ARG;

@@ -145,6 +145,9 @@ __device__ __forceinline__ void cc_record_min(uint32_t my_min, uint32_t* red32, 
 // complete iteration): it reads their destination and label, not their vectors.  R-MAT's
 // hubs have the smallest IDs, so after the first iteration most of the giant component holds
 // label 0 and the second pull reads little more than the destinations.
+// tiles whose destination and label loads the skip mode issues together
+constexpr int SKIP_TILES = 4;
+
 // double-buffered staging of the edge stream in shared memory (the bulk-copy form)
 template <int BT>
 struct CCStage {
@@ -200,49 +203,12 @@ __global__ void __launch_bounds__(BT) k_cc_pull(const uint4* __restrict__ nbr, c
         }
     }
     __syncthreads();
-    uint64_t j = 0;
-    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++j) {
-        const uint64_t i = t * BT + threadIdx.x;
-        const uint64_t v = first + i;
-        const bool live = i < nvec;
-        uint32_t key = INF, m = INF, labd = INF;
-        bool need = live;
-        bool staged = false;
-        uint4 sv = make_uint4(INF, INF, INF, INF);
-        if constexpr (BULK) {
-            if (bulk && t < nfull) {
-                const int st = (int)(j & 1);
-                const bool ok = mbar_wait_bounded(&stg.bar[st], (par >> st) & 1u);
-                if (__syncthreads_or(!ok)) {
-                    if (threadIdx.x == 0) atomicExch(err, 1u);
-                    return;
-                }
-                par ^= 1u << st;
-                sv = stg.nbr[st][threadIdx.x];
-                key = stg.dst[st][threadIdx.x];
-                staged = true;
-                __syncthreads();  // every thread has read the stage
-                const uint64_t tn = t + 2ull * gridDim.x;
-                if (threadIdx.x == 0 && tn < nfull) {
-                    fence_proxy_async_smem();
-                    mbar_arrive_expect_tx(&stg.bar[st], BT * (sizeof(uint4) + sizeof(uint32_t)));
-                    bulk_copy_g2s(stg.nbr[st], nbr + tn * BT, BT * sizeof(uint4), &stg.bar[st]);
-                    bulk_copy_g2s(stg.dst[st], dstv + tn * BT, BT * sizeof(uint32_t), &stg.bar[st]);
-                }
-            }
-        }
-        if (skip) {
-            // skip mode: the destination's label decides whether the vector is read at all
-            if (live) {
-                key = __ldcs(dstv + v);
-                labd = label[key];
-                need = labd > mprev;
-            }
-            if (!__any_sync(0xffffffffu, need)) continue;  // warp-uniform
-        }
+    // one tile's reduction and updates, once its destinations (key), their labels if known (labd,
+    // skip mode) and its vectors (staged, or loaded here when needed) are at hand
+    auto finish = [&](uint64_t v, bool live, uint32_t key, uint32_t labd, bool need, bool staged, uint4 sv) {
+        uint32_t m = INF;
         if (need) {
             const uint4 s4 = staged ? sv : __ldcs(nbr + v);
-            if (!skip && !staged) key = __ldcs(dstv + v);
             const uint32_t x[4] = { s4.x, s4.y, s4.z, s4.w };
             uint32_t val[4];
 #pragma unroll
@@ -275,6 +241,65 @@ __global__ void __launch_bounds__(BT) k_cc_pull(const uint4* __restrict__ nbr, c
                 my_min = min(my_min, m);
                 if (bit_set_first(has_next, key)) my_vote += vc.of(key);
             }
+        }
+    };
+    if (skip) {
+        // Skip mode: a vector is read only if its destination's label can still drop.  Each
+        // block takes SKIP_TILES consecutive tiles at a time and issues all their destination
+        // loads, then all their label loads, before any tile goes on: the chain destination ->
+        // label -> vector is latency-bound, so this keeps SKIP_TILES times more loads in flight.
+        constexpr int U = SKIP_TILES;
+        for (uint64_t t0 = (uint64_t)blockIdx.x * U; t0 < ntiles; t0 += (uint64_t)gridDim.x * U) {
+            uint32_t keys[U], labs[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint64_t i = (t0 + u) * BT + threadIdx.x;
+                keys[u] = i < nvec ? __ldcs(dstv + first + i) : INF;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) labs[u] = keys[u] != INF ? label[keys[u]] : INF;
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint64_t i = (t0 + u) * BT + threadIdx.x;
+                const bool live = i < nvec;
+                const bool need = live && labs[u] > mprev;
+                if (!__any_sync(0xffffffffu, need)) continue;  // warp-uniform
+                finish(first + i, live, keys[u], labs[u], need, false, make_uint4(INF, INF, INF, INF));
+            }
+        }
+    } else {
+        uint64_t j = 0;
+        for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++j) {
+            const uint64_t i = t * BT + threadIdx.x;
+            const uint64_t v = first + i;
+            const bool live = i < nvec;
+            uint32_t key = INF;
+            bool staged = false;
+            uint4 sv = make_uint4(INF, INF, INF, INF);
+            if constexpr (BULK) {
+                if (bulk && t < nfull) {
+                    const int st = (int)(j & 1);
+                    const bool ok = mbar_wait_bounded(&stg.bar[st], (par >> st) & 1u);
+                    if (__syncthreads_or(!ok)) {
+                        if (threadIdx.x == 0) atomicExch(err, 1u);
+                        return;
+                    }
+                    par ^= 1u << st;
+                    sv = stg.nbr[st][threadIdx.x];
+                    key = stg.dst[st][threadIdx.x];
+                    staged = true;
+                    __syncthreads();  // every thread has read the stage
+                    const uint64_t tn = t + 2ull * gridDim.x;
+                    if (threadIdx.x == 0 && tn < nfull) {
+                        fence_proxy_async_smem();
+                        mbar_arrive_expect_tx(&stg.bar[st], BT * (sizeof(uint4) + sizeof(uint32_t)));
+                        bulk_copy_g2s(stg.nbr[st], nbr + tn * BT, BT * sizeof(uint4), &stg.bar[st]);
+                        bulk_copy_g2s(stg.dst[st], dstv + tn * BT, BT * sizeof(uint32_t), &stg.bar[st]);
+                    }
+                }
+            }
+            if (live && !staged) key = __ldcs(dstv + v);
+            finish(v, live, key, INF, live, staged, sv);
         }
     }
     for (int o = 16; o > 0; o >>= 1) my_vote += __shfl_down_sync(0xffffffffu, my_vote, o);

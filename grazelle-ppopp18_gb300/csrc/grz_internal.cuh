@@ -295,7 +295,6 @@ struct grz_mlp;
 #define GRZ_TUNE_RUN_LIMIT_US 12
 #define GRZ_TUNE_PULL_STAGING 13
 #define GRZ_TUNE_PR_SEGMENT_BITS 14
-#define GRZ_TUNE_PR_BLOCKS 15
 #define GRZ_TUNE_CC_SEGMENTS 16
 #define GRZ_TUNE_HUBS_LOADED 100
 
@@ -316,7 +315,6 @@ struct grz_tuning {
     uint32_t run_limit_us;   // CC/BFS time bound of a run in microseconds (0: 300 s)
     uint32_t pull_staging;   // CC pull's edge stream: 0 plain streaming loads, 1 bulk copies into shared memory
     uint32_t pr_segment_bits;  // PageRank source segments: 0 by size, 1 none, b in [8, 31]: 2^b sources per segment
-    uint32_t pr_blocks;   // PageRank gather's register shape: 0 or 8 (32 registers, 8 blocks per SM), 6 (38, no spill)
     uint32_t cc_segments; // CC full pull over the source segments: 0 when built, 1 never, 2 build them by size
 };
 

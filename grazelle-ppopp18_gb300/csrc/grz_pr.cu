@@ -215,10 +215,13 @@ __device__ __forceinline__ void pr_gather_tiles(const uint4* __restrict__ nbr, c
     }
 }
 
-// MINB resident blocks per SM asked of the compiler: 8 keeps 32 registers (the most gathers in
-// flight; a 16-byte spill of the fixed-point form), 1 lets it take 38 (no spill, 6 blocks per SM)
-template <typename P, bool ADD = false, int MINB = 8>
-__global__ void __launch_bounds__(PR_THREADS, MINB) k_pr_gather(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv,
+// 8 resident blocks per SM asked of the compiler: 32 registers, the most gathers in flight (a
+// 16-byte spill in the fixed-point form).  Unbounded, the compiler takes 80 registers (3 blocks
+// per SM), which measured 47% slower at R-MAT 20.
+constexpr int PR_GATHER_MIN_BLOCKS = 8;
+
+template <typename P, bool ADD = false>
+__global__ void __launch_bounds__(PR_THREADS, PR_GATHER_MIN_BLOCKS) k_pr_gather(const uint4* __restrict__ nbr, const uint32_t* __restrict__ dstv,
                                                           uint64_t first, uint64_t nvec, uint64_t list_nvec,
                                                           const P* __restrict__ prop_fx, uint32_t V, u128* __restrict__ rowacc,
                                                           const uint32_t* __restrict__ hub_vid, uint32_t nhub, const PRConst pc)
@@ -864,14 +867,14 @@ int grz_pr_init_state(grz_graph* g, double damping)
 }
 
 // resident blocks per SM of the gather kernel (its grid is persistent: SMs x resident)
-template <typename P, bool ADD, int MINB>
+template <typename P, bool ADD>
 static int pr_gather_resident(grz_graph* g)
 {
     static int resident[64] = {};
     if (g->device < 0 || g->device >= 64) return 1;
     if (!resident[g->device]) {
         int r = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_pr_gather<P, ADD, MINB>, PR_THREADS, 0) != cudaSuccess || r < 1) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_pr_gather<P, ADD>, PR_THREADS, 0) != cudaSuccess || r < 1) {
             cudaGetLastError();
             r = 1;
         }
@@ -885,16 +888,10 @@ template <typename P, bool ADD>
 static void pr_gather_launch(grz_graph* g, const uint4* nbr, const uint32_t* dstv, uint64_t first, uint64_t count, uint64_t list_nvec,
                              const P* props, const uint32_t* hub_vid, uint32_t nhub, const PRConst& pc)
 {
-    const bool wide = g->tune.pr_blocks == 6;  // the 38-register shape
-    const uint64_t res = wide ? pr_gather_resident<P, ADD, 1>(g) : pr_gather_resident<P, ADD, 8>(g);
-    const uint64_t want = g->tune.pr_grid ? g->tune.pr_grid : (uint64_t)g->num_sms * res;
+    const uint64_t want = g->tune.pr_grid ? g->tune.pr_grid : (uint64_t)g->num_sms * pr_gather_resident<P, ADD>(g);
     const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(blocks_for(count), want));
-    if (wide)
-        k_pr_gather<P, ADD, 1><<<grid, PR_THREADS, 0, g->stream>>>(nbr, dstv, first, count, list_nvec, props, (uint32_t)g->V, g->pr_rowacc,
-                                                                   hub_vid, nhub, pc);
-    else
-        k_pr_gather<P, ADD, 8><<<grid, PR_THREADS, 0, g->stream>>>(nbr, dstv, first, count, list_nvec, props, (uint32_t)g->V, g->pr_rowacc,
-                                                                   hub_vid, nhub, pc);
+    k_pr_gather<P, ADD><<<grid, PR_THREADS, 0, g->stream>>>(nbr, dstv, first, count, list_nvec, props, (uint32_t)g->V, g->pr_rowacc,
+                                                            hub_vid, nhub, pc);
     GRZ_COUNT_LAUNCH(g);
 }
 

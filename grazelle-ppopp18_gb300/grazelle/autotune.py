@@ -76,12 +76,10 @@ def tune_cc(G, trials: int = 3, threads=(256, 512, 1024), grids_per_sm=(0, 1, 2,
             "trials": trials_out}
 
 
-def tune_pr(G, trials: int = 3, grids_per_sm=(0, 1, 2, 4, 8), forms=(1, 2, 3), shapes=(0, 6), iterations: int = 8,
-            device: int = 0) -> dict:
+def tune_pr(G, trials: int = 3, grids_per_sm=(0, 1, 2, 4, 8), forms=(1, 2, 3), iterations: int = 8, device: int = 0) -> dict:
     """PageRank: the iteration's form (two kernels, or one persistent cooperative launch with 6
-    or 8 blocks per SM) and, for two kernels, the gather's register shape (32 registers at 8
-    blocks per SM, or 38 at 6) x its persistent grid.  The objective is the device time of
-    `iterations` iterations."""
+    or 8 blocks per SM) and, for two kernels, the gather's persistent grid.  The objective is the
+    device time of `iterations` iterations."""
     sms = _sms(device)
     start = G.tuning()
 
@@ -92,18 +90,15 @@ def tune_pr(G, trials: int = 3, grids_per_sm=(0, 1, 2, 4, 8), forms=(1, 2, 3), s
     run()
     cands = []
     for form in forms:
-        if form == 1:
-            cands += [(1, shape, gps) for shape in shapes for gps in grids_per_sm]
-        else:
-            cands.append((form, 0, 0))
+        cands += [(1, gps) for gps in grids_per_sm] if form == 1 else [(form, 0)]
     trials_out = []
-    for form, shape, gps in cands:
-        G.tune(pr_persistent=form, pr_blocks=shape, pr_grid=gps * sms)
+    for form, gps in cands:
+        G.tune(pr_persistent=form, pr_grid=gps * sms)
         run()
-        trials_out.append({"pr_persistent": form, "pr_blocks": shape, "pr_grid": gps * sms, "ms": _median_ms(run, trials)})
-    keys = ("pr_persistent", "pr_blocks", "pr_grid")
-    default = next((t for t in trials_out if t["pr_grid"] == start["pr_grid"] and t["pr_persistent"] == (start["pr_persistent"] or 1)
-                    and t["pr_blocks"] == start["pr_blocks"]), None)
+        trials_out.append({"pr_persistent": form, "pr_grid": gps * sms, "ms": _median_ms(run, trials)})
+    keys = ("pr_persistent", "pr_grid")
+    default = next((t for t in trials_out if t["pr_grid"] == start["pr_grid"] and t["pr_persistent"] == (start["pr_persistent"] or 1)),
+                   None)
     best = min(trials_out, key=lambda t: t["ms"])
     G.tune(**{k: best[k] for k in keys})
     return {"objective": "%d PageRank iterations" % iterations, "best": {k: best[k] for k in keys},

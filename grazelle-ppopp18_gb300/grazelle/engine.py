@@ -79,7 +79,7 @@ class Graph:
                 "pr_persistent": native.TUNE_PR_PERSISTENT, "pr_wait_limit_us": native.TUNE_PR_WAIT_LIMIT_US,
                 "pr_withhold": native.TUNE_PR_WITHHOLD, "run_max_iterations": native.TUNE_RUN_MAX_ITERATIONS,
                 "run_limit_us": native.TUNE_RUN_LIMIT_US, "pull_staging": native.TUNE_PULL_STAGING,
-                "pr_segment_bits": native.TUNE_PR_SEGMENT_BITS, "pr_blocks": native.TUNE_PR_BLOCKS,
+                "pr_segment_bits": native.TUNE_PR_SEGMENT_BITS,
                 "cc_segments": native.TUNE_CC_SEGMENTS}
         for k, v in kw.items():
             self._ck(self.lib.grz_tune_set(self.h, keys[k], int(v)))
@@ -92,7 +92,7 @@ class Graph:
                      ("bfs_pull_scan", native.TUNE_BFS_PULL_SCAN), ("pr_props", native.TUNE_PR_PROPS),
                      ("ingest_chunks", native.TUNE_INGEST_CHUNKS), ("pr_persistent", native.TUNE_PR_PERSISTENT),
                      ("pr_wait_limit_us", native.TUNE_PR_WAIT_LIMIT_US), ("pr_withhold", native.TUNE_PR_WITHHOLD),
-                     ("run_max_iterations", native.TUNE_RUN_MAX_ITERATIONS), ("run_limit_us", native.TUNE_RUN_LIMIT_US), ("pull_staging", native.TUNE_PULL_STAGING), ("pr_segment_bits", native.TUNE_PR_SEGMENT_BITS), ("pr_blocks", native.TUNE_PR_BLOCKS), ("cc_segments", native.TUNE_CC_SEGMENTS),
+                     ("run_max_iterations", native.TUNE_RUN_MAX_ITERATIONS), ("run_limit_us", native.TUNE_RUN_LIMIT_US), ("pull_staging", native.TUNE_PULL_STAGING), ("pr_segment_bits", native.TUNE_PR_SEGMENT_BITS), ("cc_segments", native.TUNE_CC_SEGMENTS),
                      ("hubs_loaded", native.TUNE_HUBS_LOADED)):
             v = C.c_int64()
             self._ck(self.lib.grz_tune_get(self.h, p, C.byref(v)))

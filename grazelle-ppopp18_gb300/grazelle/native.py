@@ -34,7 +34,7 @@ LOAD_DERIVE_PUSH = 1
 TUNE_HUBS, TUNE_CC_CACHE, TUNE_CC_THREADS, TUNE_CC_GRID, TUNE_PR_GRID, TUNE_BFS_PULL_SCAN, TUNE_PR_PROPS = 0, 1, 2, 3, 4, 5, 6
 TUNE_INGEST_CHUNKS, TUNE_HUBS_LOADED = 7, 100
 TUNE_PR_PERSISTENT, TUNE_PR_WAIT_LIMIT_US, TUNE_PR_WITHHOLD = 8, 9, 10
-TUNE_RUN_MAX_ITERATIONS, TUNE_RUN_LIMIT_US, TUNE_PULL_STAGING, TUNE_PR_SEGMENT_BITS, TUNE_PR_BLOCKS = 11, 12, 13, 14, 15
+TUNE_RUN_MAX_ITERATIONS, TUNE_RUN_LIMIT_US, TUNE_PULL_STAGING, TUNE_PR_SEGMENT_BITS = 11, 12, 13, 14
 TUNE_CC_SEGMENTS = 16
 BATCH_TUNE_PPR_BLOCKS, BATCH_TUNE_BFS_BLOCKS, BATCH_TUNE_PPR_PROPS = 0, 1, 2
 FLAG_HOST_LOOP = 16  # grz_cc_run / grz_bfs_run: host round trip per iteration instead of one CUDA graph

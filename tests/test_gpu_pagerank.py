@@ -305,19 +305,26 @@ def test_source_segmented_gather_is_bit_identical(bits):
             assert O.relative_l1(B.pagerank(16), O.pr_pull(L, 16)) < PR_TOL
 
 
-def test_gather_register_shapes_give_identical_props():
-    """Both register shapes of the gather (32 registers at 8 blocks per SM, 38 at 6) give the
-    same props, fixed point and doubles, with and without source segments."""
+@pytest.mark.parametrize("props,seg", [(1, 1), (2, 1), (2, 10)])
+def test_props_do_not_depend_on_the_gather_grid(props, seg):
+    """The gather's persistent grid (how many blocks, hence which tiles each block walks and how
+    many blocks are resident per SM) changes nothing: fixed-point and double props, with and
+    without source segments, and the persistent forms."""
     from grazelle import graphgen as gg
     from grazelle.engine import Graph
     g = gg.rmat(15, seed=61)
     V = g.num_vertices
     pull, push = g.pull_order().pairs(), g.push_order().pairs()
     with Graph(0) as G:
+        G.tune(pr_props=props, pr_segment_bits=seg)
         G.load_pairs(V, pull, push)
-        for props, seg in ((1, 1), (2, 1), (2, 10)):
-            G.tune(pr_props=props, pr_segment_bits=seg, pr_blocks=0)
-            a = G.pagerank(9)
-            G.tune(pr_blocks=6)
-            np.testing.assert_array_equal(G.pagerank(9), a)
-        G.tune(pr_blocks=0)
+        a = G.pagerank(9)
+        for grid in (37, 152, 456, 1216, 3000):
+            G.tune(pr_grid=grid)
+            np.testing.assert_array_equal(G.pagerank(9), a, err_msg="grid %d" % grid)
+        G.tune(pr_grid=0)
+        for form in (2, 3):
+            G.tune(pr_persistent=form)
+            np.testing.assert_array_equal(G.pagerank(9), a, err_msg="form %d" % form)
+        G.tune(pr_persistent=0)
+        np.testing.assert_array_equal(G.pagerank(9), a)

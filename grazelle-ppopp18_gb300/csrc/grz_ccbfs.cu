@@ -210,19 +210,18 @@ __global__ void __launch_bounds__(BT) k_cc_pull(const uint4* __restrict__ nbr, c
         if (need) {
             const uint4 s4 = staged ? sv : __ldcs(nbr + v);
             const uint32_t x[4] = { s4.x, s4.y, s4.z, s4.w };
-            uint32_t val[4];
-#pragma unroll
-            for (int l = 0; l < 4; ++l) {
-                const uint32_t sl = x[l] - GRZ_HUB_BASE;
-                if (sl < ncache) {
-                    val[l] = s_hub[sl];
-                } else {
-                    // labels change in place during the phase: plain (coherent) loads
-                    const uint32_t id = sl < nhub ? __ldg(hub_vid + sl) : min(x[l], V);
-                    val[l] = label[id];
-                }
-            }
-            m = min(min(val[0], val[1]), min(val[2], val[3]));
+            auto fetch = [&](uint32_t xl) -> uint32_t {
+                const uint32_t sl = xl - GRZ_HUB_BASE;
+                if (sl < ncache) return s_hub[sl];
+                // labels change in place during the phase: plain (coherent) loads
+                const uint32_t id = sl < nhub ? __ldg(hub_vid + sl) : min(xl, V);
+                return label[id];
+            };
+            // A vector's lanes hold its sources in ascending order, so lane 0 is the
+            // smallest-ID source: in a power-law graph often a hub whose label is already 0.
+            // Then the minimum is 0 and the other three gathers are not issued.
+            m = fetch(x[0]);
+            if (m != 0) m = min(m, min(min(fetch(x[1]), fetch(x[2])), fetch(x[3])));
         }
         const uint32_t prevkey = __shfl_up_sync(0xffffffffu, key, 1);
         const uint32_t nextkey = __shfl_down_sync(0xffffffffu, key, 1);
@@ -854,11 +853,17 @@ __global__ void __launch_bounds__(T) k_bfs_visit(const uint32_t* __restrict__ to
 // ---------------------------------------------------------------------------------------------
 // init / output
 
+// execution_initialize_vertex_prop_cc: (double)id; entry V = +inf.  Four labels per thread with one
+// 16-byte store (the array is 256-byte aligned), the last few one by one.
 __global__ void k_cc_init(uint32_t* __restrict__ label, uint64_t V)
 {
-    const uint64_t v = (uint64_t)blockIdx.x * T + threadIdx.x;
-    if (v < V) label[v] = (uint32_t)v;  // execution_initialize_vertex_prop_cc: (double)id
-    if (v == V) label[v] = INF;
+    const uint64_t q = (uint64_t)blockIdx.x * T + threadIdx.x;
+    const uint64_t v = 4 * q;
+    if (v + 3 < V) {
+        reinterpret_cast<uint4*>(label)[q] = make_uint4((uint32_t)v, (uint32_t)v + 1, (uint32_t)v + 2, (uint32_t)v + 3);
+    } else {
+        for (uint64_t k = v; k <= V && k < v + 4; ++k) label[k] = k < V ? (uint32_t)k : INF;
+    }
 }
 
 __global__ void k_bfs_init(uint32_t* __restrict__ parent, uint32_t* __restrict__ level, uint64_t V)
@@ -1004,7 +1009,7 @@ int grz_frontier_init(grz_graph* g, int app, int flags, uint32_t root)
     cudaStream_t st = g->stream;
     GRZ_CK(g, cudaMemsetAsync(f.dev_err, 0, sizeof(unsigned), st));
     if (app == GRZ_APP_CONNECTED_COMPONENTS) {
-        k_cc_init<<<blocks_for(V + 1), T, 0, st>>>(f.label, V); GRZ_COUNT_LAUNCH(g);
+        k_cc_init<<<blocks_for(V / 4 + 1), T, 0, st>>>(f.label, V); GRZ_COUNT_LAUNCH(g);
         k_bitmap_init<<<blocks_for(W), T, 0, st>>>(f.has, W, V, 1); GRZ_COUNT_LAUNCH(g);      // HasInfo = all (execution_cc.c:66-73)
         k_bitmap_init<<<blocks_for(W), T, 0, st>>>(f.wants, W, V, 1); GRZ_COUNT_LAUNCH(g);
         // before iteration 1 every vertex counts as changed, the smallest label being 0 (tag 0)

@@ -342,7 +342,7 @@ def run_native(a):
                     "mean_launch_ms": round(mean_ms, 4),
                     "share_of_profiled_pass": round(ks[dominant]["total_ms"] / tprof.ms, 4),
                     "region": region,
-                    "traffic": profile_traffic(dominant, "%s%d" % (wl, scale))}
+                    "traffic": profile_traffic(dominant, "%s%d" % (wl, scale)) if not a.tune else None}
 
     # end to end through the C ABI from pinned host buffers
     e2e_units = 0
@@ -485,7 +485,7 @@ def pagerank_study(a, torch, stream, hbm, hbm_kind, scale=20):
                            "unit": "GB/s", "frac": round(alg / (gm * 1e-3) / 1e9 / hbm, 4) if gm else None,
                            "mean_launch_us": round(gm * 1e3, 2),
                            "iteration_frac": round(alg / (it_ms * 1e-3) / 1e9 / hbm, 4),
-                           "traffic": profile_traffic("pr_gather", "pr%d" % scale)}
+                           "traffic": profile_traffic("pr_gather", "pr%d" % scale) if not a.tune else None}
         # e2e: the -pull pairs cross the link each step (PageRank pull needs no -push list)
         for _ in range(2):
             G.load_pointers(V, E, pin_pull.data_ptr(), None)
@@ -682,7 +682,8 @@ def stress_study(a, torch, stream, dev, hbm, hbm_kind):
                               "algorithmic_bytes": alg, "achieved": round(alg / (gm * 1e-3) / 1e9, 1),
                               "frac": round(alg / (gm * 1e-3) / 1e9 / hbm, 4),
                               "gather_inclusive_bytes": alg_g, "gather_inclusive_achieved": round(alg_g / (gm * 1e-3) / 1e9, 1),
-                              "gather_inclusive_frac": round(alg_g / (gm * 1e-3) / 1e9 / hbm, 4)}
+                              "gather_inclusive_frac": round(alg_g / (gm * 1e-3) / 1e9 / hbm, 4),
+                              "traffic": profile_traffic("pr_gather", "pr%d" % scale) if not a.tune else None}
         # parity: one iteration at a seeded sample of destinations
         rng = np.random.default_rng(a.seed + 27)
         smp = np.sort(rng.choice(V, size=100000, replace=False)).astype(np.uint64)

@@ -467,7 +467,7 @@ __device__ __forceinline__ void load_rowptr(const uint32_t* __restrict__ rowptr,
 
 __global__ void __launch_bounds__(T) k_fr_count(const unsigned long long* __restrict__ bm1,
                                                 const unsigned long long* __restrict__ bm2, uint64_t V,
-                                                const uint32_t* __restrict__ rowptr, uint32_t* __restrict__ part_n,
+                                                const uint32_t* __restrict__ rowptr, uint32_t skip, uint32_t* __restrict__ part_n,
                                                 uint32_t* __restrict__ part_vec)
 {
     __shared__ uint32_t sa[T / 32 + 1], sb[T / 32 + 1];
@@ -483,7 +483,7 @@ __global__ void __launch_bounds__(T) k_fr_count(const unsigned long long* __rest
         load_rowptr(rowptr, v0, V, r);
 #pragma unroll
         for (int j = 0; j < CU; ++j)
-            if ((bits >> j) & 1u) vec += r[j + 1] - r[j];
+            if ((bits >> j) & 1u) vec += r[j + 1] - r[j] - skip;
     }
     uint32_t tn, tv;
     block_scan2(n, vec, tn, tv, sa, sb);
@@ -536,9 +536,10 @@ __global__ void __launch_bounds__(SCAN_T) k_fr_scan(uint32_t* __restrict__ part_
 // frontier[i] = i-th selected vertex (ID order), voff[i] = offset of its first vector among the
 // selected vertices' vectors, vdelta[i] = its first vector's index in the list minus voff[i]
 // (mod 2^32); tile_first[t] for the tiles that start in its range.  voff[count] = total vectors.
+// `skip` leaves out the first vectors of every selected vertex (each selected one has more).
 __global__ void __launch_bounds__(T) k_fr_write(const unsigned long long* __restrict__ bm1,
                                                 const unsigned long long* __restrict__ bm2, uint64_t V,
-                                                const uint32_t* __restrict__ rowptr, const uint32_t* __restrict__ base_n,
+                                                const uint32_t* __restrict__ rowptr, uint32_t skip, const uint32_t* __restrict__ base_n,
                                                 const uint32_t* __restrict__ base_vec, const uint32_t* __restrict__ counters,
                                                 uint32_t nb, uint32_t* __restrict__ frontier, uint32_t* __restrict__ voff,
                                                 uint32_t* __restrict__ vdelta, uint32_t* __restrict__ tile_first)
@@ -556,7 +557,7 @@ __global__ void __launch_bounds__(T) k_fr_write(const unsigned long long* __rest
         load_rowptr(rowptr, v0, V, r);
 #pragma unroll
         for (int j = 0; j < CU; ++j)
-            if ((bits >> j) & 1u) vec += r[j + 1] - r[j];
+            if ((bits >> j) & 1u) vec += r[j + 1] - r[j] - skip;
     }
     uint32_t tn, tv;
     block_scan2(n, vec, tn, tv, sa, sb);
@@ -565,10 +566,10 @@ __global__ void __launch_bounds__(T) k_fr_write(const unsigned long long* __rest
 #pragma unroll
     for (int j = 0; j < CU; ++j) {
         if (!((bits >> j) & 1u)) continue;
-        const uint32_t cnt = r[j + 1] - r[j];
+        const uint32_t cnt = r[j + 1] - r[j] - skip;
         frontier[pos] = (uint32_t)(v0 + j);
         voff[pos] = vo;
-        vdelta[pos] = r[j] - vo;
+        vdelta[pos] = r[j] + skip - vo;
         for (uint64_t t = ((uint64_t)vo + PUSH_TILE - 1) / PUSH_TILE; t * PUSH_TILE < (uint64_t)vo + cnt; ++t) tile_first[t] = pos;
         ++pos;
         vo += cnt;
@@ -770,6 +771,105 @@ __global__ void __launch_bounds__(T) k_bfs_pull_expand(const uint32_t* __restric
     }
 }
 
+// BFS pull, early-exit pass.  Every in-neighbour of a wanted (unvisited) destination that has been
+// visited is in the frontier (it was visited in the previous iteration, else it would have
+// visited the destination already), so in the big pull iterations most wanted destinations find
+// a frontier source in their first vector.  Each wanted destination reads its first `first_n`
+// vectors in order and stops at the first one with a frontier source; that vector's largest
+// frontier source is its parent, which is the full scan's rule (smallest vector index, then
+// largest source) because no earlier vector has one.  A destination decided here is visited here
+// (parent, level, WantsInfo cleared, HasInfo* set, vote), so it needs no candidate word and no
+// place in the touched list, whose single counter would serialise millions of appends.  One
+// still undecided that has more vectors is marked in `unres`, and the tiled pass
+// (k_bfs_pull_expand, then k_bfs_visit) reads the rest of its vectors.  A warp owns FW whole
+// bitmap words (64 destinations each; lane l of slot q holds destination 64 w0 + 32 q + l), so
+// it writes their WantsInfo, HasInfo* and unres words without atomics, and the first-vector
+// loads of its 2 FW slots are issued together.
+constexpr int FW = 2;
+
+__global__ void __launch_bounds__(T, 8) k_bfs_pull_first(unsigned long long* __restrict__ wants,
+                                                      const unsigned long long* __restrict__ nonempty,
+                                                      const uint32_t* __restrict__ rowptr, const uint4* __restrict__ nbr,
+                                                      uint32_t V, uint64_t W, const unsigned long long* __restrict__ has,
+                                                      const uint32_t* __restrict__ hub_vid, uint32_t nhub,
+                                                      unsigned long long* __restrict__ has_next,
+                                                      unsigned long long* __restrict__ unres, uint32_t first_n,
+                                                      uint32_t* __restrict__ parent, uint32_t* __restrict__ level,
+                                                      uint32_t iter_host, const uint32_t* __restrict__ iter_dev, VoteCfg vc,
+                                                      unsigned long long* __restrict__ vote)
+{
+    __shared__ unsigned long long red[T / 32];
+    constexpr int Q = 2 * FW;
+    const int lane = threadIdx.x & 31;
+    const uint32_t iter = iter_dev ? *iter_dev : iter_host;
+    unsigned long long my_vote = 0;
+    // the largest frontier source of vector `vec`, or INF without one
+    auto vec_best = [&](uint32_t vec) -> uint32_t {
+        const uint4 s = __ldcs(nbr + vec);
+        const uint32_t ids[4] = { grz_hub_decode(s.x, hub_vid, nhub), grz_hub_decode(s.y, hub_vid, nhub),
+                                  grz_hub_decode(s.z, hub_vid, nhub), grz_hub_decode(s.w, hub_vid, nhub) };
+        bool in[4];
+#pragma unroll
+        for (int l = 0; l < 4; ++l) in[l] = ids[l] < V && bit_of(has, ids[l]);
+        // lanes ascend by source: the largest frontier source is the last lane with one
+        return in[3] ? ids[3] : in[2] ? ids[2] : in[1] ? ids[1] : in[0] ? ids[0] : INF;
+    };
+    const uint64_t nwarps = (uint64_t)gridDim.x * (T / 32);
+    for (uint64_t w0 = ((uint64_t)blockIdx.x * (T / 32) + (threadIdx.x >> 5)) * FW; w0 < W; w0 += nwarps * FW) {  // warp-uniform
+        unsigned long long sel[FW];
+#pragma unroll
+        for (int f = 0; f < FW; ++f) sel[f] = w0 + f < W ? wants[w0 + f] & nonempty[w0 + f] : 0ull;
+        uint32_t r0[Q], n[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const uint64_t v = 64 * w0 + 32 * (uint64_t)q + lane;
+            n[q] = 0;
+            if (v < V && ((sel[q >> 1] >> (32 * (q & 1) + lane)) & 1ull)) {
+                r0[q] = rowptr[v];
+                n[q] = rowptr[v + 1] - r0[q];
+            }
+        }
+        uint32_t p[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) p[q] = n[q] ? vec_best(r0[q]) : INF;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const uint32_t m = min(n[q], first_n);
+            for (uint32_t j = 1; j < m && p[q] == INF; ++j) p[q] = vec_best(r0[q] + j);
+        }
+        unsigned long long un[FW], hn[FW];
+#pragma unroll
+        for (int f = 0; f < FW; ++f) un[f] = hn[f] = 0ull;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const uint32_t v = (uint32_t)(64 * w0 + 32 * (uint64_t)q + lane);
+            const bool hit = p[q] != INF;
+            if (hit) {
+                parent[v] = p[q];
+                level[v] = iter;
+                my_vote += vc.of(v);
+            }
+            const unsigned mh = __ballot_sync(0xffffffffu, hit);
+            const unsigned mu = __ballot_sync(0xffffffffu, !hit && n[q] > first_n);
+            hn[q >> 1] |= (unsigned long long)mh << (32 * (q & 1));
+            un[q >> 1] |= (unsigned long long)mu << (32 * (q & 1));
+        }
+        if (lane == 0) {
+#pragma unroll
+            for (int f = 0; f < FW; ++f) {
+                if (w0 + f >= W) break;
+                unres[w0 + f] = un[f];
+                if (hn[f]) {
+                    has_next[w0 + f] |= hn[f];
+                    wants[w0 + f] &= ~hn[f];
+                }
+            }
+        }
+    }
+    my_vote = block_sum_u64(my_vote, red);
+    if (threadIdx.x == 0) vote_add(vote, my_vote);
+}
+
 // BFS: visit the touched destinations (pull: decode the winning (vector, source) key; push: the
 // smallest source), in one pass over the touched list
 template <bool FromPull>
@@ -947,6 +1047,7 @@ static int ensure_frontier_state(grz_graph* g)
     GRZ_CK(g, cudaMalloc((void**)&f.tile_first, sizeof(uint32_t) * tiles));
     GRZ_CK(g, cudaMalloc((void**)&f.fr_part, sizeof(uint32_t) * 2 * (V / CCHUNK + 1)));
     GRZ_CK(g, cudaMalloc((void**)&f.nonempty_pull, sizeof(unsigned long long) * W));
+    GRZ_CK(g, cudaMalloc((void**)&f.unres, sizeof(unsigned long long) * W));
     GRZ_CK(g, cudaMalloc((void**)&f.touched, sizeof(uint32_t) * (V + 1)));
     GRZ_CK(g, cudaMalloc((void**)&f.cand64, sizeof(unsigned long long) * (V + 1)));
     GRZ_CK(g, cudaMalloc((void**)&f.cand32, sizeof(uint32_t) * (V + 1)));
@@ -1069,6 +1170,14 @@ static bool cc_use_segments(const grz_graph* g)
     return g->tune.cc_segments != 1 && g->seg_nbr && g->nseg && g->pull.nhub == 0;
 }
 
+// kernels one segmented CC pull launches per source segment (the empty segments are skipped)
+static uint64_t cc_segment_launches(const grz_graph* g)
+{
+    uint64_t n = 0;
+    for (uint32_t sg = 0; sg < g->nseg; ++sg) n += g->seg_first[sg + 1] > g->seg_first[sg];
+    return n;
+}
+
 // Shared-memory opt-in and resident blocks per SM of the CC pull kernel, per device, block size
 // and staging form.
 template <int BT, bool BULK>
@@ -1147,14 +1256,15 @@ static int launch_cc_pull(grz_graph* g, uint64_t first, uint64_t count, const Vo
 
 // Compacts the vertices selected by bm1 & bm2, with their vector ranges in `rowptr`, into
 // fr.frontier / voff / vdelta / tile_first (counts on the device in counters[0], [2]).
-static void compact(grz_graph* g, const unsigned long long* bm1, const unsigned long long* bm2, const uint32_t* rowptr)
+static void compact(grz_graph* g, const unsigned long long* bm1, const unsigned long long* bm2, const uint32_t* rowptr,
+                    uint32_t skip = 0)
 {
     grz_frontier_state& f = g->fr;
     cudaStream_t st = g->stream;
     const unsigned nb = (unsigned)(g->V / CCHUNK + 1);
-    k_fr_count<<<nb, T, 0, st>>>(bm1, bm2, g->V, rowptr, f.fr_part, f.fr_part + nb); GRZ_COUNT_LAUNCH(g);
+    k_fr_count<<<nb, T, 0, st>>>(bm1, bm2, g->V, rowptr, skip, f.fr_part, f.fr_part + nb); GRZ_COUNT_LAUNCH(g);
     k_fr_scan<<<1, SCAN_T, 0, st>>>(f.fr_part, f.fr_part + nb, nb, f.counters); GRZ_COUNT_LAUNCH(g);
-    k_fr_write<<<nb, T, 0, st>>>(bm1, bm2, g->V, rowptr, f.fr_part, f.fr_part + nb, f.counters, nb, f.frontier, f.voff,
+    k_fr_write<<<nb, T, 0, st>>>(bm1, bm2, g->V, rowptr, skip, f.fr_part, f.fr_part + nb, f.counters, nb, f.frontier, f.voff,
                                  f.vdelta, f.tile_first); GRZ_COUNT_LAUNCH(g);
 }
 
@@ -1173,7 +1283,26 @@ static int edge_phase(grz_graph* g, int pull, uint64_t first, uint64_t count)
         if (!g->pull.nbr) return grz_set_error(g, GRZ_ERR_STATE, "pull list not loaded");
         if (count == 0) return GRZ_OK;
         const bool compacted = bfs && first == 0 && count == g->pull.nvec && !g->tune.bfs_pull_scan;
-        if (compacted) {
+        const uint32_t first_n = g->tune.bfs_pull_first;
+        if (compacted && first_n) {
+            // the whole list: each wanted destination's first vectors up to the first frontier
+            // source, then the remaining vectors of those left undecided
+            if (g->stats_on) {  // the work counted is the reference's: every vector of the wanted destinations
+                compact(g, f.wants, f.nonempty_pull, g->pull.rowptr);
+                GRZ_TRY(grz_stats_count_selected(g, &g->pull, f.frontier, f.counters));
+            }
+            grz_prof_begin(g, GRZ_PROF_BFS_PULL);
+            const uint64_t pgroups = (W + FW - 1) / FW;
+            const unsigned fgrid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((pgroups + T / 32 - 1) / (T / 32),
+                                                                                       (uint64_t)g->num_sms * 8));
+            k_bfs_pull_first<<<fgrid, T, 0, st>>>(f.wants, f.nonempty_pull, g->pull.rowptr, g->pull.nbr, V, W, f.has,
+                                                  g->pull.hub_vid, g->pull.nhub, f.has_next, f.unres, first_n, f.label, f.level,
+                                                  f.iter, f.level_dev, vc, f.vote); GRZ_COUNT_LAUNCH(g);
+            compact(g, f.unres, f.unres, g->pull.rowptr, first_n);
+            k_bfs_pull_expand<<<(unsigned)g->num_sms * 8, T, 0, st>>>(f.frontier, f.voff, f.vdelta, f.tile_first, f.counters,
+                                                                     g->pull.nbr, V, f.has, f.cand64, f.touched, f.counters + 1,
+                                                                     g->pull.hub_vid, g->pull.nhub, f.has_next, f.counters + 5); GRZ_COUNT_LAUNCH(g);
+        } else if (compacted) {
             // the whole list: only the vectors of wanted destinations
             grz_prof_begin(g, GRZ_PROF_PUSH_COMPACT);
             compact(g, f.wants, f.nonempty_pull, g->pull.rowptr);
@@ -1426,7 +1555,7 @@ void grz_frontier_park(grz_graph* g)
 void grz_frontier_free(grz_graph* g)
 {
     grz_frontier_state& f = g->fr;
-    void* ptrs[] = { f.label, f.level, f.has, f.has_next, f.wants, f.nonempty_push, f.nonempty_pull, f.frontier, f.voff, f.vdelta, f.tile_first, f.chg, f.dev_err,
+    void* ptrs[] = { f.label, f.level, f.has, f.has_next, f.wants, f.nonempty_push, f.nonempty_pull, f.unres, f.frontier, f.voff, f.vdelta, f.tile_first, f.chg, f.dev_err,
                      f.fr_part, f.touched, f.cand64, f.cand32,
                      f.counters, f.vote, f.sw_out, f.snap };
     for (void* p : ptrs) cudaFree(p);
@@ -1658,7 +1787,11 @@ int grz_frontier_run_graph(grz_graph* g, uint64_t* launches)
         f.has_next = t;
     }
     const bool bfs = f.app == GRZ_APP_BREADTH_FIRST_SEARCH;
-    const uint64_t per_pull = bfs ? (g->tune.bfs_pull_scan ? 2 : 5) : 1, per_push = bfs ? 5 : 4;
+    // kernels of one pull iteration: BFS scan + visit, or (first pass,) compaction, expand, visit;
+    // CC one pull launch, or one per source segment plus the whole-list one
+    const uint64_t per_pull = bfs ? (g->tune.bfs_pull_scan ? 2 : (g->tune.bfs_pull_first ? 6 : 5))
+                                  : (f.run_seg ? cc_segment_launches(g) + 1 : 1);
+    const uint64_t per_push = bfs ? 5 : 4;
     uint64_t k = 1 + n + (uint64_t)c.npull * per_pull + (uint64_t)c.npush * per_push + (n % 2);
     g->nlaunch += k;
     if (launches) *launches = k;

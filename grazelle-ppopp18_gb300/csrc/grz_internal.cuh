@@ -296,6 +296,7 @@ struct grz_mlp;
 #define GRZ_TUNE_PULL_STAGING 13
 #define GRZ_TUNE_PR_SEGMENT_BITS 14
 #define GRZ_TUNE_CC_SEGMENTS 16
+#define GRZ_TUNE_BFS_PULL_FIRST 17
 #define GRZ_TUNE_HUBS_LOADED 100
 
 // kernel shapes chosen per graph (grz_tune_set; the autotuner searches them)
@@ -316,6 +317,7 @@ struct grz_tuning {
     uint32_t pull_staging;   // CC pull's edge stream: 0 plain streaming loads, 1 bulk copies into shared memory
     uint32_t pr_segment_bits;  // PageRank source segments: 0 by size, 1 none, b in [8, 31]: 2^b sources per segment
     uint32_t cc_segments; // CC full pull over the source segments: 0 when built, 1 never, 2 build them by size
+    uint32_t bfs_pull_first;  // BFS pull: vectors a wanted destination reads in the early-exit pass (0: no such pass)
 };
 
 // Device control block of a CC/BFS run executed as one CUDA graph (grz_ccbfs.cu): the
@@ -354,6 +356,7 @@ struct grz_frontier_state {
     unsigned long long* wants;       // WantsInfo
     unsigned long long* nonempty_push;  // vertices with out-vectors
     unsigned long long* nonempty_pull;  // vertices with in-vectors
+    unsigned long long* unres;       // BFS pull: wanted destinations the early-exit pass left undecided
     uint32_t* frontier;              // compacted active sources
     uint32_t* voff;                  // push: offset of each source's first vector among the frontier's
     uint32_t* vdelta;                // push: first vector index in the list minus voff (mod 2^32)

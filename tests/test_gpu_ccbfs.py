@@ -258,22 +258,50 @@ def test_hub_encoding_and_kernel_shapes_do_not_change_results(name):
 
 @pytest.mark.parametrize("name", golden_names())
 def test_bfs_pull_compacted_equals_scan(name):
-    """The BFS pull over only the wanted destinations' vectors (compacted, the default) and the
-    scan of every vector give the same parents, levels, iterations and engine counts, and both
-    equal the single-thread reference's."""
+    """The BFS pull forms give the same parents, levels, iterations and engine counts, all equal
+    to the single-thread reference's: the early-exit pass over each wanted destination's first
+    1, 2 or 64 vectors followed by the pass over the rest (1 is the default), the pass over every
+    vector of the wanted destinations (compacted), and the scan of every vector."""
     rec, g = load_golden(name)
+    forms = ((0, 1), (0, 0), (0, 2), (0, 64), (1, 1))
     with gpu_graph(g) as G:
         for variant, flags in BFS_VARIANTS:
             out = []
-            for scan in (0, 1):
-                G.tune(bfs_pull_scan=scan)
+            for scan, first in forms:
+                G.tune(bfs_pull_scan=scan, bfs_pull_first=first)
                 par, lv, st = G.bfs(0, flags, stats=True)
                 out.append((par, lv, (st.iterations, st.pull_iterations, st.push_iterations)))
-            np.testing.assert_array_equal(out[0][0], out[1][0], err_msg=variant)
-            np.testing.assert_array_equal(out[0][1], out[1][1], err_msg=variant)
-            assert out[0][2] == out[1][2]
+            for o, form in zip(out[1:], forms[1:]):
+                np.testing.assert_array_equal(out[0][0], o[0], err_msg="%s %s" % (variant, form))
+                np.testing.assert_array_equal(out[0][1], o[1], err_msg="%s %s" % (variant, form))
+                assert out[0][2] == o[2]
             np.testing.assert_array_equal(out[0][0], rec[variant + "_parents"], err_msg=variant)
-        G.tune(bfs_pull_scan=0)
+        G.tune(bfs_pull_scan=0, bfs_pull_first=1)
+
+
+@pytest.mark.parametrize("first", [0, 1, 3])
+def test_bfs_pull_early_exit_graph_runs(first):
+    """Whole BFS runs (one CUDA graph each) on an R-MAT 16 from 6 roots, forced pull and the
+    default switch: levels equal to the oracle's and parents identical to the full pass's, for
+    each length of the early-exit pass."""
+    from grazelle import graphgen as gg
+    from grazelle.engine import Graph
+    g = gg.rmat(16, seed=71)
+    pull, push = g.pull_order().pairs(), g.push_order().pairs()
+    roots = [0, 1, 5, 77, 1000, 40000]
+    with Graph(0) as G:
+        G.load_pairs(g.num_vertices, pull, push)
+        base = {}
+        for flags in (O.FORCE_PULL, 0):
+            G.tune(bfs_pull_first=0)
+            for r in roots:
+                base[(flags, r)] = G.bfs(r, flags)
+            G.tune(bfs_pull_first=first)
+            for r in roots:
+                par, lv = G.bfs(r, flags)
+                np.testing.assert_array_equal(par, base[(flags, r)][0], err_msg="root %d flags %d" % (r, flags))
+                np.testing.assert_array_equal(lv, base[(flags, r)][1], err_msg="root %d flags %d" % (r, flags))
+                np.testing.assert_array_equal(lv, O.bfs_levels(push, g.num_vertices, r), err_msg="root %d" % r)
 
 
 def test_profiler_off_restores_the_graph_run():

@@ -515,8 +515,10 @@ def bfs_kernel_rooflines(G, roots, outdeg, indeg, hbm, hbm_kind):
     """Algorithmic bytes over CUDA-event time of the BFS edge kernels, from profiled host-loop
     runs: iteration k's push reads the frontier F = {level k-1}: 8 x (out-edges of F) + 8|F| +
     16|U|, U = {level k} the updates; its pull reads every vector of the wanted destinations W
-    (unvisited, with in-edges): 8 x (in-edges of W) + 8|W| + 16|U| (the reference's pull scans
-    them all; the kernel's early exit reads fewer)."""
+    (unvisited, with in-edges): 8 x (in-edges of W) + 8|W| + 16|U|.  That is the reference's
+    pull, which scans them all; the early-exit pass stops at each destination's first vector with
+    a frontier source and reads far fewer, so the pull's figure is work-equivalent bandwidth (its
+    DRAM traffic is in the launch-list summary), marked by `basis`."""
     agg = {"bfs_pull": [0, 0.0, 0], "bfs_push": [0, 0.0, 0]}
     G.profile(True)
     for r in roots:
@@ -546,7 +548,9 @@ def bfs_kernel_rooflines(G, roots, outdeg, indeg, hbm, hbm_kind):
         if n:
             gbs = b / (ms * 1e-3) / 1e9
             out[kind] = {"launches": n, "total_ms": round(ms, 3), "algorithmic_bytes": b, "achieved": round(gbs, 1),
-                         "peak": hbm, "peak_kind": hbm_kind, "unit": "GB/s", "frac": round(gbs / hbm, 4)}
+                         "peak": hbm, "peak_kind": hbm_kind, "unit": "GB/s", "frac": round(gbs / hbm, 4),
+                         "basis": "bytes the reference's full pass over the wanted destinations reads (the early exit "
+                                  "reads fewer: work-equivalent)" if kind == "bfs_pull" else "bytes the push reads"}
     return out
 
 

@@ -785,9 +785,15 @@ __global__ void __launch_bounds__(T) k_bfs_pull_expand(const uint32_t* __restric
 // bitmap words (64 destinations each; lane l of slot q holds destination 64 w0 + 32 q + l), so
 // it writes their WantsInfo, HasInfo* and unres words without atomics, and the first-vector
 // loads of its 2 FW slots are issued together.
-constexpr int FW = 2;
+#ifndef GRZ_BFS_FW
+#define GRZ_BFS_FW 2
+#endif
+#ifndef GRZ_BFS_MINB
+#define GRZ_BFS_MINB 8
+#endif
+constexpr int FW = GRZ_BFS_FW;
 
-__global__ void __launch_bounds__(T, 8) k_bfs_pull_first(unsigned long long* __restrict__ wants,
+__global__ void __launch_bounds__(T, GRZ_BFS_MINB) k_bfs_pull_first(unsigned long long* __restrict__ wants,
                                                       const unsigned long long* __restrict__ nonempty,
                                                       const uint32_t* __restrict__ rowptr, const uint4* __restrict__ nbr,
                                                       uint32_t V, uint64_t W, const unsigned long long* __restrict__ has,
@@ -966,10 +972,19 @@ __global__ void k_cc_init(uint32_t* __restrict__ label, uint64_t V)
     }
 }
 
+// parent and level of entries [0, V] = INF: four of each per thread with 16-byte stores (the arrays
+// are 256-byte aligned), the last few one by one
 __global__ void k_bfs_init(uint32_t* __restrict__ parent, uint32_t* __restrict__ level, uint64_t V)
 {
-    const uint64_t v = (uint64_t)blockIdx.x * T + threadIdx.x;
-    if (v <= V) { parent[v] = INF; level[v] = INF; }
+    const uint64_t q = (uint64_t)blockIdx.x * T + threadIdx.x;
+    const uint64_t v = 4 * q;
+    const uint4 inf4 = make_uint4(INF, INF, INF, INF);
+    if (v + 3 <= V) {
+        reinterpret_cast<uint4*>(parent)[q] = inf4;
+        reinterpret_cast<uint4*>(level)[q] = inf4;
+    } else {
+        for (uint64_t u = v; u <= V; ++u) { parent[u] = INF; level[u] = INF; }
+    }
 }
 
 // bitmaps: `all_ones` sets bits [0, V); bits at and beyond V stay clear
@@ -1122,7 +1137,7 @@ int grz_frontier_init(grz_graph* g, int app, int flags, uint32_t root)
         if (!(flags & GRZ_FLAG_WITHOUT_COUNT)) f.vote_host += V;
     } else {
         if (root >= V) return grz_set_error(g, GRZ_ERR_ARG, "root %u >= V", root);
-        k_bfs_init<<<blocks_for(V + 1), T, 0, st>>>(f.label, f.level, V); GRZ_COUNT_LAUNCH(g);
+        k_bfs_init<<<blocks_for((V + 1) / 4 + 1), T, 0, st>>>(f.label, f.level, V); GRZ_COUNT_LAUNCH(g);
         k_bitmap_init<<<blocks_for(W), T, 0, st>>>(f.has, W, V, 0); GRZ_COUNT_LAUNCH(g);
         k_bitmap_init<<<blocks_for(W), T, 0, st>>>(f.wants, W, V, 1); GRZ_COUNT_LAUNCH(g);
         const unsigned long long rbit = 1ull << (root & 63);
@@ -1294,7 +1309,7 @@ static int edge_phase(grz_graph* g, int pull, uint64_t first, uint64_t count)
             grz_prof_begin(g, GRZ_PROF_BFS_PULL);
             const uint64_t pgroups = (W + FW - 1) / FW;
             const unsigned fgrid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((pgroups + T / 32 - 1) / (T / 32),
-                                                                                       (uint64_t)g->num_sms * 8));
+                                                                                       (uint64_t)g->num_sms * GRZ_BFS_MINB));
             k_bfs_pull_first<<<fgrid, T, 0, st>>>(f.wants, f.nonempty_pull, g->pull.rowptr, g->pull.nbr, V, W, f.has,
                                                   g->pull.hub_vid, g->pull.nhub, f.has_next, f.unres, first_n, f.label, f.level,
                                                   f.iter, f.level_dev, vc, f.vote); GRZ_COUNT_LAUNCH(g);

@@ -208,14 +208,14 @@ __global__ void __launch_bounds__(BT) k_cc_pull(const uint4* __restrict__ nbr, c
     auto finish = [&](uint64_t v, bool live, uint32_t key, uint32_t labd, bool need, bool staged, uint4 sv) {
         uint32_t m = INF;
         if (need) {
-            const uint4 s4 = staged ? sv : __ldcs(nbr + v);
+            const uint4 s4 = staged ? sv : ld_stream(nbr + v);
             const uint32_t x[4] = { s4.x, s4.y, s4.z, s4.w };
             auto fetch = [&](uint32_t xl) -> uint32_t {
                 const uint32_t sl = xl - GRZ_HUB_BASE;
                 if (sl < ncache) return s_hub[sl];
                 // labels change in place during the phase: plain (coherent) loads
                 const uint32_t id = sl < nhub ? __ldg(hub_vid + sl) : min(xl, V);
-                return label[id];
+                return ld_label(label + id);
             };
             // A vector's lanes hold its sources in ascending order, so lane 0 is the
             // smallest-ID source: in a power-law graph often a hub whose label is already 0.
@@ -253,10 +253,10 @@ __global__ void __launch_bounds__(BT) k_cc_pull(const uint4* __restrict__ nbr, c
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const uint64_t i = (t0 + u) * BT + threadIdx.x;
-                keys[u] = i < nvec ? __ldcs(dstv + first + i) : INF;
+                keys[u] = i < nvec ? ld_stream(dstv + first + i) : INF;
             }
 #pragma unroll
-            for (int u = 0; u < U; ++u) labs[u] = keys[u] != INF ? label[keys[u]] : INF;
+            for (int u = 0; u < U; ++u) labs[u] = keys[u] != INF ? ld_label(label + keys[u]) : INF;
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const uint64_t i = (t0 + u) * BT + threadIdx.x;
@@ -297,7 +297,7 @@ __global__ void __launch_bounds__(BT) k_cc_pull(const uint4* __restrict__ nbr, c
                     }
                 }
             }
-            if (live && !staged) key = __ldcs(dstv + v);
+            if (live && !staged) key = ld_stream(dstv + v);
             finish(v, live, key, INF, live, staged, sv);
         }
     }

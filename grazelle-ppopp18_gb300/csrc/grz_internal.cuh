@@ -210,6 +210,56 @@ __device__ __forceinline__ bool mbar_try_wait_parity(unsigned long long* bar, un
     return ok != 0;
 }
 
+// Cache policy of the edge stream (read once per pass) and of the label gathers.
+// GRZ_STREAM_LD: 0 = ld.global.cs (evict-first), 1 = non-coherent load that does not allocate
+// in L1 (L1 capacity left to the gathers), 2 = coherent load that does not allocate in L1.
+// GRZ_GATHER_LD: 0 = plain coherent load, 1 = L1::evict_last (gathered lines kept over others).
+#ifndef GRZ_STREAM_LD
+#define GRZ_STREAM_LD 0
+#endif
+#ifndef GRZ_GATHER_LD
+#define GRZ_GATHER_LD 0
+#endif
+__device__ __forceinline__ uint4 ld_stream(const uint4* p)
+{
+#if GRZ_STREAM_LD == 1
+    uint4 r;
+    asm("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p));
+    return r;
+#elif GRZ_STREAM_LD == 2
+    uint4 r;
+    asm volatile("ld.global.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p));
+    return r;
+#else
+    return __ldcs(p);
+#endif
+}
+__device__ __forceinline__ uint32_t ld_stream(const uint32_t* p)
+{
+#if GRZ_STREAM_LD == 1
+    uint32_t r;
+    asm("ld.global.nc.L1::no_allocate.u32 %0, [%1];" : "=r"(r) : "l"(p));
+    return r;
+#elif GRZ_STREAM_LD == 2
+    uint32_t r;
+    asm volatile("ld.global.L1::no_allocate.u32 %0, [%1];" : "=r"(r) : "l"(p));
+    return r;
+#else
+    return __ldcs(p);
+#endif
+}
+// a label that may change during the phase (coherent load)
+__device__ __forceinline__ uint32_t ld_label(const uint32_t* p)
+{
+#if GRZ_GATHER_LD == 1
+    uint32_t r;
+    asm volatile("ld.global.L1::evict_last.u32 %0, [%1];" : "=r"(r) : "l"(p));
+    return r;
+#else
+    return *p;
+#endif
+}
+
 // waits for the phase with the given parity to complete; false when the wait ran out (1 s)
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity)
 {

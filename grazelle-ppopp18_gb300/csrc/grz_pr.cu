@@ -36,11 +36,17 @@ constexpr int PR_THREADS = 256;
 
 __device__ __forceinline__ u128 ld_fx(const u128* p, uint32_t i)
 {
+#if GRZ_GATHER_LD == 1
+    u128 r;
+    asm("ld.global.nc.L1::evict_last.v2.u64 {%0, %1}, [%2];" : "=l"(r.lo), "=l"(r.hi) : "l"(p + i));
+    return r;
+#else
     const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(p) + i);
     u128 r;
     r.lo = v.x;
     r.hi = v.y;
     return r;
+#endif
 }
 
 // a gathered prop as fixed point: stored so (16 bytes), or as the double it exactly converts
@@ -147,8 +153,8 @@ __device__ __forceinline__ void pr_gather_tiles(const uint4* __restrict__ nbr, c
         uint32_t key = 0xffffffffu;
         u128 val = u128_zero();
         if (live) {
-            const uint4 s = __ldcs(nbr + v);
-            key = __ldcs(dstv + v);
+            const uint4 s = ld_stream(nbr + v);
+            key = ld_stream(dstv + v);
             const uint32_t i0 = min(grz_hub_decode(s.x, hub_vid, nhub), V), i1 = min(grz_hub_decode(s.y, hub_vid, nhub), V);
             const uint32_t i2 = min(grz_hub_decode(s.z, hub_vid, nhub), V), i3 = min(grz_hub_decode(s.w, hub_vid, nhub), V);
             const u128 g0 = COH ? ld_prop_coh(prop_fx, i0) : ld_prop(prop_fx, i0);

@@ -188,7 +188,17 @@ __global__ void __launch_bounds__(GT, GATHER_RESIDENT) k_ppr_gather(const uint4*
 }
 
 constexpr int APPLY_SLOTS = 64;  // graphs whose next S a block sums in shared memory (beyond: global atomics)
-constexpr int APPLY_U = 8;       // tiles whose accumulators a thread loads before it stores anything
+#ifndef GRZ_PPR_APPLY_U
+#define GRZ_PPR_APPLY_U 1
+#endif
+#ifndef GRZ_PPR_APPLY_MINB
+#define GRZ_PPR_APPLY_MINB 8
+#endif
+// Tiles whose accumulators a thread loads before it stores anything, and resident apply blocks
+// per SM.  GB300 sweep (256 PPR x 20 iterations on the 32-graph batch): 8 tiles at 3 blocks per SM
+// (80 registers) 100.9 ms, 4 at 4 95.3 ms, 2 at 6 91.5 ms, 1 at 8 (32 registers) 89.7 ms: the
+// apply wants every warp slot more than loads in flight per thread.
+constexpr int APPLY_U = GRZ_PPR_APPLY_U;
 
 // bit j of word t: vertex 32t + j has pull vectors in two or more gather tiles, so its
 // accumulator is summed with atomics and the apply must clear it.  Every other accumulator is
@@ -214,8 +224,8 @@ __device__ __forceinline__ void s_flush(u128* s_part, u128* S_next, uint32_t g, 
 
 // vertex phase of all instances; thread per (vertex, instance).  The grid strides over tiles of
 // 32 vertices (all blocks on one moving front of the arrays), APPLY_U tiles at a time: their
-// accumulators are loaded first, so that enough bytes are in flight to cover DRAM latency.
-__global__ void __launch_bounds__(GT, 3) k_ppr_apply(u128* __restrict__ rowacc, const uint32_t* __restrict__ cut,
+// accumulators are loaded first, then the tiles are finished in order.
+__global__ void __launch_bounds__(GT, GRZ_PPR_APPLY_MINB) k_ppr_apply(u128* __restrict__ rowacc, const uint32_t* __restrict__ cut,
                                                      const double* __restrict__ inv_deg,
                                                      const uint32_t* __restrict__ degree, uint32_t V,
                                                      const uint32_t* __restrict__ voff_g, uint32_t G,
@@ -621,8 +631,8 @@ static int enqueue_ppr_chain(grz_batch* b, cudaStream_t cs, uint32_t iterations,
     }
     const uint64_t gtiles = (u->pull.nvec + TV - 1) / TV;
     const unsigned ggrid = persistent_grid(b, (gtiles + GT / 32 - 1) / (GT / 32), std::min(b->ppr_blocks, gres));
-    // 3 blocks per SM fit the apply's registers (8 tiles of accumulators per thread in flight)
-    const unsigned agrid = persistent_grid(b, (V + TV - 1) / TV, std::min(b->ppr_blocks, 3));
+    // GRZ_PPR_APPLY_MINB blocks per SM fit the apply's registers
+    const unsigned agrid = persistent_grid(b, (V + TV - 1) / TV, std::min(b->ppr_blocks, GRZ_PPR_APPLY_MINB));
     int cur = 0;
     for (uint32_t it = 0; it < iterations; ++it) {
         if (dmode)

@@ -75,18 +75,27 @@ __device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long x
     return x;
 }
 
-// Appends `val` to list[] for the lanes with `pred`, one atomicAdd per warp.  All 32 lanes must
-// call it together (the callers' loops are warp-uniform).
-__device__ __forceinline__ void warp_append(bool pred, uint32_t val, uint32_t* __restrict__ list, uint32_t* __restrict__ count)
+// Appends `val` to the BFS touched list for the lanes with `pred`, one atomicAdd per warp (all 32
+// lanes call it together; the callers' loops are warp-uniform), until the list holds
+// V / VISIT_DENSE_RATIO + 1 entries.  From there on k_bfs_visit sweeps all vertices instead of
+// reading the list (the count only grows), so further appends are skipped: a plain load of the
+// counter replaces the atomic, and a large iteration no longer queues millions of atomics on one
+// address.  Each destination is first-touched once per phase, so the list never outgrows V.
+__device__ __forceinline__ void touched_append(bool pred, uint32_t val, uint32_t* __restrict__ list, uint32_t* __restrict__ count,
+                                               uint32_t V)
 {
     const unsigned m = __ballot_sync(0xffffffffu, pred);
     if (!m) return;
     const int lane = threadIdx.x & 31;
     const int leader = __ffs(m) - 1;
+    const uint32_t cap = (uint32_t)((uint64_t)V / VISIT_DENSE_RATIO + 1);
     uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+    if (lane == leader) {
+        base = *(volatile const uint32_t*)count;
+        base = base >= cap ? INF : atomicAdd(count, (uint32_t)__popc(m));
+    }
     base = __shfl_sync(0xffffffffu, base, leader);
-    if (pred) list[base + __popc(m & ((1u << lane) - 1u))] = val;
+    if (pred && base != INF) list[base + __popc(m & ((1u << lane) - 1u))] = val;
 }
 
 struct VoteCfg {
@@ -381,7 +390,7 @@ __global__ void __launch_bounds__(T) k_bfs_pull(const uint4* __restrict__ nbr, c
                 first_touch = atomicMin(cand + key, k) == ~0ull;
                 if (first_touch) atomicOr(has_next + (key >> 6), 1ull << (key & 63));
             }
-            warp_append(first_touch, key, touched, ntouched);
+            touched_append(first_touch, key, touched, ntouched, V);
         }
     }
 }
@@ -637,7 +646,7 @@ __global__ void __launch_bounds__(T) k_push_expand(const uint32_t* __restrict__ 
                         first_touch = atomicMin(cand32 + d, u) == INF;
                         if (first_touch) atomicOr(has_next + (d >> 6), 1ull << (d & 63));
                     }
-                    warp_append(first_touch, d, touched, ntouched);
+                    touched_append(first_touch, d, touched, ntouched, V);
                 }
             } else if (live) {
                 const uint32_t msg = label[u];
@@ -764,7 +773,7 @@ __global__ void __launch_bounds__(T) k_bfs_pull_expand(const uint32_t* __restric
                     first_touch = atomicMin(cand + key, k) == ~0ull;
                     if (first_touch) atomicOr(has_next + (key >> 6), 1ull << (key & 63));
                 }
-                warp_append(first_touch, key, touched, ntouched);
+                touched_append(first_touch, key, touched, ntouched, V);
             }
             __syncthreads();
         }

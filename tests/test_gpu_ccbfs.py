@@ -281,9 +281,10 @@ def test_bfs_pull_compacted_equals_scan(name):
 
 @pytest.mark.parametrize("first", [0, 1, 3])
 def test_bfs_pull_early_exit_graph_runs(first):
-    """Whole BFS runs (one CUDA graph each) on an R-MAT 16 from 6 roots, forced pull and the
-    default switch: levels equal to the oracle's and parents identical to the full pass's, for
-    each length of the early-exit pass."""
+    """Whole BFS runs (one CUDA graph each) on an R-MAT 16 from 6 roots, forced pull, forced push
+    and the default switch: levels equal to the oracle's and parents identical to the full pass's,
+    for each length of the early-exit pass.  The big iterations touch more than V / 128
+    destinations, so the touched list stops growing and the visit sweeps all vertices."""
     from grazelle import graphgen as gg
     from grazelle.engine import Graph
     g = gg.rmat(16, seed=71)
@@ -292,7 +293,7 @@ def test_bfs_pull_early_exit_graph_runs(first):
     with Graph(0) as G:
         G.load_pairs(g.num_vertices, pull, push)
         base = {}
-        for flags in (O.FORCE_PULL, 0):
+        for flags in (O.FORCE_PULL, O.FORCE_PUSH, 0):
             G.tune(bfs_pull_first=0)
             for r in roots:
                 base[(flags, r)] = G.bfs(r, flags)

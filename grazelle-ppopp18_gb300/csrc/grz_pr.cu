@@ -260,10 +260,18 @@ __device__ __forceinline__ u128 block_reduce_u128(u128 s, u128* red)
 // iteration's sum of accumulators.  Of the accumulators it clears only those the next gather
 // adds to atomically (bit set in `cut`); the others are overwritten by the next gather's stores.
 // The grid strides over the vertices, PR_APPLY_U vertices per thread at a time whose
-// accumulators are loaded before anything is stored, so that enough bytes are in flight to
-// cover DRAM latency; one partial of S' per block.
-constexpr int PR_APPLY_U = 8;
-constexpr int PR_APPLY_RESIDENT = 3;  // blocks per SM that the launch bounds fit
+// accumulators are loaded before anything is stored; one partial of S' per block.  GB300 sweep of
+// vertices in flight per thread x blocks per SM: 8 x 3 (80 registers) 16.7 us at V = 2^20 and
+// 2.08 ms at V = 2^27; 4 x 4 14.5 us; 2 x 6 14.5 us and 1.25 ms; 1 x 8 (31 registers) 14.5 us and
+// 1.15 ms (5.2 TB/s of 44V bytes).  Occupancy hides the latency better than loads in flight.
+#ifndef GRZ_PR_APPLY_U
+#define GRZ_PR_APPLY_U 1
+#endif
+#ifndef GRZ_PR_APPLY_MINB
+#define GRZ_PR_APPLY_MINB 8
+#endif
+constexpr int PR_APPLY_U = GRZ_PR_APPLY_U;
+constexpr int PR_APPLY_RESIDENT = GRZ_PR_APPLY_MINB;  // blocks per SM that the launch bounds fit
 
 // the apply over vertices block*PR_THREADS + tid, strided by nblocks*PR_THREADS, U vertices per
 // thread loaded before any is stored; returns the block's partial of S' (valid in thread 0;

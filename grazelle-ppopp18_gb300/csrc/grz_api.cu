@@ -167,6 +167,7 @@ extern "C" int grz_graph_create(grz_graph** out, int device, void* stream)
     g->tune.pr_grid = 0;
     g->tune.pr_props = 0;
     g->tune.bfs_pull_first = 1;
+    g->tune.cc_pull_first = 1;
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g->l2_bytes, cudaDevAttrL2CacheSize, device);
@@ -893,6 +894,10 @@ extern "C" int grz_tune_set(grz_graph* g, int param, int64_t value)
         if (value > 1) return grz_set_error(g, GRZ_ERR_ARG, "pull staging must be 0 (loads) or 1 (bulk copies)");
         g->tune.pull_staging = (uint32_t)value;
         return GRZ_OK;
+    case GRZ_TUNE_CC_PULL_FIRST:
+        if (value > 1) return grz_set_error(g, GRZ_ERR_ARG, "CC first-vector pass must be 0 or 1");
+        g->tune.cc_pull_first = (uint32_t)value;
+        return GRZ_OK;
     case GRZ_TUNE_BFS_PULL_FIRST:
         if (value > 64) return grz_set_error(g, GRZ_ERR_ARG, "BFS pull first pass must read 0..64 vectors");
         g->tune.bfs_pull_first = (uint32_t)value;
@@ -936,6 +941,7 @@ extern "C" int grz_tune_get(const grz_graph* g, int param, int64_t* value)
     case GRZ_TUNE_PR_SEGMENT_BITS: *value = g->tune.pr_segment_bits; return GRZ_OK;
     case GRZ_TUNE_CC_SEGMENTS: *value = g->tune.cc_segments; return GRZ_OK;
     case GRZ_TUNE_BFS_PULL_FIRST: *value = g->tune.bfs_pull_first; return GRZ_OK;
+    case GRZ_TUNE_CC_PULL_FIRST: *value = g->tune.cc_pull_first; return GRZ_OK;
     case GRZ_TUNE_HUBS_LOADED: *value = g->pull.nhub; return GRZ_OK;
     default: return GRZ_ERR_ARG;
     }

@@ -44,6 +44,14 @@ constexpr uint32_t INF = 0xffffffffu;
 constexpr uint64_t VISIT_DENSE_RATIO = 128;
 // tiles of T vectors per step of the BFS pull kernel
 constexpr int BFS_PULL_TILES = 4;
+// bitmap words (64 destinations each) a warp of the first-vector passes owns, and their blocks per SM
+#ifndef GRZ_BFS_FW
+#define GRZ_BFS_FW 2
+#endif
+#ifndef GRZ_BFS_MINB
+#define GRZ_BFS_MINB 8
+#endif
+constexpr int FW = GRZ_BFS_FW;
 
 unsigned blocks_for(uint64_t n) { return (unsigned)((n + T - 1) / T); }
 
@@ -182,10 +190,16 @@ __global__ void __launch_bounds__(BT) k_cc_pull(const uint4* __restrict__ nbr, c
     for (uint32_t k = threadIdx.x; k < ncache; k += BT) s_hub[k] = label[__ldg(hub_vid + k)];
     const uint32_t ep = epoch_dev ? *epoch_dev : epoch;
     uint32_t mprev = 0;
-    const bool skip = use_prev && cc_prev_min(chg, ep, &mprev);
+    bool skip = use_prev && cc_prev_min(chg, ep, &mprev);
     // use_prev 2: a source-segment pass, which runs only when the skip is off (the full pass);
     // use_prev 3: the pass over the whole list that runs only when it is on (the grid agrees)
     if ((use_prev == 2 && skip) || (use_prev == 3 && !skip)) return;
+    // use_prev 4: after k_cc_pull_first, which ran because the skip is off: the destinations
+    // whose label is already 0, the smallest there is, need none of their vectors
+    if (use_prev == 4 && !skip) {
+        skip = true;
+        mprev = 0;
+    }
     const int lane = threadIdx.x & 31;
     unsigned long long my_vote = 0;
     uint32_t my_min = INF;
@@ -318,6 +332,98 @@ __global__ void __launch_bounds__(BT) k_cc_pull(const uint4* __restrict__ nbr, c
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
         if (threadIdx.x == 0) vote_add(vote, x);
     }
+}
+
+// CC pull, first-vector pass of an iteration without a usable previous minimum (the first pull of
+// a run).  Each destination's first vector holds its smallest-ID sources; in a power-law graph
+// one of them is usually a hub whose label is 0 by the time it is read (in place, as the full
+// pass reads them), and then the destination's label is final for this iteration: 0 cannot be
+// lowered.  This pass evaluates every destination's first vector (lane 0 first, as in
+// k_cc_pull), one destination per thread, and writes the new labels; the pass over the whole
+// list that follows (k_cc_pull with use_prev 4) skips the vectors of the destinations at 0 and
+// evaluates all vectors of the others, so the iteration's result is the full pull's.  A warp owns
+// CFW bitmap words (64 destinations each), so it writes their HasInfo* bits without atomics; the
+// pass records its smallest label written for the next iteration's skip.
+#ifndef GRZ_CC_FW
+#define GRZ_CC_FW 2
+#endif
+constexpr int CFW = GRZ_CC_FW;  // bitmap words a warp of k_cc_pull_first owns
+
+__global__ void __launch_bounds__(T, 8) k_cc_pull_first(const uint32_t* __restrict__ rowptr, const uint4* __restrict__ nbr,
+                                                      uint32_t V, uint64_t W, uint32_t* __restrict__ label,
+                                                      const uint32_t* __restrict__ hub_vid, uint32_t nhub,
+                                                      unsigned long long* __restrict__ has_next, VoteCfg vc,
+                                                      unsigned long long* __restrict__ vote, unsigned long long* __restrict__ chg,
+                                                      uint32_t epoch, const uint32_t* __restrict__ epoch_dev)
+{
+    __shared__ unsigned long long red[T / 32];
+    __shared__ uint32_t red32[T / 32];
+    const uint32_t ep = epoch_dev ? *epoch_dev : epoch;
+    uint32_t mprev = 0;
+    if (cc_prev_min(chg, ep, &mprev)) return;  // the skip pass does this iteration alone (block-uniform)
+    constexpr int Q = 2 * CFW;
+    const int lane = threadIdx.x & 31;
+    unsigned long long my_vote = 0;
+    uint32_t my_min = INF;
+    auto fetch = [&](uint32_t xl) -> uint32_t {
+        const uint32_t sl = xl - GRZ_HUB_BASE;
+        const uint32_t id = sl < nhub ? __ldg(hub_vid + sl) : min(xl, V);
+        return ld_label(label + id);
+    };
+    const uint64_t nwarps = (uint64_t)gridDim.x * (T / 32);
+    for (uint64_t w0 = ((uint64_t)blockIdx.x * (T / 32) + (threadIdx.x >> 5)) * CFW; w0 < W; w0 += nwarps * CFW) {  // warp-uniform
+        uint32_t r0[Q], n[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const uint64_t v = 64 * w0 + 32 * (uint64_t)q + lane;
+            n[q] = 0;
+            if (v < V) {
+                r0[q] = rowptr[v];
+                n[q] = rowptr[v + 1] - r0[q];
+            }
+        }
+        uint4 sv[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) sv[q] = n[q] ? ld_stream(nbr + r0[q]) : make_uint4(INF, INF, INF, INF);
+        uint32_t m[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) m[q] = n[q] ? fetch(sv[q].x) : INF;
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+            if (m[q] != 0 && n[q]) m[q] = min(m[q], min(min(fetch(sv[q].y), fetch(sv[q].z)), fetch(sv[q].w)));
+#pragma unroll
+        for (int f = 0; f < CFW; ++f) {
+            // word w0 + f: new labels of its 64 destinations, then its HasInfo* bits (set by lane 0;
+            // a destination counts in the vote if its bit was clear)
+            unsigned long long hn = 0ull;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int q = 2 * f + h;
+                const uint32_t v = (uint32_t)(64 * w0 + 32 * (uint64_t)q + lane);
+                bool ch = false;
+                if (n[q] && m[q] < ld_label(label + v)) {
+                    label[v] = m[q];  // this thread is the destination's only writer in this pass
+                    my_min = min(my_min, m[q]);
+                    ch = true;
+                }
+                hn |= (unsigned long long)__ballot_sync(0xffffffffu, ch) << (32 * h);
+            }
+            if (!hn) continue;  // warp-uniform
+            unsigned long long old = 0ull;
+            if (lane == 0) {
+                old = has_next[w0 + f];
+                has_next[w0 + f] = old | hn;
+            }
+            const unsigned long long fresh = hn & ~__shfl_sync(0xffffffffu, old, 0);
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                if ((fresh >> (32 * h + lane)) & 1ull) my_vote += vc.of((uint32_t)(64 * (w0 + f) + 32 * h + lane));
+        }
+    }
+    my_vote = block_sum_u64(my_vote, red);
+    if (threadIdx.x == 0) vote_add(vote, my_vote);
+    __syncthreads();
+    cc_record_min<T>(my_min, red32, chg, ep);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -794,13 +900,6 @@ __global__ void __launch_bounds__(T) k_bfs_pull_expand(const uint32_t* __restric
 // bitmap words (64 destinations each; lane l of slot q holds destination 64 w0 + 32 q + l), so
 // it writes their WantsInfo, HasInfo* and unres words without atomics, and the first-vector
 // loads of its 2 FW slots are issued together.
-#ifndef GRZ_BFS_FW
-#define GRZ_BFS_FW 2
-#endif
-#ifndef GRZ_BFS_MINB
-#define GRZ_BFS_MINB 8
-#endif
-constexpr int FW = GRZ_BFS_FW;
 
 __global__ void __launch_bounds__(T, GRZ_BFS_MINB) k_bfs_pull_first(unsigned long long* __restrict__ wants,
                                                       const unsigned long long* __restrict__ nonempty,
@@ -1191,7 +1290,7 @@ static unsigned visit_grid(const grz_graph* g)
 // grz_frontier_init under GRZ_TUNE_CC_SEGMENTS = 2); they need a pull list without hub encoding.
 static bool cc_use_segments(const grz_graph* g)
 {
-    return g->tune.cc_segments != 1 && g->seg_nbr && g->nseg && g->pull.nhub == 0;
+    return g->tune.cc_segments != 1 && g->seg_nbr && g->nseg && g->pull.nhub == 0 && !g->tune.cc_pull_first;
 }
 
 // kernels one segmented CC pull launches per source segment (the empty segments are skipped)
@@ -1244,6 +1343,20 @@ static int launch_cc_pull_bt(grz_graph* g, uint64_t first, uint64_t count, const
     // the skip needs every earlier iteration to have been complete (the whole list, or the whole
     // frontier): true for the driver loops, not once a phases.h call covered part of the list
     const bool whole = !f.cc_partial && first == 0 && count == g->pull.nvec;
+    if (whole && g->tune.cc_pull_first) {
+        // each destination's first vector, then the whole list without the destinations at 0
+        // (both decide on the device whether this is an iteration without a usable previous
+        // minimum; if not, the first returns at once and the second runs the skip pass)
+        const uint64_t W = words_of(g->V), groups = (W + CFW - 1) / CFW;
+        const unsigned fgrid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((groups + T / 32 - 1) / (T / 32),
+                                                                                   (uint64_t)g->num_sms * 8));
+        k_cc_pull_first<<<fgrid, T, 0, g->stream>>>(g->pull.rowptr, g->pull.nbr, (uint32_t)g->V, W, f.label, g->pull.hub_vid,
+                                                     g->pull.nhub, f.has_next, vc, f.vote, f.chg, f.iter, f.level_dev); GRZ_COUNT_LAUNCH(g);
+        k_cc_pull<BT, BULK><<<(unsigned)grid, BT, smem, g->stream>>>(g->pull.nbr, g->pull.shared, first, count, (uint32_t)g->V, f.label,
+                                                                    g->pull.hub_vid, g->pull.nhub, ncache, f.has_next, vc, f.vote, f.chg,
+                                                                    f.iter, f.level_dev, 4, f.dev_err); GRZ_COUNT_LAUNCH(g);
+        return GRZ_OK;
+    }
     if (whole && cc_use_segments(g)) {
         // The full pass (no skip yet) reads the source-segmented lists, so that each segment's
         // labels stay in L2 while its edges stream; the pass with the skip reads the whole list
@@ -1814,7 +1927,7 @@ int grz_frontier_run_graph(grz_graph* g, uint64_t* launches)
     // kernels of one pull iteration: BFS scan + visit, or (first pass,) compaction, expand, visit;
     // CC one pull launch, or one per source segment plus the whole-list one
     const uint64_t per_pull = bfs ? (g->tune.bfs_pull_scan ? 2 : (g->tune.bfs_pull_first ? 6 : 5))
-                                  : (f.run_seg ? cc_segment_launches(g) + 1 : 1);
+                                  : (f.run_seg ? cc_segment_launches(g) + 1 : (g->tune.cc_pull_first ? 2 : 1));
     const uint64_t per_push = bfs ? 5 : 4;
     uint64_t k = 1 + n + (uint64_t)c.npull * per_pull + (uint64_t)c.npush * per_push + (n % 2);
     g->nlaunch += k;

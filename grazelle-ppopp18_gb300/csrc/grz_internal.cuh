@@ -347,6 +347,7 @@ struct grz_mlp;
 #define GRZ_TUNE_PR_SEGMENT_BITS 14
 #define GRZ_TUNE_CC_SEGMENTS 16
 #define GRZ_TUNE_BFS_PULL_FIRST 17
+#define GRZ_TUNE_CC_PULL_FIRST 18
 #define GRZ_TUNE_HUBS_LOADED 100
 
 // kernel shapes chosen per graph (grz_tune_set; the autotuner searches them)
@@ -368,6 +369,7 @@ struct grz_tuning {
     uint32_t pr_segment_bits;  // PageRank source segments: 0 by size, 1 none, b in [8, 31]: 2^b sources per segment
     uint32_t cc_segments; // CC full pull over the source segments: 0 when built, 1 never, 2 build them by size
     uint32_t bfs_pull_first;  // BFS pull: vectors a wanted destination reads in the early-exit pass (0: no such pass)
+    uint32_t cc_pull_first;   // CC: each destination's first vector before the whole-list pass of a first pull (0: off)
 };
 
 // Device control block of a CC/BFS run executed as one CUDA graph (grz_ccbfs.cu): the

@@ -69,7 +69,7 @@ class Graph:
         return [(self.lib.grz_profile_kind_name(kinds[i]).decode(), ms[i]) for i in range(n)]
 
     def tune(self, **kw):
-        """Set kernel shapes: hubs=, cc_cache=, cc_threads=, cc_grid=, pr_grid=, bfs_pull_scan=, bfs_pull_first=,
+        """Set kernel shapes: hubs=, cc_cache=, cc_threads=, cc_grid=, pr_grid=, bfs_pull_scan=, bfs_pull_first=, cc_pull_first=,
         pr_props=, ingest_chunks=, pr_persistent=, pull_staging=, pr_segment_bits=, cc_segments= (results never depend on them; hubs and ingest_chunks take effect
         at the next load), and the bounds of the device-side waits: pr_wait_limit_us=, run_max_iterations=,
         run_limit_us= (pr_withhold= injects a barrier fault for tests)."""
@@ -80,7 +80,7 @@ class Graph:
                 "pr_withhold": native.TUNE_PR_WITHHOLD, "run_max_iterations": native.TUNE_RUN_MAX_ITERATIONS,
                 "run_limit_us": native.TUNE_RUN_LIMIT_US, "pull_staging": native.TUNE_PULL_STAGING,
                 "pr_segment_bits": native.TUNE_PR_SEGMENT_BITS,
-                "cc_segments": native.TUNE_CC_SEGMENTS, "bfs_pull_first": native.TUNE_BFS_PULL_FIRST}
+                "cc_segments": native.TUNE_CC_SEGMENTS, "bfs_pull_first": native.TUNE_BFS_PULL_FIRST, "cc_pull_first": native.TUNE_CC_PULL_FIRST}
         for k, v in kw.items():
             self._ck(self.lib.grz_tune_set(self.h, keys[k], int(v)))
         return self
@@ -92,7 +92,7 @@ class Graph:
                      ("bfs_pull_scan", native.TUNE_BFS_PULL_SCAN), ("pr_props", native.TUNE_PR_PROPS),
                      ("ingest_chunks", native.TUNE_INGEST_CHUNKS), ("pr_persistent", native.TUNE_PR_PERSISTENT),
                      ("pr_wait_limit_us", native.TUNE_PR_WAIT_LIMIT_US), ("pr_withhold", native.TUNE_PR_WITHHOLD),
-                     ("run_max_iterations", native.TUNE_RUN_MAX_ITERATIONS), ("run_limit_us", native.TUNE_RUN_LIMIT_US), ("pull_staging", native.TUNE_PULL_STAGING), ("pr_segment_bits", native.TUNE_PR_SEGMENT_BITS), ("cc_segments", native.TUNE_CC_SEGMENTS), ("bfs_pull_first", native.TUNE_BFS_PULL_FIRST),
+                     ("run_max_iterations", native.TUNE_RUN_MAX_ITERATIONS), ("run_limit_us", native.TUNE_RUN_LIMIT_US), ("pull_staging", native.TUNE_PULL_STAGING), ("pr_segment_bits", native.TUNE_PR_SEGMENT_BITS), ("cc_segments", native.TUNE_CC_SEGMENTS), ("bfs_pull_first", native.TUNE_BFS_PULL_FIRST), ("cc_pull_first", native.TUNE_CC_PULL_FIRST),
                      ("hubs_loaded", native.TUNE_HUBS_LOADED)):
             v = C.c_int64()
             self._ck(self.lib.grz_tune_get(self.h, p, C.byref(v)))

@@ -37,6 +37,7 @@ TUNE_PR_PERSISTENT, TUNE_PR_WAIT_LIMIT_US, TUNE_PR_WITHHOLD = 8, 9, 10
 TUNE_RUN_MAX_ITERATIONS, TUNE_RUN_LIMIT_US, TUNE_PULL_STAGING, TUNE_PR_SEGMENT_BITS = 11, 12, 13, 14
 TUNE_CC_SEGMENTS = 16
 TUNE_BFS_PULL_FIRST = 17
+TUNE_CC_PULL_FIRST = 18
 BATCH_TUNE_PPR_BLOCKS, BATCH_TUNE_BFS_BLOCKS, BATCH_TUNE_PPR_PROPS = 0, 1, 2
 FLAG_HOST_LOOP = 16  # grz_cc_run / grz_bfs_run: host round trip per iteration instead of one CUDA graph
 MLP_FEATURES, MLP_HIDDEN, MLP_PARAMS = 12, 32, 1505

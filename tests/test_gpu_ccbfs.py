@@ -402,3 +402,32 @@ def test_cc_full_pull_over_source_segments():
             G.pagerank(2)                                                 # builds them
             np.testing.assert_array_equal(G.connected_components(), ref)   # the run graph is captured again
             np.testing.assert_array_equal(G.bfs(0)[1], O.bfs_levels(push, V, 0))
+
+
+@pytest.mark.parametrize("first", [0, 1])
+def test_cc_first_vector_pass(first):
+    """CC with and without the first-vector pass (GRZ_TUNE_CC_PULL_FIRST): labels equal to the
+    golden reference's on every golden graph and build variant, and to the oracle's on symmetric
+    and directed R-MAT 16, through whole runs (graph path) and the host loop, with hub encoding too."""
+    from grazelle import graphgen as gg
+    from grazelle.engine import Graph
+    for name in golden_names():
+        rec, g = load_golden(name)
+        with gpu_graph(g) as G:
+            G.tune(cc_pull_first=first)
+            for variant, flags in CC_VARIANTS:
+                np.testing.assert_array_equal(G.connected_components(flags), rec[variant + "_labels"], err_msg="%s %s" % (name, variant))
+    for sym in (True, False):
+        g = gg.rmat(16, seed=91, symmetric=sym)
+        pull, push = g.pull_order().pairs(), g.push_order().pairs()
+        ref = O.cc_min_labels(pull, g.num_vertices).astype(np.float64)
+        for hubs in (0, 256):
+            with Graph(0) as G:
+                G.tune(hubs=hubs, cc_cache=128, cc_pull_first=first)
+                G.load_pairs(g.num_vertices, pull, push)
+                for _ in range(2):
+                    np.testing.assert_array_equal(G.connected_components(), ref, err_msg="sym %s hubs %d" % (sym, hubs))
+                np.testing.assert_array_equal(G.connected_components(O.FORCE_PULL), ref)
+                G.profile(True)  # the host loop, one launch per kernel
+                np.testing.assert_array_equal(G.connected_components(), ref)
+                G.profile(False)

@@ -895,7 +895,7 @@ extern "C" int grz_tune_set(grz_graph* g, int param, int64_t value)
         g->tune.pull_staging = (uint32_t)value;
         return GRZ_OK;
     case GRZ_TUNE_CC_PULL_FIRST:
-        if (value > 1) return grz_set_error(g, GRZ_ERR_ARG, "CC first-vector pass must be 0 or 1");
+        if (value > 2) return grz_set_error(g, GRZ_ERR_ARG, "CC first-vector pass must be 0, 1 or 2");
         g->tune.cc_pull_first = (uint32_t)value;
         return GRZ_OK;
     case GRZ_TUNE_BFS_PULL_FIRST:

@@ -342,25 +342,32 @@ __global__ void __launch_bounds__(BT) k_cc_pull(const uint4* __restrict__ nbr, c
 // k_cc_pull), one destination per thread, and writes the new labels; the pass over the whole
 // list that follows (k_cc_pull with use_prev 4) skips the vectors of the destinations at 0 and
 // evaluates all vectors of the others, so the iteration's result is the full pull's.  A warp owns
-// CFW bitmap words (64 destinations each), so it writes their HasInfo* bits without atomics; the
-// pass records its smallest label written for the next iteration's skip.
+// CFW bitmap words (64 destinations each), so it writes their HasInfo* bits (and, for the
+// compacted form, their `unres` bits: destinations still above 0 with more vectors) without
+// atomics; the pass records its smallest label written for the next iteration's skip, and sets
+// *gate to 1 in an iteration it runs, 0 in one it leaves to the skip pass.
 #ifndef GRZ_CC_FW
-#define GRZ_CC_FW 2
+#define GRZ_CC_FW 1
 #endif
-constexpr int CFW = GRZ_CC_FW;  // bitmap words a warp of k_cc_pull_first owns
+// bitmap words a warp of k_cc_pull_first owns (GB300, R-MAT 24 sym: 1 word 0.42 ms for the first pull,
+// 2 words 0.46 ms, with 60 bytes of spills at 32 registers)
+constexpr int CFW = GRZ_CC_FW;
 
 __global__ void __launch_bounds__(T, 8) k_cc_pull_first(const uint32_t* __restrict__ rowptr, const uint4* __restrict__ nbr,
                                                       uint32_t V, uint64_t W, uint32_t* __restrict__ label,
                                                       const uint32_t* __restrict__ hub_vid, uint32_t nhub,
                                                       unsigned long long* __restrict__ has_next, VoteCfg vc,
                                                       unsigned long long* __restrict__ vote, unsigned long long* __restrict__ chg,
-                                                      uint32_t epoch, const uint32_t* __restrict__ epoch_dev)
+                                                      uint32_t epoch, const uint32_t* __restrict__ epoch_dev,
+                                                      unsigned long long* __restrict__ unres, uint32_t* __restrict__ gate)
 {
     __shared__ unsigned long long red[T / 32];
     __shared__ uint32_t red32[T / 32];
     const uint32_t ep = epoch_dev ? *epoch_dev : epoch;
     uint32_t mprev = 0;
-    if (cc_prev_min(chg, ep, &mprev)) return;  // the skip pass does this iteration alone (block-uniform)
+    const bool skip_iteration = cc_prev_min(chg, ep, &mprev);  // the same on every thread
+    if (gate && blockIdx.x == 0 && threadIdx.x == 0) *gate = skip_iteration ? 0u : 1u;
+    if (skip_iteration) return;  // the skip pass does this iteration alone
     constexpr int Q = 2 * CFW;
     const int lane = threadIdx.x & 31;
     unsigned long long my_vote = 0;
@@ -395,19 +402,25 @@ __global__ void __launch_bounds__(T, 8) k_cc_pull_first(const uint32_t* __restri
         for (int f = 0; f < CFW; ++f) {
             // word w0 + f: new labels of its 64 destinations, then its HasInfo* bits (set by lane 0;
             // a destination counts in the vote if its bit was clear)
-            unsigned long long hn = 0ull;
+            unsigned long long hn = 0ull, un = 0ull;
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 const int q = 2 * f + h;
                 const uint32_t v = (uint32_t)(64 * w0 + 32 * (uint64_t)q + lane);
-                bool ch = false;
-                if (n[q] && m[q] < ld_label(label + v)) {
-                    label[v] = m[q];  // this thread is the destination's only writer in this pass
-                    my_min = min(my_min, m[q]);
-                    ch = true;
+                bool ch = false, more = false;
+                if (n[q]) {
+                    const uint32_t cur = ld_label(label + v);
+                    if (m[q] < cur) {
+                        label[v] = m[q];  // this thread is the destination's only writer in this pass
+                        my_min = min(my_min, m[q]);
+                        ch = true;
+                    }
+                    more = n[q] > 1 && min(m[q], cur) != 0;  // still open: its other vectors are read next
                 }
                 hn |= (unsigned long long)__ballot_sync(0xffffffffu, ch) << (32 * h);
+                un |= (unsigned long long)__ballot_sync(0xffffffffu, more) << (32 * h);
             }
+            if (unres && lane == 0 && w0 + f < W) unres[w0 + f] = un;
             if (!hn) continue;  // warp-uniform
             unsigned long long old = 0ull;
             if (lane == 0) {
@@ -582,12 +595,13 @@ __device__ __forceinline__ void load_rowptr(const uint32_t* __restrict__ rowptr,
 
 __global__ void __launch_bounds__(T) k_fr_count(const unsigned long long* __restrict__ bm1,
                                                 const unsigned long long* __restrict__ bm2, uint64_t V,
-                                                const uint32_t* __restrict__ rowptr, uint32_t skip, uint32_t* __restrict__ part_n,
-                                                uint32_t* __restrict__ part_vec)
+                                                const uint32_t* __restrict__ rowptr, uint32_t skip, const uint32_t* __restrict__ gate,
+                                                uint32_t* __restrict__ part_n, uint32_t* __restrict__ part_vec)
 {
     __shared__ uint32_t sa[T / 32 + 1], sb[T / 32 + 1];
     const uint64_t v0 = (uint64_t)blockIdx.x * CCHUNK + (uint64_t)threadIdx.x * CU;
-    const uint32_t bits = selected_bits(bm1, bm2, v0, V);
+    // a zero gate selects nothing (the bitmaps were not written in this phase)
+    const uint32_t bits = (gate && *gate == 0u) ? 0u : selected_bits(bm1, bm2, v0, V);
     if (!__syncthreads_or(bits)) {
         if (threadIdx.x == 0) { part_n[blockIdx.x] = 0; part_vec[blockIdx.x] = 0; }
         return;
@@ -884,6 +898,102 @@ __global__ void __launch_bounds__(T) k_bfs_pull_expand(const uint32_t* __restric
             __syncthreads();
         }
     }
+}
+
+// CC pull over the remaining vectors of the destinations k_cc_pull_first left open (label above 0
+// after their first vector), compacted with their vector ranges as the BFS pull's are (the same
+// tiles, queue and binary search as k_bfs_pull_expand).  A vector whose destination reached 0
+// meanwhile needs no gathers; the others take the minimum of their lanes' labels (lane 0 first),
+// reduced per destination within the warp, and the run's last lane lowers the label in place.
+__global__ void __launch_bounds__(T) k_cc_pull_expand(const uint32_t* __restrict__ dests, const uint32_t* __restrict__ voff,
+                                                      const uint32_t* __restrict__ vdelta, const uint32_t* __restrict__ tile_first,
+                                                      const uint32_t* __restrict__ counters, const uint4* __restrict__ nbr,
+                                                      uint32_t V, uint32_t* __restrict__ label, const uint32_t* __restrict__ hub_vid,
+                                                      uint32_t nhub, unsigned long long* __restrict__ has_next, VoteCfg vc,
+                                                      unsigned long long* __restrict__ vote, unsigned long long* __restrict__ chg,
+                                                      uint32_t epoch, const uint32_t* __restrict__ epoch_dev,
+                                                      uint32_t* __restrict__ queue)
+{
+    __shared__ uint32_t s_dst[PUSH_TILE + 1];
+    __shared__ uint32_t s_off[PUSH_TILE + 1];
+    __shared__ uint32_t s_delta[PUSH_TILE + 1];
+    __shared__ uint32_t s_chunk;
+    __shared__ unsigned long long red[T / 32];
+    __shared__ uint32_t red32[T / 32];
+    const uint32_t ep = epoch_dev ? *epoch_dev : epoch;
+    const uint32_t nd = counters[0], total = counters[2];
+    const uint32_t ntiles = (total + PUSH_TILE - 1) / PUSH_TILE;
+    const int lane = threadIdx.x & 31;
+    unsigned long long my_vote = 0;
+    uint32_t my_min = INF;
+    auto fetch = [&](uint32_t xl) -> uint32_t {
+        const uint32_t sl = xl - GRZ_HUB_BASE;
+        const uint32_t id = sl < nhub ? __ldg(hub_vid + sl) : min(xl, V);
+        return ld_label(label + id);
+    };
+    for (;;) {
+        if (threadIdx.x == 0) s_chunk = atomicAdd(queue, 1u);
+        __syncthreads();
+        const uint32_t chunk = s_chunk;
+        __syncthreads();  // every thread has read s_chunk before it is replaced
+        if ((uint64_t)chunk * PULL_CHUNK >= ntiles) break;
+        const uint32_t chunk_end = min(ntiles, (chunk + 1) * PULL_CHUNK);
+        for (uint32_t tile = chunk * PULL_CHUNK; tile < chunk_end; ++tile) {
+            const uint32_t first = tile_first[tile];
+            const uint32_t t0 = tile * PUSH_TILE;
+            const uint32_t tend = min(total, t0 + PUSH_TILE);
+            const uint32_t nw = min(PUSH_TILE, nd - first);
+            for (uint32_t i = threadIdx.x; i <= nw; i += T) {
+                s_off[i] = voff[first + i];
+                if (i < nw) {
+                    s_dst[i] = dests[first + i];
+                    s_delta[i] = vdelta[first + i];
+                }
+            }
+            __syncthreads();
+            for (uint32_t base = t0; base < tend; base += T) {  // warp-uniform trip count
+                const uint32_t gv = base + threadIdx.x;
+                uint32_t key = INF, m = INF;
+                if (gv < tend) {
+                    int lo = 0, hi = (int)nw - 1;  // last entry with s_off <= gv
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (s_off[mid] <= gv) lo = mid; else hi = mid - 1;
+                    }
+                    key = s_dst[lo];
+                    if (ld_label(label + key) != 0) {
+                        const uint4 sv = ld_stream(nbr + (uint32_t)(gv + s_delta[lo]));
+                        m = fetch(sv.x);
+                        if (m != 0) m = min(m, min(min(fetch(sv.y), fetch(sv.z)), fetch(sv.w)));
+                    }
+                }
+                if (!__any_sync(0xffffffffu, m != INF)) continue;
+                const uint32_t prevkey = __shfl_up_sync(0xffffffffu, key, 1);
+                const uint32_t nextkey = __shfl_down_sync(0xffffffffu, key, 1);
+                const bool head = lane == 0 || key != prevkey;
+                const bool tail = lane == 31 || key != nextkey;
+                const unsigned heads = __ballot_sync(0xffffffffu, head);
+                const int segstart = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+                const int maxlen = __reduce_max_sync(0xffffffffu, (unsigned)(lane - segstart + 1));
+                for (int off = 1; off < maxlen; off <<= 1) {
+                    const uint32_t o = __shfl_up_sync(0xffffffffu, m, off);
+                    if (lane - off >= segstart) m = min(m, o);
+                }
+                if (tail && m != INF && m < ld_label(label + key)) {
+                    const uint32_t old = atomicMin(label + key, m);
+                    if (m < old) {
+                        my_min = min(my_min, m);
+                        if (bit_set_first(has_next, key)) my_vote += vc.of(key);
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    my_vote = block_sum_u64(my_vote, red);
+    if (threadIdx.x == 0) vote_add(vote, my_vote);
+    __syncthreads();
+    cc_record_min<T>(my_min, red32, chg, ep);
 }
 
 // BFS pull, early-exit pass.  Every in-neighbour of a wanted (unvisited) destination that has been
@@ -1328,6 +1438,10 @@ static int cc_pull_config_any(grz_graph* g, size_t smem, int* resident)
     return g->tune.pull_staging ? cc_pull_config<BT, true>(g, smem, resident) : cc_pull_config<BT, false>(g, smem, resident);
 }
 
+// Compacts the vertices selected by bm1 & bm2 (defined below)
+static void compact(grz_graph* g, const unsigned long long* bm1, const unsigned long long* bm2, const uint32_t* rowptr,
+                    uint32_t skip = 0, const uint32_t* gate = nullptr);
+
 template <int BT, bool BULK>
 static int launch_cc_pull_bt(grz_graph* g, uint64_t first, uint64_t count, const VoteCfg& vc)
 {
@@ -1344,17 +1458,31 @@ static int launch_cc_pull_bt(grz_graph* g, uint64_t first, uint64_t count, const
     // frontier): true for the driver loops, not once a phases.h call covered part of the list
     const bool whole = !f.cc_partial && first == 0 && count == g->pull.nvec;
     if (whole && g->tune.cc_pull_first) {
-        // each destination's first vector, then the whole list without the destinations at 0
-        // (both decide on the device whether this is an iteration without a usable previous
-        // minimum; if not, the first returns at once and the second runs the skip pass)
+        // Each destination's first vector (k_cc_pull_first, which decides on the device whether
+        // this is an iteration without a usable previous minimum and otherwise returns at once).
+        // Form 1: the whole list without the destinations at 0.  Form 2: the destinations it left
+        // open are compacted with their remaining vectors and pulled (gated, empty in a skip
+        // iteration), and the skip pass over the whole list runs only in a skip iteration; its
+        // first pull is shorter, but it propagates less in place and the runs take one iteration
+        // more (GB300, R-MAT 24 sym: 0.81 against 0.76 ms per run).
+        const bool open_list = g->tune.cc_pull_first == 2;
+        uint32_t* gate = f.counters + 6;
         const uint64_t W = words_of(g->V), groups = (W + CFW - 1) / CFW;
         const unsigned fgrid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((groups + T / 32 - 1) / (T / 32),
                                                                                    (uint64_t)g->num_sms * 8));
         k_cc_pull_first<<<fgrid, T, 0, g->stream>>>(g->pull.rowptr, g->pull.nbr, (uint32_t)g->V, W, f.label, g->pull.hub_vid,
-                                                     g->pull.nhub, f.has_next, vc, f.vote, f.chg, f.iter, f.level_dev); GRZ_COUNT_LAUNCH(g);
+                                                     g->pull.nhub, f.has_next, vc, f.vote, f.chg, f.iter, f.level_dev,
+                                                     open_list ? f.unres : nullptr, gate); GRZ_COUNT_LAUNCH(g);
+        if (open_list) {
+            compact(g, f.unres, f.unres, g->pull.rowptr, 1, gate);
+            k_cc_pull_expand<<<(unsigned)g->num_sms * 8, T, 0, g->stream>>>(f.frontier, f.voff, f.vdelta, f.tile_first, f.counters,
+                                                                           g->pull.nbr, (uint32_t)g->V, f.label, g->pull.hub_vid,
+                                                                           g->pull.nhub, f.has_next, vc, f.vote, f.chg, f.iter,
+                                                                           f.level_dev, f.counters + 5); GRZ_COUNT_LAUNCH(g);
+        }
         k_cc_pull<BT, BULK><<<(unsigned)grid, BT, smem, g->stream>>>(g->pull.nbr, g->pull.shared, first, count, (uint32_t)g->V, f.label,
                                                                     g->pull.hub_vid, g->pull.nhub, ncache, f.has_next, vc, f.vote, f.chg,
-                                                                    f.iter, f.level_dev, 4, f.dev_err); GRZ_COUNT_LAUNCH(g);
+                                                                    f.iter, f.level_dev, open_list ? 3 : 4, f.dev_err); GRZ_COUNT_LAUNCH(g);
         return GRZ_OK;
     }
     if (whole && cc_use_segments(g)) {
@@ -1394,12 +1522,12 @@ static int launch_cc_pull(grz_graph* g, uint64_t first, uint64_t count, const Vo
 // Compacts the vertices selected by bm1 & bm2, with their vector ranges in `rowptr`, into
 // fr.frontier / voff / vdelta / tile_first (counts on the device in counters[0], [2]).
 static void compact(grz_graph* g, const unsigned long long* bm1, const unsigned long long* bm2, const uint32_t* rowptr,
-                    uint32_t skip = 0)
+                    uint32_t skip, const uint32_t* gate)
 {
     grz_frontier_state& f = g->fr;
     cudaStream_t st = g->stream;
     const unsigned nb = (unsigned)(g->V / CCHUNK + 1);
-    k_fr_count<<<nb, T, 0, st>>>(bm1, bm2, g->V, rowptr, skip, f.fr_part, f.fr_part + nb); GRZ_COUNT_LAUNCH(g);
+    k_fr_count<<<nb, T, 0, st>>>(bm1, bm2, g->V, rowptr, skip, gate, f.fr_part, f.fr_part + nb); GRZ_COUNT_LAUNCH(g);
     k_fr_scan<<<1, SCAN_T, 0, st>>>(f.fr_part, f.fr_part + nb, nb, f.counters); GRZ_COUNT_LAUNCH(g);
     k_fr_write<<<nb, T, 0, st>>>(bm1, bm2, g->V, rowptr, skip, f.fr_part, f.fr_part + nb, f.counters, nb, f.frontier, f.voff,
                                  f.vdelta, f.tile_first); GRZ_COUNT_LAUNCH(g);
@@ -1927,7 +2055,7 @@ int grz_frontier_run_graph(grz_graph* g, uint64_t* launches)
     // kernels of one pull iteration: BFS scan + visit, or (first pass,) compaction, expand, visit;
     // CC one pull launch, or one per source segment plus the whole-list one
     const uint64_t per_pull = bfs ? (g->tune.bfs_pull_scan ? 2 : (g->tune.bfs_pull_first ? 6 : 5))
-                                  : (f.run_seg ? cc_segment_launches(g) + 1 : (g->tune.cc_pull_first ? 2 : 1));
+                                  : (f.run_seg ? cc_segment_launches(g) + 1 : (g->tune.cc_pull_first == 2 ? 6 : (g->tune.cc_pull_first ? 2 : 1)));
     const uint64_t per_push = bfs ? 5 : 4;
     uint64_t k = 1 + n + (uint64_t)c.npull * per_pull + (uint64_t)c.npush * per_push + (n % 2);
     g->nlaunch += k;

@@ -404,9 +404,11 @@ def test_cc_full_pull_over_source_segments():
             np.testing.assert_array_equal(G.bfs(0)[1], O.bfs_levels(push, V, 0))
 
 
-@pytest.mark.parametrize("first", [0, 1])
+@pytest.mark.parametrize("first", [0, 1, 2])
 def test_cc_first_vector_pass(first):
-    """CC with and without the first-vector pass (GRZ_TUNE_CC_PULL_FIRST): labels equal to the
+    """CC without the first-vector pass and with it in both forms (GRZ_TUNE_CC_PULL_FIRST: then
+    the whole list without the destinations at 0, or the open destinations' remaining vectors):
+    labels equal to the
     golden reference's on every golden graph and build variant, and to the oracle's on symmetric
     and directed R-MAT 16, through whole runs (graph path) and the host loop, with hub encoding too."""
     from grazelle import graphgen as gg

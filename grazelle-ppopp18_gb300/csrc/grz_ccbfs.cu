@@ -196,7 +196,9 @@ __global__ void __launch_bounds__(BT) k_cc_pull(const uint4* __restrict__ nbr, c
     if ((use_prev == 2 && skip) || (use_prev == 3 && !skip)) return;
     // use_prev 4: after k_cc_pull_first, which ran because the skip is off: the destinations
     // whose label is already 0, the smallest there is, need none of their vectors
-    if (use_prev == 4 && !skip) {
+    // use_prev 5: the same, but only then (a later iteration is left to the open-destination pass)
+    if (use_prev == 5 && skip) return;
+    if ((use_prev == 4 || use_prev == 5) && !skip) {
         skip = true;
         mprev = 0;
     }
@@ -437,6 +439,32 @@ __global__ void __launch_bounds__(T, 8) k_cc_pull_first(const uint32_t* __restri
     if (threadIdx.x == 0) vote_add(vote, my_vote);
     __syncthreads();
     cc_record_min<T>(my_min, red32, chg, ep);
+}
+
+// CC pull of an iteration with a usable previous minimum m (the skip of k_cc_pull): marks in
+// `unres` the destinations with in-vectors whose label is above m, the only ones the iteration can
+// lower, for the compaction and k_cc_pull_expand; *gate = 1.  In an iteration without a usable
+// minimum it only sets *gate = 0.  A warp per bitmap word: each lane reads two labels.
+__global__ void __launch_bounds__(T) k_cc_mark_open(const uint32_t* __restrict__ label, const unsigned long long* __restrict__ nonempty,
+                                                    uint64_t V, uint64_t W, const unsigned long long* __restrict__ chg, uint32_t epoch,
+                                                    const uint32_t* __restrict__ epoch_dev, unsigned long long* __restrict__ unres,
+                                                    uint32_t* __restrict__ gate)
+{
+    const uint32_t ep = epoch_dev ? *epoch_dev : epoch;
+    uint32_t mprev = 0;
+    const bool skip_iteration = cc_prev_min(chg, ep, &mprev);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *gate = skip_iteration ? 1u : 0u;
+    if (!skip_iteration) return;
+    const int lane = threadIdx.x & 31;
+    const uint64_t nwarps = (uint64_t)gridDim.x * (T / 32);
+    for (uint64_t w = (uint64_t)blockIdx.x * (T / 32) + (threadIdx.x >> 5); w < W; w += nwarps) {  // warp-uniform
+        const uint64_t v0 = 64 * w + lane, v1 = v0 + 32;
+        const bool o0 = v0 < V && ld_label(label + v0) > mprev;
+        const bool o1 = v1 < V && ld_label(label + v1) > mprev;
+        const unsigned long long m = (unsigned long long)__ballot_sync(0xffffffffu, o0) |
+                                     ((unsigned long long)__ballot_sync(0xffffffffu, o1) << 32);
+        if (lane == 0) unres[w] = m & nonempty[w];
+    }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1473,16 +1501,32 @@ static int launch_cc_pull_bt(grz_graph* g, uint64_t first, uint64_t count, const
         k_cc_pull_first<<<fgrid, T, 0, g->stream>>>(g->pull.rowptr, g->pull.nbr, (uint32_t)g->V, W, f.label, g->pull.hub_vid,
                                                      g->pull.nhub, f.has_next, vc, f.vote, f.chg, f.iter, f.level_dev,
                                                      open_list ? f.unres : nullptr, gate); GRZ_COUNT_LAUNCH(g);
-        if (open_list) {
-            compact(g, f.unres, f.unres, g->pull.rowptr, 1, gate);
+        auto expand = [&]() {
             k_cc_pull_expand<<<(unsigned)g->num_sms * 8, T, 0, g->stream>>>(f.frontier, f.voff, f.vdelta, f.tile_first, f.counters,
                                                                            g->pull.nbr, (uint32_t)g->V, f.label, g->pull.hub_vid,
                                                                            g->pull.nhub, f.has_next, vc, f.vote, f.chg, f.iter,
                                                                            f.level_dev, f.counters + 5); GRZ_COUNT_LAUNCH(g);
+        };
+        if (open_list) {
+            compact(g, f.unres, f.unres, g->pull.rowptr, 1, gate);
+            expand();
         }
+        // form 3: the whole list only in the first iteration; in a skip iteration the destinations
+        // above the previous minimum are marked, compacted and pulled instead of the whole list
+        const bool open_skip = g->tune.cc_pull_first == 3;
         k_cc_pull<BT, BULK><<<(unsigned)grid, BT, smem, g->stream>>>(g->pull.nbr, g->pull.shared, first, count, (uint32_t)g->V, f.label,
                                                                     g->pull.hub_vid, g->pull.nhub, ncache, f.has_next, vc, f.vote, f.chg,
-                                                                    f.iter, f.level_dev, open_list ? 3 : 4, f.dev_err); GRZ_COUNT_LAUNCH(g);
+                                                                    f.iter, f.level_dev, open_list ? 3 : (open_skip ? 5 : 4),
+                                                                    f.dev_err); GRZ_COUNT_LAUNCH(g);
+        if (open_skip) {
+            uint32_t* gate2 = f.counters + 7;
+            const unsigned mgrid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((W + T / 32 - 1) / (T / 32),
+                                                                                       (uint64_t)g->num_sms * 8));
+            k_cc_mark_open<<<mgrid, T, 0, g->stream>>>(f.label, f.nonempty_pull, g->V, W, f.chg, f.iter, f.level_dev, f.unres,
+                                                        gate2); GRZ_COUNT_LAUNCH(g);
+            compact(g, f.unres, f.nonempty_pull, g->pull.rowptr, 0, gate2);
+            expand();
+        }
         return GRZ_OK;
     }
     if (whole && cc_use_segments(g)) {
@@ -2055,7 +2099,7 @@ int grz_frontier_run_graph(grz_graph* g, uint64_t* launches)
     // kernels of one pull iteration: BFS scan + visit, or (first pass,) compaction, expand, visit;
     // CC one pull launch, or one per source segment plus the whole-list one
     const uint64_t per_pull = bfs ? (g->tune.bfs_pull_scan ? 2 : (g->tune.bfs_pull_first ? 6 : 5))
-                                  : (f.run_seg ? cc_segment_launches(g) + 1 : (g->tune.cc_pull_first == 2 ? 6 : (g->tune.cc_pull_first ? 2 : 1)));
+                                  : (f.run_seg ? cc_segment_launches(g) + 1 : (g->tune.cc_pull_first == 2 ? 6 : (g->tune.cc_pull_first == 3 ? 7 : (g->tune.cc_pull_first ? 2 : 1))));
     const uint64_t per_push = bfs ? 5 : 4;
     uint64_t k = 1 + n + (uint64_t)c.npull * per_pull + (uint64_t)c.npush * per_push + (n % 2);
     g->nlaunch += k;

@@ -380,17 +380,31 @@ __global__ void __launch_bounds__(T, 8) k_cc_pull_first(const uint32_t* __restri
         return ld_label(label + id);
     };
     const uint64_t nwarps = (uint64_t)gridDim.x * (T / 32);
-    for (uint64_t w0 = ((uint64_t)blockIdx.x * (T / 32) + (threadIdx.x >> 5)) * CFW; w0 < W; w0 += nwarps * CFW) {  // warp-uniform
+    // row pointers of a group of destinations (a and b: start and end of each slot's range)
+    auto rows = [&](uint64_t w, uint32_t* a, uint32_t* b) {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const uint64_t v = 64 * w + 32 * (uint64_t)q + lane;
+            a[q] = b[q] = 0;
+            if (w < W && v < V) {
+                a[q] = rowptr[v];
+                b[q] = rowptr[v + 1];
+            }
+        }
+    };
+    uint64_t w0 = ((uint64_t)blockIdx.x * (T / 32) + (threadIdx.x >> 5)) * CFW;
+    uint32_t ra[Q], rb[Q];
+    rows(w0, ra, rb);
+    for (; w0 < W; w0 += nwarps * CFW) {  // warp-uniform
         uint32_t r0[Q], n[Q];
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
-            const uint64_t v = 64 * w0 + 32 * (uint64_t)q + lane;
-            n[q] = 0;
-            if (v < V) {
-                r0[q] = rowptr[v];
-                n[q] = rowptr[v + 1] - r0[q];
-            }
+            r0[q] = ra[q];
+            n[q] = rb[q] - ra[q];
         }
+        // the next group's row pointers go out now, while this group's chain runs (GB300, R-MAT 24
+        // sym: first pull 0.443 against 0.446 ms when they are loaded at the end of the step)
+        rows(w0 + nwarps * CFW, ra, rb);
         uint4 sv[Q];
 #pragma unroll
         for (int q = 0; q < Q; ++q) sv[q] = n[q] ? ld_stream(nbr + r0[q]) : make_uint4(INF, INF, INF, INF);

@@ -641,9 +641,11 @@ __global__ void __launch_bounds__(T) k_fr_count(const unsigned long long* __rest
                                                 uint32_t* __restrict__ part_n, uint32_t* __restrict__ part_vec)
 {
     __shared__ uint32_t sa[T / 32 + 1], sb[T / 32 + 1];
+    // a zero gate selects nothing (the bitmaps were not written in this phase): k_fr_scan then
+    // reports an empty list without reading the partials, and k_fr_write returns at once
+    if (gate && *gate == 0u) return;
     const uint64_t v0 = (uint64_t)blockIdx.x * CCHUNK + (uint64_t)threadIdx.x * CU;
-    // a zero gate selects nothing (the bitmaps were not written in this phase)
-    const uint32_t bits = (gate && *gate == 0u) ? 0u : selected_bits(bm1, bm2, v0, V);
+    const uint32_t bits = selected_bits(bm1, bm2, v0, V);
     if (!__syncthreads_or(bits)) {
         if (threadIdx.x == 0) { part_n[blockIdx.x] = 0; part_vec[blockIdx.x] = 0; }
         return;
@@ -666,9 +668,13 @@ __global__ void __launch_bounds__(T) k_fr_count(const unsigned long long* __rest
 constexpr int SCAN_T = 1024;
 
 __global__ void __launch_bounds__(SCAN_T) k_fr_scan(uint32_t* __restrict__ part_n, uint32_t* __restrict__ part_vec, uint32_t nb,
-                                                    uint32_t* __restrict__ counters)
+                                                    uint32_t* __restrict__ counters, const uint32_t* __restrict__ gate)
 {
     __shared__ uint32_t sa[SCAN_T / 32 + 1], sb[SCAN_T / 32 + 1];
+    if (gate && *gate == 0u) {  // gated off: an empty list (the partials were not written)
+        if (threadIdx.x == 0) { counters[0] = 0; counters[2] = 0; }
+        return;
+    }
     const uint32_t per = (nb + SCAN_T - 1) / SCAN_T;
     const uint32_t lo = min(nb, threadIdx.x * per), hi = min(nb, lo + per);
     uint32_t sn = 0, sv = 0;
@@ -713,9 +719,11 @@ __global__ void __launch_bounds__(T) k_fr_write(const unsigned long long* __rest
                                                 const uint32_t* __restrict__ rowptr, uint32_t skip, const uint32_t* __restrict__ base_n,
                                                 const uint32_t* __restrict__ base_vec, const uint32_t* __restrict__ counters,
                                                 uint32_t nb, uint32_t* __restrict__ frontier, uint32_t* __restrict__ voff,
-                                                uint32_t* __restrict__ vdelta, uint32_t* __restrict__ tile_first)
+                                                uint32_t* __restrict__ vdelta, uint32_t* __restrict__ tile_first,
+                                                const uint32_t* __restrict__ gate)
 {
     __shared__ uint32_t sa[T / 32 + 1], sb[T / 32 + 1];
+    if (gate && *gate == 0u) return;  // gated off: nothing selected
     if (blockIdx.x == 0 && threadIdx.x == 0) voff[counters[0]] = counters[2];
     const uint32_t b0 = base_n[blockIdx.x];
     const uint32_t b1 = blockIdx.x + 1 < nb ? base_n[blockIdx.x + 1] : counters[0];
@@ -1586,9 +1594,9 @@ static void compact(grz_graph* g, const unsigned long long* bm1, const unsigned 
     cudaStream_t st = g->stream;
     const unsigned nb = (unsigned)(g->V / CCHUNK + 1);
     k_fr_count<<<nb, T, 0, st>>>(bm1, bm2, g->V, rowptr, skip, gate, f.fr_part, f.fr_part + nb); GRZ_COUNT_LAUNCH(g);
-    k_fr_scan<<<1, SCAN_T, 0, st>>>(f.fr_part, f.fr_part + nb, nb, f.counters); GRZ_COUNT_LAUNCH(g);
+    k_fr_scan<<<1, SCAN_T, 0, st>>>(f.fr_part, f.fr_part + nb, nb, f.counters, gate); GRZ_COUNT_LAUNCH(g);
     k_fr_write<<<nb, T, 0, st>>>(bm1, bm2, g->V, rowptr, skip, f.fr_part, f.fr_part + nb, f.counters, nb, f.frontier, f.voff,
-                                 f.vdelta, f.tile_first); GRZ_COUNT_LAUNCH(g);
+                                 f.vdelta, f.tile_first, gate); GRZ_COUNT_LAUNCH(g);
 }
 
 // One edge phase on a vector range of the pull (pull=1) or push list.  Leaves the vote of the

@@ -167,7 +167,7 @@ extern "C" int grz_graph_create(grz_graph** out, int device, void* stream)
     g->tune.pr_grid = 0;
     g->tune.pr_props = 0;
     g->tune.bfs_pull_first = 1;
-    g->tune.cc_pull_first = 3;
+    g->tune.cc_pull_first = 4;
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g->l2_bytes, cudaDevAttrL2CacheSize, device);
@@ -895,7 +895,7 @@ extern "C" int grz_tune_set(grz_graph* g, int param, int64_t value)
         g->tune.pull_staging = (uint32_t)value;
         return GRZ_OK;
     case GRZ_TUNE_CC_PULL_FIRST:
-        if (value > 3) return grz_set_error(g, GRZ_ERR_ARG, "CC first-vector pass must be 0, 1, 2 or 3");
+        if (value > 4) return grz_set_error(g, GRZ_ERR_ARG, "CC pull form must be 0..4");
         g->tune.cc_pull_first = (uint32_t)value;
         return GRZ_OK;
     case GRZ_TUNE_BFS_PULL_FIRST:

@@ -361,7 +361,8 @@ __global__ void __launch_bounds__(T, 8) k_cc_pull_first(const uint32_t* __restri
                                                       unsigned long long* __restrict__ has_next, VoteCfg vc,
                                                       unsigned long long* __restrict__ vote, unsigned long long* __restrict__ chg,
                                                       uint32_t epoch, const uint32_t* __restrict__ epoch_dev,
-                                                      unsigned long long* __restrict__ unres, uint32_t* __restrict__ gate)
+                                                      unsigned long long* __restrict__ unres, uint32_t* __restrict__ gate,
+                                                      int open_all)
 {
     __shared__ unsigned long long red[T / 32];
     __shared__ uint32_t red32[T / 32];
@@ -431,7 +432,8 @@ __global__ void __launch_bounds__(T, 8) k_cc_pull_first(const uint32_t* __restri
                         my_min = min(my_min, m[q]);
                         ch = true;
                     }
-                    more = n[q] > 1 && min(m[q], cur) != 0;  // still open: its other vectors are read next
+                    // still open: its other vectors (open_all: all of them again) are read next
+                    more = (open_all || n[q] > 1) && min(m[q], cur) != 0;
                 }
                 hn |= (unsigned long long)__ballot_sync(0xffffffffu, ch) << (32 * h);
                 un |= (unsigned long long)__ballot_sync(0xffffffffu, more) << (32 * h);
@@ -467,7 +469,7 @@ __global__ void __launch_bounds__(T) k_cc_mark_open(const uint32_t* __restrict__
     const uint32_t ep = epoch_dev ? *epoch_dev : epoch;
     uint32_t mprev = 0;
     const bool skip_iteration = cc_prev_min(chg, ep, &mprev);
-    if (blockIdx.x == 0 && threadIdx.x == 0) *gate = skip_iteration ? 1u : 0u;
+    if (gate && blockIdx.x == 0 && threadIdx.x == 0) *gate = skip_iteration ? 1u : 0u;
     if (!skip_iteration) return;
     const int lane = threadIdx.x & 31;
     const uint64_t nwarps = (uint64_t)gridDim.x * (T / 32);
@@ -1520,15 +1522,28 @@ static int launch_cc_pull_bt(grz_graph* g, uint64_t first, uint64_t count, const
         const uint64_t W = words_of(g->V), groups = (W + CFW - 1) / CFW;
         const unsigned fgrid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((groups + T / 32 - 1) / (T / 32),
                                                                                    (uint64_t)g->num_sms * 8));
+        const bool open_all = g->tune.cc_pull_first == 4;
         k_cc_pull_first<<<fgrid, T, 0, g->stream>>>(g->pull.rowptr, g->pull.nbr, (uint32_t)g->V, W, f.label, g->pull.hub_vid,
                                                      g->pull.nhub, f.has_next, vc, f.vote, f.chg, f.iter, f.level_dev,
-                                                     open_list ? f.unres : nullptr, gate); GRZ_COUNT_LAUNCH(g);
+                                                     (open_list || open_all) ? f.unres : nullptr, gate, open_all ? 1 : 0); GRZ_COUNT_LAUNCH(g);
         auto expand = [&]() {
             k_cc_pull_expand<<<(unsigned)g->num_sms * 8, T, 0, g->stream>>>(f.frontier, f.voff, f.vdelta, f.tile_first, f.counters,
                                                                            g->pull.nbr, (uint32_t)g->V, f.label, g->pull.hub_vid,
                                                                            g->pull.nhub, f.has_next, vc, f.vote, f.chg, f.iter,
                                                                            f.level_dev, f.counters + 5); GRZ_COUNT_LAUNCH(g);
         };
+        if (open_all) {
+            // form 4: every pull over the open destinations only, marked by the first-vector pass
+            // (first iteration: every vector of those still above 0) or by k_cc_mark_open (later
+            // iterations); one of the two writes the whole bitmap in each iteration
+            const unsigned mgrid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((W + T / 32 - 1) / (T / 32),
+                                                                                       (uint64_t)g->num_sms * 8));
+            k_cc_mark_open<<<mgrid, T, 0, g->stream>>>(f.label, f.nonempty_pull, g->V, W, f.chg, f.iter, f.level_dev, f.unres,
+                                                        nullptr); GRZ_COUNT_LAUNCH(g);
+            compact(g, f.unres, f.nonempty_pull, g->pull.rowptr, 0, nullptr);
+            expand();
+            return GRZ_OK;
+        }
         if (open_list) {
             compact(g, f.unres, f.unres, g->pull.rowptr, 1, gate);
             expand();
@@ -2121,7 +2136,7 @@ int grz_frontier_run_graph(grz_graph* g, uint64_t* launches)
     // kernels of one pull iteration: BFS scan + visit, or (first pass,) compaction, expand, visit;
     // CC one pull launch, or one per source segment plus the whole-list one
     const uint64_t per_pull = bfs ? (g->tune.bfs_pull_scan ? 2 : (g->tune.bfs_pull_first ? 6 : 5))
-                                  : (f.run_seg ? cc_segment_launches(g) + 1 : (g->tune.cc_pull_first == 2 ? 6 : (g->tune.cc_pull_first == 3 ? 7 : (g->tune.cc_pull_first ? 2 : 1))));
+                                  : (f.run_seg ? cc_segment_launches(g) + 1 : (g->tune.cc_pull_first == 2 ? 6 : (g->tune.cc_pull_first == 3 ? 7 : (g->tune.cc_pull_first == 4 ? 6 : (g->tune.cc_pull_first ? 2 : 1)))));
     const uint64_t per_push = bfs ? 5 : 4;
     uint64_t k = 1 + n + (uint64_t)c.npull * per_pull + (uint64_t)c.npush * per_push + (n % 2);
     g->nlaunch += k;

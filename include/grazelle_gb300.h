@@ -163,7 +163,7 @@ int grz_read_levels(grz_graph* g, int64_t* host_levels, uint64_t capacity);
 #define GRZ_TUNE_PULL_STAGING 13 /* CC pull's edge stream: 0 = streaming loads, 1 = bulk copies (cp.async.bulk) into shared memory, two tiles ahead; results identical */
 #define GRZ_TUNE_CC_SEGMENTS 16 /* CC's first (full) pull over the source-segmented lists of GRZ_TUNE_PR_SEGMENT_BITS: 0 = when they are built (by grz_pr_init), 1 = never, 2 = built at the CC initialisation (with the default segment size when the graph is below the size threshold); results identical */
 #define GRZ_TUNE_BFS_PULL_FIRST 17 /* BFS pull over the whole list: vectors each wanted destination reads, in order, in a first pass that stops at the first vector with a frontier source (1..64; 0 = no such pass, every vector of the wanted destinations is read); destinations left undecided are finished by the pass over their remaining vectors; results identical */
-#define GRZ_TUNE_CC_PULL_FIRST 18 /* CC pull of an iteration without a usable previous minimum (the first of a run): each destination's first vector first, one destination per thread, then 1 = the whole list without the destinations at 0, 2 = only the remaining vectors of the destinations still above 0 (compacted; fewer bytes, but one iteration more on R-MAT), 3 (default) = as 1, and the later pulls read only the destinations above the previous iteration's smallest written label (marked and compacted) instead of every vector's destination; 0 = the whole list directly.  Results identical */
+#define GRZ_TUNE_CC_PULL_FIRST 18 /* CC pull of an iteration without a usable previous minimum (the first of a run): each destination's first vector first, one destination per thread, then 1 = the whole list without the destinations at 0, 2 = only the remaining vectors of the destinations still above 0 (compacted; fewer bytes, but one iteration more on R-MAT), 3 = as 1, and the later pulls read only the destinations above the previous iteration's smallest written label (marked and compacted) instead of every vector's destination, 4 (default) = every pull over marked and compacted open destinations: in the first, every vector of the destinations still above 0 after their first vector; 0 = the whole list directly.  Results identical */
 #define GRZ_TUNE_PR_SEGMENT_BITS 14 /* PageRank source segments, from the next grz_pr_init: 0 = by size (when the double props exceed 4x L2), 1 = none, 8..31 = 2^bits sources per segment.  The pull list is also kept cut by source segment, and each iteration gathers segment by segment so that a segment's props stay in L2; results identical (not with hub encoding) */
 #define GRZ_TUNE_PR_WAIT_LIMIT_US 9 /* bound of one grid-barrier wait of the persistent PageRank kernel in microseconds (0 = 2 s); a wait that runs out makes grz_pr_iterate return GRZ_ERR_TIMEOUT and leaves PageRank uninitialised */
 #define GRZ_TUNE_PR_WITHHOLD 10  /* fault injection for tests: block + 1 of the persistent PageRank kernel that never arrives at its first barrier (0 = none) */

@@ -404,7 +404,7 @@ def test_cc_full_pull_over_source_segments():
             np.testing.assert_array_equal(G.bfs(0)[1], O.bfs_levels(push, V, 0))
 
 
-@pytest.mark.parametrize("first", [0, 1, 2, 3])
+@pytest.mark.parametrize("first", [0, 1, 2, 3, 4])
 def test_cc_first_vector_pass(first):
     """CC without the first-vector pass and with it in both forms (GRZ_TUNE_CC_PULL_FIRST: then
     the whole list without the destinations at 0, or the open destinations' remaining vectors):

@@ -94,31 +94,45 @@ def profile_traffic(kernel: str, workload: str):
         return None
 
 
-def cc_first_pull_bytes(G, V):
-    """Bytes the first CC pull of a run must move in its two-pass form (k_cc_pull_first, then the
-    whole list without the destinations whose label became 0), when every destination is decided
-    by its first vector: row pointers 4(V+1); per destination with in-vectors its first vector (16)
-    and its label read and written (8); HasInfo* V/8; the whole-list pass's destination stream 4N
-    and one label per destination 4V.  The vectors of destinations still above 0 after the first
-    pass come on top, so this is a lower bound.  Returns (bytes, destinations with in-vectors, N)."""
+def nonempty_destinations(G, V):
+    """Vertices with in-vectors (the pull list's vertex index marks the others)."""
     vi = G.vertex_index()[:V]
-    vne = int(np.count_nonzero(vi < np.uint64(0x7fffffffffffffff)))
+    n = int(np.count_nonzero(vi < np.uint64(0x7fffffffffffffff)))
     del vi
+    return n
+
+
+def cc_first_pull_bytes(G, V, open_vectors=None):
+    """Bytes the first CC pull of a run moves in its default form (GRZ_TUNE_CC_PULL_FIRST 4):
+    row pointers 4(V+1); per destination with in-vectors its first vector (16) and its label read
+    and written (8); HasInfo* V/8; the compaction's two bitmaps V/4; and per vector of the
+    destinations still above 0 (counted on the device while profiling) its 16 bytes and its
+    destination's label (4).  In form 1 or 3 the whole-list pass reads the 4N-byte destination
+    stream and a label per destination instead of those vectors (a lower bound: the open
+    destinations' vectors come on top).  Returns (bytes, basis)."""
+    vne = nonempty_destinations(G, V)
     N = int(G.info().pull_vectors)
-    return 4 * (V + 1) + 24 * vne + V // 8 + 4 * N + 4 * V, vne, N
+    base = 4 * (V + 1) + 24 * vne + V // 8
+    if open_vectors is not None:
+        return base + V // 4 + 20 * open_vectors, (
+            "first-vector pass and open-destination pull: row pointers, each destination's first vector and label, "
+            "HasInfo*, the compaction's bitmaps, and the %d vectors of the destinations still above 0 "
+            "(%d destinations with in-vectors)" % (open_vectors, vne))
+    return base + 4 * N + 4 * V, (
+        "first-vector pass and whole-list pass: row pointers, each destination's first vector and label, HasInfo*, "
+        "the destination stream and labels (%d destinations with in-vectors, %d vectors; the vectors of destinations "
+        "still above 0 come on top)" % (vne, N))
 
 
-def cc_first_pull_roofline(G, V, E, ms, hbm, hbm_kind):
+def cc_first_pull_roofline(G, V, E, ms, hbm, hbm_kind, open_vectors=None):
     """Roofline entry of the first CC pull of a run (the dominant launch).  With the first-vector
     pass (the default), the algorithmic bytes are cc_first_pull_bytes; the bytes of the full pass
     over every vector (8E + 16V + V/4, the reference's pull) are reported as work-equivalent."""
     full = 8 * E + 16 * V + V // 4
     wk = full / (ms * 1e-3) / 1e9
-    if G.tuning().get("cc_pull_first", 0):
-        b, vne, n = cc_first_pull_bytes(G, V)
-        basis = ("two-pass first pull: row pointers, each destination's first vector and label, HasInfo*, the "
-                 "destination stream and labels of the whole-list pass (%d destinations with in-vectors, %d vectors; "
-                 "the vectors of destinations still above 0 come on top)" % (vne, n))
+    form = G.tuning().get("cc_pull_first", 0)
+    if form:
+        b, basis = cc_first_pull_bytes(G, V, open_vectors if form == 4 else None)
     else:
         b, basis = full, "full pass over every vector (8E + 16V + V/4)"
     ach = b / (ms * 1e-3) / 1e9
@@ -343,17 +357,18 @@ def run_native(a):
     # profiling on.  The event pairs need host-launched kernels, so CC/BFS run their host loop
     # here (the same kernels as the graph the headline region launches).
     G.profile(True)
+    G.profile_work()
     recs, first_pull = [], []
     with Timer(torch, stream) as tprof:
         for i in range(a.steps):
             step(i)
             r = G.profile_read()
             recs += r
-            # the first pull launch of a CC run is the full pass over every vector (the converged-
-            # destination skip starts in the next iteration)
+            # the first pull record of a CC run (no previous minimum to skip by yet)
             fp = [ms for k, ms in r if k == "cc_pull"]
             if fp:
                 first_pull.append(fp[0])
+    open_vectors = G.profile_work()[0] // max(1, len(first_pull))
     G.profile(False)
     ks = kernel_stats(recs)
     dominant = max(ks.items(), key=lambda kv: kv[1]["total_ms"])[0] if ks else None
@@ -370,7 +385,7 @@ def run_native(a):
             region += ", first pull of each run"
         mean_s = mean_ms * 1e-3
         if dominant == "cc_pull" and first_pull:
-            roof = cc_first_pull_roofline(G, V, E, mean_ms, hbm, hbm_kind)
+            roof = cc_first_pull_roofline(G, V, E, mean_ms, hbm, hbm_kind, open_vectors)
             roof.update({"share_of_profiled_pass": round(ks[dominant]["total_ms"] / tprof.ms, 4), "region": region,
                          "traffic": profile_traffic(dominant, "%s%d" % (wl, scale)) if not a.tune else None})
         elif dominant in alg:
@@ -744,15 +759,17 @@ def stress_study(a, torch, stream, dev, hbm, hbm_kind):
             ms.append(st.ms)
             its = (st.iterations, st.pull_iterations, st.push_iterations)
         G.profile(True)
+        G.profile_work()
         G.cc_run()
         recs = G.profile_read()
+        open_vectors = G.profile_work()[0]
         G.profile(False)
         fp = [m for k, m in recs if k == "cc_pull"]
         cc = {"gteps": round(E * its[0] / (np.mean(ms) * 1e-3) / 1e9, 3), "ms_per_run": round(float(np.mean(ms)), 3),
               "iterations_pull_push": list(its),
               "kernels_us": {k: round(v["mean_ms"] * 1e3, 1) for k, v in kernel_stats(recs).items()}}
         if fp:
-            cc["roofline"] = cc_first_pull_roofline(G, V, E, fp[0], hbm, hbm_kind)
+            cc["roofline"] = cc_first_pull_roofline(G, V, E, fp[0], hbm, hbm_kind, open_vectors)
             cc["roofline"]["launch"] = "first pull of the run"
         lab = G.props()
         # e2e: load + 16 PageRank iterations + props back; load + CC + labels back

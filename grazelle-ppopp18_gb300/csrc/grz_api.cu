@@ -275,6 +275,20 @@ extern "C" int grz_profile_read(grz_graph* g, int* kinds, float* ms, int capacit
     return n;
 }
 
+extern "C" int grz_profile_work(grz_graph* g, uint64_t* first_pull_vectors, uint64_t* later_pull_vectors)
+{
+    if (!g || !first_pull_vectors || !later_pull_vectors) return GRZ_ERR_ARG;
+    unsigned long long h[2] = { 0, 0 };
+    if (g->prof_work) {
+        GRZ_CK(g, cudaMemcpyAsync(h, g->prof_work, sizeof(h), cudaMemcpyDeviceToHost, g->stream));
+        GRZ_CK(g, cudaMemsetAsync(g->prof_work, 0, sizeof(h), g->stream));
+        GRZ_CK(g, cudaStreamSynchronize(g->stream));
+    }
+    *first_pull_vectors = h[0];
+    *later_pull_vectors = h[1];
+    return GRZ_OK;
+}
+
 extern "C" const char* grz_profile_kind_name(int kind)
 {
     static const char* names[] = { "none", "pr_gather", "pr_apply", "pr_push", "pr_vertex", "cc_pull", "cc_push",
@@ -296,6 +310,7 @@ extern "C" void grz_graph_destroy(grz_graph* g)
     free_graph_data(g);
     cudaStreamSynchronize(g->stream);
     if (g->stats_dev) cudaFree(g->stats_dev);
+    if (g->prof_work) cudaFree(g->prof_work);
     if (g->pr_bar) cudaFree(g->pr_bar);
     if (g->pr_bar_host) cudaFreeHost(g->pr_bar_host);
     if (g->copy_stream) {

@@ -964,7 +964,7 @@ __global__ void __launch_bounds__(T) k_cc_pull_expand(const uint32_t* __restrict
                                                       uint32_t nhub, unsigned long long* __restrict__ has_next, VoteCfg vc,
                                                       unsigned long long* __restrict__ vote, unsigned long long* __restrict__ chg,
                                                       uint32_t epoch, const uint32_t* __restrict__ epoch_dev,
-                                                      uint32_t* __restrict__ queue)
+                                                      uint32_t* __restrict__ queue, unsigned long long* __restrict__ work)
 {
     __shared__ uint32_t s_dst[PUSH_TILE + 1];
     __shared__ uint32_t s_off[PUSH_TILE + 1];
@@ -976,7 +976,7 @@ __global__ void __launch_bounds__(T) k_cc_pull_expand(const uint32_t* __restrict
     const uint32_t nd = counters[0], total = counters[2];
     const uint32_t ntiles = (total + PUSH_TILE - 1) / PUSH_TILE;
     const int lane = threadIdx.x & 31;
-    unsigned long long my_vote = 0;
+    unsigned long long my_vote = 0, my_vecs = 0;
     uint32_t my_min = INF;
     auto fetch = [&](uint32_t xl) -> uint32_t {
         const uint32_t sl = xl - GRZ_HUB_BASE;
@@ -1014,6 +1014,7 @@ __global__ void __launch_bounds__(T) k_cc_pull_expand(const uint32_t* __restrict
                     }
                     key = s_dst[lo];
                     if (ld_label(label + key) != 0) {
+                        ++my_vecs;
                         const uint4 sv = ld_stream(nbr + (uint32_t)(gv + s_delta[lo]));
                         m = fetch(sv.x);
                         if (m != 0) m = min(m, min(min(fetch(sv.y), fetch(sv.z)), fetch(sv.w)));
@@ -1045,6 +1046,13 @@ __global__ void __launch_bounds__(T) k_cc_pull_expand(const uint32_t* __restrict
     my_vote = block_sum_u64(my_vote, red);
     if (threadIdx.x == 0) vote_add(vote, my_vote);
     __syncthreads();
+    if (work) {  // profiling: vectors read, by kind of iteration
+        uint32_t mp = 0;
+        const int slot = cc_prev_min(chg, ep, &mp) ? 1 : 0;
+        my_vecs = block_sum_u64(my_vecs, red);
+        if (threadIdx.x == 0 && my_vecs) atomicAdd(work + slot, my_vecs);
+        __syncthreads();
+    }
     cc_record_min<T>(my_min, red32, chg, ep);
 }
 
@@ -1526,11 +1534,19 @@ static int launch_cc_pull_bt(grz_graph* g, uint64_t first, uint64_t count, const
         k_cc_pull_first<<<fgrid, T, 0, g->stream>>>(g->pull.rowptr, g->pull.nbr, (uint32_t)g->V, W, f.label, g->pull.hub_vid,
                                                      g->pull.nhub, f.has_next, vc, f.vote, f.chg, f.iter, f.level_dev,
                                                      (open_list || open_all) ? f.unres : nullptr, gate, open_all ? 1 : 0); GRZ_COUNT_LAUNCH(g);
+        unsigned long long* work = nullptr;
+        if (g->prof && g->prof->on) {
+            if (!g->prof_work) {
+                GRZ_CK(g, cudaMalloc((void**)&g->prof_work, sizeof(unsigned long long) * 2));
+                GRZ_CK(g, cudaMemsetAsync(g->prof_work, 0, sizeof(unsigned long long) * 2, g->stream));
+            }
+            work = g->prof_work;
+        }
         auto expand = [&]() {
             k_cc_pull_expand<<<(unsigned)g->num_sms * 8, T, 0, g->stream>>>(f.frontier, f.voff, f.vdelta, f.tile_first, f.counters,
                                                                            g->pull.nbr, (uint32_t)g->V, f.label, g->pull.hub_vid,
                                                                            g->pull.nhub, f.has_next, vc, f.vote, f.chg, f.iter,
-                                                                           f.level_dev, f.counters + 5); GRZ_COUNT_LAUNCH(g);
+                                                                           f.level_dev, f.counters + 5, work); GRZ_COUNT_LAUNCH(g);
         };
         if (open_all) {
             // form 4: every pull over the open destinations only, marked by the first-vector pass

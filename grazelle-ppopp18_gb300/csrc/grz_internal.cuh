@@ -505,6 +505,7 @@ struct grz_graph {
     // iteration stats (grz_stats.cu): vectors and valid lanes the edge phases processed
     int stats_on;
     unsigned long long* stats_dev;  // [vectors counted on the device, valid lanes]
+    unsigned long long* prof_work;  // while profiling: vectors the CC open-destination pulls read [first pulls, later pulls]
     uint64_t stats_host[1];         // vectors of whole ranges, counted on the host
     uint32_t max_degree;
     int max_degree_known;

@@ -68,6 +68,13 @@ class Graph:
             native.check(n, self.h)
         return [(self.lib.grz_profile_kind_name(kinds[i]).decode(), ms[i]) for i in range(n)]
 
+    def profile_work(self) -> tuple[int, int]:
+        """Vectors the CC open-destination pulls read while profiling (first pulls, later pulls)
+        since the last call."""
+        a, b = C.c_uint64(), C.c_uint64()
+        self._ck(self.lib.grz_profile_work(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def tune(self, **kw):
         """Set kernel shapes: hubs=, cc_cache=, cc_threads=, cc_grid=, pr_grid=, bfs_pull_scan=, bfs_pull_first=, cc_pull_first=,
         pr_props=, ingest_chunks=, pr_persistent=, pull_staging=, pr_segment_bits=, cc_segments= (results never depend on them; hubs and ingest_chunks take effect

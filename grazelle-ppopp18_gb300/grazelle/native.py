@@ -123,6 +123,7 @@ SIGNATURES = {
     "grz_profile_enable": (_I, [_VP, _I]),
     "grz_profile_read": (_I, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_float), _I]),
     "grz_profile_kind_name": (C.c_char_p, [_I]),
+    "grz_profile_work": (_I, [_VP, _PU64, _PU64]),
     "grz_launch_count": (C.c_ulonglong, [_VP]),
     "grz_fixed_point_roundtrip": (_I, [_D, _PD]),
     "grz_pr_step_noalloc": (_I, [_VP, _U64, _U64, _VP, _VP, _D, _VP, _VP]),

@@ -266,6 +266,9 @@ int grz_frontier_next_timed(grz_graph* g, int engine, int* engine_used, uint64_t
 int grz_profile_enable(grz_graph* g, int on);
 int grz_profile_read(grz_graph* g, int* kinds, float* ms, int capacity);
 const char* grz_profile_kind_name(int kind);
+/* while profiling: pull vectors the CC open-destination pulls (GRZ_TUNE_CC_PULL_FIRST 4) read, in
+ * first pulls and in later pulls, since the last call (which resets them) */
+int grz_profile_work(grz_graph* g, uint64_t* first_pull_vectors, uint64_t* later_pull_vectors);
 /* number of kernels this graph has launched so far (monotonic) */
 unsigned long long grz_launch_count(const grz_graph* g);
 

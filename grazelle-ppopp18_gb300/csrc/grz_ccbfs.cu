@@ -341,13 +341,16 @@ __global__ void __launch_bounds__(BT) k_cc_pull(const uint4* __restrict__ nbr, c
 // one of them is usually a hub whose label is 0 by the time it is read (in place, as the full
 // pass reads them), and then the destination's label is final for this iteration: 0 cannot be
 // lowered.  This pass evaluates every destination's first vector (lane 0 first, as in
-// k_cc_pull), one destination per thread, and writes the new labels; the pass over the whole
-// list that follows (k_cc_pull with use_prev 4) skips the vectors of the destinations at 0 and
-// evaluates all vectors of the others, so the iteration's result is the full pull's.  A warp owns
-// CFW bitmap words (64 destinations each), so it writes their HasInfo* bits (and, for the
-// compacted form, their `unres` bits: destinations still above 0 with more vectors) without
-// atomics; the pass records its smallest label written for the next iteration's skip, and sets
-// *gate to 1 in an iteration it runs, 0 in one it leaves to the skip pass.
+// k_cc_pull), one destination per thread, and writes the new labels.  What follows reads the
+// other vectors of the destinations still above 0, so the iteration's result is the full pull's:
+// in the default form (GRZ_TUNE_CC_PULL_FIRST 4) the compaction of the destinations this pass
+// marks in `unres` (open_all: every one still above 0) and k_cc_pull_expand over all their
+// vectors; in form 2 the same for the remaining vectors of those with more than one; in forms 1
+// and 3 the pass over the whole list (k_cc_pull with use_prev 4 or 5) that skips the
+// destinations at 0.  A warp owns CFW bitmap words (64 destinations each), so it writes their
+// HasInfo* and `unres` bits without atomics; the pass records its smallest label written for the
+// next iteration's skip, and sets *gate to 1 in an iteration it runs, 0 in one it leaves to the
+// later-pull kernels.
 #ifndef GRZ_CC_FW
 #define GRZ_CC_FW 1
 #endif

@@ -42,11 +42,13 @@ def _median_ms(run, trials: int) -> float:
 
 
 def tune_cc(G, trials: int = 3, threads=(256, 512, 1024), grids_per_sm=(0, 1, 2, 4), caches=(0,), stagings=(0, 1),
-            device: int = 0) -> dict:
-    """CC: pull-kernel block size x persistent grid x edge-stream staging (streaming loads or bulk
-    copies into shared memory) (x hub-label cache when hubs are loaded).  The objective is the
-    whole run to convergence (one CUDA graph launch, device time), which is what the knobs are
-    for: the first pull scans every vector, the later ones skip converged destinations."""
+            forms=(4, 3, 1, 0), device: int = 0) -> dict:
+    """CC: the pull form (GRZ_TUNE_CC_PULL_FIRST: 4 open destinations in every pull, 3 and 1 the
+    first-vector pass then the whole list, 0 the full first pull), and for the full pull the
+    kernel's block size x persistent grid x edge-stream staging (streaming loads or bulk copies
+    into shared memory) (x hub-label cache when hubs are loaded); the forms that read the whole
+    list in fewer pulls run at the starting shape.  The objective is the whole run to convergence
+    (one CUDA graph launch, device time), which is what the knobs are for."""
     sms = _sms(device)
     start = G.tuning()
 
@@ -55,19 +57,28 @@ def tune_cc(G, trials: int = 3, threads=(256, 512, 1024), grids_per_sm=(0, 1, 2,
 
     run()  # warm-up
     trials_out = []
-    for th in threads:
-        for gps in grids_per_sm:
-            for stg in stagings:
-                for cache in caches:
-                    if cache and start["hubs_loaded"] == 0:
-                        continue
-                    G.tune(cc_threads=th, cc_grid=gps * sms, cc_cache=cache, pull_staging=stg)
-                    run()  # the run graph is captured again for a new shape
-                    trials_out.append({"cc_threads": th, "cc_grid": gps * sms, "cc_cache": cache, "pull_staging": stg,
-                                       "ms": _median_ms(run, trials)})
-    keys = ("cc_threads", "cc_grid", "cc_cache", "pull_staging")
-    default = next((t for t in trials_out if t["cc_threads"] == start["cc_threads"] and t["cc_grid"] == start["cc_grid"]
-                    and t["cc_cache"] == (start["cc_cache"] if start["hubs_loaded"] else 0)
+
+    def trial(form, th, grid, cache, stg):
+        G.tune(cc_pull_first=form, cc_threads=th, cc_grid=grid, cc_cache=cache, pull_staging=stg)
+        run()  # the run graph is captured again for a new shape
+        trials_out.append({"cc_pull_first": form, "cc_threads": th, "cc_grid": grid, "cc_cache": cache, "pull_staging": stg,
+                           "ms": _median_ms(run, trials)})
+
+    start_cache = start["cc_cache"] if start["hubs_loaded"] else 0
+    for form in forms:
+        if form != 0:
+            trial(form, start["cc_threads"], start["cc_grid"], start_cache, start["pull_staging"])
+            continue
+        for th in threads:
+            for gps in grids_per_sm:
+                for stg in stagings:
+                    for cache in caches:
+                        if cache and start["hubs_loaded"] == 0:
+                            continue
+                        trial(0, th, gps * sms, cache, stg)
+    keys = ("cc_pull_first", "cc_threads", "cc_grid", "cc_cache", "pull_staging")
+    default = next((t for t in trials_out if t["cc_pull_first"] == start["cc_pull_first"] and t["cc_threads"] == start["cc_threads"]
+                    and t["cc_grid"] == start["cc_grid"] and t["cc_cache"] == start_cache
                     and t["pull_staging"] == start["pull_staging"]), None)
     best = min(trials_out, key=lambda t: t["ms"])
     G.tune(**{k: best[k] for k in keys})

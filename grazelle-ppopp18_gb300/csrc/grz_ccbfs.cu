@@ -89,21 +89,25 @@ __device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long x
 // reading the list (the count only grows), so further appends are skipped: a plain load of the
 // counter replaces the atomic, and a large iteration no longer queues millions of atomics on one
 // address.  Each destination is first-touched once per phase, so the list never outgrows V.
-__device__ __forceinline__ void touched_append(bool pred, uint32_t val, uint32_t* __restrict__ list, uint32_t* __restrict__ count,
-                                               uint32_t V)
+__device__ __forceinline__ bool touched_full(const uint32_t* count, uint32_t V)
 {
+    return *(volatile const uint32_t*)count >= (uint32_t)((uint64_t)V / VISIT_DENSE_RATIO + 1);
+}
+
+// `full`: touched_full as the caller last read it (once per tile or step, warp-uniform); the
+// count can pass the bound between two reads, which only lets a few more appends through
+__device__ __forceinline__ void touched_append(bool pred, uint32_t val, uint32_t* __restrict__ list, uint32_t* __restrict__ count,
+                                               bool full)
+{
+    if (full) return;
     const unsigned m = __ballot_sync(0xffffffffu, pred);
     if (!m) return;
     const int lane = threadIdx.x & 31;
     const int leader = __ffs(m) - 1;
-    const uint32_t cap = (uint32_t)((uint64_t)V / VISIT_DENSE_RATIO + 1);
     uint32_t base = 0;
-    if (lane == leader) {
-        base = *(volatile const uint32_t*)count;
-        base = base >= cap ? INF : atomicAdd(count, (uint32_t)__popc(m));
-    }
+    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
     base = __shfl_sync(0xffffffffu, base, leader);
-    if (pred && base != INF) list[base + __popc(m & ((1u << lane) - 1u))] = val;
+    if (pred) list[base + __popc(m & ((1u << lane) - 1u))] = val;
 }
 
 struct VoteCfg {
@@ -524,6 +528,7 @@ __global__ void __launch_bounds__(T) k_bfs_pull(const uint4* __restrict__ nbr, c
         }
 #pragma unroll
         for (int j = 0; j < U; ++j) want[j] = keys[j] != INF && bit_of(wants, keys[j]);  // strong check
+        const bool full = __shfl_sync(0xffffffffu, lane == 0 ? touched_full(ntouched, V) : false, 0);
 #pragma unroll
         for (int j = 0; j < U; ++j) {
             if (!__ballot_sync(0xffffffffu, want[j])) continue;  // warp-uniform
@@ -563,7 +568,7 @@ __global__ void __launch_bounds__(T) k_bfs_pull(const uint4* __restrict__ nbr, c
                 first_touch = atomicMin(cand + key, k) == ~0ull;
                 if (first_touch) atomicOr(has_next + (key >> 6), 1ull << (key & 63));
             }
-            touched_append(first_touch, key, touched, ntouched, V);
+            touched_append(first_touch, key, touched, ntouched, full);
         }
     }
 }
@@ -787,6 +792,7 @@ __global__ void __launch_bounds__(T) k_push_expand(const uint32_t* __restrict__ 
     __shared__ uint32_t s_off[PUSH_TILE + 1];
     __shared__ uint32_t s_delta[PUSH_TILE + 1];
     __shared__ unsigned long long red[T / 32];
+    __shared__ bool s_full;  // BFS: the touched list is long enough for the visit to sweep (read per tile)
     const uint32_t nf = counters[0], total = counters[2];
     const uint32_t ntiles = (total + PUSH_TILE - 1) / PUSH_TILE;
     unsigned long long my_vote = 0;
@@ -803,6 +809,7 @@ __global__ void __launch_bounds__(T) k_push_expand(const uint32_t* __restrict__ 
                 s_delta[i] = vdelta[first + i];
             }
         }
+        if (IsBfs && threadIdx.x == 0) s_full = touched_full(ntouched, V);
         __syncthreads();
         for (uint32_t base = t0; base < tend; base += T) {  // warp-uniform trip count
             const uint32_t gv = base + threadIdx.x;
@@ -828,7 +835,7 @@ __global__ void __launch_bounds__(T) k_push_expand(const uint32_t* __restrict__ 
                         first_touch = atomicMin(cand32 + d, u) == INF;
                         if (first_touch) atomicOr(has_next + (d >> 6), 1ull << (d & 63));
                     }
-                    touched_append(first_touch, d, touched, ntouched, V);
+                    touched_append(first_touch, d, touched, ntouched, s_full);
                 }
             } else if (live) {
                 const uint32_t msg = label[u];
@@ -881,6 +888,7 @@ __global__ void __launch_bounds__(T) k_bfs_pull_expand(const uint32_t* __restric
     __shared__ uint32_t s_off[PUSH_TILE + 1];
     __shared__ uint32_t s_delta[PUSH_TILE + 1];
     __shared__ uint32_t s_chunk;
+    __shared__ bool s_full;  // the touched list is long enough for the visit to sweep (read per tile)
     const uint32_t nd = counters[0], total = counters[2];
     const uint32_t ntiles = (total + PUSH_TILE - 1) / PUSH_TILE;
     const int lane = threadIdx.x & 31;
@@ -903,6 +911,7 @@ __global__ void __launch_bounds__(T) k_bfs_pull_expand(const uint32_t* __restric
                     s_delta[i] = vdelta[first + i];
                 }
             }
+            if (threadIdx.x == 0) s_full = touched_full(ntouched, V);
             __syncthreads();
             for (uint32_t base = t0; base < tend; base += T) {  // warp-uniform trip count
                 const uint32_t gv = base + threadIdx.x;
@@ -955,7 +964,7 @@ __global__ void __launch_bounds__(T) k_bfs_pull_expand(const uint32_t* __restric
                     first_touch = atomicMin(cand + key, k) == ~0ull;
                     if (first_touch) atomicOr(has_next + (key >> 6), 1ull << (key & 63));
                 }
-                touched_append(first_touch, key, touched, ntouched, V);
+                touched_append(first_touch, key, touched, ntouched, s_full);
             }
             __syncthreads();
         }

@@ -14,8 +14,13 @@ threshold engine switch.  One step is one full CC run.
             both copies both lists instead), builds the vector-sparse layout on the device,
             runs CC and reads the labels back (D2H).
   roofline  the dominant kernel's algorithmic bytes per launch over its mean CUDA-event
-            duration, against the measured HBM copy peak
-  apps      PageRank (R-MAT scale 20, 16 pull iterations) and BFS on the same graph
+            duration, against the measured HBM copy peak.  For CC the dominant record is a
+            run's first pull; its bytes are those of the default pull form (row pointers, first
+            vectors and labels, bitmaps, the vectors of the destinations still above 0, counted
+            on the device), with the reference's full-pass bytes beside them (work_equivalent)
+  apps      PageRank (R-MAT 20), BFS (R-MAT 26, 64 roots, both engine policies), the batch of
+            PPR and multi-source BFS, the R-MAT 27 stress graph (PageRank and CC), each with
+            parity, roofline, e2e and a CPU baseline where one fits
   cpu_baseline  the reference's algorithm on the host cores: the reference binary where it
             runs (x86-64 AVX2), else the OpenMP restatement in oracle/
 

@@ -433,3 +433,28 @@ def test_cc_first_vector_pass(first):
                 G.profile(True)  # the host loop, one launch per kernel
                 np.testing.assert_array_equal(G.connected_components(), ref)
                 G.profile(False)
+
+
+def test_profile_work_counts_open_destination_vectors():
+    """While profiling, grz_profile_work reports the vectors the CC open-destination pulls read
+    (first pulls, later pulls) and resets them; with profiling off nothing is counted.  The counts
+    are bounded by the pull list's length per pull, and the labels stay the oracle's."""
+    from grazelle import graphgen as gg
+    from grazelle.engine import Graph
+    g = gg.rmat(16, seed=93, symmetric=True)
+    pull, push = g.pull_order().pairs(), g.push_order().pairs()
+    ref = O.cc_min_labels(pull, g.num_vertices).astype(np.float64)
+    with Graph(0) as G:
+        G.load_pairs(g.num_vertices, pull, push)
+        nvec = G.info().pull_vectors
+        G.profile(True)
+        assert G.profile_work() == (0, 0)
+        lab, st = G.connected_components(stats=True)
+        first, later = G.profile_work()
+        assert 0 <= first <= nvec and 0 <= later <= nvec * max(1, st.pull_iterations)
+        assert G.profile_work() == (0, 0)
+        G.profile_read()
+        G.profile(False)
+        np.testing.assert_array_equal(lab, ref)
+        np.testing.assert_array_equal(G.connected_components(), ref)
+        assert G.profile_work() == (0, 0)

@@ -143,7 +143,8 @@ def test_trained_switch_beats_threshold():
     """Trained on per-iteration timings from seeded R-MAT and Erdos-Renyi graphs, evaluated on
     held-out graphs.  Edge-phase time summed over the iterations along each run: the learned
     choices must beat the threshold's overall and come within 15% of the best choice per
-    iteration (the regret bound).  Results are identical under both policies."""
+    iteration (the regret bound); whole BFS runs must be faster under the learned policy too.
+    Results are identical under both policies."""
     from grazelle import graphgen as gg
     from grazelle import switch as sw
     train_graphs = [("rmat17", gg.rmat(17, seed=201)), ("rmat19", gg.rmat(19, seed=202)),
@@ -164,3 +165,10 @@ def test_trained_switch_beats_threshold():
         assert r["bfs"]["identical_results"] and r["cc"]["identical_results"], name
     assert learned <= thr
     assert learned <= 1.15 * best
+    # whole BFS runs (one CUDA graph each, the decision kernels included): the learned policy
+    # wins over the held-out graphs taken together (GB300: 4.47 against 4.81 ms).  On CC both
+    # policies make the same choices on these graphs, and the network's inference is not free.
+    bfs_thr = sum(r["bfs"]["threshold_ms"] for r in report.values())
+    bfs_learned = sum(r["bfs"]["learned_ms"] for r in report.values())
+    print("bfs whole runs ms: threshold %.3f learned %.3f" % (bfs_thr, bfs_learned))
+    assert bfs_learned <= bfs_thr
